@@ -1,0 +1,1221 @@
+/*
+ * vh_oracle.c -- CPU restatement of the voxelhashmt depth-fusion path.
+ *
+ * TEST INFRASTRUCTURE ONLY (parity oracle and CPU timing baseline); the CUDA
+ * product never links it.  Every function cites the reference lines it follows.
+ * Paths are relative to the reference project root.  Build with
+ * -ffp-contract=off and without fast-math (see oracle/Makefile).
+ */
+#define _GNU_SOURCE
+#include "vh_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define GPU VO_FLAVOR_REF_GPU
+#define CPU VO_FLAVOR_REF_CPU
+#define BLOCK 8
+#define BLOCK_VOLUME 512
+#define DIRS 6
+#define LAYERS 3
+
+/* ------------------------------------------------------------------ vectors */
+/* math_types.h:44-101, cuda_tsdf_integrator.cu:181-217 */
+typedef struct {
+  float x, y, z;
+} v3;
+
+static inline v3 mk(float x, float y, float z) {
+  v3 r;
+  r.x = x;
+  r.y = y;
+  r.z = z;
+  return r;
+}
+static inline v3 vsub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 vadd(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vmul(v3 v, float s) { return mk(v.x * s, v.y * s, v.z * s); }
+static inline v3 vdivs(v3 v, float s) { return mk(v.x / s, v.y / s, v.z / s); }
+static inline float vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 vcross(v3 a, v3 b) {
+  return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline float vnorm(v3 v) { return sqrtf(vdot(v, v)); }
+
+/* GPU: cuda_tsdf_integrator.cu:201-209 and cuda_block_allocator.cu:127-135 (<=1e-6, multiply by 1/len);
+ * CPU: math_types.h:95-101 (<=1e-8, divide by len). */
+static inline v3 vnormalize(int fl, v3 v) {
+  const float len = vnorm(v);
+  if (fl == GPU) {
+    if (len <= 1e-6f) return mk(0.0f, 0.0f, 0.0f);
+    const float inv = 1.0f / len;
+    return mk(v.x * inv, v.y * inv, v.z * inv);
+  }
+  if (len <= 1e-8f) return mk(0.0f, 0.0f, 0.0f);
+  return vdivs(v, len);
+}
+
+/* CPU std::max/std::min (a<b?b:a) vs GPU fmaxf/fminf: equal for the finite non-NaN values used here. */
+static inline float fmax_f(float a, float b) { return (a < b) ? b : a; }
+static inline float fmin_f(float a, float b) { return (b < a) ? b : a; }
+static inline float clamp_f(float v, float lo, float hi) { return fmax_f(lo, fmin_f(hi, v)); }
+
+/* math_types.h:180-198 / cuda_tsdf_integrator.cu:452-466 */
+static inline v3 pose_point(const vo_pose* P, v3 p) {
+  return mk(P->R[0] * p.x + P->R[1] * p.y + P->R[2] * p.z + P->t[0],
+            P->R[3] * p.x + P->R[4] * p.y + P->R[5] * p.z + P->t[1],
+            P->R[6] * p.x + P->R[7] * p.y + P->R[8] * p.z + P->t[2]);
+}
+static inline v3 pose_vector(const vo_pose* P, v3 p) {
+  return mk(P->R[0] * p.x + P->R[1] * p.y + P->R[2] * p.z, P->R[3] * p.x + P->R[4] * p.y + P->R[5] * p.z,
+            P->R[6] * p.x + P->R[7] * p.y + P->R[8] * p.z);
+}
+/* Pose::inverse, math_types.h:192-197: R' = R^T, t' = R' * (t * -1) */
+static void pose_inverse(const vo_pose* P, vo_pose* out) {
+  const float* R = P->R;
+  const float Rt[9] = {R[0], R[3], R[6], R[1], R[4], R[7], R[2], R[5], R[8]};
+  const float nt[3] = {P->t[0] * -1.0f, P->t[1] * -1.0f, P->t[2] * -1.0f};
+  memcpy(out->R, Rt, sizeof(Rt));
+  out->t[0] = Rt[0] * nt[0] + Rt[1] * nt[1] + Rt[2] * nt[2];
+  out->t[1] = Rt[3] * nt[0] + Rt[4] * nt[1] + Rt[5] * nt[2];
+  out->t[2] = Rt[6] * nt[0] + Rt[7] * nt[1] + Rt[8] * nt[2];
+}
+
+/* math_types.h:228-232, cuda_block_allocator.cu:145-151 */
+static inline v3 back_project(int u, int v, float d, const vo_intrinsics* K) {
+  return mk(((float)u - K->cx) * d / K->fx, ((float)v - K->cy) * d / K->fy, d);
+}
+/* voxel_hash_tsdf.h:586-593, cuda_tsdf_integrator.cu:570-579 */
+static inline v3 back_project_cont(float u, float v, float d, const vo_intrinsics* K) {
+  return mk((u - K->cx) * d / K->fx, (v - K->cy) * d / K->fy, d);
+}
+/* math_types.h:234-244, cuda_tsdf_integrator.cu:468-477 */
+static inline int project_point(v3 pc, const vo_intrinsics* K, float* u, float* v) {
+  if (pc.z <= 1e-6f) return 0;
+  *u = K->fx * pc.x / pc.z + K->cx;
+  *v = K->fy * pc.y / pc.z + K->cy;
+  return *u >= 0.0f && *u <= (float)(K->width - 1) && *v >= 0.0f && *v <= (float)(K->height - 1);
+}
+
+/* ---------------------------------------------------------------------- exp */
+/* Own single-precision exp used by the CUDA product (same constants, same fmaf sequence):
+ * Cody-Waite reduction x = k ln2 + r with ln2 split into an 11-trailing-zero high part and a low part,
+ * then e^r by the degree-7 Taylor polynomial in Horner form (|r| <= ln2/2, truncation < 6e-9 relative),
+ * then scaling by 2^k through the exponent field (two steps below 2^-126). */
+float vo_expf_own(float x) {
+  if (!(x > -104.0f)) return 0.0f;
+  if (x > 0x1.62e42ep+6f) return INFINITY;
+  const float k = rintf(x * 0x1.715476p+0f);
+  float r = fmaf(k, -0x1.62e400p-1f, x);
+  r = fmaf(k, -0x1.7f7d1cp-20f, r);
+  float p = 0x1.a01a02p-13f;
+  p = fmaf(p, r, 0x1.6c16c2p-10f);
+  p = fmaf(p, r, 0x1.111112p-7f);
+  p = fmaf(p, r, 0x1.555556p-5f);
+  p = fmaf(p, r, 0x1.555556p-3f);
+  p = fmaf(p, r, 0x1.000000p-1f);
+  p = fmaf(p, r, 1.0f);
+  p = fmaf(p, r, 1.0f);
+  const int ki = (int)k;
+  union {
+    uint32_t u;
+    float f;
+  } s;
+  if (ki > 127) {
+    s.u = (uint32_t)(127 + 127) << 23;
+    return (p * s.f) * 2.0f;
+  }
+  if (ki >= -126) {
+    s.u = (uint32_t)(ki + 127) << 23;
+    return p * s.f;
+  }
+  s.u = (uint32_t)(ki + 127 + 64) << 23;
+  return (p * s.f) * 0x1p-64f;
+}
+
+static inline float vo_exp(const vo_config* c, float x) {
+  return c->exp_impl == VO_EXP_OWN ? vo_expf_own(x) : expf(x);
+}
+/* voxel_hash_tsdf.h:552-554, cuda_tsdf_integrator.cu:173-175 */
+static inline float gaussian(const vo_config* c, float sq, float inv_two_sigma_sq) {
+  return vo_exp(c, -sq * inv_two_sigma_sq);
+}
+static inline float inv_two_sigma_sq(float s) { return 1.0f / (2.0f * s * s); }
+
+/* ------------------------------------------------------------------- config */
+void vo_config_default(vo_config* c, int32_t flavor) {
+  memset(c, 0, sizeof(*c));
+  c->flavor = flavor;
+  c->exp_impl = VO_EXP_LIBM;
+  c->filter_radius = 2;                /* cuda_tsdf_integrator.cu:31, reconstruction_backend.cpp:26 */
+  c->filter_sigma_spatial = 1.5f;      /* :32 / :27 */
+  c->filter_sigma_range = 0.0012f;     /* :33 / :28 */
+  c->filter_sigma_angular = 0.35f;     /* :34 / :29 */
+  c->normal_radius = 1;                /* cuda_tsdf_integrator.cu:23, voxel_hash_tsdf.h:196 */
+  c->normal_sigma_spatial = 1.0f;      /* :24 / :197 */
+  c->normal_sigma_range = 0.0012f;     /* :25 / :198 */
+  c->normal_sigma_angular = 0.35f;     /* :26 / :199 */
+  c->layer_merge_scale = 0.25f;        /* :29 / :202 */
+  c->layer_extract_scale = 0.55f;      /* cuda_mesh_extractor.cu:20, voxel_hash_tsdf.h:203 */
+  c->max_weight = 100.0f;              /* cuda_tsdf_integrator.cu:18, voxel_hash_tsdf.h:194 */
+  c->depth_sigma = 1.5f;               /* :19 / :565 */
+  c->huber_delta = 0.35f;              /* :20 / :571 */
+  c->min_obs_weight = 0.05f;           /* :21 / :580 */
+  c->min_view_weight = 0.15f;          /* :22 / :195 */
+  c->threads = 1;
+  if (flavor == GPU) {
+    c->disc_base = 0.012f;             /* cuda_tsdf_integrator.cu:27 */
+    c->disc_rel = 0.025f;              /* :28 */
+    c->filter_min_cos = 0.9f;          /* :35 */
+    c->layer_normal_cos = 0.9f;        /* :30 */
+  } else {
+    c->disc_base = 0.0012f;            /* reconstruction_backend.cpp:30, voxel_hash_tsdf.h:200 */
+    c->disc_rel = 0.0025f;             /* :31 / :201 */
+    c->filter_min_cos = 0.6f;          /* reconstruction_backend.cpp:32 */
+    c->layer_normal_cos = 0.75f;       /* voxel_hash_tsdf.h:204 */
+  }
+}
+
+/* -------------------------------------------------------------- parallel for */
+typedef void (*pf_fn)(void* ctx, int64_t i);
+typedef struct {
+  pf_fn fn;
+  void* ctx;
+  int64_t n;
+  int64_t next;
+} pf_state;
+
+static void* pf_worker(void* arg) {
+  pf_state* s = (pf_state*)arg;
+  for (;;) {
+    const int64_t i = __atomic_fetch_add(&s->next, 1, __ATOMIC_RELAXED);
+    if (i >= s->n) break;
+    s->fn(s->ctx, i);
+  }
+  return NULL;
+}
+
+static void parallel_for(int threads, int64_t n, pf_fn fn, void* ctx) {
+  if (threads <= 1 || n <= 1) {
+    for (int64_t i = 0; i < n; ++i) fn(ctx, i);
+    return;
+  }
+  if (threads > 256) threads = 256;
+  if ((int64_t)threads > n) threads = (int)n;
+  pf_state s = {fn, ctx, n, 0};
+  pthread_t tid[256];
+  int started = 0;
+  for (int t = 1; t < threads; ++t) {
+    if (pthread_create(&tid[started], NULL, pf_worker, &s) == 0) ++started;
+  }
+  pf_worker(&s);
+  for (int t = 0; t < started; ++t) pthread_join(tid[t], NULL);
+}
+
+/* ----------------------------------------------------------- depth helpers */
+/* cuda_tsdf_integrator.cu:177-179, voxel_hash_tsdf.h:226-228, reconstruction_backend.cpp:38-40 */
+static inline float disc_threshold(const vo_config* c, float ref) {
+  return fmax_f(c->disc_base, c->disc_rel * fmax_f(ref, 0.0f));
+}
+
+/* cuda_tsdf_integrator.cu:219-226, voxel_hash_tsdf.h:230-237 */
+static inline v3 orient_toward_camera(int fl, v3 n, v3 pc) {
+  if (vnorm(n) <= 1e-6f || vnorm(pc) <= 1e-6f) return n;
+  const v3 view = vnormalize(fl, pc);
+  return vdot(n, view) > 0.0f ? vmul(n, -1.0f) : n;
+}
+
+/* cuda_tsdf_integrator.cu:581-627, reconstruction_backend.cpp:57-94 */
+static int pixel_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, int u, int v, v3* normal) {
+  const int W = K->width, H = K->height;
+  if (u <= 0 || v <= 0 || u + 1 >= W || v + 1 >= H) return 0;
+  const float dc = depth[(size_t)v * W + u];
+  const float dl = depth[(size_t)v * W + u - 1];
+  const float dr = depth[(size_t)v * W + u + 1];
+  const float du = depth[(size_t)(v - 1) * W + u];
+  const float dd = depth[(size_t)(v + 1) * W + u];
+  if (!(dc > 0.0f) || !(dl > 0.0f) || !(dr > 0.0f) || !(du > 0.0f) || !(dd > 0.0f)) return 0;
+  const float thr = disc_threshold(c, dc);
+  if (fabsf(dl - dc) > thr || fabsf(dr - dc) > thr || fabsf(du - dc) > thr || fabsf(dd - dc) > thr) return 0;
+  const v3 pl = back_project_cont((float)(u - 1), (float)v, dl, K);
+  const v3 pr = back_project_cont((float)(u + 1), (float)v, dr, K);
+  const v3 pu = back_project_cont((float)u, (float)(v - 1), du, K);
+  const v3 pd = back_project_cont((float)u, (float)(v + 1), dd, K);
+  const v3 dx = vsub(pr, pl);
+  const v3 dy = vsub(pd, pu);
+  v3 n = vnormalize(c->flavor, vcross(dy, dx));
+  if (vnorm(n) <= 1e-6f) return 0;
+  const v3 cp = back_project_cont((float)u, (float)v, dc, K);
+  n = orient_toward_camera(c->flavor, n, cp);
+  *normal = n;
+  return vnorm(n) > 1e-6f;
+}
+
+typedef struct {
+  const vo_config* c;
+  const float* depth;
+  const vo_intrinsics* K;
+  float* normals;
+  uint8_t* valid;
+  float* out;
+} filter_ctx;
+
+static void normals_row(void* p, int64_t v) {
+  filter_ctx* f = (filter_ctx*)p;
+  const int W = f->K->width;
+  for (int u = 0; u < W; ++u) {
+    const size_t idx = (size_t)v * W + u;
+    v3 n = mk(0.0f, 0.0f, 0.0f);
+    if (pixel_normal(f->c, f->depth, f->K, u, (int)v, &n)) {
+      f->normals[3 * idx + 0] = n.x;
+      f->normals[3 * idx + 1] = n.y;
+      f->normals[3 * idx + 2] = n.z;
+      f->valid[idx] = 1;
+    } else {
+      f->normals[3 * idx + 0] = 0.0f;
+      f->normals[3 * idx + 1] = 0.0f;
+      f->normals[3 * idx + 2] = 0.0f;
+      f->valid[idx] = 0;
+    }
+  }
+}
+
+/* cuda_tsdf_integrator.cu:650-725, reconstruction_backend.cpp:125-186 */
+static void bilateral_row(void* p, int64_t vv) {
+  filter_ctx* f = (filter_ctx*)p;
+  const vo_config* c = f->c;
+  const int W = f->K->width, H = f->K->height, v = (int)vv, R = c->filter_radius;
+  const float ks = inv_two_sigma_sq(c->filter_sigma_spatial);
+  const float kr = inv_two_sigma_sq(c->filter_sigma_range);
+  const float ka = inv_two_sigma_sq(c->filter_sigma_angular);
+  for (int u = 0; u < W; ++u) {
+    const size_t ci = (size_t)v * W + u;
+    const float center = f->depth[ci];
+    if (center <= 0.0f) {
+      f->out[ci] = 0.0f;
+      continue;
+    }
+    const int has_cn = f->valid[ci] != 0;
+    const v3 cn = has_cn ? mk(f->normals[3 * ci], f->normals[3 * ci + 1], f->normals[3 * ci + 2]) : mk(0.0f, 0.0f, 0.0f);
+    const float thr = disc_threshold(c, center);
+    float wds = 0.0f, ws = 0.0f;
+    for (int dv = -R; dv <= R; ++dv) {
+      const int sv = v + dv;
+      if (sv < 0 || sv >= H) continue;
+      for (int du = -R; du <= R; ++du) {
+        const int su = u + du;
+        if (su < 0 || su >= W) continue;
+        const size_t si = (size_t)sv * W + su;
+        const float sd = f->depth[si];
+        if (sd <= 0.0f || fabsf(sd - center) > thr) continue;
+        const float spatial = (float)(du * du + dv * dv);
+        const float delta = sd - center;
+        const float range = delta * delta;
+        float w = gaussian(c, spatial, ks) * gaussian(c, range, kr);
+        if (has_cn) {
+          if (f->valid[si] == 0) continue;
+          const v3 sn = mk(f->normals[3 * si], f->normals[3 * si + 1], f->normals[3 * si + 2]);
+          const float cosine = clamp_f(vdot(cn, sn), -1.0f, 1.0f);
+          if (cosine < c->filter_min_cos) continue;
+          const float ad = 1.0f - cosine;
+          w *= gaussian(c, ad * ad, ka);
+        }
+        wds += w * sd;
+        ws += w;
+      }
+    }
+    f->out[ci] = ws > 1e-6f ? (wds / ws) : center;
+  }
+}
+
+void vo_depth_normals(const vo_config* c, const float* depth, const vo_intrinsics* K, float* normals,
+                      uint8_t* valid) {
+  filter_ctx f = {c, depth, K, normals, valid, NULL};
+  parallel_for(c->threads, K->height, normals_row, &f);
+}
+
+void vo_filter_depth(const vo_config* c, const float* depth, const vo_intrinsics* K, float* out) {
+  const size_t n = (size_t)K->width * (size_t)K->height;
+  if (K->width <= 0 || K->height <= 0) return;
+  float* normals = (float*)malloc(3 * n * sizeof(float));
+  uint8_t* valid = (uint8_t*)malloc(n);
+  filter_ctx f = {c, depth, K, normals, valid, out};
+  parallel_for(c->threads, K->height, normals_row, &f);
+  parallel_for(c->threads, K->height, bilateral_row, &f);
+  free(normals);
+  free(valid);
+}
+
+/* ---------------------------------------------------------------- sampling */
+/* cuda_tsdf_integrator.cu:479-489 (floorf(x+0.5)), voxel_hash_tsdf.h:673-682 (lround) */
+static inline int sample_nearest(int fl, const float* depth, const vo_intrinsics* K, float u, float v, float* d) {
+  int ui, vi;
+  if (fl == GPU) {
+    ui = (int)floorf(u + 0.5f);
+    vi = (int)floorf(v + 0.5f);
+  } else {
+    ui = (int)lroundf(u);
+    vi = (int)lroundf(v);
+  }
+  if (ui < 0 || ui >= K->width || vi < 0 || vi >= K->height) return 0;
+  *d = depth[(size_t)vi * K->width + ui];
+  return *d > 0.0f;
+}
+
+/* cuda_tsdf_integrator.cu:504-568, voxel_hash_tsdf.h:684-748 */
+static int sample_bilinear(const vo_config* c, const float* depth, const vo_intrinsics* K, float u, float v,
+                           float* out) {
+  const int W = K->width, H = K->height;
+  if (W <= 0 || H <= 0) return 0;
+  if (u < 0.0f || v < 0.0f || u > (float)(W - 1) || v > (float)(H - 1)) return 0;
+  const int x0 = (int)floorf(u);
+  const int y0 = (int)floorf(v);
+  const int x1 = x0 + 1 < W - 1 ? x0 + 1 : W - 1;
+  const int y1 = y0 + 1 < H - 1 ? y0 + 1 : H - 1;
+  const float tx = u - (float)x0;
+  const float ty = v - (float)y0;
+  const float d00 = depth[(size_t)y0 * W + x0];
+  const float d10 = depth[(size_t)y0 * W + x1];
+  const float d01 = depth[(size_t)y1 * W + x0];
+  const float d11 = depth[(size_t)y1 * W + x1];
+  if (d00 > 0.0f && d10 > 0.0f && d01 > 0.0f && d11 > 0.0f) {
+    float ref = 0.0f;
+    if (!sample_nearest(c->flavor, depth, K, u, v, &ref)) ref = d00;
+    const float thr = disc_threshold(c, ref);
+    const float mn = fmin_f(fmin_f(d00, d10), fmin_f(d01, d11));
+    const float mx = fmax_f(fmax_f(d00, d10), fmax_f(d01, d11));
+    const float top = d00 + (d10 - d00) * tx;
+    const float bottom = d01 + (d11 - d01) * tx;
+    if (mx - mn <= thr) {
+      *out = top + (bottom - top) * ty;
+      return 1;
+    }
+    const float bw[4] = {(1.0f - tx) * (1.0f - ty), tx * (1.0f - ty), (1.0f - tx) * ty, tx * ty};
+    const float nd[4] = {d00, d10, d01, d11};
+    float wds = 0.0f, ws = 0.0f;
+    for (int i = 0; i < 4; ++i) {
+      if (fabsf(nd[i] - ref) > thr) continue;
+      wds += bw[i] * nd[i];
+      ws += bw[i];
+    }
+    if (ws > 1e-6f) {
+      *out = wds / ws;
+      return 1;
+    }
+  }
+  return sample_nearest(c->flavor, depth, K, u, v, out);
+}
+
+/* cuda_tsdf_integrator.cu:727-752, voxel_hash_tsdf.h:750-771 */
+static int base_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, float u, float v, v3* n) {
+  float dl = 0.0f, dr = 0.0f, du = 0.0f, dd = 0.0f;
+  if (!sample_bilinear(c, depth, K, u - 1.0f, v, &dl) || !sample_bilinear(c, depth, K, u + 1.0f, v, &dr) ||
+      !sample_bilinear(c, depth, K, u, v - 1.0f, &du) || !sample_bilinear(c, depth, K, u, v + 1.0f, &dd)) {
+    return 0;
+  }
+  const v3 pl = back_project_cont(u - 1.0f, v, dl, K);
+  const v3 pr = back_project_cont(u + 1.0f, v, dr, K);
+  const v3 pu = back_project_cont(u, v - 1.0f, du, K);
+  const v3 pd = back_project_cont(u, v + 1.0f, dd, K);
+  const v3 dx = vsub(pr, pl);
+  const v3 dy = vsub(pd, pu);
+  *n = vnormalize(c->flavor, vcross(dy, dx));
+  return vnorm(*n) > 1e-6f;
+}
+
+/* cuda_tsdf_integrator.cu:754-832, voxel_hash_tsdf.h:773-840 */
+static int surface_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, float u, float v,
+                          v3* normal) {
+  const int fl = c->flavor;
+  v3 cn = mk(0.0f, 0.0f, 0.0f);
+  if (!base_normal(c, depth, K, u, v, &cn)) return 0;
+  float cd = 0.0f;
+  if (!sample_bilinear(c, depth, K, u, v, &cd)) return 0;
+  const v3 cp = back_project_cont(u, v, cd, K);
+  cn = orient_toward_camera(fl, cn, cp);
+  const float ks = inv_two_sigma_sq(c->normal_sigma_spatial);
+  const float kr = inv_two_sigma_sq(c->normal_sigma_range);
+  const float ka = inv_two_sigma_sq(c->normal_sigma_angular);
+  v3 wsum = mk(0.0f, 0.0f, 0.0f);
+  float ws = 0.0f;
+  const int R = c->normal_radius;
+  for (int dv = -R; dv <= R; ++dv) {
+    for (int du = -R; du <= R; ++du) {
+      const float su = u + (float)du;
+      const float sv = v + (float)dv;
+      v3 sn = mk(0.0f, 0.0f, 0.0f);
+      if (!base_normal(c, depth, K, su, sv, &sn)) continue;
+      float sd = 0.0f;
+      if (!sample_bilinear(c, depth, K, su, sv, &sd)) continue;
+      const v3 sp = back_project_cont(su, sv, sd, K);
+      sn = orient_toward_camera(fl, sn, sp);
+      const float spatial = (float)(du * du + dv * dv);
+      const float delta = sd - cd;
+      const float range = delta * delta;
+      const float cosine = clamp_f(vdot(cn, sn), -1.0f, 1.0f);
+      const float ad = 1.0f - cosine;
+      const float as = ad * ad;
+      const float w = gaussian(c, spatial, ks) * gaussian(c, range, kr) * gaussian(c, as, ka);
+      wsum.x += sn.x * w;
+      wsum.y += sn.y * w;
+      wsum.z += sn.z * w;
+      ws += w;
+    }
+  }
+  if (ws <= 1e-6f) {
+    *normal = cn;
+    return 1;
+  }
+  const float inv = 1.0f / ws;
+  v3 n = vnormalize(fl, mk(wsum.x * inv, wsum.y * inv, wsum.z * inv));
+  n = orient_toward_camera(fl, n, cp);
+  if (vnorm(n) <= 1e-6f) n = cn;
+  *normal = n;
+  return vnorm(n) > 1e-6f;
+}
+
+/* -------------------------------------------------------------- weighting */
+/* cuda_tsdf_integrator.cu:429-450, voxel_hash_tsdf.h:556-584 */
+float vo_observation_weight(const vo_config* c, float depth, float sd, float trunc, float view) {
+  if (depth <= 0.0f || trunc <= 1e-6f) return 0.0f;
+  const float dr = depth / c->depth_sigma;
+  const float dw = 1.0f / (1.0f + dr * dr);
+  const float nr = fabsf(sd) / trunc;
+  float rw = 1.0f;
+  if (nr > c->huber_delta) rw = c->huber_delta / nr;
+  const float bw = 1.0f - 0.5f * clamp_f(nr, 0.0f, 1.0f);
+  const float base = fmax_f(c->min_obs_weight, dw * rw * bw);
+  const float aw = clamp_f(view, c->min_view_weight, 1.0f);
+  return base * aw;
+}
+
+/* cuda_tsdf_integrator.cu:228-243, voxel_hash_tsdf.h:239-254 */
+static inline int dominant_direction(v3 n) {
+  const float nx = fabsf(n.x), ny = fabsf(n.y), nz = fabsf(n.z);
+  if (nx <= 1e-6f && ny <= 1e-6f && nz <= 1e-6f) return -1;
+  if (nx >= ny && nx >= nz) return n.x >= 0.0f ? 0 : 1;
+  if (ny >= nx && ny >= nz) return n.y >= 0.0f ? 2 : 3;
+  return n.z >= 0.0f ? 4 : 5;
+}
+
+/* GPU: cuda_tsdf_integrator.cu:296-313; CPU: voxel_hash_tsdf.h:311-330 (dot with the unit axis) */
+static inline float coordinate_along(int fl, v3 p, int d) {
+  if (fl == GPU) {
+    switch (d) {
+      case 0: return p.x;
+      case 1: return -p.x;
+      case 2: return p.y;
+      case 3: return -p.y;
+      case 4: return p.z;
+      default: return -p.z;
+    }
+  }
+  static const float axes[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  return vdot(p, mk(axes[d][0], axes[d][1], axes[d][2]));
+}
+
+static inline float sign_not_zero(float v) { return v >= 0.0f ? 1.0f : -1.0f; }
+
+/* GPU: cuda_tsdf_integrator.cu:253-278 (floorf(x*65535+0.5)); CPU: voxel_hash_tsdf.h:268-289 (lround) */
+static uint32_t pack_normal(int fl, v3 raw) {
+  const v3 n = vnormalize(fl, raw);
+  const float s = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
+  if (s <= 1e-6f) return 0U;
+  v3 p = vdivs(n, s);
+  if (p.z < 0.0f) {
+    const float px = (1.0f - fabsf(p.y)) * sign_not_zero(p.x);
+    const float py = (1.0f - fabsf(p.x)) * sign_not_zero(p.y);
+    p.x = px;
+    p.y = py;
+  }
+  uint32_t q[2];
+  const float comp[2] = {p.x, p.y};
+  for (int i = 0; i < 2; ++i) {
+    const float cl = clamp_f(comp[i] * 0.5f + 0.5f, 0.0f, 1.0f);
+    if (fl == GPU) {
+      q[i] = (uint32_t)floorf(cl * 65535.0f + 0.5f);
+    } else {
+      q[i] = (uint32_t)lroundf(cl * 65535.0f);
+    }
+  }
+  return q[0] | (q[1] << 16U);
+}
+
+/* GPU integrator: cuda_tsdf_integrator.cu:258-294 (normalizeVec, zero on degenerate);
+ * GPU mesh extractor: cuda_mesh_extractor.cu:233-257 ((0,0,1) on degenerate);
+ * CPU: voxel_hash_tsdf.h:291-309 (normalized). */
+static v3 unpack_normal(int fl, int mesh_variant, uint32_t packed) {
+  v3 n = mk((float)(packed & 0xffffU) / 65535.0f * 2.0f - 1.0f,
+            (float)((packed >> 16U) & 0xffffU) / 65535.0f * 2.0f - 1.0f, 0.0f);
+  n.z = 1.0f - fabsf(n.x) - fabsf(n.y);
+  if (n.z < 0.0f) {
+    const float px = (1.0f - fabsf(n.y)) * sign_not_zero(n.x);
+    const float py = (1.0f - fabsf(n.x)) * sign_not_zero(n.y);
+    n.x = px;
+    n.y = py;
+  }
+  if (fl == GPU && mesh_variant) {
+    const float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+    if (len <= 1e-6f) return mk(0.0f, 0.0f, 1.0f);
+    const float inv = 1.0f / len;
+    return mk(n.x * inv, n.y * inv, n.z * inv);
+  }
+  return vnormalize(fl, n);
+}
+
+uint32_t vo_pack_normal(int32_t flavor, const float n[3]) { return pack_normal(flavor, mk(n[0], n[1], n[2])); }
+void vo_unpack_normal(int32_t flavor, int32_t mesh_variant, uint32_t packed, float out[3]) {
+  const v3 n = unpack_normal(flavor, mesh_variant, packed);
+  out[0] = n.x;
+  out[1] = n.y;
+  out[2] = n.z;
+}
+
+/* ---------------------------------------------------------- layer update */
+/* cuda_tsdf_integrator.cu:319-336, voxel_hash_tsdf.h:341-355 */
+static void sort_layers(vo_layer* L) {
+  for (int pass = 0; pass < LAYERS - 1; ++pass) {
+    for (int i = 0; i < LAYERS - pass - 1; ++i) {
+      const int lv = L[i].weight > 0.0f;
+      const int rv = L[i + 1].weight > 0.0f;
+      const int swap = (!lv && rv) || (lv && rv && L[i].surface_coord > L[i + 1].surface_coord);
+      if (swap) {
+        const vo_layer t = L[i];
+        L[i] = L[i + 1];
+        L[i + 1] = t;
+      }
+    }
+  }
+}
+
+/* cuda_tsdf_integrator.cu:338-372, voxel_hash_tsdf.h:357-392 */
+static int find_layer_slot(int fl, const vo_layer* L, float sc, v3 n, float tol, float min_cos) {
+  int empty = -1, best = -1;
+  float best_delta = fl == GPU ? 1e30f : FLT_MAX;
+  for (int i = 0; i < LAYERS; ++i) {
+    if (!(L[i].weight > 0.0f)) {
+      if (empty < 0) empty = i;
+      continue;
+    }
+    const v3 ln = unpack_normal(fl, 0, L[i].packed_normal);
+    if (vdot(ln, n) < min_cos) continue;
+    const float delta = fabsf(L[i].surface_coord - sc);
+    if (delta < best_delta) {
+      best_delta = delta;
+      best = i;
+    }
+  }
+  if (best >= 0 && best_delta <= tol) return best;
+  return empty;
+}
+
+/* cuda_tsdf_integrator.cu:374-427, voxel_hash_tsdf.h:479-529 */
+static void integrate_sample(const vo_config* c, float vs, vo_voxel* voxel, int d, float sc, v3 sp, v3 nw,
+                             float obs) {
+  const int fl = c->flavor;
+  if (d < 0 || d >= DIRS || obs <= 0.0f) return;
+  const v3 n = vnormalize(fl, nw);
+  if (vnorm(n) <= 1e-6f) return;
+  const float plane_offset = vdot(n, sp);
+  const float tol = fmax_f(1e-6f, vs * c->layer_merge_scale);
+  vo_layer* L = voxel->layers[d];
+  const int li = find_layer_slot(fl, L, sc, n, tol, c->layer_normal_cos);
+  if (li < 0) return;
+  vo_layer* layer = &L[li];
+  const float pw = layer->weight;
+  const float ew = fmin_f(obs, fmax_f(0.0f, c->max_weight - pw));
+  if (ew <= 0.0f) return;
+  const float nwt = pw + ew;
+  v3 blended = n;
+  layer->surface_coord = pw > 0.0f ? ((layer->surface_coord * pw + sc * ew) / nwt) : sc;
+  layer->plane_offset = pw > 0.0f ? ((layer->plane_offset * pw + plane_offset * ew) / nwt) : plane_offset;
+  if (pw > 0.0f) {
+    const v3 pn = unpack_normal(fl, 0, layer->packed_normal);
+    if (fl == GPU) {
+      blended = vnormalize(fl, vmul(vadd(vmul(pn, pw), vmul(n, ew)), 1.0f / nwt));
+    } else {
+      blended = vnormalize(fl, vdivs(vadd(vmul(pn, pw), vmul(n, ew)), nwt));
+    }
+    if (vnorm(blended) <= 1e-6f) blended = n;
+  }
+  layer->weight = nwt;
+  layer->packed_normal = pack_normal(fl, blended);
+  sort_layers(L);
+}
+
+/* ------------------------------------------------------------ block keys */
+/* cuda_block_allocator.cu:153-159 */
+uint32_t vo_hash_block_key(int32_t x, int32_t y, int32_t z) {
+  uint32_t seed = 0U;
+  seed ^= (uint32_t)x * 73856093U + 0x9e3779b9U + (seed << 6U) + (seed >> 2U);
+  seed ^= (uint32_t)y * 19349663U + 0x9e3779b9U + (seed << 6U) + (seed >> 2U);
+  seed ^= (uint32_t)z * 83492791U + 0x9e3779b9U + (seed << 6U) + (seed >> 2U);
+  return seed;
+}
+
+/* cuda_block_allocator.cu:161-174 (21 bits per axis, bias 2^20) */
+int32_t vo_pack_block_key(int32_t x, int32_t y, int32_t z, uint64_t* packed) {
+  const int32_t bias = 1 << 20;
+  if (x < -bias || x > bias - 1 || y < -bias || y > bias - 1 || z < -bias || z > bias - 1) return 0;
+  *packed = (uint64_t)(x + bias) | ((uint64_t)(y + bias) << 21) | ((uint64_t)(z + bias) << 42);
+  return 1;
+}
+
+/* voxel_hash_tsdf.h:531-546 */
+static inline int floor_div(int value, int divisor) {
+  int q = value / divisor;
+  const int r = value % divisor;
+  if (r != 0 && ((r < 0) != (divisor < 0))) --q;
+  return q;
+}
+static inline int positive_mod(int value, int divisor) {
+  int r = value % divisor;
+  if (r < 0) r += divisor;
+  return r;
+}
+
+/* simple open-addressing key set/map used by the oracle (not the reference's structure) */
+typedef struct {
+  vo_key* keys;
+  int64_t* vals;
+  int64_t cap, count;
+} keymap;
+
+static uint64_t key_hash(vo_key k) {
+  uint64_t h = (uint64_t)(uint32_t)k.x * 0x9E3779B97F4A7C15ULL;
+  h ^= (uint64_t)(uint32_t)k.y * 0xC2B2AE3D27D4EB4FULL + (h << 6) + (h >> 2);
+  h ^= (uint64_t)(uint32_t)k.z * 0x165667B19E3779F9ULL + (h << 6) + (h >> 2);
+  h ^= h >> 29;
+  return h;
+}
+
+static void keymap_init(keymap* m, int64_t cap) {
+  int64_t c = 16;
+  while (c < cap * 2) c <<= 1;
+  m->cap = c;
+  m->count = 0;
+  m->keys = (vo_key*)malloc((size_t)c * sizeof(vo_key));
+  m->vals = (int64_t*)malloc((size_t)c * sizeof(int64_t));
+  for (int64_t i = 0; i < c; ++i) m->vals[i] = -1;
+}
+static void keymap_free(keymap* m) {
+  free(m->keys);
+  free(m->vals);
+  memset(m, 0, sizeof(*m));
+}
+static int64_t keymap_find(const keymap* m, vo_key k) {
+  if (m->cap == 0) return -1;
+  int64_t s = (int64_t)(key_hash(k) & (uint64_t)(m->cap - 1));
+  for (;;) {
+    if (m->vals[s] < 0) return -1;
+    if (m->keys[s].x == k.x && m->keys[s].y == k.y && m->keys[s].z == k.z) return m->vals[s];
+    s = (s + 1) & (m->cap - 1);
+  }
+}
+static void keymap_put(keymap* m, vo_key k, int64_t v);
+static void keymap_grow(keymap* m) {
+  keymap n;
+  keymap_init(&n, m->cap);
+  for (int64_t i = 0; i < m->cap; ++i)
+    if (m->vals[i] >= 0) keymap_put(&n, m->keys[i], m->vals[i]);
+  keymap_free(m);
+  *m = n;
+}
+/* inserts if absent; returns 1 if inserted */
+static int keymap_insert(keymap* m, vo_key k, int64_t v) {
+  if ((m->count + 1) * 2 > m->cap) keymap_grow(m);
+  int64_t s = (int64_t)(key_hash(k) & (uint64_t)(m->cap - 1));
+  for (;;) {
+    if (m->vals[s] < 0) {
+      m->keys[s] = k;
+      m->vals[s] = v;
+      ++m->count;
+      return 1;
+    }
+    if (m->keys[s].x == k.x && m->keys[s].y == k.y && m->keys[s].z == k.z) return 0;
+    s = (s + 1) & (m->cap - 1);
+  }
+}
+static void keymap_put(keymap* m, vo_key k, int64_t v) { (void)keymap_insert(m, k, v); }
+
+static int key_cmp(const void* a, const void* b) {
+  const vo_key* p = (const vo_key*)a;
+  const vo_key* q = (const vo_key*)b;
+  if (p->x != q->x) return p->x < q->x ? -1 : 1;
+  if (p->y != q->y) return p->y < q->y ? -1 : 1;
+  if (p->z != q->z) return p->z < q->z ? -1 : 1;
+  return 0;
+}
+
+/* GPU: cuda_block_allocator.cu:198-272 (floorf(p / (8 vs)), 27 neighbours, range-checked packing);
+ * CPU: voxel_hash_tsdf.h:595-671 (floorDiv(floor(p / vs), 8), 27 neighbours). */
+static int insert_neighbourhood(int fl, v3 p, float vs, keymap* set) {
+  int bx, by, bz;
+  if (fl == GPU) {
+    const float bws = vs * 8.0f;
+    bx = (int)floorf(p.x / bws);
+    by = (int)floorf(p.y / bws);
+    bz = (int)floorf(p.z / bws);
+  } else {
+    bx = floor_div((int)floorf(p.x / vs), BLOCK);
+    by = floor_div((int)floorf(p.y / vs), BLOCK);
+    bz = floor_div((int)floorf(p.z / vs), BLOCK);
+  }
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx) {
+        const vo_key k = {bx + dx, by + dy, bz + dz};
+        if (fl == GPU) {
+          uint64_t packed;
+          if (!vo_pack_block_key(k.x, k.y, k.z, &packed)) return 0;
+        }
+        keymap_insert(set, k, 0);
+      }
+  return 1;
+}
+
+static int collect_into(const vo_config* c, const float* depth, const vo_intrinsics* K, const vo_pose* T, float vs,
+                        float trunc, int32_t stride, keymap* set) {
+  const int fl = c->flavor;
+  const int s = stride > 1 ? stride : 1;
+  const v3 cam = mk(T->t[0], T->t[1], T->t[2]);
+  for (int v = 0; v < K->height; v += s) {
+    for (int u = 0; u < K->width; u += s) {
+      const float d = depth[(size_t)v * K->width + u];
+      if (d <= 0.0f) continue;
+      const v3 pc = back_project(u, v, d, K);
+      const v3 pw = pose_point(T, pc);
+      const v3 ray = vnormalize(fl, vsub(pw, cam));
+      const v3 front = vsub(pw, vmul(ray, trunc));
+      const v3 back = vadd(pw, vmul(ray, trunc));
+      if (!insert_neighbourhood(fl, pw, vs, set)) return 0;
+      if (!insert_neighbourhood(fl, front, vs, set)) return 0;
+      if (!insert_neighbourhood(fl, back, vs, set)) return 0;
+    }
+  }
+  return 1;
+}
+
+int64_t vo_collect_blocks(const vo_config* c, const float* depth, const vo_intrinsics* K, const vo_pose* T, float vs,
+                          float trunc, int32_t stride, vo_key* out, int64_t max_out) {
+  keymap set;
+  keymap_init(&set, 1024);
+  if (!collect_into(c, depth, K, T, vs, trunc, stride, &set)) {
+    keymap_free(&set);
+    return -1;
+  }
+  if (set.count > max_out) {
+    const int64_t n = set.count;
+    keymap_free(&set);
+    return n > 0 ? -2 : 0;
+  }
+  int64_t n = 0;
+  for (int64_t i = 0; i < set.cap; ++i)
+    if (set.vals[i] >= 0) out[n++] = set.keys[i];
+  qsort(out, (size_t)n, sizeof(vo_key), key_cmp);
+  keymap_free(&set);
+  return n;
+}
+
+/* ------------------------------------------------------------------ volume */
+struct vo_volume {
+  vo_config cfg;
+  float vs, trunc;
+  keymap map;
+  vo_key* keys;
+  vo_voxel* voxels;
+  int64_t count, cap;
+};
+
+vo_volume* vo_volume_new(const vo_config* c, float vs, float trunc) {
+  vo_volume* v = (vo_volume*)calloc(1, sizeof(vo_volume));
+  v->cfg = *c;
+  v->vs = vs;
+  v->trunc = trunc;
+  keymap_init(&v->map, 1024);
+  return v;
+}
+
+void vo_volume_free(vo_volume* v) {
+  if (!v) return;
+  keymap_free(&v->map);
+  free(v->keys);
+  free(v->voxels);
+  free(v);
+}
+
+void vo_free(void* p) { free(p); }
+
+static int64_t volume_ensure(vo_volume* v, vo_key k) {
+  const int64_t f = keymap_find(&v->map, k);
+  if (f >= 0) return f;
+  if (v->count == v->cap) {
+    const int64_t nc = v->cap ? v->cap * 2 : 64;
+    v->keys = (vo_key*)realloc(v->keys, (size_t)nc * sizeof(vo_key));
+    v->voxels = (vo_voxel*)realloc(v->voxels, (size_t)nc * BLOCK_VOLUME * sizeof(vo_voxel));
+    v->cap = nc;
+  }
+  const int64_t idx = v->count++;
+  v->keys[idx] = k;
+  memset(&v->voxels[idx * BLOCK_VOLUME], 0, BLOCK_VOLUME * sizeof(vo_voxel));
+  keymap_insert(&v->map, k, idx);
+  return idx;
+}
+
+int64_t vo_volume_block_count(const vo_volume* v) { return v->count; }
+
+int64_t vo_volume_find_block(const vo_volume* v, int32_t x, int32_t y, int32_t z) {
+  const vo_key k = {x, y, z};
+  return keymap_find(&v->map, k);
+}
+
+void vo_volume_get_block(const vo_volume* v, int64_t i, vo_key* key, vo_voxel* voxels) {
+  if (key) *key = v->keys[i];
+  if (voxels) memcpy(voxels, &v->voxels[i * BLOCK_VOLUME], BLOCK_VOLUME * sizeof(vo_voxel));
+}
+
+void vo_volume_set_block(vo_volume* v, vo_key key, const vo_voxel* voxels) {
+  const int64_t idx = volume_ensure(v, key);
+  memcpy(&v->voxels[idx * BLOCK_VOLUME], voxels, BLOCK_VOLUME * sizeof(vo_voxel));
+}
+
+/* voxel_hash_tsdf.h:113-123, cuda_tsdf_integrator.cu:905-930 */
+int64_t vo_volume_observed_voxels(const vo_volume* v) {
+  int64_t n = 0;
+  for (int64_t i = 0; i < v->count * BLOCK_VOLUME; ++i) {
+    const vo_voxel* vx = &v->voxels[i];
+    int obs = 0;
+    for (int d = 0; d < DIRS && !obs; ++d)
+      for (int l = 0; l < LAYERS; ++l)
+        if (vx->layers[d][l].weight > 0.0f) {
+          obs = 1;
+          break;
+        }
+    n += obs;
+  }
+  return n;
+}
+
+typedef struct {
+  vo_volume* vol;
+  const int64_t* idx;
+  const float* depth;
+  const vo_intrinsics* K;
+  const vo_pose* T_wc;
+  vo_pose T_cw;
+} integ_ctx;
+
+/* one block: cuda_tsdf_integrator.cu:834-903 (one thread per voxel), voxel_hash_tsdf.h:985-1060 */
+static void integrate_block(void* p, int64_t i) {
+  integ_ctx* g = (integ_ctx*)p;
+  vo_volume* vol = g->vol;
+  const vo_config* c = &vol->cfg;
+  const int fl = c->flavor;
+  const int64_t bi = g->idx[i];
+  const vo_key key = vol->keys[bi];
+  vo_voxel* vox = &vol->voxels[bi * BLOCK_VOLUME];
+  const float vs = vol->vs, trunc = vol->trunc;
+  for (int lz = 0; lz < BLOCK; ++lz)
+    for (int ly = 0; ly < BLOCK; ++ly)
+      for (int lx = 0; lx < BLOCK; ++lx) {
+        const v3 pw = mk(((float)(key.x * BLOCK + lx) + 0.5f) * vs, ((float)(key.y * BLOCK + ly) + 0.5f) * vs,
+                         ((float)(key.z * BLOCK + lz) + 0.5f) * vs);
+        const v3 pc = pose_point(&g->T_cw, pw);
+        if (pc.z <= 0.0f) continue;
+        float u = 0.0f, v = 0.0f;
+        if (!project_point(pc, g->K, &u, &v)) continue;
+        float d = 0.0f;
+        if (!sample_bilinear(c, g->depth, g->K, u, v, &d)) continue;
+        const float sd = d - pc.z;
+        if (sd <= -trunc) continue;
+        const v3 view = vnormalize(fl, pc);
+        float view_w = 1.0f;
+        v3 nc = vmul(view, -1.0f);
+        if (surface_normal(c, g->depth, g->K, u, v, &nc)) view_w = fabsf(vdot(nc, view));
+        const float obs = vo_observation_weight(c, d, sd, trunc, view_w);
+        if (obs <= 0.0f) continue;
+        const v3 spc = back_project_cont(u, v, d, g->K);
+        const v3 spw = pose_point(g->T_wc, spc);
+        const v3 nw = vnormalize(fl, pose_vector(g->T_wc, nc));
+        const int dir = dominant_direction(nw);
+        if (dir < 0 || dir >= DIRS) continue;
+        const float sc = coordinate_along(fl, spw, dir);
+        integrate_sample(c, vs, &vox[lx + BLOCK * (ly + BLOCK * lz)], dir, sc, spw, nw, obs);
+      }
+}
+
+void vo_volume_integrate_blocks(vo_volume* vol, const vo_key* keys, int64_t n, const float* depth,
+                                const vo_intrinsics* K, const vo_pose* T_wc) {
+  int64_t* idx = (int64_t*)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  for (int64_t i = 0; i < n; ++i) idx[i] = volume_ensure(vol, keys[i]);
+  integ_ctx g;
+  g.vol = vol;
+  g.idx = idx;
+  g.depth = depth;
+  g.K = K;
+  g.T_wc = T_wc;
+  pose_inverse(T_wc, &g.T_cw);
+  parallel_for(vol->cfg.threads, n, integrate_block, &g);
+  free(idx);
+}
+
+/* GPU: cuda_tsdf_integrator.cu:946-1010 (filter -> allocate on the filtered depth -> cache -> integrate);
+ * CPU: reconstruction_backend.cpp:259-267 + voxel_hash_tsdf.h:70-73, 133-139. */
+int64_t vo_volume_integrate_frame(vo_volume* vol, const float* depth, const vo_intrinsics* K, const vo_pose* T_wc,
+                                  int32_t stride) {
+  const size_t n = (size_t)K->width * (size_t)K->height;
+  if (n == 0) return 0;
+  float* filtered = (float*)malloc(n * sizeof(float));
+  vo_filter_depth(&vol->cfg, depth, K, filtered);
+  keymap set;
+  keymap_init(&set, 1024);
+  if (!collect_into(&vol->cfg, filtered, K, T_wc, vol->vs, vol->trunc, stride, &set)) {
+    keymap_free(&set);
+    free(filtered);
+    return -1;
+  }
+  vo_key* keys = (vo_key*)malloc((size_t)(set.count > 0 ? set.count : 1) * sizeof(vo_key));
+  int64_t m = 0;
+  for (int64_t i = 0; i < set.cap; ++i)
+    if (set.vals[i] >= 0) keys[m++] = set.keys[i];
+  keymap_free(&set);
+  qsort(keys, (size_t)m, sizeof(vo_key), key_cmp);
+  if (m > 0) vo_volume_integrate_blocks(vol, keys, m, filtered, K, T_wc);
+  free(keys);
+  free(filtered);
+  return m;
+}
+
+/* --------------------------------------------------------- marching cubes */
+/* The marching-cubes tables (three.js, MIT; reference marching_cubes_tables.h) shared with the
+ * product: vh_mc_tables.h, generated by oracle/gen_mc_tables.py. */
+#include "vh_mc_tables.h"
+
+static const int kCorner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                  {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+static const int kEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                 {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+/* cuda_mesh_extractor.cu:188-211, voxel_hash_tsdf.h:941-950 */
+static const vo_voxel* find_voxel(const vo_volume* v, int vx, int vy, int vz) {
+  const vo_key k = {floor_div(vx, BLOCK), floor_div(vy, BLOCK), floor_div(vz, BLOCK)};
+  const int64_t bi = keymap_find(&v->map, k);
+  if (bi < 0) return NULL;
+  const int li = positive_mod(vx, BLOCK) + BLOCK * (positive_mod(vy, BLOCK) + BLOCK * positive_mod(vz, BLOCK));
+  return &v->voxels[bi * BLOCK_VOLUME + li];
+}
+
+/* cuda_mesh_extractor.cu:259-262, voxel_hash_tsdf.h:336-339 */
+static inline float plane_sd(int fl, const vo_layer* L, v3 p) {
+  const v3 n = unpack_normal(fl, 1, L->packed_normal);
+  return n.x * p.x + n.y * p.y + n.z * p.z - L->plane_offset;
+}
+
+/* cuda_mesh_extractor.cu:305-356, voxel_hash_tsdf.h:423-477 */
+static int complete_cube(float values[8], int valid[8]) {
+  int cnt = 0;
+  float sum = 0.0f;
+  for (int c = 0; c < 8; ++c) {
+    if (!valid[c]) continue;
+    ++cnt;
+    sum += values[c];
+  }
+  if (cnt == 8) return 1;
+  if (cnt < 6) return 0;
+  const float global = cnt > 0 ? (sum / (float)cnt) : 0.0f;
+  for (int c = 0; c < 8; ++c) {
+    if (valid[c]) continue;
+    float ns = 0.0f;
+    int nc = 0;
+    for (int e = 0; e < 12; ++e) {
+      const int c0 = kEdge[e][0], c1 = kEdge[e][1];
+      int nb = -1;
+      if (c0 == c) {
+        nb = c1;
+      } else if (c1 == c) {
+        nb = c0;
+      }
+      if (nb < 0 || !valid[nb]) continue;
+      ns += values[nb];
+      ++nc;
+    }
+    values[c] = nc > 0 ? (ns / (float)nc) : global;
+    valid[c] = 1;
+  }
+  return 1;
+}
+
+/* marching_cubes.h:34-46, cuda_mesh_extractor.cu:358-374 */
+static inline v3 interp_vertex(v3 p0, v3 p1, float v0, float v1, float iso) {
+  const float delta = v1 - v0;
+  if (fabsf(delta) < 1e-6f) return p0;
+  const float t = clamp_f((iso - v0) / delta, 0.0f, 1.0f);
+  return mk(p0.x + (p1.x - p0.x) * t, p0.y + (p1.y - p0.y) * t, p0.z + (p1.z - p0.z) * t);
+}
+
+typedef struct {
+  vo_triangle* t;
+  int64_t n, cap;
+} tri_buf;
+
+static void tri_push(tri_buf* b, v3 a, v3 c, v3 d) {
+  if (b->n == b->cap) {
+    b->cap = b->cap ? b->cap * 2 : 64;
+    b->t = (vo_triangle*)realloc(b->t, (size_t)b->cap * sizeof(vo_triangle));
+  }
+  vo_triangle* t = &b->t[b->n++];
+  t->v[0] = a.x;
+  t->v[1] = a.y;
+  t->v[2] = a.z;
+  t->v[3] = c.x;
+  t->v[4] = c.y;
+  t->v[5] = c.z;
+  t->v[6] = d.x;
+  t->v[7] = d.y;
+  t->v[8] = d.z;
+}
+
+/* marching_cubes.h:48-94, cuda_mesh_extractor.cu:376-437 */
+static void polygonise(const v3 pos[8], const float val[8], float iso, tri_buf* out) {
+  int ci = 0;
+  for (int c = 0; c < 8; ++c)
+    if (val[c] < iso) ci |= (1 << c);
+  const int em = vh_mc_edge_table[ci];
+  if (em == 0) return;
+  v3 ev[12];
+  memset(ev, 0, sizeof(ev));
+  for (int e = 0; e < 12; ++e) {
+    if ((em & (1 << e)) == 0) continue;
+    const int c0 = kEdge[e][0], c1 = kEdge[e][1];
+    ev[e] = interp_vertex(pos[c0], pos[c1], val[c0], val[c1], iso);
+  }
+  for (int i = 0; i < 16; i += 3) {
+    const int e0 = vh_mc_tri_table[ci][i];
+    if (e0 < 0) break;
+    tri_push(out, ev[e0], ev[vh_mc_tri_table[ci][i + 1]], ev[vh_mc_tri_table[ci][i + 2]]);
+  }
+}
+
+typedef struct {
+  const vo_volume* vol;
+  float iso;
+  int dir;
+  tri_buf* bufs;
+} mesh_ctx;
+
+/* GPU: cuda_mesh_extractor.cu:439-551 (+ kernels :553-632); CPU: voxel_hash_tsdf.h:842-939 */
+static void mesh_block(void* p, int64_t bi) {
+  mesh_ctx* m = (mesh_ctx*)p;
+  const vo_volume* vol = m->vol;
+  const vo_config* c = &vol->cfg;
+  const int fl = c->flavor, d = m->dir;
+  const float vs = vol->vs;
+  const float tol = fmax_f(1e-6f, vs * c->layer_extract_scale);
+  const vo_key key = vol->keys[bi];
+  tri_buf* out = &m->bufs[bi];
+  out->n = 0;
+  for (int lz = 0; lz < BLOCK; ++lz)
+    for (int ly = 0; ly < BLOCK; ++ly)
+      for (int lx = 0; lx < BLOCK; ++lx) {
+        const int bx = key.x * BLOCK + lx, by = key.y * BLOCK + ly, bz = key.z * BLOCK + lz;
+        v3 cc;
+        if (fl == GPU) {
+          cc = mk(((float)bx + 1.0f) * vs, ((float)by + 1.0f) * vs, ((float)bz + 1.0f) * vs);
+        } else {
+          cc = mk(((float)bx + 0.5f) * vs + 0.5f * vs, ((float)by + 0.5f) * vs + 0.5f * vs,
+                  ((float)bz + 0.5f) * vs + 0.5f * vs);
+        }
+        const vo_voxel* corners[8];
+        v3 pos[8];
+        float cand[24];
+        int nc = 0;
+        for (int k = 0; k < 8; ++k) {
+          const int vx = bx + kCorner[k][0], vy = by + kCorner[k][1], vz = bz + kCorner[k][2];
+          pos[k] = mk(((float)vx + 0.5f) * vs, ((float)vy + 0.5f) * vs, ((float)vz + 0.5f) * vs);
+          corners[k] = find_voxel(vol, vx, vy, vz);
+          if (!corners[k]) continue;
+          for (int l = 0; l < LAYERS; ++l) {
+            const vo_layer* L = &corners[k]->layers[d][l];
+            if (!(L->weight > 0.0f)) continue;
+            if (nc < 24) cand[nc++] = plane_sd(fl, L, cc);
+          }
+        }
+        if (nc <= 0) continue;
+        /* insertion sort (GPU, :264-274); std::sort (CPU) yields the same order */
+        for (int i = 1; i < nc; ++i) {
+          const float x = cand[i];
+          int j = i - 1;
+          while (j >= 0 && cand[j] > x) {
+            cand[j + 1] = cand[j];
+            --j;
+          }
+          cand[j + 1] = x;
+        }
+        float centers[24];
+        int sizes[24];
+        int ncl = 0;
+        for (int i = 0; i < nc; ++i) {
+          const float key_i = cand[i];
+          if (ncl == 0 || fabsf(key_i - centers[ncl - 1]) > tol) {
+            centers[ncl] = key_i;
+            sizes[ncl] = 1;
+            ++ncl;
+            continue;
+          }
+          const int last = ncl - 1;
+          const int cnt = sizes[last];
+          centers[last] = (centers[last] * (float)cnt + key_i) / (float)(cnt + 1);
+          sizes[last] = cnt + 1;
+        }
+        for (int ci = 0; ci < ncl; ++ci) {
+          const float sk = centers[ci];
+          float values[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          int valid[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          for (int k = 0; k < 8; ++k) {
+            if (!corners[k]) continue;
+            int best = -1;
+            float best_delta = fl == GPU ? 1e30f : FLT_MAX;
+            for (int l = 0; l < LAYERS; ++l) {
+              const vo_layer* L = &corners[k]->layers[d][l];
+              if (!(L->weight > 0.0f)) continue;
+              const float delta = fabsf(plane_sd(fl, L, cc) - sk);
+              if (delta <= tol && delta < best_delta) {
+                best_delta = delta;
+                best = l;
+              }
+            }
+            if (best < 0) continue;
+            values[k] = plane_sd(fl, &corners[k]->layers[d][best], pos[k]);
+            valid[k] = 1;
+          }
+          if (!complete_cube(values, valid)) continue;
+          polygonise(pos, values, m->iso, out);
+        }
+      }
+}
+
+int64_t vo_volume_extract_mesh(const vo_volume* vol, float iso, vo_triangle** out) {
+  const int64_t nb = vol->count;
+  tri_buf* bufs = (tri_buf*)calloc((size_t)(nb > 0 ? nb : 1), sizeof(tri_buf));
+  tri_buf all = {NULL, 0, 0};
+  for (int d = 0; d < DIRS; ++d) {
+    mesh_ctx m = {vol, iso, d, bufs};
+    parallel_for(vol->cfg.threads, nb, mesh_block, &m);
+    for (int64_t b = 0; b < nb; ++b) {
+      for (int64_t i = 0; i < bufs[b].n; ++i) {
+        if (all.n == all.cap) {
+          all.cap = all.cap ? all.cap * 2 : 256;
+          all.t = (vo_triangle*)realloc(all.t, (size_t)all.cap * sizeof(vo_triangle));
+        }
+        all.t[all.n++] = bufs[b].t[i];
+      }
+    }
+  }
+  for (int64_t b = 0; b < nb; ++b) free(bufs[b].t);
+  free(bufs);
+  *out = all.t;
+  return all.n;
+}

@@ -1,0 +1,304 @@
+"""Seeded analytic scenes and a numpy depth ray-caster for the depth-fusion path.
+
+The reference renders its demo depth on the CPU by ray casting a sphere and a box
+(src/main.cpp:189-335: ray-sphere, ray-AABB, depth = camera-space z, then noise and dropouts).
+This module generates the workloads the fusion path is measured on with the same recipe:
+
+* ``orbit_scene`` -- ground plane z=0, a sphere r=0.5 m and an axis-aligned box 0.4x0.3x0.6 m
+  with seeded centres in a 1 m cube; the camera orbits at radius 1.5 m, height 0.8 m, looking
+  at the origin; 320x240, fx=fy=277, cx=160, cy=120.
+* ``room_scene`` -- the inside of a 4x5x3 m box room holding seeded spheres (r 0.1-0.6 m),
+  boxes (0.1-1 m sides) and vertical cylinders; a hand-held random walk (1 cm/frame
+  translation, 1 degree/frame yaw/pitch jitter); 640x480, fx=fy=525, cx=319.5, cy=239.5.
+
+Noise model for both: depth += N(0, (0.0012 z^2)^2) and 1 % of pixels dropped to 0.
+
+Camera convention (src/main.cpp:177-187): x right, y down, z forward; ``Pose`` maps camera to
+world (R row-major, t = camera centre).  World is z-up here.
+
+Primitive records are float32 rows of ``PRIM_FIELDS`` values so the same scene can be handed
+to the CUDA renderer (voxelhashmt_gb300/csrc/render.cu) unchanged:
+    [type, a0, a1, a2, b0, b1, b2, r, h, 0]
+    type 0 plane      n=(a0,a1,a2), offset r  (points p with n.p = r)
+    type 1 sphere     centre a, radius r
+    type 2 box        min corner a, max corner b
+    type 3 cylinder   base centre a, radius r, height h (axis +z)
+    type 4 room       min corner a, max corner b, seen from the inside
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PRIM_FIELDS = 10
+PLANE, SPHERE, BOX, CYLINDER, ROOM = 0, 1, 2, 3, 4
+
+
+@dataclass
+class Intrinsics:
+    """math_types.h:200-207."""
+    width: int
+    height: int
+    fx: float
+    fy: float
+    cx: float
+    cy: float
+
+    def k4(self):
+        return np.array([self.fx, self.fy, self.cx, self.cy], dtype=np.float32)
+
+
+@dataclass
+class Pose:
+    """Camera-to-world rigid transform, math_types.h:180-198 (R row-major 3x3, t)."""
+    R: np.ndarray = field(default_factory=lambda: np.eye(3, dtype=np.float32))
+    t: np.ndarray = field(default_factory=lambda: np.zeros(3, dtype=np.float32))
+
+    def as12(self):
+        return np.concatenate([np.asarray(self.R, np.float32).reshape(9),
+                               np.asarray(self.t, np.float32).reshape(3)]).astype(np.float32)
+
+
+@dataclass
+class Scene:
+    prims: np.ndarray                 # (P, PRIM_FIELDS) float32
+    intrinsics: Intrinsics
+    poses: list                       # list[Pose]
+    seed: int
+    noise_sigma_z2: float = 0.0012    # sigma = k * z^2
+    dropout: float = 0.01
+    voxel_size: float = 0.01
+    truncation: float = 0.04
+    hash_buckets: int = 1 << 16
+    name: str = ""
+    max_depth: float = 4.0            # returns outside (0.1, max_depth) are dropped (src/main.cpp:328)
+
+
+def look_at(eye, target, up=(0.0, 0.0, 1.0)) -> Pose:
+    """Camera x right, y down, z forward (the convention of src/main.cpp:177-187, with a z-up world)."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f /= np.linalg.norm(f)
+    r = np.cross(f, np.asarray(up, np.float64))
+    r /= np.linalg.norm(r)
+    d = np.cross(f, r)
+    R = np.stack([r, d, f], axis=1)
+    return Pose(R.astype(np.float32), eye.astype(np.float32))
+
+
+def _prim(kind, a=(0, 0, 0), b=(0, 0, 0), r=0.0, h=0.0):
+    return [float(kind), *map(float, a), *map(float, b), float(r), float(h), 0.0]
+
+
+def orbit_scene(seed=0, frames=64, width=320, height=240, fx=277.0, fy=277.0, cx=160.0, cy=120.0,
+                radius=1.5, cam_height=0.8) -> Scene:
+    rng = np.random.default_rng(seed)
+    sphere_c = rng.uniform([-0.5, -0.5, 0.0], [0.5, 0.5, 1.0])
+    box_c = rng.uniform([-0.5, -0.5, 0.0], [0.5, 0.5, 1.0])
+    half = np.array([0.2, 0.15, 0.3])
+    prims = [
+        _prim(PLANE, (0, 0, 1), r=0.0),
+        _prim(SPHERE, sphere_c, r=0.5),
+        _prim(BOX, box_c - half, box_c + half),
+    ]
+    K = Intrinsics(width, height, fx, fy, cx, cy)
+    poses = []
+    for i in range(frames):
+        a = 2.0 * math.pi * i / max(1, frames)
+        eye = (radius * math.cos(a), radius * math.sin(a), cam_height)
+        poses.append(look_at(eye, (0.0, 0.0, 0.0)))
+    return Scene(np.asarray(prims, np.float32), K, poses, seed, name="orbit",
+                 voxel_size=0.01, truncation=0.04, hash_buckets=1 << 16, max_depth=4.0)
+
+
+def room_scene(seed=0, frames=1000, width=640, height=480, fx=525.0, fy=525.0, cx=319.5, cy=239.5,
+               n_prims=40, room=(4.0, 5.0, 3.0)) -> Scene:
+    rng = np.random.default_rng(seed)
+    lo = np.zeros(3)
+    hi = np.asarray(room, np.float64)
+    start = np.array([hi[0] / 2, hi[1] / 2, 1.5])
+    prims = [_prim(ROOM, lo, hi)]
+    placed = 0
+    while placed < n_prims:
+        kind = rng.integers(0, 3)
+        c = rng.uniform(lo + 0.2, hi - 0.2)
+        if kind == 0:
+            r = rng.uniform(0.1, 0.6)
+            if np.linalg.norm(c - start) < r + 0.9:
+                continue
+            prims.append(_prim(SPHERE, c, r=r))
+        elif kind == 1:
+            s = rng.uniform(0.1, 1.0, size=3)
+            if np.linalg.norm(c - start) < 0.9 + np.linalg.norm(s) / 2:
+                continue
+            prims.append(_prim(BOX, c - s / 2, c + s / 2))
+        else:
+            r = rng.uniform(0.08, 0.4)
+            h = rng.uniform(0.3, 2.0)
+            base = np.array([c[0], c[1], 0.0])
+            if np.linalg.norm((c - start)[:2]) < r + 0.9:
+                continue
+            prims.append(_prim(CYLINDER, base, r=r, h=min(h, hi[2])))
+        placed += 1
+    K = Intrinsics(width, height, fx, fy, cx, cy)
+    poses = []
+    pos = start.copy()
+    yaw = rng.uniform(0, 2 * math.pi)
+    pitch = 0.0
+    step = 0.01
+    jitter = math.radians(1.0)
+    for _ in range(frames):
+        fwd = np.array([math.cos(pitch) * math.cos(yaw), math.cos(pitch) * math.sin(yaw), math.sin(pitch)])
+        poses.append(look_at(pos, pos + fwd))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        pos = np.clip(pos + step * d, start - 0.5, start + 0.5)
+        yaw += rng.uniform(-jitter, jitter)
+        pitch = float(np.clip(pitch + rng.uniform(-jitter, jitter), -0.5, 0.5))
+    return Scene(np.asarray(prims, np.float32), K, poses, seed, name="room",
+                 voxel_size=0.005, truncation=0.02, hash_buckets=1 << 20, max_depth=8.0)
+
+
+def _hash_u32(x):
+    """lowbias32 integer hash (public domain, C. Wellons); uint32 in, uint32 out."""
+    x = np.asarray(x, np.uint32)
+    x = x ^ (x >> np.uint32(16))
+    x = (x * np.uint32(0x7FEB352D)).astype(np.uint32)
+    x = x ^ (x >> np.uint32(15))
+    x = (x * np.uint32(0x846CA68B)).astype(np.uint32)
+    x = x ^ (x >> np.uint32(16))
+    return x
+
+
+def _uniforms(seed, frame, n, stream):
+    idx = np.arange(n, dtype=np.uint32)
+    key = np.uint32((seed * 0x9E3779B1 + frame * 0x85EBCA77 + stream * 0xC2B2AE3D) & 0xFFFFFFFF)
+    h = _hash_u32(idx ^ _hash_u32(np.full(n, key, np.uint32)))
+    return (h.astype(np.float64) + 0.5) / 4294967296.0
+
+
+def _intersect(prims, o, d):
+    """Nearest positive hit distance along unit rays d (N,3) from origin o (3,)."""
+    n = d.shape[0]
+    best = np.full(n, np.inf)
+    eps = 1e-4
+    for p in prims:
+        kind = int(p[0])
+        a = p[1:4].astype(np.float64)
+        b = p[4:7].astype(np.float64)
+        r = float(p[7])
+        h = float(p[8])
+        if kind == PLANE:
+            denom = d @ a
+            with np.errstate(divide="ignore", invalid="ignore"):
+                t = (r - o @ a) / denom
+            t[~np.isfinite(t) | (t <= eps)] = np.inf
+        elif kind == SPHERE:
+            oc = o - a
+            bb = d @ oc
+            c = oc @ oc - r * r
+            disc = bb * bb - c
+            sq = np.sqrt(np.maximum(disc, 0.0))
+            t0 = -bb - sq
+            t1 = -bb + sq
+            t = np.where(t0 > eps, t0, t1)
+            t[(disc < 0) | (t <= eps)] = np.inf
+        elif kind in (BOX, ROOM):
+            with np.errstate(divide="ignore", invalid="ignore"):
+                inv = 1.0 / d
+                ta = (a - o) * inv
+                tb = (b - o) * inv
+            tmin = np.nanmax(np.minimum(ta, tb), axis=1)
+            tmax = np.nanmin(np.maximum(ta, tb), axis=1)
+            if kind == BOX:
+                t = np.where(tmin > eps, tmin, tmax)
+                t[(tmax < tmin) | (tmax <= eps)] = np.inf
+            else:
+                t = tmax.copy()
+                t[t <= eps] = np.inf
+        elif kind == CYLINDER:
+            ox, oy = o[0] - a[0], o[1] - a[1]
+            dx, dy = d[:, 0], d[:, 1]
+            qa = dx * dx + dy * dy
+            qb = ox * dx + oy * dy
+            qc = ox * ox + oy * oy - r * r
+            disc = qb * qb - qa * qc
+            with np.errstate(divide="ignore", invalid="ignore"):
+                sq = np.sqrt(np.maximum(disc, 0.0))
+                t0 = (-qb - sq) / qa
+                t1 = (-qb + sq) / qa
+            t = np.full(n, np.inf)
+            for tc in (t1, t0):
+                z = o[2] + tc * d[:, 2]
+                ok = (disc >= 0) & (tc > eps) & (z >= a[2]) & (z <= a[2] + h) & (qa > 1e-12)
+                t = np.where(ok, tc, t)
+            # caps
+            for zc in (a[2], a[2] + h):
+                with np.errstate(divide="ignore", invalid="ignore"):
+                    tc = (zc - o[2]) / d[:, 2]
+                px = ox + tc * dx
+                py = oy + tc * dy
+                ok = np.isfinite(tc) & (tc > eps) & (px * px + py * py <= r * r)
+                t = np.where(ok & (tc < t), tc, t)
+        else:
+            raise ValueError(kind)
+        best = np.minimum(best, t)
+    return best
+
+
+def render_depth(scene: Scene, frame: int, noise=True) -> np.ndarray:
+    """Ray-cast depth (camera z, metres, float32 HxW, 0 = no return) for one frame."""
+    K = scene.intrinsics
+    P = scene.poses[frame]
+    u, v = np.meshgrid(np.arange(K.width, dtype=np.float64), np.arange(K.height, dtype=np.float64))
+    dc = np.stack([(u - K.cx) / K.fx, (v - K.cy) / K.fy, np.ones_like(u)], axis=-1).reshape(-1, 3)
+    dc /= np.linalg.norm(dc, axis=1, keepdims=True)
+    R = np.asarray(P.R, np.float64)
+    dw = dc @ R.T
+    t = _intersect(scene.prims, np.asarray(P.t, np.float64), dw)
+    z = t * dc[:, 2]
+    z[~np.isfinite(z)] = 0.0
+    if noise:
+        n = z.shape[0]
+        u1 = _uniforms(scene.seed, frame, n, 0)
+        u2 = _uniforms(scene.seed, frame, n, 1)
+        g = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+        z = z + g * scene.noise_sigma_z2 * z * z
+        drop = _uniforms(scene.seed, frame, n, 2) < scene.dropout
+        z[drop] = 0.0
+    z[(z < 0.1) | (z > scene.max_depth)] = 0.0
+    return z.reshape(K.height, K.width).astype(np.float32)
+
+
+def scene_sdf(prims: np.ndarray, pts: np.ndarray) -> np.ndarray:
+    """Unsigned distance from points (N,3) to the union of the scene's analytic surfaces."""
+    pts = np.asarray(pts, np.float64)
+    best = np.full(pts.shape[0], np.inf)
+    for p in prims:
+        kind = int(p[0])
+        a = p[1:4].astype(np.float64)
+        b = p[4:7].astype(np.float64)
+        r = float(p[7])
+        h = float(p[8])
+        if kind == PLANE:
+            dist = np.abs(pts @ a - r)
+        elif kind == SPHERE:
+            dist = np.abs(np.linalg.norm(pts - a, axis=1) - r)
+        elif kind in (BOX, ROOM):
+            c = (a + b) / 2
+            e = (b - a) / 2
+            q = np.abs(pts - c) - e
+            outside = np.linalg.norm(np.maximum(q, 0.0), axis=1)
+            inside = np.minimum(np.max(q, axis=1), 0.0)
+            dist = np.abs(outside + inside)
+        elif kind == CYLINDER:
+            rr = np.linalg.norm(pts[:, :2] - a[:2], axis=1) - r
+            zz = np.abs(pts[:, 2] - (a[2] + h / 2)) - h / 2
+            q = np.stack([rr, zz], axis=1)
+            dist = np.abs(np.linalg.norm(np.maximum(q, 0.0), axis=1) + np.minimum(np.max(q, axis=1), 0.0))
+        else:
+            raise ValueError(kind)
+        best = np.minimum(best, dist)
+    return best
