@@ -1,0 +1,161 @@
+/*
+ * voxelhash_gb300.h -- C ABI of the GB300-native voxelhashmt depth-fusion path.
+ *
+ * One opaque handle (vh_volume) owns one voxel-hashed volume in device memory: a persistent spatial hash
+ * of 8^3-voxel blocks and a pool of directional multi-layer voxels (6 signed dominant-axis bins x 3 layers
+ * of {weight, surface_coord, plane_offset, packed octahedral normal}, 288 bytes per voxel).  The entry
+ * points replace the reference's CUDA interfaces (paths relative to the reference project):
+ *
+ *   vh_integrate            integrateDepthFrameCuda            src/cuda_tsdf_integrator.h:16-19
+ *   vh_allocate             allocateActiveBlocksCuda           src/cuda_block_allocator.h:17-22
+ *   vh_visible_block_keys   the active block list integrateDepthFrameCuda builds (src/cuda_tsdf_integrator.cu:985-994)
+ *   vh_extract_mesh/_copy   extractMeshCuda                    src/cuda_mesh_extractor.h:9
+ *   vh_query_device         queryCudaBackendStatus             src/cuda_tsdf_integrator.h:9-14
+ *   vh_block_count          gpuVolumeCacheBlockCount           src/cuda_tsdf_integrator.h:22
+ *   vh_observed_voxel_count gpuVolumeCacheObservedVoxelCount   src/cuda_tsdf_integrator.h:23
+ *   vh_export_blocks        gpuVolumeCacheBlockKeys / gpuVolumeCacheFlatBlocks  src/cuda_tsdf_integrator.h:24-25
+ *   vh_filter_depth         estimateDepthNormalsKernel + bilateralFilterDepthKernel (src/cuda_tsdf_integrator.cu:629-725)
+ *
+ * Conventions (include/tsdfmc/math_types.h:180-244): depth is row-major float32 metres, index v*width+u,
+ * <= 0 means no measurement; vh_pose is camera->world with R row-major; pinhole intrinsics without
+ * distortion; camera x right, y down, z forward.  Block key = floor(world / (8 * voxel_size)).
+ *
+ * Execution model: calls that take a `stream` (a cudaStream_t, NULL = legacy default stream) only
+ * enqueue device work and return; errors detected on the device (hash full, pool full, key range)
+ * accumulate in the volume and are returned -- and cleared -- by vh_synchronize().  Calls that return
+ * host-visible results (counts, keys, meshes) synchronise the stream first.  A volume is not
+ * thread-safe; use one stream per volume at a time.  Results of the plain FP32 form are bit-identical
+ * to a host evaluation of the reference CUDA algorithm (see oracle/).
+ */
+#ifndef VOXELHASH_GB300_H
+#define VOXELHASH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VH_ABI_VERSION 1
+
+typedef enum vh_status {
+  VH_OK = 0,
+  VH_ERR_INVALID_ARGUMENT = 1,
+  VH_ERR_CUDA = 2,              /* a CUDA runtime call failed (reference: std::runtime_error, src/cuda_support.h:11-19) */
+  VH_ERR_NO_DEVICE = 3,         /* no usable CUDA device (reference: TsdfIntegrationBackend(kGpu) throws) */
+  VH_ERR_OUT_OF_MEMORY = 4,
+  VH_ERR_KEY_RANGE = 5,         /* a block coordinate left the 21-bit packed range (reference: CudaActiveBlockAllocationFallback) */
+  VH_ERR_HASH_FULL = 6,         /* no free hash slot (reference: CudaActiveBlockAllocationFallback) */
+  VH_ERR_POOL_FULL = 7,         /* more blocks than vh_params.max_blocks */
+  VH_ERR_BUFFER_TOO_SMALL = 8   /* caller's output buffer is smaller than the result; *count holds the size */
+} vh_status;
+
+typedef struct vh_volume vh_volume;
+
+/* include/tsdfmc/math_types.h:200-207 */
+typedef struct vh_intrinsics {
+  int32_t width, height;
+  float fx, fy, cx, cy;
+} vh_intrinsics;
+
+/* include/tsdfmc/math_types.h:180-198: camera -> world, R row-major */
+typedef struct vh_pose {
+  float R[9];
+  float t[3];
+} vh_pose;
+
+/* VoxelHashTSDF(voxel_size, truncation_distance), include/tsdfmc/voxel_hash_tsdf.h:67-68, plus the device sizing */
+typedef struct vh_params {
+  float voxel_size;
+  float truncation_distance;
+  uint32_t hash_buckets; /* power of two; slots of the persistent block hash */
+  uint32_t max_blocks;   /* pool capacity in blocks, 147,456 bytes each; 0 = keys-only volume (vh_allocate only) */
+  int32_t device;        /* CUDA device ordinal */
+  int32_t reserved;
+} vh_params;
+
+/* Algorithm constants; defaults are the reference CUDA path's (src/cuda_tsdf_integrator.cu:18-35,
+ * src/cuda_mesh_extractor.cu:20).  The filter radius may not exceed 2. */
+typedef struct vh_algorithm {
+  float depth_discontinuity_base, depth_discontinuity_relative;
+  int32_t filter_radius;
+  float filter_sigma_spatial, filter_sigma_range, filter_sigma_angular, filter_min_cosine;
+  int32_t normal_radius;
+  float normal_sigma_spatial, normal_sigma_range, normal_sigma_angular;
+  float layer_merge_voxel_scale, layer_normal_cosine, layer_extract_voxel_scale;
+  float max_voxel_weight, depth_sigma, huber_delta, min_observation_weight, min_view_angle_weight;
+} vh_algorithm;
+
+/* per-frame statistics of the last integrated/allocated frame */
+typedef struct vh_frame_stats {
+  uint64_t visible_blocks;   /* unique blocks the frame touched (the reference's active block list) */
+  uint64_t new_blocks;       /* blocks the frame allocated */
+  uint64_t updated_voxels;   /* voxel layer updates the frame applied */
+  uint64_t total_blocks;     /* blocks in the volume */
+  uint64_t observed_voxels;  /* voxels with any layer weight > 0 */
+} vh_frame_stats;
+
+void vh_params_default(vh_params* params);
+void vh_algorithm_default(vh_algorithm* algorithm);
+const char* vh_status_string(vh_status status);
+
+/* queryCudaBackendStatus: VH_OK and a "N CUDA device(s) detected" message, or VH_ERR_NO_DEVICE */
+vh_status vh_query_device(char* message, size_t message_len);
+
+/* Allocates the hash, the zeroed block pool and the counters on params->device.  algorithm may be NULL. */
+vh_status vh_create(const vh_params* params, const vh_algorithm* algorithm, vh_volume** out);
+void vh_destroy(vh_volume* volume);
+/* Empties the volume (all blocks removed, pool re-zeroed); keeps the allocations. */
+vh_status vh_reset(vh_volume* volume, void* stream);
+/* Last error message of the volume (never NULL). */
+const char* vh_last_error(const vh_volume* volume);
+
+/* integrateDepthFrameCuda: bilateral filter -> block allocation on the filtered depth -> layer update.
+ * depth: width*height floats, in host memory (depth_on_device = 0) or device memory (1). */
+vh_status vh_integrate(vh_volume* volume, const float* depth, int32_t depth_on_device, const vh_intrinsics* K,
+                       const vh_pose* T_wc, int32_t allocation_stride, void* stream);
+
+/* allocateActiveBlocksCuda: allocation only, on the given (unfiltered) depth; adds the blocks to the volume
+ * and returns the frame's unique block keys (3 int32 each, unordered) in keys_out (host memory).  With
+ * keys_out == NULL only *count is returned.  Synchronises. */
+vh_status vh_allocate(vh_volume* volume, const float* depth, int32_t depth_on_device, const vh_intrinsics* K,
+                      const vh_pose* T_wc, int32_t allocation_stride, int32_t* keys_out, size_t max_keys,
+                      size_t* count, void* stream);
+
+/* Unique block keys (3 int32 each, unordered, host memory) the last vh_integrate / vh_allocate frame touched
+ * -- the reference's per-frame active block list.  *count receives the number of keys.  Synchronises. */
+vh_status vh_visible_block_keys(vh_volume* volume, int32_t* keys_out, size_t max_keys, size_t* count, void* stream);
+
+/* The depth bilateral filter alone (device buffers), with the volume's algorithm constants. */
+vh_status vh_filter_depth(vh_volume* volume, const float* depth_in, float* depth_out, const vh_intrinsics* K,
+                          void* stream);
+/* The filter's per-pixel normals (device buffers): normals 3*W*H floats, valid W*H bytes. */
+vh_status vh_depth_normals(vh_volume* volume, const float* depth_in, float* normals, uint8_t* valid,
+                           const vh_intrinsics* K, void* stream);
+
+/* Waits for the stream and returns (then clears) the device-side errors accumulated since the last call. */
+vh_status vh_synchronize(vh_volume* volume, void* stream);
+
+/* extractMeshCuda: directional multi-layer marching cubes over every block; the triangle soup stays in
+ * the volume's device buffer.  *triangle_count receives its size.  Synchronises. */
+vh_status vh_extract_mesh(vh_volume* volume, float iso_level, size_t* triangle_count, void* stream);
+/* Copies the last extracted soup, 9 floats per triangle (v0, v1, v2), to host or device memory. */
+vh_status vh_copy_mesh(vh_volume* volume, float* out, size_t max_triangles, int32_t out_on_device, void* stream);
+
+vh_status vh_block_count(vh_volume* volume, uint64_t* count);
+vh_status vh_observed_voxel_count(vh_volume* volume, uint64_t* count);
+/* Recounts observed voxels from the pool (the incremental counter's cross-check). */
+vh_status vh_recount_observed_voxels(vh_volume* volume, uint64_t* count, void* stream);
+vh_status vh_frame_stats_get(vh_volume* volume, vh_frame_stats* stats, void* stream);
+
+/* Blocks [first, first + count) in allocation order: keys (3 int32 each) and voxels in the reference's
+ * Voxel layout (include/tsdfmc/voxel_hash_tsdf.h:18-31: 512 voxels x 6 directions x 3 layers x 16 bytes
+ * per block), into host memory (out_on_device = 0) or device memory (1).  Either pointer may be NULL. */
+vh_status vh_export_blocks(vh_volume* volume, uint64_t first, uint64_t count, int32_t* keys, void* voxels,
+                           int32_t out_on_device, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VOXELHASH_GB300_H */

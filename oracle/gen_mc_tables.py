@@ -69,13 +69,18 @@ def main():
         "#define VH_MC_TABLES_H",
         "#include <stdint.h>",
         "",
-        "static const uint16_t vh_mc_edge_table[256] = {",
+        "/* storage class of the tables: plain static data by default, e.g. `static __constant__` in CUDA */",
+        "#ifndef VH_MC_TABLE_QUALIFIER",
+        "#define VH_MC_TABLE_QUALIFIER static",
+        "#endif",
+        "",
+        "VH_MC_TABLE_QUALIFIER const uint16_t vh_mc_edge_table[256] = {",
     ]
     for i in range(0, 256, 8):
         lines.append("    " + ", ".join("%4d" % v for v in edge[i:i + 8]) + ",")
     lines.append("};")
     lines.append("")
-    lines.append("static const int8_t vh_mc_tri_table[256][16] = {")
+    lines.append("VH_MC_TABLE_QUALIFIER const int8_t vh_mc_tri_table[256][16] = {")
     for row in tri:
         lines.append("    {" + ", ".join("%2d" % v for v in row) + "},")
     lines.append("};")

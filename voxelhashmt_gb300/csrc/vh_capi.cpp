@@ -1,0 +1,557 @@
+// vh_capi.cpp -- the C ABI of include/voxelhash_gb300.h: volume lifetime, buffers, launch sequences.
+//
+// Host code is compiled with -ffp-contract=off: the world->camera pose (Pose::inverse, math_types.h:192-197)
+// and the 1/(2 sigma^2) factors are float expressions whose rounding must match the reference's.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/voxelhash_gb300.h"
+#include "vh_common.cuh"
+#include "vh_kernels.h"
+
+struct vh_volume {
+  vh_params params{};
+  vh_algorithm algo{};
+  vh::Volume dev{};
+  vh::Counters* h_counters = nullptr;  // pinned mirror for read-back
+  float* d_depth_in = nullptr;
+  float* d_depth_filtered = nullptr;
+  size_t depth_capacity = 0;  // pixels
+  uint32_t* d_mc_counts = nullptr;
+  unsigned long long* d_mc_offsets = nullptr;
+  unsigned long long* d_scalar = nullptr;  // [0] mesh total, [1] recount
+  float* d_tris = nullptr;
+  size_t tri_capacity = 0;
+  size_t mesh_triangles = 0;
+  int* d_keys = nullptr;
+  float4* d_export = nullptr;
+  int* d_export_keys = nullptr;
+  size_t export_capacity = 0;  // blocks
+  std::string error;
+};
+
+namespace {
+
+constexpr size_t kBlockBytes = static_cast<size_t>(vh::kDirs) * vh::kBlockVoxels * vh::kLayers * sizeof(float4);
+constexpr size_t kExportChunk = 1024;  // blocks per export staging pass
+
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int device) {
+    if (cudaGetDevice(&prev_) != cudaSuccess) prev_ = -1;
+    if (prev_ != device) cudaSetDevice(device);
+  }
+  ~DeviceGuard() {
+    if (prev_ >= 0) cudaSetDevice(prev_);
+  }
+
+ private:
+  int prev_ = -1;
+};
+
+vh_status fail(vh_volume* v, vh_status s, const std::string& msg) {
+  if (v) v->error = msg;
+  return s;
+}
+
+vh_status cuda_fail(vh_volume* v, cudaError_t e, const char* what) {
+  const vh_status s = e == cudaErrorMemoryAllocation ? VH_ERR_OUT_OF_MEMORY : VH_ERR_CUDA;
+  return fail(v, s, std::string(what) + " failed: " + cudaGetErrorString(e));
+}
+
+#define VH_CUDA(v, call)                                        \
+  do {                                                          \
+    const cudaError_t vh_e_ = (call);                           \
+    if (vh_e_ != cudaSuccess) return cuda_fail((v), vh_e_, #call); \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+template <class T>
+cudaError_t dalloc(T** p, size_t count) {
+  return cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(count, 1) * sizeof(T));
+}
+
+template <class T>
+void dfree(T*& p) {
+  if (p) cudaFree(p);
+  p = nullptr;
+}
+
+bool valid_intrinsics(const vh_intrinsics* K) {
+  return K && K->width > 0 && K->height > 0 && K->fx != 0.0f && K->fy != 0.0f;
+}
+
+vh::Params make_params(const vh_volume* v, const vh_intrinsics* K, const vh_pose* T, int stride) {
+  vh::Params p{};
+  const vh_algorithm& a = v->algo;
+  p.width = K->width;
+  p.height = K->height;
+  p.fx = K->fx;
+  p.fy = K->fy;
+  p.cx = K->cx;
+  p.cy = K->cy;
+  if (T) {
+    for (int i = 0; i < 9; ++i) p.T_wc.r[i] = T->R[i];
+    for (int i = 0; i < 3; ++i) p.T_wc.t[i] = T->t[i];
+    // Pose::inverse: R' = R^T, t' = R' * (t * -1)
+    const float* R = T->R;
+    const float Rt[9] = {R[0], R[3], R[6], R[1], R[4], R[7], R[2], R[5], R[8]};
+    const float nt[3] = {T->t[0] * -1.0f, T->t[1] * -1.0f, T->t[2] * -1.0f};
+    for (int i = 0; i < 9; ++i) p.T_cw.r[i] = Rt[i];
+    for (int i = 0; i < 3; ++i) p.T_cw.t[i] = Rt[3 * i] * nt[0] + Rt[3 * i + 1] * nt[1] + Rt[3 * i + 2] * nt[2];
+  }
+  const float vs = v->params.voxel_size;
+  p.voxel_size = vs;
+  p.truncation = v->params.truncation_distance;
+  p.block_world_size = vs * 8.0f;
+  p.stride = std::max(1, stride);
+  p.sample_width = (K->width + p.stride - 1) / p.stride;
+  p.sample_height = (K->height + p.stride - 1) / p.stride;
+  p.disc_base = a.depth_discontinuity_base;
+  p.disc_rel = a.depth_discontinuity_relative;
+  p.filter_radius = a.filter_radius;
+  p.filter_k_spatial = 1.0f / (2.0f * a.filter_sigma_spatial * a.filter_sigma_spatial);
+  p.filter_k_range = 1.0f / (2.0f * a.filter_sigma_range * a.filter_sigma_range);
+  p.filter_k_angular = 1.0f / (2.0f * a.filter_sigma_angular * a.filter_sigma_angular);
+  p.filter_min_cos = a.filter_min_cosine;
+  p.normal_radius = a.normal_radius;
+  p.normal_k_spatial = 1.0f / (2.0f * a.normal_sigma_spatial * a.normal_sigma_spatial);
+  p.normal_k_range = 1.0f / (2.0f * a.normal_sigma_range * a.normal_sigma_range);
+  p.normal_k_angular = 1.0f / (2.0f * a.normal_sigma_angular * a.normal_sigma_angular);
+  p.merge_tol = std::max(1e-6f, vs * a.layer_merge_voxel_scale);
+  p.layer_normal_cos = a.layer_normal_cosine;
+  p.extract_tol = std::max(1e-6f, vs * a.layer_extract_voxel_scale);
+  p.max_weight = a.max_voxel_weight;
+  p.depth_sigma = a.depth_sigma;
+  p.huber_delta = a.huber_delta;
+  p.min_obs_weight = a.min_observation_weight;
+  p.min_view_weight = a.min_view_angle_weight;
+  p.iso = 0.0f;
+  return p;
+}
+
+vh_status ensure_depth(vh_volume* v, size_t pixels) {
+  if (pixels <= v->depth_capacity) return VH_OK;
+  dfree(v->d_depth_in);
+  dfree(v->d_depth_filtered);
+  v->depth_capacity = 0;
+  VH_CUDA(v, dalloc(&v->d_depth_in, pixels));
+  VH_CUDA(v, dalloc(&v->d_depth_filtered, pixels));
+  v->depth_capacity = pixels;
+  return VH_OK;
+}
+
+vh_status read_counters(vh_volume* v, cudaStream_t s) {
+  VH_CUDA(v, cudaMemcpyAsync(v->h_counters, v->dev.counters, sizeof(vh::Counters), cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  return VH_OK;
+}
+
+vh_status stage_depth(vh_volume* v, const float* depth, int on_device, const vh_intrinsics* K, cudaStream_t s,
+                      const float** src) {
+  const size_t pixels = static_cast<size_t>(K->width) * static_cast<size_t>(K->height);
+  const vh_status st = ensure_depth(v, pixels);
+  if (st != VH_OK) return st;
+  if (on_device) {
+    *src = depth;
+  } else {
+    VH_CUDA(v, cudaMemcpyAsync(v->d_depth_in, depth, pixels * sizeof(float), cudaMemcpyHostToDevice, s));
+    *src = v->d_depth_in;
+  }
+  return VH_OK;
+}
+
+uint64_t block_total(const vh_volume* v) {
+  return std::min<uint64_t>(v->h_counters->num_blocks, v->dev.max_blocks);
+}
+
+}  // namespace
+
+extern "C" {
+
+void vh_params_default(vh_params* p) {
+  if (!p) return;
+  p->voxel_size = 0.01f;
+  p->truncation_distance = 0.04f;
+  p->hash_buckets = 1u << 16;
+  p->max_blocks = 1u << 14;
+  p->device = 0;
+  p->reserved = 0;
+}
+
+void vh_algorithm_default(vh_algorithm* a) {
+  if (!a) return;
+  a->depth_discontinuity_base = 0.012f;     // cuda_tsdf_integrator.cu:27
+  a->depth_discontinuity_relative = 0.025f; // :28
+  a->filter_radius = 2;                     // :31
+  a->filter_sigma_spatial = 1.5f;           // :32
+  a->filter_sigma_range = 0.0012f;          // :33
+  a->filter_sigma_angular = 0.35f;          // :34
+  a->filter_min_cosine = 0.9f;              // :35
+  a->normal_radius = 1;                     // :23
+  a->normal_sigma_spatial = 1.0f;           // :24
+  a->normal_sigma_range = 0.0012f;          // :25
+  a->normal_sigma_angular = 0.35f;          // :26
+  a->layer_merge_voxel_scale = 0.25f;       // :29
+  a->layer_normal_cosine = 0.9f;            // :30
+  a->layer_extract_voxel_scale = 0.55f;     // cuda_mesh_extractor.cu:20
+  a->max_voxel_weight = 100.0f;             // cuda_tsdf_integrator.cu:18
+  a->depth_sigma = 1.5f;                    // :19
+  a->huber_delta = 0.35f;                   // :20
+  a->min_observation_weight = 0.05f;        // :21
+  a->min_view_angle_weight = 0.15f;         // :22
+}
+
+const char* vh_status_string(vh_status s) {
+  switch (s) {
+    case VH_OK: return "ok";
+    case VH_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case VH_ERR_CUDA: return "CUDA error";
+    case VH_ERR_NO_DEVICE: return "no CUDA device";
+    case VH_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case VH_ERR_KEY_RANGE: return "block coordinate outside the 21-bit packed key range";
+    case VH_ERR_HASH_FULL: return "block hash table full";
+    case VH_ERR_POOL_FULL: return "block pool full";
+    case VH_ERR_BUFFER_TOO_SMALL: return "output buffer too small";
+  }
+  return "unknown status";
+}
+
+vh_status vh_query_device(char* message, size_t len) {
+  int count = 0;
+  const cudaError_t e = cudaGetDeviceCount(&count);
+  char buf[256];
+  vh_status st = VH_OK;
+  if (e != cudaSuccess) {
+    std::snprintf(buf, sizeof(buf), "%s", cudaGetErrorString(e));
+    st = VH_ERR_NO_DEVICE;
+  } else if (count <= 0) {
+    std::snprintf(buf, sizeof(buf), "no CUDA device detected");
+    st = VH_ERR_NO_DEVICE;
+  } else {
+    std::snprintf(buf, sizeof(buf), "%d CUDA device(s) detected", count);
+  }
+  if (message && len) {
+    std::strncpy(message, buf, len - 1);
+    message[len - 1] = '\0';
+  }
+  return st;
+}
+
+vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume** out) {
+  if (!params || !out) return VH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const uint32_t buckets = params->hash_buckets;
+  if (!(params->voxel_size > 0.0f) || !(params->truncation_distance > 0.0f) || buckets < 2 ||
+      (buckets & (buckets - 1)) != 0) {
+    return VH_ERR_INVALID_ARGUMENT;
+  }
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || params->device < 0 || params->device >= count) {
+    return VH_ERR_NO_DEVICE;
+  }
+  vh_volume* v = new (std::nothrow) vh_volume();
+  if (!v) return VH_ERR_OUT_OF_MEMORY;
+  v->params = *params;
+  if (algo) {
+    v->algo = *algo;
+  } else {
+    vh_algorithm_default(&v->algo);
+  }
+  if (v->algo.filter_radius < 0 || v->algo.filter_radius > 2 || v->algo.normal_radius != 1) {
+    delete v;
+    return VH_ERR_INVALID_ARGUMENT;
+  }
+  DeviceGuard guard(params->device);
+  vh::Volume& V = v->dev;
+  V.capacity = buckets;
+  V.mask = buckets - 1;
+  V.max_blocks = params->max_blocks;
+  const size_t nb = params->max_blocks;
+  cudaError_t e = cudaSuccess;
+  auto step = [&](cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  };
+  step(dalloc(&V.slot_keys, buckets));
+  step(dalloc(&V.slot_block, buckets));
+  step(dalloc(&V.slot_stamp, buckets));
+  step(dalloc(&V.visible, buckets));
+  step(cudaMalloc(reinterpret_cast<void**>(&V.layers), std::max<size_t>(nb, 1) * kBlockBytes));
+  step(dalloc(&V.block_keys, nb));
+  step(dalloc(&V.obs_mask, nb * (vh::kBlockVoxels / 32)));
+  step(dalloc(&V.counters, 1));
+  step(cudaMallocHost(reinterpret_cast<void**>(&v->h_counters), sizeof(vh::Counters)));
+  step(dalloc(&v->d_scalar, 2));
+  if (e == cudaSuccess) {
+    step(cudaMemset(V.slot_keys, 0xFF, buckets * sizeof(unsigned long long)));
+    step(cudaMemset(V.slot_block, 0xFF, buckets * sizeof(uint32_t)));
+    step(cudaMemset(V.slot_stamp, 0, buckets * sizeof(uint32_t)));
+    step(cudaMemset(V.layers, 0, std::max<size_t>(nb, 1) * kBlockBytes));
+    step(cudaMemset(V.obs_mask, 0, nb * (vh::kBlockVoxels / 32) * sizeof(uint32_t)));
+    step(cudaMemset(V.counters, 0, sizeof(vh::Counters)));
+    step(cudaDeviceSynchronize());
+  }
+  if (e != cudaSuccess) {
+    const vh_status st = e == cudaErrorMemoryAllocation ? VH_ERR_OUT_OF_MEMORY : VH_ERR_CUDA;
+    cudaGetLastError();
+    vh_destroy(v);
+    return st;
+  }
+  std::memset(v->h_counters, 0, sizeof(vh::Counters));
+  *out = v;
+  return VH_OK;
+}
+
+void vh_destroy(vh_volume* v) {
+  if (!v) return;
+  DeviceGuard guard(v->params.device);
+  vh::Volume& V = v->dev;
+  dfree(V.slot_keys);
+  dfree(V.slot_block);
+  dfree(V.slot_stamp);
+  dfree(V.visible);
+  dfree(V.layers);
+  dfree(V.block_keys);
+  dfree(V.obs_mask);
+  dfree(V.counters);
+  if (v->h_counters) cudaFreeHost(v->h_counters);
+  dfree(v->d_depth_in);
+  dfree(v->d_depth_filtered);
+  dfree(v->d_mc_counts);
+  dfree(v->d_mc_offsets);
+  dfree(v->d_scalar);
+  dfree(v->d_tris);
+  dfree(v->d_keys);
+  dfree(v->d_export);
+  dfree(v->d_export_keys);
+  delete v;
+}
+
+const char* vh_last_error(const vh_volume* v) { return v ? v->error.c_str() : "null volume"; }
+
+vh_status vh_reset(vh_volume* v, void* stream) {
+  if (!v) return VH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  const vh_status st = read_counters(v, s);
+  if (st != VH_OK) return st;
+  vh::Volume& V = v->dev;
+  const size_t used = block_total(v);
+  VH_CUDA(v, cudaMemsetAsync(V.slot_keys, 0xFF, V.capacity * sizeof(unsigned long long), s));
+  VH_CUDA(v, cudaMemsetAsync(V.slot_block, 0xFF, V.capacity * sizeof(uint32_t), s));
+  VH_CUDA(v, cudaMemsetAsync(V.slot_stamp, 0, V.capacity * sizeof(uint32_t), s));
+  VH_CUDA(v, cudaMemsetAsync(V.layers, 0, used * kBlockBytes, s));
+  VH_CUDA(v, cudaMemsetAsync(V.obs_mask, 0, used * (vh::kBlockVoxels / 32) * sizeof(uint32_t), s));
+  VH_CUDA(v, cudaMemsetAsync(V.counters, 0, sizeof(vh::Counters), s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  v->mesh_triangles = 0;
+  return VH_OK;
+}
+
+vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, const vh_intrinsics* K,
+                       const vh_pose* T_wc, int32_t stride, void* stream) {
+  if (!v || !depth || !valid_intrinsics(K) || !T_wc) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_integrate: bad argument");
+  if (v->dev.max_blocks == 0) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_integrate: keys-only volume (max_blocks 0)");
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  const float* src = nullptr;
+  vh_status st = stage_depth(v, depth, on_device, K, s, &src);
+  if (st != VH_OK) return st;
+  const vh::Params p = make_params(v, K, T_wc, stride);
+  VH_CUDA(v, vh::launch_filter(src, v->d_depth_filtered, p, v->dev.counters, s));
+  VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
+  VH_CUDA(v, vh::launch_integrate(v->d_depth_filtered, v->dev, p, 0, s));
+  return VH_OK;
+}
+
+vh_status vh_allocate(vh_volume* v, const float* depth, int32_t on_device, const vh_intrinsics* K, const vh_pose* T_wc,
+                      int32_t stride, int32_t* keys_out, size_t max_keys, size_t* count, void* stream) {
+  if (!v || !depth || !valid_intrinsics(K) || !T_wc || !count) {
+    return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_allocate: bad argument");
+  }
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  const float* src = nullptr;
+  vh_status st = stage_depth(v, depth, on_device, K, s, &src);
+  if (st != VH_OK) return st;
+  const vh::Params p = make_params(v, K, T_wc, stride);
+  VH_CUDA(v, vh::launch_begin_frame(v->dev.counters, s));
+  VH_CUDA(v, vh::launch_alloc(src, v->dev, p, s));
+  st = vh_synchronize(v, stream);
+  if (st != VH_OK) return st;
+  return vh_visible_block_keys(v, keys_out, max_keys, count, stream);
+}
+
+vh_status vh_visible_block_keys(vh_volume* v, int32_t* keys_out, size_t max_keys, size_t* count, void* stream) {
+  if (!v || !count) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_visible_block_keys: bad argument");
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  const vh_status st = read_counters(v, s);
+  if (st != VH_OK) return st;
+  const size_t n = v->h_counters->visible_count;
+  *count = n;
+  if (!keys_out || n == 0) return VH_OK;
+  if (n > max_keys) return fail(v, VH_ERR_BUFFER_TOO_SMALL, "vh_visible_block_keys: keys_out too small");
+  dfree(v->d_keys);
+  VH_CUDA(v, dalloc(&v->d_keys, 3 * n));
+  VH_CUDA(v, vh::launch_visible_keys(v->dev, v->d_keys, s));
+  VH_CUDA(v, cudaMemcpyAsync(keys_out, v->d_keys, 3 * n * sizeof(int), cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  return VH_OK;
+}
+
+vh_status vh_filter_depth(vh_volume* v, const float* in, float* out, const vh_intrinsics* K, void* stream) {
+  if (!v || !in || !out || !valid_intrinsics(K)) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_filter_depth: bad argument");
+  DeviceGuard guard(v->params.device);
+  const vh::Params p = make_params(v, K, nullptr, 1);
+  VH_CUDA(v, vh::launch_filter(in, out, p, nullptr, as_stream(stream)));
+  return VH_OK;
+}
+
+vh_status vh_depth_normals(vh_volume* v, const float* in, float* normals, uint8_t* valid, const vh_intrinsics* K,
+                           void* stream) {
+  if (!v || !in || !normals || !valid || !valid_intrinsics(K)) {
+    return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_depth_normals: bad argument");
+  }
+  DeviceGuard guard(v->params.device);
+  const vh::Params p = make_params(v, K, nullptr, 1);
+  VH_CUDA(v, vh::launch_depth_normals(in, normals, valid, p, as_stream(stream)));
+  return VH_OK;
+}
+
+vh_status vh_synchronize(vh_volume* v, void* stream) {
+  if (!v) return VH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  vh_status st = read_counters(v, s);
+  if (st != VH_OK) return st;
+  const uint32_t err = v->h_counters->error;
+  if (err == 0U) return VH_OK;
+  VH_CUDA(v, cudaMemsetAsync(&v->dev.counters->error, 0, sizeof(uint32_t), s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  if (err & vh::kErrKeyRange) return fail(v, VH_ERR_KEY_RANGE, "block coordinate outside the 21-bit packed key range");
+  if (err & vh::kErrHashFull) return fail(v, VH_ERR_HASH_FULL, "block hash table full (raise hash_buckets)");
+  return fail(v, VH_ERR_POOL_FULL, "block pool full (raise max_blocks)");
+}
+
+vh_status vh_extract_mesh(vh_volume* v, float iso, size_t* triangle_count, void* stream) {
+  if (!v || !triangle_count) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_extract_mesh: bad argument");
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  if (!v->d_mc_counts) {
+    VH_CUDA(v, dalloc(&v->d_mc_counts, v->dev.max_blocks));
+    VH_CUDA(v, dalloc(&v->d_mc_offsets, v->dev.max_blocks));
+  }
+  vh_intrinsics K{1, 1, 1.0f, 1.0f, 0.0f, 0.0f};
+  vh::Params p = make_params(v, &K, nullptr, 1);
+  p.iso = iso;
+  VH_CUDA(v, vh::launch_mc_count(v->dev, p, v->d_mc_counts, s));
+  VH_CUDA(v, vh::launch_mc_scan(v->dev, v->d_mc_counts, v->d_mc_offsets, v->d_scalar, s));
+  unsigned long long total = 0;
+  VH_CUDA(v, cudaMemcpyAsync(&total, v->d_scalar, sizeof(total), cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  if (total > v->tri_capacity) {
+    dfree(v->d_tris);
+    v->tri_capacity = 0;
+    const size_t cap = static_cast<size_t>(total) + static_cast<size_t>(total) / 8 + 1024;
+    VH_CUDA(v, dalloc(&v->d_tris, cap * 9));
+    v->tri_capacity = cap;
+  }
+  if (total > 0) VH_CUDA(v, vh::launch_mc_emit(v->dev, p, v->d_mc_offsets, v->d_tris, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  v->mesh_triangles = static_cast<size_t>(total);
+  *triangle_count = v->mesh_triangles;
+  return VH_OK;
+}
+
+vh_status vh_copy_mesh(vh_volume* v, float* out, size_t max_triangles, int32_t on_device, void* stream) {
+  if (!v || (!out && v->mesh_triangles)) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_copy_mesh: bad argument");
+  if (max_triangles < v->mesh_triangles) return fail(v, VH_ERR_BUFFER_TOO_SMALL, "vh_copy_mesh: buffer too small");
+  if (v->mesh_triangles == 0) return VH_OK;
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  VH_CUDA(v, cudaMemcpyAsync(out, v->d_tris, v->mesh_triangles * 9 * sizeof(float),
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  return VH_OK;
+}
+
+vh_status vh_block_count(vh_volume* v, uint64_t* count) {
+  if (!v || !count) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_block_count: bad argument");
+  DeviceGuard guard(v->params.device);
+  const vh_status st = read_counters(v, nullptr);
+  if (st != VH_OK) return st;
+  *count = block_total(v);
+  return VH_OK;
+}
+
+vh_status vh_observed_voxel_count(vh_volume* v, uint64_t* count) {
+  if (!v || !count) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_observed_voxel_count: bad argument");
+  DeviceGuard guard(v->params.device);
+  const vh_status st = read_counters(v, nullptr);
+  if (st != VH_OK) return st;
+  *count = v->h_counters->observed_voxels;
+  return VH_OK;
+}
+
+vh_status vh_recount_observed_voxels(vh_volume* v, uint64_t* count, void* stream) {
+  if (!v || !count) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_recount_observed_voxels: bad argument");
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  VH_CUDA(v, vh::launch_recount(v->dev, v->d_scalar + 1, s));
+  unsigned long long n = 0;
+  VH_CUDA(v, cudaMemcpyAsync(&n, v->d_scalar + 1, sizeof(n), cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  *count = n;
+  return VH_OK;
+}
+
+vh_status vh_frame_stats_get(vh_volume* v, vh_frame_stats* stats, void* stream) {
+  if (!v || !stats) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_frame_stats_get: bad argument");
+  DeviceGuard guard(v->params.device);
+  const vh_status st = read_counters(v, as_stream(stream));
+  if (st != VH_OK) return st;
+  stats->visible_blocks = v->h_counters->visible_count;
+  stats->new_blocks = v->h_counters->new_blocks;
+  stats->updated_voxels = v->h_counters->integrated_voxels;
+  stats->total_blocks = block_total(v);
+  stats->observed_voxels = v->h_counters->observed_voxels;
+  return VH_OK;
+}
+
+vh_status vh_export_blocks(vh_volume* v, uint64_t first, uint64_t count, int32_t* keys, void* voxels,
+                           int32_t on_device, void* stream) {
+  if (!v) return VH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  vh_status st = read_counters(v, s);
+  if (st != VH_OK) return st;
+  if (first + count > block_total(v)) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_export_blocks: range beyond block count");
+  if (count == 0 || (!keys && !voxels)) return VH_OK;
+  if (!v->d_export) {
+    VH_CUDA(v, cudaMalloc(reinterpret_cast<void**>(&v->d_export), kExportChunk * kBlockBytes));
+    VH_CUDA(v, dalloc(&v->d_export_keys, 3 * kExportChunk));
+    v->export_capacity = kExportChunk;
+  }
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  for (uint64_t done = 0; done < count; done += kExportChunk) {
+    const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(kExportChunk, count - done));
+    VH_CUDA(v, vh::launch_export(v->dev, static_cast<uint32_t>(first + done), n, v->d_export_keys, v->d_export, s));
+    if (voxels) {
+      VH_CUDA(v, cudaMemcpyAsync(static_cast<char*>(voxels) + done * kBlockBytes, v->d_export, n * kBlockBytes, kind, s));
+    }
+    if (keys) {
+      VH_CUDA(v, cudaMemcpyAsync(keys + 3 * done, v->d_export_keys, 3 * n * sizeof(int32_t), kind, s));
+    }
+  }
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  return VH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,211 @@
+// vh_common.cuh -- device-side layout, parameters and exact-order math shared by the GB300 kernels.
+//
+// Every floating-point expression below is written in the operation order of the reference CUDA
+// sources (src/cuda_tsdf_integrator.cu, src/cuda_block_allocator.cu, src/cuda_mesh_extractor.cu) and
+// the library is compiled with -fmad=false, so each a*b+c rounds twice exactly as the source reads;
+// IEEE division and square root are the nvcc defaults (-prec-div=true -prec-sqrt=true).  The only
+// deliberate difference from the reference is vh_expf (see below), which makes the plain FP32 form
+// reproducible bit-for-bit on the host.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace vh {
+
+constexpr int kBlockSide = 8;
+constexpr int kBlockVoxels = 512;
+constexpr int kDirs = 6;
+constexpr int kLayers = 3;
+constexpr unsigned long long kEmptyKey = ~0ULL;  // cuda_block_allocator.cu:19
+constexpr uint32_t kInvalidBlock = 0xffffffffu;
+constexpr int kKeyBits = 21;                      // cuda_block_allocator.cu:20-22
+constexpr int kKeyBias = 1 << (kKeyBits - 1);
+constexpr unsigned long long kKeyMask = (1ULL << kKeyBits) - 1ULL;
+
+// sticky error bits in Counters::error
+constexpr uint32_t kErrKeyRange = 1u;  // block coordinate outside the 21-bit packed range
+constexpr uint32_t kErrHashFull = 2u;  // no free slot within `capacity` probes
+constexpr uint32_t kErrPoolFull = 4u;  // more blocks than the pool holds
+
+// Device-resident counters of one volume (one cache line; read back with one D2H copy).
+struct Counters {
+  uint32_t num_blocks;      // blocks ever allocated (pool high-water mark)
+  uint32_t visible_count;   // unique blocks touched by the current frame
+  uint32_t error;           // sticky kErr* bits
+  uint32_t frame;           // frame stamp of the current frame (starts at 1)
+  unsigned long long observed_voxels;  // voxels with any layer weight > 0
+  uint32_t new_blocks;      // blocks allocated by the current frame
+  uint32_t integrated_voxels;  // voxel updates applied by the current frame
+  uint32_t pad[8];
+};
+
+// Device view of one volume.  HBM layout:
+//   slot_keys   u64[capacity]           packed block keys (open addressing, linear probing)
+//   slot_block  u32[capacity]           pool index of the key in the slot
+//   slot_stamp  u32[capacity]           last frame that put the slot on the visible list
+//   layers      float4[max_blocks][6][512][3]   {weight, surface_coord, plane_offset, packed_normal bits}
+//                                       direction-major inside a block so that a warp of voxels with the
+//                                       same dominant direction reads/writes 32 x 48 contiguous bytes
+//   block_keys  int4[max_blocks]        {x, y, z, frame the block was allocated in}
+//   obs_mask    u32[max_blocks][16]     one bit per voxel: any layer observed
+//   visible     u32[capacity]           slots touched by the current frame (unordered)
+struct Volume {
+  unsigned long long* slot_keys;
+  uint32_t* slot_block;
+  uint32_t* slot_stamp;
+  float4* layers;
+  int4* block_keys;
+  uint32_t* obs_mask;
+  uint32_t* visible;
+  Counters* counters;
+  uint32_t capacity;
+  uint32_t mask;
+  uint32_t max_blocks;
+  uint32_t pad;
+};
+
+struct Mat34 {
+  float r[9];
+  float t[3];
+};
+
+// Per-call algorithm parameters (constants of cuda_tsdf_integrator.cu:16-35 and cuda_mesh_extractor.cu:14-23,
+// with the derived 1/(2 sigma^2) factors computed on the host in float exactly as the reference's constexprs).
+struct Params {
+  int width, height;
+  float fx, fy, cx, cy;
+  Mat34 T_wc;  // camera -> world
+  Mat34 T_cw;  // world -> camera, Pose::inverse() computed on the host (math_types.h:192-197)
+  float voxel_size;
+  float truncation;
+  float block_world_size;  // voxel_size * 8 (cuda_block_allocator.cu:342)
+  int stride;
+  int sample_width, sample_height;
+  float disc_base, disc_rel;
+  int filter_radius;
+  float filter_k_spatial, filter_k_range, filter_k_angular, filter_min_cos;
+  int normal_radius;
+  float normal_k_spatial, normal_k_range, normal_k_angular;
+  float merge_tol, layer_normal_cos, extract_tol;
+  float max_weight, depth_sigma, huber_delta, min_obs_weight, min_view_weight;
+  float iso;
+};
+
+struct f3 {
+  float x, y, z;
+};
+
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ f3 add3(f3 a, f3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ f3 mul3(f3 v, float s) { return mk3(v.x * s, v.y * s, v.z * s); }
+__device__ __forceinline__ float dot3(f3 a, f3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+  return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float norm3(f3 v) { return sqrtf(dot3(v, v)); }
+// cuda_tsdf_integrator.cu:201-209
+__device__ __forceinline__ f3 normalize3(f3 v) {
+  const float len = norm3(v);
+  if (len <= 1e-6f) return mk3(0.0f, 0.0f, 0.0f);
+  const float inv = 1.0f / len;
+  return mk3(v.x * inv, v.y * inv, v.z * inv);
+}
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(hi, fmaxf(lo, v)); }
+
+__device__ __forceinline__ f3 xform_point(const Mat34& P, f3 p) {
+  return mk3(P.r[0] * p.x + P.r[1] * p.y + P.r[2] * p.z + P.t[0], P.r[3] * p.x + P.r[4] * p.y + P.r[5] * p.z + P.t[1],
+             P.r[6] * p.x + P.r[7] * p.y + P.r[8] * p.z + P.t[2]);
+}
+__device__ __forceinline__ f3 xform_vector(const Mat34& P, f3 p) {
+  return mk3(P.r[0] * p.x + P.r[1] * p.y + P.r[2] * p.z, P.r[3] * p.x + P.r[4] * p.y + P.r[5] * p.z,
+             P.r[6] * p.x + P.r[7] * p.y + P.r[8] * p.z);
+}
+// cuda_tsdf_integrator.cu:570-579
+__device__ __forceinline__ f3 backproject(float u, float v, float d, const Params& p) {
+  return mk3((u - p.cx) * d / p.fx, (v - p.cy) * d / p.fy, d);
+}
+
+// Single-precision exp: Cody-Waite reduction x = k ln2 + r (ln2 split in an 11-trailing-zero high part and a
+// low part), e^r by the degree-7 Taylor polynomial in Horner form with fused multiply-adds (|r| <= ln2/2,
+// truncation error < 6e-9 relative), scaling by 2^k through the exponent field (two steps below 2^-126).
+// The host oracle evaluates the identical fmaf sequence, so results agree bit-for-bit.
+__device__ __forceinline__ float vh_expf(float x) {
+  if (!(x > -104.0f)) return 0.0f;
+  if (x > 0x1.62e42ep+6f) return __int_as_float(0x7f800000);
+  const float k = rintf(x * 0x1.715476p+0f);
+  float r = __fmaf_rn(k, -0x1.62e400p-1f, x);
+  r = __fmaf_rn(k, -0x1.7f7d1cp-20f, r);
+  float q = 0x1.a01a02p-13f;
+  q = __fmaf_rn(q, r, 0x1.6c16c2p-10f);
+  q = __fmaf_rn(q, r, 0x1.111112p-7f);
+  q = __fmaf_rn(q, r, 0x1.555556p-5f);
+  q = __fmaf_rn(q, r, 0x1.555556p-3f);
+  q = __fmaf_rn(q, r, 0x1.000000p-1f);
+  q = __fmaf_rn(q, r, 1.0f);
+  q = __fmaf_rn(q, r, 1.0f);
+  const int ki = static_cast<int>(k);
+  if (ki > 127) return (q * __int_as_float((127 + 127) << 23)) * 2.0f;
+  if (ki >= -126) return q * __int_as_float((ki + 127) << 23);
+  return (q * __int_as_float((ki + 127 + 64) << 23)) * 0x1p-64f;
+}
+
+// cuda_tsdf_integrator.cu:173-179
+__device__ __forceinline__ float gaussian(float sq, float k) { return vh_expf(-sq * k); }
+__device__ __forceinline__ float disc_threshold(const Params& p, float ref) {
+  return fmaxf(p.disc_base, p.disc_rel * fmaxf(ref, 0.0f));
+}
+// cuda_tsdf_integrator.cu:219-226
+__device__ __forceinline__ f3 orient_toward_camera(f3 n, f3 pc) {
+  if (norm3(n) <= 1e-6f || norm3(pc) <= 1e-6f) return n;
+  const f3 view = normalize3(pc);
+  return dot3(n, view) > 0.0f ? mul3(n, -1.0f) : n;
+}
+
+// cuda_block_allocator.cu:153-159
+__device__ __forceinline__ uint32_t hash_block_key(int x, int y, int z) {
+  uint32_t seed = 0U;
+  // unsigned multiply: the same bits as the reference's wrapping int product, without signed overflow
+  seed ^= static_cast<uint32_t>(x) * 73856093U + 0x9e3779b9U + (seed << 6U) + (seed >> 2U);
+  seed ^= static_cast<uint32_t>(y) * 19349663U + 0x9e3779b9U + (seed << 6U) + (seed >> 2U);
+  seed ^= static_cast<uint32_t>(z) * 83492791U + 0x9e3779b9U + (seed << 6U) + (seed >> 2U);
+  return seed;
+}
+// cuda_block_allocator.cu:161-174
+__device__ __forceinline__ bool pack_block_key(int x, int y, int z, unsigned long long& packed) {
+  if (x < -kKeyBias || x > kKeyBias - 1 || y < -kKeyBias || y > kKeyBias - 1 || z < -kKeyBias || z > kKeyBias - 1) {
+    return false;
+  }
+  packed = static_cast<unsigned long long>(x + kKeyBias) |
+           (static_cast<unsigned long long>(y + kKeyBias) << kKeyBits) |
+           (static_cast<unsigned long long>(z + kKeyBias) << (2 * kKeyBits));
+  return true;
+}
+__device__ __forceinline__ void unpack_block_key(unsigned long long k, int& x, int& y, int& z) {
+  x = static_cast<int>(k & kKeyMask) - kKeyBias;
+  y = static_cast<int>((k >> kKeyBits) & kKeyMask) - kKeyBias;
+  z = static_cast<int>((k >> (2 * kKeyBits)) & kKeyMask) - kKeyBias;
+}
+
+// Hash lookup (read-only): pool index of block (x,y,z) or kInvalidBlock.  Probes at most `capacity` slots.
+__device__ __forceinline__ uint32_t lookup_block(const Volume& V, int x, int y, int z) {
+  unsigned long long key;
+  if (!pack_block_key(x, y, z, key)) return kInvalidBlock;
+  uint32_t slot = hash_block_key(x, y, z) & V.mask;
+  for (uint32_t probe = 0; probe < V.capacity; ++probe) {
+    const unsigned long long cur = V.slot_keys[slot];
+    if (cur == key) return V.slot_block[slot];
+    if (cur == kEmptyKey) return kInvalidBlock;
+    slot = (slot + 1U) & V.mask;
+  }
+  return kInvalidBlock;
+}
+
+// float4 index of layer l of voxel li, direction d, block b
+__device__ __forceinline__ size_t layer_index(uint32_t b, int d, int li, int l) {
+  return ((static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + li) * kLayers + l;
+}
+
+}  // namespace vh

@@ -1,0 +1,470 @@
+// vh_integrate.cu -- directional multi-layer TSDF update of the visible blocks.
+//
+// Reference: integrateActiveBlocksKernel (src/cuda_tsdf_integrator.cu:834-903) with its helpers
+// (:319-568, :727-832).  One CTA per visible block (taken from a device work cursor, so the grid is a fixed
+// number of persistent CTAs and the launch needs no host read-back), 256 threads x 2 voxels.  Layer storage
+// is direction-major (vh_common.cuh), so a warp reads and writes the 3 layers of its voxels' bin as 16-byte
+// vector accesses over contiguous memory; a voxel's other 5 bins are never touched.  The observed-voxel
+// bitmask (one u32 per warp of voxels, so one writer per word) keeps the observed-voxel count incremental.
+//
+// The per-voxel bilateral normal (estimateSurfaceNormalCamera, :754-832) evaluates 9 base normals, each from
+// 4 bilinear depth samples, plus 10 more samples: 50 bilinear samples per voxel, all at (u + i, v + j) for
+// integer i, j in [-2, 2].  Whenever the shifted coordinates are exact -- (u-1)+1 == u, (u+1)-1 == u and the
+// same for v, which the kernel checks -- the reference evaluates every one of those samples at the same
+// float coordinates, so the 21 distinct samples are computed once and reused; the result is bit-identical.
+// Otherwise (u or v within 2 of a power of two, or below 1) the literal 50-sample sequence runs.
+#include "vh_common.cuh"
+#include "vh_kernels.h"
+
+namespace vh {
+namespace {
+
+constexpr int kThreads = 256;
+
+// sampleDepthNearest (cuda_tsdf_integrator.cu:479-489)
+__device__ __forceinline__ bool sample_nearest(const float* __restrict__ depth, const Params& p, float u, float v,
+                                               float& d) {
+  const int ui = static_cast<int>(floorf(u + 0.5f));
+  const int vi = static_cast<int>(floorf(v + 0.5f));
+  if (ui < 0 || ui >= p.width || vi < 0 || vi >= p.height) return false;
+  d = __ldg(&depth[static_cast<size_t>(vi) * p.width + ui]);
+  return d > 0.0f;
+}
+
+// sampleDepthBilinear (cuda_tsdf_integrator.cu:504-568)
+__device__ __forceinline__ bool sample_bilinear(const float* __restrict__ depth, const Params& p, float u, float v,
+                                                float& out) {
+  if (u < 0.0f || v < 0.0f || u > static_cast<float>(p.width - 1) || v > static_cast<float>(p.height - 1)) {
+    return false;
+  }
+  const int x0 = static_cast<int>(floorf(u));
+  const int y0 = static_cast<int>(floorf(v));
+  const int x1 = min(x0 + 1, p.width - 1);
+  const int y1 = min(y0 + 1, p.height - 1);
+  const float tx = u - static_cast<float>(x0);
+  const float ty = v - static_cast<float>(y0);
+  const float* r0 = depth + static_cast<size_t>(y0) * p.width;
+  const float* r1 = depth + static_cast<size_t>(y1) * p.width;
+  const float d00 = __ldg(r0 + x0), d10 = __ldg(r0 + x1), d01 = __ldg(r1 + x0), d11 = __ldg(r1 + x1);
+  if (d00 > 0.0f && d10 > 0.0f && d01 > 0.0f && d11 > 0.0f) {
+    // sampleDepthNearest always lands on one of the four taps here (u <= W-1 keeps floor(u+0.5) <= x0+1 and
+    // x1 == x0 only when u == W-1), and all four are valid: select it instead of reloading.
+    const int ui = static_cast<int>(floorf(u + 0.5f));
+    const int vi = static_cast<int>(floorf(v + 0.5f));
+    const float ref = (ui == x0) ? (vi == y0 ? d00 : d01) : (vi == y0 ? d10 : d11);
+    const float thr = disc_threshold(p, ref);
+    const float mn = fminf(fminf(d00, d10), fminf(d01, d11));
+    const float mx = fmaxf(fmaxf(d00, d10), fmaxf(d01, d11));
+    const float top = d00 + (d10 - d00) * tx;
+    const float bottom = d01 + (d11 - d01) * tx;
+    if (mx - mn <= thr) {
+      out = top + (bottom - top) * ty;
+      return true;
+    }
+    const float w00 = (1.0f - tx) * (1.0f - ty), w10 = tx * (1.0f - ty), w01 = (1.0f - tx) * ty, w11 = tx * ty;
+    float wds = 0.0f, ws = 0.0f;
+    if (!(fabsf(d00 - ref) > thr)) {
+      wds += w00 * d00;
+      ws += w00;
+    }
+    if (!(fabsf(d10 - ref) > thr)) {
+      wds += w10 * d10;
+      ws += w10;
+    }
+    if (!(fabsf(d01 - ref) > thr)) {
+      wds += w01 * d01;
+      ws += w01;
+    }
+    if (!(fabsf(d11 - ref) > thr)) {
+      wds += w11 * d11;
+      ws += w11;
+    }
+    if (ws > 1e-6f) {
+      out = wds / ws;
+      return true;
+    }
+  }
+  return sample_nearest(depth, p, u, v, out);
+}
+
+// estimateSurfaceNormalBaseCamera (cuda_tsdf_integrator.cu:727-752)
+__device__ bool base_normal_literal(const float* __restrict__ depth, const Params& p, float u, float v, f3& n) {
+  float dl, dr, du, dd;
+  if (!sample_bilinear(depth, p, u - 1.0f, v, dl) || !sample_bilinear(depth, p, u + 1.0f, v, dr) ||
+      !sample_bilinear(depth, p, u, v - 1.0f, du) || !sample_bilinear(depth, p, u, v + 1.0f, dd)) {
+    return false;
+  }
+  const f3 pl = backproject(u - 1.0f, v, dl, p);
+  const f3 pr = backproject(u + 1.0f, v, dr, p);
+  const f3 pu = backproject(u, v - 1.0f, du, p);
+  const f3 pd = backproject(u, v + 1.0f, dd, p);
+  n = normalize3(cross3(sub3(pd, pu), sub3(pr, pl)));
+  return norm3(n) > 1e-6f;
+}
+
+// estimateSurfaceNormalCamera (cuda_tsdf_integrator.cu:754-832), literal evaluation order
+__device__ __noinline__ bool surface_normal_literal(const float* __restrict__ depth, const Params& p, float u,
+                                                    float v, const float gs[3], f3& normal) {
+  f3 cn;
+  if (!base_normal_literal(depth, p, u, v, cn)) return false;
+  float cd;
+  if (!sample_bilinear(depth, p, u, v, cd)) return false;
+  const f3 cp = backproject(u, v, cd, p);
+  cn = orient_toward_camera(cn, cp);
+  f3 wsum = mk3(0.0f, 0.0f, 0.0f);
+  float ws = 0.0f;
+  for (int dv = -1; dv <= 1; ++dv) {
+    for (int du = -1; du <= 1; ++du) {
+      const float su = u + static_cast<float>(du);
+      const float sv = v + static_cast<float>(dv);
+      f3 sn;
+      if (!base_normal_literal(depth, p, su, sv, sn)) continue;
+      float sd;
+      if (!sample_bilinear(depth, p, su, sv, sd)) continue;
+      sn = orient_toward_camera(sn, backproject(su, sv, sd, p));
+      const float delta = sd - cd;
+      const float cosine = clampf(dot3(cn, sn), -1.0f, 1.0f);
+      const float ad = 1.0f - cosine;
+      const float w = gs[du * du + dv * dv] * gaussian(delta * delta, p.normal_k_range) *
+                      gaussian(ad * ad, p.normal_k_angular);
+      wsum.x += sn.x * w;
+      wsum.y += sn.y * w;
+      wsum.z += sn.z * w;
+      ws += w;
+    }
+  }
+  if (ws <= 1e-6f) {
+    normal = cn;
+    return true;
+  }
+  const float inv = 1.0f / ws;
+  f3 n = normalize3(mk3(wsum.x * inv, wsum.y * inv, wsum.z * inv));
+  n = orient_toward_camera(n, cp);
+  if (norm3(n) <= 1e-6f) n = cn;
+  normal = n;
+  return norm3(n) > 1e-6f;
+}
+
+// Same function through the 21 distinct samples (valid when the shifted coordinates are exact).
+__device__ __forceinline__ bool surface_normal(const float* __restrict__ depth, const Params& p, float u, float v,
+                                               const float gs[3], f3& normal) {
+  const float um1 = u - 1.0f, up1 = u + 1.0f, vm1 = v - 1.0f, vp1 = v + 1.0f;
+  if (!(um1 + 1.0f == u && up1 - 1.0f == u && vm1 + 1.0f == v && vp1 - 1.0f == v)) {
+    return surface_normal_literal(depth, p, u, v, gs, normal);
+  }
+  const float U[5] = {um1 - 1.0f, um1, u, up1, up1 + 1.0f};
+  const float V[5] = {vm1 - 1.0f, vm1, v, vp1, vp1 + 1.0f};
+  // backprojected sample points P[j][i] at (U[i], V[j]); the 4 corners are never used
+  f3 P[5][5];
+  uint32_t ok = 0U;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      if ((i == 0 || i == 4) && (j == 0 || j == 4)) continue;
+      float d;
+      if (sample_bilinear(depth, p, U[i], V[j], d)) {
+        ok |= 1U << (j * 5 + i);
+        P[j][i] = backproject(U[i], V[j], d, p);
+      } else {
+        P[j][i] = mk3(0.0f, 0.0f, 0.0f);
+      }
+    }
+  }
+  // base normals at (i, j) in [1, 3]^2
+  f3 N[3][3];
+  uint32_t nok = 0U;
+#pragma unroll
+  for (int j = 1; j <= 3; ++j) {
+#pragma unroll
+    for (int i = 1; i <= 3; ++i) {
+      const uint32_t need = (1U << (j * 5 + i - 1)) | (1U << (j * 5 + i + 1)) | (1U << ((j - 1) * 5 + i)) |
+                            (1U << ((j + 1) * 5 + i));
+      N[j - 1][i - 1] = mk3(0.0f, 0.0f, 0.0f);
+      if ((ok & need) == need) {
+        const f3 n = normalize3(cross3(sub3(P[j + 1][i], P[j - 1][i]), sub3(P[j][i + 1], P[j][i - 1])));
+        if (norm3(n) > 1e-6f) {
+          N[j - 1][i - 1] = n;
+          nok |= 1U << ((j - 1) * 3 + (i - 1));
+        }
+      }
+    }
+  }
+  if (!(nok & (1U << 4))) return false;
+  if (!(ok & (1U << 12))) return false;
+  const f3 cp = P[2][2];
+  const float cd = cp.z;
+  const f3 cn = orient_toward_camera(N[1][1], cp);
+  f3 wsum = mk3(0.0f, 0.0f, 0.0f);
+  float ws = 0.0f;
+#pragma unroll
+  for (int j = 1; j <= 3; ++j) {
+#pragma unroll
+    for (int i = 1; i <= 3; ++i) {
+      if (!(nok & (1U << ((j - 1) * 3 + (i - 1))))) continue;
+      if (!(ok & (1U << (j * 5 + i)))) continue;
+      const f3 sp = P[j][i];
+      const f3 sn = orient_toward_camera(N[j - 1][i - 1], sp);
+      const float delta = sp.z - cd;
+      const float cosine = clampf(dot3(cn, sn), -1.0f, 1.0f);
+      const float ad = 1.0f - cosine;
+      const int r2 = (i - 2) * (i - 2) + (j - 2) * (j - 2);
+      const float w = gs[r2] * gaussian(delta * delta, p.normal_k_range) * gaussian(ad * ad, p.normal_k_angular);
+      wsum.x += sn.x * w;
+      wsum.y += sn.y * w;
+      wsum.z += sn.z * w;
+      ws += w;
+    }
+  }
+  if (ws <= 1e-6f) {
+    normal = cn;
+    return true;
+  }
+  const float inv = 1.0f / ws;
+  f3 n = normalize3(mk3(wsum.x * inv, wsum.y * inv, wsum.z * inv));
+  n = orient_toward_camera(n, cp);
+  if (norm3(n) <= 1e-6f) n = cn;
+  normal = n;
+  return norm3(n) > 1e-6f;
+}
+
+// computeObservationWeightGpu (cuda_tsdf_integrator.cu:429-450)
+__device__ __forceinline__ float observation_weight(const Params& p, float depth, float sd, float view) {
+  if (depth <= 0.0f || p.truncation <= 1e-6f) return 0.0f;
+  const float dr = depth / p.depth_sigma;
+  const float dw = 1.0f / (1.0f + dr * dr);
+  const float nr = fabsf(sd) / p.truncation;
+  float rw = 1.0f;
+  if (nr > p.huber_delta) rw = p.huber_delta / nr;
+  const float bw = 1.0f - 0.5f * clampf(nr, 0.0f, 1.0f);
+  const float base = fmaxf(p.min_obs_weight, dw * rw * bw);
+  const float aw = clampf(view, p.min_view_weight, 1.0f);
+  return base * aw;
+}
+
+// dominantDirectionIndexGpu (:228-243)
+__device__ __forceinline__ int dominant_direction(f3 n) {
+  const float nx = fabsf(n.x), ny = fabsf(n.y), nz = fabsf(n.z);
+  if (nx <= 1e-6f && ny <= 1e-6f && nz <= 1e-6f) return -1;
+  if (nx >= ny && nx >= nz) return n.x >= 0.0f ? 0 : 1;
+  if (ny >= nx && ny >= nz) return n.y >= 0.0f ? 2 : 3;
+  return n.z >= 0.0f ? 4 : 5;
+}
+
+// coordinateAlongDirectionGpu (:296-313)
+__device__ __forceinline__ float coordinate_along(f3 p, int d) {
+  switch (d) {
+    case 0: return p.x;
+    case 1: return -p.x;
+    case 2: return p.y;
+    case 3: return -p.y;
+    case 4: return p.z;
+    default: return -p.z;
+  }
+}
+
+__device__ __forceinline__ float sign_not_zero(float v) { return v >= 0.0f ? 1.0f : -1.0f; }
+
+// packNormalOctahedralGpu (:253-278)
+__device__ __forceinline__ uint32_t pack_normal(f3 raw) {
+  const f3 n = normalize3(raw);
+  const float s = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
+  if (s <= 1e-6f) return 0U;
+  float px = n.x / s, py = n.y / s;
+  const float pz = n.z / s;
+  if (pz < 0.0f) {
+    const float fx = (1.0f - fabsf(py)) * sign_not_zero(px);
+    const float fy = (1.0f - fabsf(px)) * sign_not_zero(py);
+    px = fx;
+    py = fy;
+  }
+  const uint32_t qx = static_cast<uint32_t>(floorf(fminf(1.0f, fmaxf(0.0f, px * 0.5f + 0.5f)) * 65535.0f + 0.5f));
+  const uint32_t qy = static_cast<uint32_t>(floorf(fminf(1.0f, fmaxf(0.0f, py * 0.5f + 0.5f)) * 65535.0f + 0.5f));
+  return qx | (qy << 16U);
+}
+
+// unpackNormalOctahedralGpu (:258-294)
+__device__ __forceinline__ f3 unpack_normal(uint32_t packed) {
+  f3 n = mk3(static_cast<float>(packed & 0xffffU) / 65535.0f * 2.0f - 1.0f,
+             static_cast<float>((packed >> 16U) & 0xffffU) / 65535.0f * 2.0f - 1.0f, 0.0f);
+  n.z = 1.0f - fabsf(n.x) - fabsf(n.y);
+  if (n.z < 0.0f) {
+    const float fx = (1.0f - fabsf(n.y)) * sign_not_zero(n.x);
+    const float fy = (1.0f - fabsf(n.x)) * sign_not_zero(n.y);
+    n.x = fx;
+    n.y = fy;
+  }
+  return normalize3(n);
+}
+
+__device__ __forceinline__ bool layer_valid(const float4& l) { return l.x > 0.0f; }
+
+__device__ __forceinline__ void cswap(float4& a, float4& b, bool c) {
+  const float4 t = a;
+  a = c ? b : a;
+  b = c ? t : b;
+}
+
+// sortDirectionalLayersGpu (:319-336): bubble sort, observed layers first, ascending surface_coord
+__device__ __forceinline__ void sort_layers(float4& a, float4& b, float4& c) {
+  auto should = [](const float4& l, const float4& r) {
+    const bool lv = layer_valid(l), rv = layer_valid(r);
+    return (!lv && rv) || (lv && rv && l.y > r.y);
+  };
+  cswap(a, b, should(a, b));
+  cswap(b, c, should(b, c));
+  cswap(a, b, should(a, b));
+}
+
+// findLayerSlotForObservationGpu + integrateDirectionalSampleGpu (:338-427) on the 3 layers of one bin.
+// Returns true when a layer was updated.
+__device__ __forceinline__ bool integrate_sample(const Params& p, float4& L0, float4& L1, float4& L2, float sc,
+                                                 f3 sp, f3 nw, float obs) {
+  if (obs <= 0.0f) return false;
+  const f3 n = normalize3(nw);
+  if (norm3(n) <= 1e-6f) return false;
+  const float plane_offset = dot3(n, sp);
+  int empty = -1, best = -1;
+  float best_delta = 1e30f;
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    const float4& L = l == 0 ? L0 : (l == 1 ? L1 : L2);
+    if (!layer_valid(L)) {
+      if (empty < 0) empty = l;
+      continue;
+    }
+    const f3 ln = unpack_normal(__float_as_uint(L.w));
+    if (dot3(ln, n) < p.layer_normal_cos) continue;
+    const float delta = fabsf(L.y - sc);
+    if (delta < best_delta) {
+      best_delta = delta;
+      best = l;
+    }
+  }
+  const int li = (best >= 0 && best_delta <= p.merge_tol) ? best : empty;
+  if (li < 0) return false;
+  float4 L = li == 0 ? L0 : (li == 1 ? L1 : L2);
+  const float pw = L.x;
+  const float ew = fminf(obs, fmaxf(0.0f, p.max_weight - pw));
+  if (ew <= 0.0f) return false;
+  const float nwt = pw + ew;
+  f3 blended = n;
+  L.y = pw > 0.0f ? ((L.y * pw + sc * ew) / nwt) : sc;
+  L.z = pw > 0.0f ? ((L.z * pw + plane_offset * ew) / nwt) : plane_offset;
+  if (pw > 0.0f) {
+    const f3 pn = unpack_normal(__float_as_uint(L.w));
+    blended = normalize3(mul3(add3(mul3(pn, pw), mul3(n, ew)), 1.0f / nwt));
+    if (norm3(blended) <= 1e-6f) blended = n;
+  }
+  L.x = nwt;
+  L.w = __uint_as_float(pack_normal(blended));
+  if (li == 0) L0 = L;
+  if (li == 1) L1 = L;
+  if (li == 2) L2 = L;
+  sort_layers(L0, L1, L2);
+  return true;
+}
+
+// Everything integrateActiveBlocksKernel computes for one voxel before touching its layers (:849-899).
+// Returns the direction bin, or -1 when the voxel is not updated this frame.
+__device__ __forceinline__ int observe_voxel(const float* __restrict__ depth, const Params& p, const int4& bk,
+                                             int lx, int ly, int lz, const float gs[3], float& sc, f3& spw, f3& nw,
+                                             float& obs) {
+  const f3 pw = mk3((static_cast<float>(bk.x * kBlockSide + lx) + 0.5f) * p.voxel_size,
+                    (static_cast<float>(bk.y * kBlockSide + ly) + 0.5f) * p.voxel_size,
+                    (static_cast<float>(bk.z * kBlockSide + lz) + 0.5f) * p.voxel_size);
+  const f3 pc = xform_point(p.T_cw, pw);
+  if (pc.z <= 0.0f) return -1;
+  if (pc.z <= 1e-6f) return -1;
+  const float u = p.fx * pc.x / pc.z + p.cx;
+  const float v = p.fy * pc.y / pc.z + p.cy;
+  if (!(u >= 0.0f && u <= static_cast<float>(p.width - 1) && v >= 0.0f && v <= static_cast<float>(p.height - 1))) {
+    return -1;
+  }
+  float d;
+  if (!sample_bilinear(depth, p, u, v, d)) return -1;
+  const float sd = d - pc.z;
+  if (sd <= -p.truncation) return -1;
+  const f3 view = normalize3(pc);
+  float view_w = 1.0f;
+  f3 nc = mul3(view, -1.0f);
+  if (surface_normal(depth, p, u, v, gs, nc)) view_w = fabsf(dot3(nc, view));
+  obs = observation_weight(p, d, sd, view_w);
+  if (obs <= 0.0f) return -1;
+  spw = xform_point(p.T_wc, backproject(u, v, d, p));
+  nw = normalize3(xform_vector(p.T_wc, nc));
+  const int dir = dominant_direction(nw);
+  if (dir < 0 || dir >= kDirs) return -1;
+  sc = coordinate_along(spw, dir);
+  return dir;
+}
+
+__global__ void __launch_bounds__(kThreads, 2) integrate_kernel(const float* __restrict__ depth, const Volume V,
+                                                                const Params p) {
+  __shared__ uint32_t s_item;
+  const uint32_t nvis = V.counters->visible_count;
+  const int tid = threadIdx.x, lane = tid & 31;
+  // spatial factor of the normal bilateral for du^2+dv^2 in {0,1,2}: depends on (du,dv) only
+  const float gs[3] = {gaussian(0.0f, p.normal_k_spatial), gaussian(1.0f, p.normal_k_spatial),
+                       gaussian(2.0f, p.normal_k_spatial)};
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(&V.counters->pad[0], 1U);
+    __syncthreads();
+    const uint32_t item = s_item;
+    __syncthreads();
+    if (item >= nvis) break;
+    const uint32_t b = V.slot_block[V.visible[item]];
+    if (b == kInvalidBlock) continue;
+    const int4 bk = V.block_keys[b];
+#pragma unroll 1
+    for (int half = 0; half < 2; ++half) {
+      const int li = tid + kThreads * half;
+      float sc = 0.0f, obs = 0.0f;
+      f3 spw = mk3(0.0f, 0.0f, 0.0f), nw = spw;
+      const int dir = observe_voxel(depth, p, bk, li & 7, (li >> 3) & 7, li >> 6, gs, sc, spw, nw, obs);
+      bool updated = false;
+      if (dir >= 0) {
+        float4* base = V.layers + layer_index(b, dir, li, 0);
+        float4 L0 = base[0], L1 = base[1], L2 = base[2];
+        updated = integrate_sample(p, L0, L1, L2, sc, spw, nw, obs);
+        if (updated) {
+          base[0] = L0;
+          base[1] = L1;
+          base[2] = L2;
+        }
+      }
+      const uint32_t upd = __ballot_sync(0xffffffffU, updated);
+      if (lane == 0 && upd) {
+        const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
+        const uint32_t old = V.obs_mask[w];
+        const uint32_t now = old | upd;
+        if (now != old) {
+          V.obs_mask[w] = now;
+          atomicAdd(&V.counters->observed_voxels, static_cast<unsigned long long>(__popc(now & ~old)));
+        }
+        atomicAdd(&V.counters->integrated_voxels, static_cast<uint32_t>(__popc(upd)));
+      }
+    }
+  }
+}
+
+}  // namespace
+
+int integrate_grid_size() {
+  static int grid = 0;
+  if (grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrate_kernel, kThreads, 0);
+    grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+  }
+  return grid;
+}
+
+cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s) {
+  integrate_kernel<<<grid > 0 ? grid : integrate_grid_size(), kThreads, 0, s>>>(depth, V, p);
+  return cudaGetLastError();
+}
+
+}  // namespace vh

@@ -1,0 +1,39 @@
+// vh_kernels.h -- host-side launchers of the GB300 kernels (internal to the library).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "vh_common.cuh"
+
+namespace vh {
+
+// depth bilateral filter (normals + 5x5 joint bilateral in one kernel); begin_frame != nullptr also
+// starts a new frame on that volume's counters (frame stamp + 1, per-frame counters cleared).
+cudaError_t launch_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s);
+// per-pixel normals of the filter, for kernel-level parity checks: normals[3*W*H], valid[W*H]
+cudaError_t launch_depth_normals(const float* in, float* normals, unsigned char* valid, const Params& p,
+                                 cudaStream_t s);
+cudaError_t launch_begin_frame(Counters* c, cudaStream_t s);
+// allocation: 3 points x 27-neighbourhood per sampled pixel -> persistent hash + visible list
+cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, cudaStream_t s);
+// directional multi-layer update of every visible block; grid = persistent CTAs
+cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s);
+int integrate_grid_size();
+// marching cubes over all allocated blocks: pass 1 writes per-block triangle counts,
+// the scan turns them into offsets (+ total), pass 2 writes triangles (9 floats each)
+cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_mc_scan(const Volume& V, const uint32_t* counts, unsigned long long* offsets,
+                           unsigned long long* total, cudaStream_t s);
+cudaError_t launch_mc_emit(const Volume& V, const Params& p, const unsigned long long* offsets, float* tris,
+                           cudaStream_t s);
+int mc_grid_size();
+// full recount of observed voxels (any layer weight > 0) over the pool
+cudaError_t launch_recount(const Volume& V, unsigned long long* out, cudaStream_t s);
+// keys of the current frame's visible blocks (int3 each, unordered)
+cudaError_t launch_visible_keys(const Volume& V, int* keys, cudaStream_t s);
+// copy blocks [first, first+count) to the reference layout: keys int32[count][3],
+// voxels [count][512][6][3] x {f32 weight, f32 surface_coord, f32 plane_offset, u32 packed_normal}
+cudaError_t launch_export(const Volume& V, uint32_t first, uint32_t count, int* keys, float4* voxels,
+                          cudaStream_t s);
+
+}  // namespace vh

@@ -1,0 +1,377 @@
+// vh_mesh.cu -- directional multi-layer marching cubes, two passes with block-level prefix sums.
+//
+// Reference: extractMeshCuda (src/cuda_mesh_extractor.cu:636-720) rebuilds a host lookup table per call and
+// runs count + extract kernels once per direction (12 launches, 12 syncs, 6 readbacks); every cell copies
+// its 8 corner voxels whole (288 B each) through a device hash lookup, twice.  Here each CTA owns one block:
+// it resolves its 7 (+x, +y, +z) neighbour blocks once through the persistent hash, then for each of the 6
+// directions stages that direction's bin of the 9x9x9 voxel region (block + one-voxel halo) in shared
+// memory with the octahedral normals decoded once per layer, and every thread processes one cell from shared
+// memory.  Pass 1 writes the per-block triangle count, a scan turns counts into offsets, pass 2 recomputes
+// and writes each block's triangles at its offset: the output is deterministic (block, direction, cell,
+// cluster, table order) and needs no atomics.
+//
+// Per cell the arithmetic is the reference's collectSurfaceClusters / loadCubeForSurface /
+// completeCubeValuesWithFallbackGpu / emitCubeTriangles (:259-551) in the same operation order.
+#include "vh_common.cuh"
+#include "vh_kernels.h"
+
+#define VH_MC_TABLE_QUALIFIER static __constant__
+#include "vh_mc_tables.h"
+
+namespace vh {
+namespace {
+
+constexpr int kThreads = 512;  // one per cell
+constexpr int kSide = 9;
+constexpr int kStaged = kSide * kSide * kSide;
+constexpr int kMaxCand = 24;  // 8 corners x 3 layers (cuda_mesh_extractor.cu:18)
+
+__constant__ int c_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                   {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+__constant__ int c_edge_corners[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                          {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+
+struct Shared {
+  float4 plane[3][kStaged];  // {n.x, n.y, n.z, plane_offset} per layer
+  uint8_t valid[3][kStaged];
+  int8_t tri[256][16];
+  uint16_t edge[256];
+  uint32_t nbr[8];
+  uint32_t warp_sums[kThreads / 32];
+  uint32_t total;
+};
+
+// unpackNormalOctahedralGpu of the mesh extractor (:237-257): degenerate -> (0,0,1)
+__device__ __forceinline__ f3 unpack_normal_mesh(uint32_t packed) {
+  f3 n = mk3(static_cast<float>(packed & 0xffffU) / 65535.0f * 2.0f - 1.0f,
+             static_cast<float>((packed >> 16U) & 0xffffU) / 65535.0f * 2.0f - 1.0f, 0.0f);
+  n.z = 1.0f - fabsf(n.x) - fabsf(n.y);
+  if (n.z < 0.0f) {
+    const float fx = (1.0f - fabsf(n.y)) * (n.x >= 0.0f ? 1.0f : -1.0f);
+    const float fy = (1.0f - fabsf(n.x)) * (n.y >= 0.0f ? 1.0f : -1.0f);
+    n.x = fx;
+    n.y = fy;
+  }
+  const float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+  if (len <= 1e-6f) return mk3(0.0f, 0.0f, 1.0f);
+  const float inv = 1.0f / len;
+  return mk3(n.x * inv, n.y * inv, n.z * inv);
+}
+
+// planeSignedDistanceGpu (:259-262)
+__device__ __forceinline__ float plane_sd(const float4& pl, f3 p) {
+  return pl.x * p.x + pl.y * p.y + pl.z * p.z - pl.w;
+}
+
+__device__ __forceinline__ int staged_index(int x, int y, int z) { return (z * kSide + y) * kSide + x; }
+
+__device__ void stage_direction(Shared& S, const Volume& V, int d, int tid) {
+  for (int i = tid; i < kStaged * kLayers; i += kThreads) {
+    const int l = i % kLayers;
+    const int vi = i / kLayers;
+    const int sx = vi % kSide, sy = (vi / kSide) % kSide, sz = vi / (kSide * kSide);
+    const uint32_t nb = S.nbr[(sx >> 3) | ((sy >> 3) << 1) | ((sz >> 3) << 2)];
+    float4 pl = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    uint8_t ok = 0;
+    if (nb != kInvalidBlock) {
+      const int li = (sx & 7) + kBlockSide * ((sy & 7) + kBlockSide * (sz & 7));
+      const float4 L = V.layers[layer_index(nb, d, li, l)];
+      if (L.x > 0.0f) {
+        const f3 n = unpack_normal_mesh(__float_as_uint(L.w));
+        pl = make_float4(n.x, n.y, n.z, L.z);
+        ok = 1;
+      }
+    }
+    S.plane[l][vi] = pl;
+    S.valid[l][vi] = ok;
+  }
+}
+
+// interpolateVertexGpu (:358-374)
+__device__ __forceinline__ f3 interp(f3 p0, f3 p1, float v0, float v1, float iso) {
+  const float delta = v1 - v0;
+  if (fabsf(delta) < 1e-6f) return p0;
+  const float t = fminf(1.0f, fmaxf(0.0f, (iso - v0) / delta));
+  return mk3(p0.x + (p1.x - p0.x) * t, p0.y + (p1.y - p0.y) * t, p0.z + (p1.z - p0.z) * t);
+}
+
+// One cell of one direction: returns its triangle count; with kEmit writes them to out (9 floats each).
+template <bool kEmit>
+__device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, int gz, int lx, int ly, int lz,
+                            float* __restrict__ out) {
+  const float vs = p.voxel_size;
+  const f3 cc = mk3((static_cast<float>(gx) + 1.0f) * vs, (static_cast<float>(gy) + 1.0f) * vs,
+                    (static_cast<float>(gz) + 1.0f) * vs);
+  int si[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) si[k] = staged_index(lx + c_corner[k][0], ly + c_corner[k][1], lz + c_corner[k][2]);
+
+  // collectSurfaceClusters (:439-507)
+  float cand[kMaxCand];
+  int nc = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+#pragma unroll
+    for (int l = 0; l < kLayers; ++l) {
+      if (S.valid[l][si[k]]) cand[nc++] = plane_sd(S.plane[l][si[k]], cc);
+    }
+  }
+  if (nc == 0) return 0;
+  for (int i = 1; i < nc; ++i) {
+    const float x = cand[i];
+    int j = i - 1;
+    while (j >= 0 && cand[j] > x) {
+      cand[j + 1] = cand[j];
+      --j;
+    }
+    cand[j + 1] = x;
+  }
+  const float tol = p.extract_tol;
+  float centers[kMaxCand];
+  int sizes[kMaxCand];
+  int ncl = 0;
+  for (int i = 0; i < nc; ++i) {
+    const float key = cand[i];
+    if (ncl == 0 || fabsf(key - centers[ncl - 1]) > tol) {
+      centers[ncl] = key;
+      sizes[ncl] = 1;
+      ++ncl;
+      continue;
+    }
+    const int last = ncl - 1;
+    const int cnt = sizes[last];
+    centers[last] = (centers[last] * static_cast<float>(cnt) + key) / static_cast<float>(cnt + 1);
+    sizes[last] = cnt + 1;
+  }
+
+  f3 pos[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    pos[k] = mk3((static_cast<float>(gx + c_corner[k][0]) + 0.5f) * vs,
+                 (static_cast<float>(gy + c_corner[k][1]) + 0.5f) * vs,
+                 (static_cast<float>(gz + c_corner[k][2]) + 0.5f) * vs);
+  }
+  int total = 0;
+  for (int ci = 0; ci < ncl; ++ci) {
+    const float key = centers[ci];
+    // loadCubeForSurface + selectClosestLayerForSurfaceGpu (:276-303, :509-551)
+    float val[8];
+    uint32_t mask = 0U;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      int best = -1;
+      float best_delta = 1e30f;
+#pragma unroll
+      for (int l = 0; l < kLayers; ++l) {
+        if (!S.valid[l][si[k]]) continue;
+        const float delta = fabsf(plane_sd(S.plane[l][si[k]], cc) - key);
+        if (delta <= tol && delta < best_delta) {
+          best_delta = delta;
+          best = l;
+        }
+      }
+      val[k] = 0.0f;
+      if (best >= 0) {
+        val[k] = plane_sd(S.plane[best][si[k]], pos[k]);
+        mask |= 1U << k;
+      }
+    }
+    // completeCubeValuesWithFallbackGpu (:305-356)
+    if (mask != 0xffU) {
+      int cnt = 0;
+      float sum = 0.0f;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (!(mask & (1U << k))) continue;
+        ++cnt;
+        sum += val[k];
+      }
+      if (cnt < 6) continue;
+      const float global = sum / static_cast<float>(cnt);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (mask & (1U << k)) continue;
+        float ns = 0.0f;
+        int nn = 0;
+#pragma unroll
+        for (int e = 0; e < 12; ++e) {
+          const int c0 = c_edge_corners[e][0], c1 = c_edge_corners[e][1];
+          const int nb = c0 == k ? c1 : (c1 == k ? c0 : -1);
+          if (nb < 0 || !(mask & (1U << nb))) continue;
+          ns += val[nb];
+          ++nn;
+        }
+        val[k] = nn > 0 ? (ns / static_cast<float>(nn)) : global;
+        mask |= 1U << k;
+      }
+    }
+    // computeCubeIndex / countCubeTriangles / emitCubeTriangles (:376-437)
+    int cube = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if (val[k] < p.iso) cube |= 1 << k;
+    const int em = S.edge[cube];
+    if (em == 0) continue;
+    int ntri = 0;
+    while (ntri < 5 && S.tri[cube][3 * ntri] >= 0) ++ntri;
+    if (kEmit) {
+      f3 ev[12];
+#pragma unroll
+      for (int e = 0; e < 12; ++e) {
+        ev[e] = mk3(0.0f, 0.0f, 0.0f);
+        if (em & (1 << e)) {
+          const int c0 = c_edge_corners[e][0], c1 = c_edge_corners[e][1];
+          ev[e] = interp(pos[c0], pos[c1], val[c0], val[c1], p.iso);
+        }
+      }
+      for (int t = 0; t < ntri; ++t) {
+        float* o = out + static_cast<size_t>(total + t) * 9;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const f3 v = ev[S.tri[cube][3 * t + q]];
+          o[3 * q] = v.x;
+          o[3 * q + 1] = v.y;
+          o[3 * q + 2] = v.z;
+        }
+      }
+    }
+    total += ntri;
+  }
+  return total;
+}
+
+// exclusive scan of one value per thread over the CTA; returns the prefix, S.total = CTA sum
+__device__ __forceinline__ uint32_t block_scan(Shared& S, uint32_t v, int tid) {
+  const int lane = tid & 31, warp = tid >> 5;
+  uint32_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffU, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) S.warp_sums[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kThreads / 32 ? S.warp_sums[lane] : 0U;
+    uint32_t wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffU, wi, o);
+      if (lane >= o) wi += t;
+    }
+    if (lane < kThreads / 32) S.warp_sums[lane] = wi - w;
+    if (lane == 31) S.total = wi;
+  }
+  __syncthreads();
+  const uint32_t r = S.warp_sums[warp] + incl - v;
+  return r;
+}
+
+template <bool kEmit>
+__global__ void __launch_bounds__(kThreads) mc_kernel(const Volume V, const Params p, uint32_t* __restrict__ counts,
+                                                      const unsigned long long* __restrict__ offsets,
+                                                      float* __restrict__ tris) {
+  __shared__ Shared S;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 256 * 16; i += kThreads) S.tri[i / 16][i % 16] = vh_mc_tri_table[i / 16][i % 16];
+  for (int i = tid; i < 256; i += kThreads) S.edge[i] = vh_mc_edge_table[i];
+  const uint32_t nblocks = min(V.counters->num_blocks, V.max_blocks);
+  const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
+  for (uint32_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+    const int4 bk = V.block_keys[b];
+    __syncthreads();  // previous block's readers are done with S.nbr / S.plane
+    if (tid < 8) {
+      S.nbr[tid] = tid == 0 ? b : lookup_block(V, bk.x + (tid & 1), bk.y + ((tid >> 1) & 1), bk.z + (tid >> 2));
+    }
+    __syncthreads();
+    const int gx = bk.x * kBlockSide + lx, gy = bk.y * kBlockSide + ly, gz = bk.z * kBlockSide + lz;
+    uint32_t run = 0U;
+    const unsigned long long base = kEmit ? offsets[b] : 0ULL;
+    for (int d = 0; d < kDirs; ++d) {
+      stage_direction(S, V, d, tid);
+      __syncthreads();
+      const uint32_t n = static_cast<uint32_t>(process_cell<false>(S, p, gx, gy, gz, lx, ly, lz, nullptr));
+      const uint32_t prefix = block_scan(S, n, tid);
+      if (kEmit && n > 0U) {
+        process_cell<true>(S, p, gx, gy, gz, lx, ly, lz, tris + (base + run + prefix) * 9ULL);
+      }
+      run += S.total;
+      __syncthreads();  // S.total / S.plane reused by the next direction
+    }
+    if (!kEmit && tid == 0) counts[b] = run;
+  }
+}
+
+// exclusive scan of counts[0..n) -> offsets, total; one CTA (the count array is a few MB at most)
+__global__ void __launch_bounds__(1024) scan_kernel(const Volume V, const uint32_t* __restrict__ counts,
+                                                    unsigned long long* __restrict__ offsets,
+                                                    unsigned long long* __restrict__ total) {
+  __shared__ unsigned long long s_w[32];
+  __shared__ unsigned long long s_carry;
+  const uint32_t n = min(V.counters->num_blocks, V.max_blocks);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_carry = 0ULL;
+  __syncthreads();
+  for (uint32_t start = 0; start < n; start += 1024U) {
+    const uint32_t i = start + tid;
+    const unsigned long long v = i < n ? counts[i] : 0ULL;
+    unsigned long long incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffU, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane == 31) s_w[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const unsigned long long w = s_w[lane];
+      unsigned long long wi = w;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffU, wi, o);
+        if (lane >= o) wi += t;
+      }
+      s_w[lane] = wi - w;
+    }
+    __syncthreads();
+    const unsigned long long carry = s_carry;
+    if (i < n) offsets[i] = carry + s_w[warp] + incl - v;
+    __syncthreads();
+    if (tid == 1023) s_carry = carry + s_w[warp] + incl;
+    __syncthreads();
+  }
+  if (tid == 0) *total = s_carry;
+}
+
+}  // namespace
+
+int mc_grid_size() {
+  static int grid = 0;
+  if (grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<true>, kThreads, 0);
+    grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+  }
+  return grid;
+}
+
+cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, cudaStream_t s) {
+  mc_kernel<false><<<mc_grid_size(), kThreads, 0, s>>>(V, p, counts, nullptr, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mc_scan(const Volume& V, const uint32_t* counts, unsigned long long* offsets,
+                           unsigned long long* total, cudaStream_t s) {
+  scan_kernel<<<1, 1024, 0, s>>>(V, counts, offsets, total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mc_emit(const Volume& V, const Params& p, const unsigned long long* offsets, float* tris,
+                           cudaStream_t s) {
+  mc_kernel<true><<<mc_grid_size(), kThreads, 0, s>>>(V, p, nullptr, offsets, tris);
+  return cudaGetLastError();
+}
+
+}  // namespace vh
