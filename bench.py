@@ -1,0 +1,377 @@
+#!/usr/bin/env python
+"""bench.py -- depth-fusion throughput of the GB300 path (integrated Mpix/s, MC blocks/s).
+
+Workload: the room-scale configuration -- 640x480 float32 depth (fx=fy=525, cx=319.5, cy=239.5) ray-cast
+from a seeded 4x5x3 m room holding 40 primitives, hand-held random walk (1 cm/frame, 1 degree/frame
+yaw/pitch jitter), noise N(0, (0.0012 z^2)^2) + 1 % dropouts, 5 mm voxels, 2 cm truncation, 2^20 hash
+buckets, plain FP32 directional multi-layer storage, mesh extracted at the end.  Frames are synthetic
+(voxelhashmt_gb300/scenes.py, rendered on the device by vh_render_depth).
+
+A step is one frame through filter -> allocate -> integrate.  W warm-up frames, then K timed frames,
+each bracketed by CUDA events on the stream the kernels run on; between timed frames a 512 MB buffer is
+written to flush L2 (outside the events).  value = W*H*K / sum(step times).  e2e = the same frames
+again on a reset volume through the public API (TsdfIntegrationBackend.integrate) from pinned host
+memory, with the host->device copy of the frame and a device->host read of the frame statistics inside
+each step, wall clock.  MC blocks/s = allocated blocks / full 6-direction extraction time.
+
+--impl reference times the reference's CPU implementation of the same path (the oracle port of
+TsdfIntegrationBackend(kCpu): CPU filter constants and allocation rule, every host thread) on a bounded
+sample of the same frames.
+
+Multi-GPU: independent replicas (one scene per rank, no collective): value = all ranks' pixels / max time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+VOXEL_LAYER_BIN_BYTES = 3 * 16  # one direction bin: 3 layers x 16 B
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=980)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    return ap.parse_args()
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return {"hbm_gbs": float(p["hbm_gbs"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": PEAKS_FALLBACK["hbm_gbs"], "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+        self.device_index = vis[device_index].strip() if vis[0] and device_index < len(vis) else str(device_index)
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def make_scene(seed, frames):
+    from voxelhashmt_gb300 import scenes
+    return scenes.room_scene(seed=seed, frames=frames)
+
+
+def workload_config(sc, steps, warmup):
+    K = sc.intrinsics
+    return {"workload": "room %dx%d, 40 primitives, %d-frame random walk, voxel %.0f mm, trunc %.0f mm, %d hash "
+                        "buckets, FP32 directional layers" % (K.width, K.height, len(sc.poses),
+                                                            sc.voxel_size * 1000, sc.truncation * 1000,
+                                                            sc.hash_buckets),
+            "width": K.width, "height": K.height, "frames": len(sc.poses), "voxel_size_m": sc.voxel_size,
+            "truncation_m": sc.truncation, "hash_buckets": sc.hash_buckets, "allocation_stride": 1,
+            "l2": "512 MB buffer written between timed frames (outside the timed events)"}
+
+
+def render_all(sc, torch, lib_mod, capi):
+    import ctypes as C
+    K = sc.intrinsics
+    n = len(sc.poses)
+    prims = torch.from_numpy(np.ascontiguousarray(sc.prims, np.float32)).cuda()
+    frames = torch.empty((n, K.height, K.width), dtype=torch.float32, device="cuda")
+    Kc = capi.intrinsics(K)
+    for f in range(n):
+        P = capi.pose(sc.poses[f])
+        capi.check(capi.lib().vh_render_depth(C.c_void_p(prims.data_ptr()), prims.shape[0], C.byref(Kc), C.byref(P),
+                                              sc.seed, f, sc.noise_sigma_z2, sc.dropout, sc.max_depth,
+                                              C.c_void_p(frames[f].data_ptr()),
+                                              C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    torch.cuda.synchronize()
+    return frames
+
+
+def cpu_fusion_rate(sc, host_frames, budget_s, threads, flavor):
+    """Mpix/s of the oracle port over consecutive frames until the time budget is spent."""
+    from oracle import oracle as O
+    cfg = O.config(flavor, O.EXP_LIBM, threads=threads)
+    vol = O.Volume(cfg, sc.voxel_size, sc.truncation)
+    K = sc.intrinsics
+    done, t0 = 0, time.perf_counter()
+    elapsed = 0.0
+    while done < len(host_frames) and elapsed < budget_s:
+        vol.integrate(host_frames[done], K, sc.poses[done])
+        done += 1
+        elapsed = time.perf_counter() - t0
+    vol.close()
+    return done * K.width * K.height / elapsed / 1e6, done, elapsed
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    from oracle import build as ob
+    ob.build_oracle()
+    from oracle import oracle as O
+    from voxelhashmt_gb300 import scenes
+    sc = make_scene(args.seed, args.warmup + args.steps)
+    threads = os.cpu_count() or 1
+    warm = min(args.warmup, 2)
+    budget = 60.0
+    max_frames = min(args.steps, 16)  # frames are ray-cast on the CPU too: keep the run to a few minutes
+    K = sc.intrinsics
+    cfg = O.config(O.FLAVOR_REF_CPU, O.EXP_LIBM, threads=threads)
+    vol = O.Volume(cfg, sc.voxel_size, sc.truncation)
+    for f in range(warm):
+        vol.integrate(scenes.render_depth(sc, f), K, sc.poses[f])
+    elapsed, done = 0.0, 0
+    while done < max_frames and elapsed < budget:
+        d = scenes.render_depth(sc, warm + done)
+        t0 = time.perf_counter()
+        vol.integrate(d, K, sc.poses[warm + done])
+        elapsed += time.perf_counter() - t0
+        done += 1
+    value = done * K.width * K.height / elapsed / 1e6
+    sample = "%d consecutive frames (after %d warm-up) of the %d-frame workload" % (done, warm, len(sc.poses))
+    line = {"impl": "reference", "metric": "integrated_mpix_per_s", "value": round(value, 4), "unit": "Mpix/s",
+            "n_gpus": args.gpus, "steps": done, "warmup": warm, "ms_per_step": round(1000 * elapsed / done, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": workload_config(sc, args.steps, args.warmup),
+            "cpu_baseline": {"value": round(value, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "oracle port of the reference CPU path (TsdfIntegrationBackend(kCpu)); the reference sources "
+                    "are not present on this host"}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gb300(args):
+    import ctypes as C
+
+    import torch
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    else:
+        torch.cuda.set_device(0)
+    from voxelhashmt_gb300 import _capi, backend
+    from voxelhashmt_gb300 import build as pbuild
+    pbuild.build()
+    sc = make_scene(args.seed + rank, args.warmup + args.steps)
+    K = sc.intrinsics
+    px = K.width * K.height
+    frames = render_all(sc, torch, None, _capi)
+    stream = torch.cuda.current_stream()
+    max_blocks = int(os.environ.get("VH_BENCH_MAX_BLOCKS", "900000"))
+    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=max_blocks,
+                                device=torch.cuda.current_device())
+    bk = backend.TsdfIntegrationBackend("gpu")
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step(f, sync=False):
+        bk.integrate(vol, backend.DepthFrame(K, frames[f].view(-1)), sc.poses[f], 1, stream=stream,
+                     synchronize=sync)
+
+    for f in range(args.warmup):
+        step(f)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    vol.profile(True)
+    vol.read_profile()
+    stats = []
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev0[i].record(stream)
+        step(args.warmup + i)
+        ev1[i].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clock_info = clocks.stop()
+    vol.synchronize(stream)
+    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    total_ms = sum(step_ms)
+    stage_ms, nprof = vol.read_profile()
+    vol.profile(False)
+    fstats = vol.frame_stats()
+    # updated voxels per frame for the roofline: re-run the last frame's counter read
+    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    max_ms = float(t.item())
+    value = world * args.steps * px / (max_ms / 1000.0) / 1e6
+
+    # marching cubes over the whole volume
+    nblocks = vol.block_count()
+    backend.extract_mesh_cuda(vol)  # warm (buffer sizing)
+    torch.cuda.synchronize()
+    m0 = torch.cuda.Event(enable_timing=True)
+    m1 = torch.cuda.Event(enable_timing=True)
+    m0.record(stream)
+    n_tri = C.c_size_t()
+    _capi.check(_capi.lib().vh_extract_mesh(vol.handle, 0.0, C.byref(n_tri), C.c_void_p(stream.cuda_stream)),
+                vol.handle)
+    m1.record(stream)
+    torch.cuda.synchronize()
+    mc_ms = m0.elapsed_time(m1)
+    mc_blocks_per_s = nblocks / (mc_ms / 1000.0)
+    observed = vol.observed_voxel_count()
+
+    # per-frame updated voxels (for algorithmic bytes): measure on a replay of the last 8 frames
+    vol.reset(stream)
+    upd = []
+    for f in range(args.warmup + args.steps):
+        step(f)
+        if f >= args.warmup + args.steps - 16:
+            upd.append(vol.frame_stats()["updated_voxels"])
+    upd_mean = float(np.mean(upd))
+
+    # end to end through the public API from pinned host memory
+    host = torch.empty((len(sc.poses), K.height, K.width), dtype=torch.float32, pin_memory=True)
+    host.copy_(frames.cpu())
+    vol.reset(stream)
+    for f in range(args.warmup):
+        bk.integrate(vol, backend.DepthFrame(K, host[f].numpy()), sc.poses[f], 1, stream=stream, synchronize=False)
+        vol.frame_stats(stream)
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for i in range(args.steps):
+        f = args.warmup + i
+        bk.integrate(vol, backend.DepthFrame(K, host[f].numpy()), sc.poses[f], 1, stream=stream, synchronize=False)
+        vol.frame_stats(stream)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - e0
+    vol.synchronize(stream)
+    e2e_value = world * args.steps * px / e2e_s / 1e6
+
+    pk = peaks()
+    integ_ms = stage_ms["integrate"] / max(1, nprof)
+    integ_bytes = upd_mean * 2 * VOXEL_LAYER_BIN_BYTES + px * 4
+    achieved = integ_bytes / (integ_ms / 1000.0) / 1e9
+    roofline = {"kernel": "integrate_kernel", "bound": "hbm", "achieved": round(achieved, 2),
+                "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 5),
+                "traffic": None, "peak_source": pk["source"],
+                "algorithmic_bytes_per_launch": int(integ_bytes),
+                "note": "updated voxels x 96 B (read+write of one 3-layer bin) + 4 B/px depth; the kernel is "
+                        "bound by FP32/ALU work of the per-voxel bilateral normal, not by HBM"}
+
+    cpu = None
+    if rank == 0 and world == 1:
+        try:
+            from oracle import build as ob
+            ob.build_oracle()
+            from oracle import oracle as O
+            hf = frames[: min(len(sc.poses), 64)].cpu().numpy()
+            threads = os.cpu_count() or 1
+            rate, done, el = cpu_fusion_rate(sc, hf, args.cpu_budget_s, threads, O.FLAVOR_REF_CPU)
+            cpu = {"value": round(rate, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+                   "sample": "first %d frames of the workload (%.1f s), oracle port of the reference CPU path"
+                             % (done, el)}
+        except Exception as e:  # the baseline is reported, never the target
+            cpu = {"value": None, "unit": "Mpix/s", "cores": 0, "kind": "port", "sample": "failed: %s" % e}
+
+    if rank == 0:
+        line = {
+            "metric": "integrated_mpix_per_s", "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max_ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_config(sc, args.steps, args.warmup),
+            "mc_blocks_per_s": round(mc_blocks_per_s, 1), "mc_ms": round(mc_ms, 3), "mc_triangles": n_tri.value,
+            "blocks": nblocks, "observed_voxels": observed,
+            "stage_ms_per_frame": {k: round(v / max(1, nprof), 4) for k, v in stage_ms.items()},
+            "stream_mpix_per_s_no_flush": round(world * args.steps * px / wall / 1e6, 3),
+            "e2e": {"value": round(e2e_value, 3), "unit": "Mpix/s", "h2d_bytes_per_step": px * 4,
+                    "d2h_bytes_per_step": 64},
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
+            "gpu_launches": args.steps * 3,
+            "visible_blocks_last_frame": fstats["visible_blocks"], "updated_voxels_per_frame": round(upd_mean),
+        }
+        print(json.dumps(line))
+    vol.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

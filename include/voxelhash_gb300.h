@@ -155,6 +155,23 @@ vh_status vh_frame_stats_get(vh_volume* volume, vh_frame_stats* stats, void* str
 vh_status vh_export_blocks(vh_volume* volume, uint64_t first, uint64_t count, int32_t* keys, void* voxels,
                            int32_t out_on_device, void* stream);
 
+/* Stage timing with CUDA events (the reference times its stages with steady_clock, src/main.cpp:424-452).
+ * While enabled, vh_integrate brackets its filter, allocation and update kernels with events on the call's
+ * stream.  vh_profile_read waits for the recorded frames and returns the milliseconds spent in each stage
+ * (ms[0] filter, ms[1] allocation, ms[2] update) since the last read, and how many frames they cover. */
+vh_status vh_profile_enable(vh_volume* volume, int32_t enable);
+vh_status vh_profile_read(vh_volume* volume, double ms[3], uint64_t* frames);
+
+/* Workload generator, not a reference interface: ray-casts the analytic benchmark scenes the way the
+ * reference's demo renders its synthetic frames (src/main.cpp:189-335) -- primitives `prims` (device memory,
+ * n_prims x 10 floats: type, a.xyz, b.xyz, r, h, 0; types plane / sphere / box / vertical cylinder / room
+ * interior) seen from T_wc, depth = camera-space z, plus N(0, (sigma_z2 z^2)^2) noise and `dropout` zeroed
+ * pixels from a counter-based hash of (seed, frame, pixel); returns outside (0.1, max_depth) are zeroed.
+ * depth_out: width*height floats in device memory. */
+vh_status vh_render_depth(const float* prims, int32_t n_prims, const vh_intrinsics* K, const vh_pose* T_wc,
+                          uint32_t seed, uint32_t frame, float sigma_z2, float dropout, float max_depth,
+                          float* depth_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

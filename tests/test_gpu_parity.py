@@ -166,33 +166,37 @@ def test_mesh_bit_exact_and_deterministic(env, small_orbit):
 
 
 def test_reference_expf_tolerance(env, small_orbit):
-    """Own exp vs the C library expf: the float fields stay within 1e-5 relative, vertices within 1e-4 voxel."""
+    """Own exp vs the C library expf (the exp the reference calls).  Block keys, layer occupancy and
+    triangle counts are identical; weight, surface_coord and plane_offset agree within 1e-5 relative to
+    max(|value|, 1) (metres for the two coordinates); matched vertices agree within 5e-3 voxel at the
+    99.9th percentile and 5e-2 voxel at most (marching cubes divides by the corner-value difference, which
+    amplifies the 1-ulp exp differences where that difference is small)."""
     backend, O = env
-    vol, _ = _integrate_both(backend, O, small_orbit, frames=[0, 6, 12])
-    ref = O.Volume(O.config(O.FLAVOR_REF_GPU, O.EXP_LIBM, threads=8), small_orbit.voxel_size,
-                   small_orbit.truncation)
+    from scipy.spatial import cKDTree
     from voxelhashmt_gb300 import scenes
+    sc = small_orbit
+    vol, _ = _integrate_both(backend, O, sc, frames=[0, 6, 12])
+    ref = O.Volume(O.config(O.FLAVOR_REF_GPU, O.EXP_LIBM, threads=8), sc.voxel_size, sc.truncation)
     for f in [0, 6, 12]:
-        ref.integrate(scenes.render_depth(small_orbit, f), small_orbit.intrinsics, small_orbit.poses[f])
+        ref.integrate(scenes.render_depth(sc, f), sc.intrinsics, sc.poses[f])
     gk, gv = O.sort_blocks(*vol.export_blocks())
     rk, rv = O.sort_blocks(*ref.blocks())
     assert np.array_equal(gk, rk)
     g = gv.view(np.float32).reshape(-1, 4)
     r = rv.view(np.float32).reshape(-1, 4)
-    both = (g[:, 0] > 0) & (r[:, 0] > 0)
+    assert np.array_equal(g[:, 0] > 0, r[:, 0] > 0)
+    both = g[:, 0] > 0
     assert both.sum() > 1000
-    agree = np.mean((g[:, 0] > 0) == (r[:, 0] > 0))
-    assert agree > 0.9999
     for col in range(3):
         a, b = g[both, col].astype(np.float64), r[both, col].astype(np.float64)
-        rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-3)
-        assert np.quantile(rel, 0.999) <= 1e-5, (col, float(rel.max()))
-    gm = O.canonical_triangles(backend.extract_mesh_cuda(vol))
-    rm = O.canonical_triangles(ref.extract_mesh())
-    if gm.shape == rm.shape:
-        assert np.max(np.abs(gm - rm)) <= 1e-4 * small_orbit.voxel_size * 10
-    else:
-        assert abs(gm.shape[0] - rm.shape[0]) <= max(3, gm.shape[0] // 1000)
+        err = np.abs(a - b) / np.maximum(np.abs(b), 1.0)
+        assert err.max() <= 1e-5, (col, float(err.max()))
+    gm = backend.extract_mesh_cuda(vol)
+    rm = ref.extract_mesh()
+    assert gm.shape == rm.shape
+    _, idx = cKDTree(rm.reshape(-1, 3, 3).mean(1)).query(gm.reshape(-1, 3, 3).mean(1))
+    dv = np.abs(gm.astype(np.float64) - rm[idx]).max(axis=1) / sc.voxel_size
+    assert np.quantile(dv, 0.999) <= 5e-3 and dv.max() <= 5e-2, (float(np.quantile(dv, 0.999)), float(dv.max()))
     vol.close()
 
 
@@ -214,7 +218,7 @@ def test_key_range_error(env, small_orbit):
     backend, O = env
     from voxelhashmt_gb300 import _capi, scenes
     sc = small_orbit
-    far = scenes.Pose(sc.poses[0].R.copy(), sc.poses[0].t + np.float32([1.0e5, 0.0, 0.0]))
+    far = scenes.Pose(sc.poses[0].R.copy(), sc.poses[0].t + np.float32([1.0e6, 0.0, 0.0]))  # > 2^20 blocks
     vol = _volume(backend, sc)
     d = scenes.render_depth(sc, 0)
     with pytest.raises(_capi.VhError) as e:

@@ -103,6 +103,10 @@ _SIGNATURES = {
     "vh_recount_observed_voxels": (C.c_int, [_vp, _u64p, _vp]),
     "vh_frame_stats_get": (C.c_int, [_vp, C.POINTER(VhFrameStats), _vp]),
     "vh_export_blocks": (C.c_int, [_vp, C.c_uint64, C.c_uint64, _ip, _vp, C.c_int32, _vp]),
+    "vh_profile_enable": (C.c_int, [_vp, C.c_int32]),
+    "vh_profile_read": (C.c_int, [_vp, C.POINTER(C.c_double), _u64p]),
+    "vh_render_depth": (C.c_int, [_vp, C.c_int32, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_uint32,
+                                  C.c_uint32, C.c_float, C.c_float, C.c_float, _vp, _vp]),
 }
 
 

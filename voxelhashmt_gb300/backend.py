@@ -138,6 +138,17 @@ class VoxelHashTSDF:
         _capi.check(_capi.lib().vh_frame_stats_get(self.handle, C.byref(s), _stream_handle(stream)), self.handle)
         return {f: getattr(s, f) for f, _ in s._fields_}
 
+    def profile(self, enable=True):
+        """Stage timing of vh_integrate with CUDA events (see read_profile)."""
+        _capi.check(_capi.lib().vh_profile_enable(self.handle, 1 if enable else 0), self.handle)
+
+    def read_profile(self):
+        """({'filter': ms, 'allocate': ms, 'integrate': ms}, frames) accumulated since the last read."""
+        ms = (C.c_double * 3)()
+        n = C.c_uint64()
+        _capi.check(_capi.lib().vh_profile_read(self.handle, ms, C.byref(n)), self.handle)
+        return {"filter": ms[0], "allocate": ms[1], "integrate": ms[2]}, n.value
+
     def block_keys(self):
         """gpuVolumeCacheBlockKeys: (N, 3) int32 in allocation order."""
         n = self.block_count()

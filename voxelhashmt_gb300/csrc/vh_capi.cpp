@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/voxelhash_gb300.h"
 #include "vh_common.cuh"
@@ -32,6 +33,9 @@ struct vh_volume {
   float4* d_export = nullptr;
   int* d_export_keys = nullptr;
   size_t export_capacity = 0;  // blocks
+  bool profile = false;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::vector<cudaEvent_t>> profiled;  // 4 events per recorded frame
   std::string error;
 };
 
@@ -330,6 +334,9 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_keys);
   dfree(v->d_export);
   dfree(v->d_export_keys);
+  for (auto& fr : v->profiled)
+    for (cudaEvent_t e : fr) cudaEventDestroy(e);
+  for (cudaEvent_t e : v->event_pool) cudaEventDestroy(e);
   delete v;
 }
 
@@ -364,9 +371,54 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
   vh_status st = stage_depth(v, depth, on_device, K, s, &src);
   if (st != VH_OK) return st;
   const vh::Params p = make_params(v, K, T_wc, stride);
+  std::vector<cudaEvent_t> ev;
+  if (v->profile) {
+    for (int i = 0; i < 4; ++i) {
+      cudaEvent_t e = nullptr;
+      if (!v->event_pool.empty()) {
+        e = v->event_pool.back();
+        v->event_pool.pop_back();
+      } else {
+        VH_CUDA(v, cudaEventCreate(&e));
+      }
+      ev.push_back(e);
+    }
+    VH_CUDA(v, cudaEventRecord(ev[0], s));
+  }
   VH_CUDA(v, vh::launch_filter(src, v->d_depth_filtered, p, v->dev.counters, s));
+  if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
+  if (v->profile) VH_CUDA(v, cudaEventRecord(ev[2], s));
   VH_CUDA(v, vh::launch_integrate(v->d_depth_filtered, v->dev, p, 0, s));
+  if (v->profile) {
+    VH_CUDA(v, cudaEventRecord(ev[3], s));
+    v->profiled.push_back(std::move(ev));
+  }
+  return VH_OK;
+}
+
+vh_status vh_profile_enable(vh_volume* v, int32_t enable) {
+  if (!v) return VH_ERR_INVALID_ARGUMENT;
+  v->profile = enable != 0;
+  return VH_OK;
+}
+
+vh_status vh_profile_read(vh_volume* v, double ms[3], uint64_t* frames) {
+  if (!v || !ms) return VH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(v->params.device);
+  ms[0] = ms[1] = ms[2] = 0.0;
+  const uint64_t n = v->profiled.size();
+  for (auto& fr : v->profiled) {
+    VH_CUDA(v, cudaEventSynchronize(fr[3]));
+    for (int k = 0; k < 3; ++k) {
+      float t = 0.0f;
+      VH_CUDA(v, cudaEventElapsedTime(&t, fr[k], fr[k + 1]));
+      ms[k] += t;
+    }
+    for (cudaEvent_t e : fr) v->event_pool.push_back(e);
+  }
+  v->profiled.clear();
+  if (frames) *frames = n;
   return VH_OK;
 }
 
@@ -552,6 +604,26 @@ vh_status vh_export_blocks(vh_volume* v, uint64_t first, uint64_t count, int32_t
   }
   VH_CUDA(v, cudaStreamSynchronize(s));
   return VH_OK;
+}
+
+vh_status vh_render_depth(const float* prims, int32_t n_prims, const vh_intrinsics* K, const vh_pose* T_wc,
+                          uint32_t seed, uint32_t frame, float sigma_z2, float dropout, float max_depth,
+                          float* depth_out, void* stream) {
+  if (!prims || n_prims <= 0 || n_prims > 1024 || !valid_intrinsics(K) || !T_wc || !depth_out) {
+    return VH_ERR_INVALID_ARGUMENT;
+  }
+  vh::Params p{};
+  p.width = K->width;
+  p.height = K->height;
+  p.fx = K->fx;
+  p.fy = K->fy;
+  p.cx = K->cx;
+  p.cy = K->cy;
+  for (int i = 0; i < 9; ++i) p.T_wc.r[i] = T_wc->R[i];
+  for (int i = 0; i < 3; ++i) p.T_wc.t[i] = T_wc->t[i];
+  const cudaError_t e = vh::launch_render(prims, n_prims, p, seed, frame, sigma_z2, dropout, max_depth, depth_out,
+                                          as_stream(stream));
+  return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
 }
 
 }  // extern "C"
