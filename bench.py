@@ -329,7 +329,7 @@ def run_gb300(args):
                         "bound by FP32/ALU work of the per-voxel bilateral normal, not by HBM"}
 
     cpu = None
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and args.cpu_budget_s > 0:
         try:
             from oracle import build as ob
             ob.build_oracle()
