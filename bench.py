@@ -292,12 +292,15 @@ def run_gb300(args):
 
     # per-frame updated voxels (for algorithmic bytes): measure on a replay of the last 8 frames
     vol.reset(stream)
-    upd = []
+    upd, act = [], []
     for f in range(args.warmup + args.steps):
         step(f)
         if f >= args.warmup + args.steps - 16:
-            upd.append(vol.frame_stats()["updated_voxels"])
+            st = vol.frame_stats()
+            upd.append(st["updated_voxels"])
+            act.append(st["active_voxels"])
     upd_mean = float(np.mean(upd))
+    act_mean = float(np.mean(act))
 
     # end to end through the public API from pinned host memory
     host = torch.empty((len(sc.poses), K.height, K.width), dtype=torch.float32, pin_memory=True)
@@ -358,6 +361,7 @@ def run_gb300(args):
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
             "gpu_launches": args.steps * 3,
             "visible_blocks_last_frame": fstats["visible_blocks"], "updated_voxels_per_frame": round(upd_mean),
+            "active_voxels_per_frame": round(act_mean),
         }
         print(json.dumps(line))
     vol.close()

@@ -70,7 +70,7 @@ typedef struct vh_params {
   float voxel_size;
   float truncation_distance;
   uint32_t hash_buckets; /* power of two; slots of the persistent block hash */
-  uint32_t max_blocks;   /* pool capacity in blocks, 147,456 bytes each; 0 = keys-only volume (vh_allocate only) */
+  uint32_t max_blocks;   /* pool capacity in blocks (<= 2^23), 147,456 bytes each; 0 = keys-only volume (vh_allocate only) */
   int32_t device;        /* CUDA device ordinal */
   int32_t reserved;
 } vh_params;
@@ -91,6 +91,7 @@ typedef struct vh_algorithm {
 typedef struct vh_frame_stats {
   uint64_t visible_blocks;   /* unique blocks the frame touched (the reference's active block list) */
   uint64_t new_blocks;       /* blocks the frame allocated */
+  uint64_t active_voxels;    /* voxels that passed projection, depth and truncation tests (reached the update) */
   uint64_t updated_voxels;   /* voxel layer updates the frame applied */
   uint64_t total_blocks;     /* blocks in the volume */
   uint64_t observed_voxels;  /* voxels with any layer weight > 0 */

@@ -56,7 +56,8 @@ class VhPose(C.Structure):
 
 
 class VhFrameStats(C.Structure):
-    _fields_ = [("visible_blocks", C.c_uint64), ("new_blocks", C.c_uint64), ("updated_voxels", C.c_uint64),
+    _fields_ = [("visible_blocks", C.c_uint64), ("new_blocks", C.c_uint64), ("active_voxels", C.c_uint64),
+                ("updated_voxels", C.c_uint64),
                 ("total_blocks", C.c_uint64), ("observed_voxels", C.c_uint64)]
 
 

@@ -253,8 +253,8 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   *out = nullptr;
   const uint32_t buckets = params->hash_buckets;
   if (!(params->voxel_size > 0.0f) || !(params->truncation_distance > 0.0f) || buckets < 2 ||
-      (buckets & (buckets - 1)) != 0) {
-    return VH_ERR_INVALID_ARGUMENT;
+      (buckets & (buckets - 1)) != 0 || params->max_blocks > (1u << 23)) {
+    return VH_ERR_INVALID_ARGUMENT;  // pool indices are packed with the voxel index in 32 bits
   }
   int count = 0;
   if (cudaGetDeviceCount(&count) != cudaSuccess || params->device < 0 || params->device >= count) {
@@ -286,6 +286,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   step(dalloc(&V.slot_block, buckets));
   step(dalloc(&V.slot_stamp, buckets));
   step(dalloc(&V.visible, buckets));
+  step(dalloc(&V.active, nb * vh::kBlockVoxels));
   step(cudaMalloc(reinterpret_cast<void**>(&V.layers), std::max<size_t>(nb, 1) * kBlockBytes));
   step(dalloc(&V.block_keys, nb));
   step(dalloc(&V.obs_mask, nb * (vh::kBlockVoxels / 32)));
@@ -320,6 +321,7 @@ void vh_destroy(vh_volume* v) {
   dfree(V.slot_block);
   dfree(V.slot_stamp);
   dfree(V.visible);
+  dfree(V.active);
   dfree(V.layers);
   dfree(V.block_keys);
   dfree(V.obs_mask);
@@ -571,6 +573,7 @@ vh_status vh_frame_stats_get(vh_volume* v, vh_frame_stats* stats, void* stream) 
   if (st != VH_OK) return st;
   stats->visible_blocks = v->h_counters->visible_count;
   stats->new_blocks = v->h_counters->new_blocks;
+  stats->active_voxels = v->h_counters->active_voxels;
   stats->updated_voxels = v->h_counters->integrated_voxels;
   stats->total_blocks = block_total(v);
   stats->observed_voxels = v->h_counters->observed_voxels;

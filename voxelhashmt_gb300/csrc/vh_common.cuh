@@ -29,17 +29,19 @@ constexpr uint32_t kErrKeyRange = 1u;  // block coordinate outside the 21-bit pa
 constexpr uint32_t kErrHashFull = 2u;  // no free slot within `capacity` probes
 constexpr uint32_t kErrPoolFull = 4u;  // more blocks than the pool holds
 
-// Device-resident counters of one volume (one cache line; read back with one D2H copy).
+// Device-resident counters of one volume (64 bytes; read back with one D2H copy).
 struct Counters {
-  uint32_t num_blocks;      // blocks ever allocated (pool high-water mark)
-  uint32_t visible_count;   // unique blocks touched by the current frame
-  uint32_t error;           // sticky kErr* bits
-  uint32_t frame;           // frame stamp of the current frame (starts at 1)
+  uint32_t num_blocks;         // blocks ever allocated (pool high-water mark)
+  uint32_t visible_count;      // unique blocks touched by the current frame
+  uint32_t error;              // sticky kErr* bits
+  uint32_t frame;              // frame stamp of the current frame (starts at 1)
   unsigned long long observed_voxels;  // voxels with any layer weight > 0
-  uint32_t new_blocks;      // blocks allocated by the current frame
-  uint32_t integrated_voxels;  // voxel updates applied by the current frame
-  uint32_t pad[8];
+  uint32_t new_blocks;         // blocks allocated by the current frame
+  uint32_t integrated_voxels;  // voxel layer updates applied by the current frame
+  uint32_t active_voxels;      // voxels of the current frame that reached the layer update stage
+  uint32_t pad[7];
 };
+static_assert(sizeof(Counters) == 64, "Counters is read back as one 64-byte copy");
 
 // Device view of one volume.  HBM layout:
 //   slot_keys   u64[capacity]           packed block keys (open addressing, linear probing)
@@ -51,6 +53,8 @@ struct Counters {
 //   block_keys  int4[max_blocks]        {x, y, z, frame the block was allocated in}
 //   obs_mask    u32[max_blocks][16]     one bit per voxel: any layer observed
 //   visible     u32[capacity]           slots touched by the current frame (unordered)
+//   active      u32[max_blocks * 512]   (block << 9 | voxel) of the current frame's voxels that pass the
+//                                       projection / depth / truncation tests (unordered)
 struct Volume {
   unsigned long long* slot_keys;
   uint32_t* slot_block;
@@ -59,6 +63,7 @@ struct Volume {
   int4* block_keys;
   uint32_t* obs_mask;
   uint32_t* visible;
+  uint32_t* active;
   Counters* counters;
   uint32_t capacity;
   uint32_t mask;

@@ -74,7 +74,7 @@ __global__ void __launch_bounds__(kTX* kTY) filter_kernel(const float* __restric
     counters->visible_count = 0U;
     counters->new_blocks = 0U;
     counters->integrated_voxels = 0U;
-    counters->pad[0] = 0U;  // integrate work cursor
+    counters->active_voxels = 0U;
   }
   const int R = p.filter_radius;
   if (tid < (2 * kR + 1) * (2 * kR + 1)) {
@@ -145,7 +145,7 @@ __global__ void begin_frame_kernel(Counters* counters) {
   counters->visible_count = 0U;
   counters->new_blocks = 0U;
   counters->integrated_voxels = 0U;
-  counters->pad[0] = 0U;
+  counters->active_voxels = 0U;
 }
 
 }  // namespace

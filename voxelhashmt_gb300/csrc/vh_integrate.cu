@@ -1,11 +1,14 @@
 // vh_integrate.cu -- directional multi-layer TSDF update of the visible blocks.
 //
 // Reference: integrateActiveBlocksKernel (src/cuda_tsdf_integrator.cu:834-903) with its helpers
-// (:319-568, :727-832).  One CTA per visible block (taken from a device work cursor, so the grid is a fixed
-// number of persistent CTAs and the launch needs no host read-back), 256 threads x 2 voxels.  Layer storage
-// is direction-major (vh_common.cuh), so a warp reads and writes the 3 layers of its voxels' bin as 16-byte
-// vector accesses over contiguous memory; a voxel's other 5 bins are never touched.  The observed-voxel
-// bitmask (one u32 per warp of voxels, so one writer per word) keeps the observed-voxel count incremental.
+// (:319-568, :727-832), one CTA per active block and one thread per voxel.  Here the same per-voxel function
+// runs as two persistent grid-stride passes whose launches need no host read-back: classify_kernel runs the
+// cheap prefix (projection, bilinear depth, truncation test) over every voxel of the visible blocks and
+// compacts the survivors into an active-voxel list; update_kernel runs the bilateral normal and the layer
+// update over that list, one voxel per thread.  Layer storage is direction-major (vh_common.cuh), so a warp
+// of neighbouring voxels with the same dominant direction reads and writes its 3 layers as 16-byte vector
+// accesses over contiguous memory; a voxel's other 5 bins are never touched.  The observed-voxel bitmask
+// keeps the observed-voxel count incremental.
 //
 // The per-voxel bilateral normal (estimateSurfaceNormalCamera, :754-832) evaluates 9 base normals, each from
 // 4 bilinear depth samples, plus 10 more samples: 50 bilinear samples per voxel, all at (u + i, v + j) for
@@ -365,26 +368,32 @@ __device__ __forceinline__ bool integrate_sample(const Params& p, float4& L0, fl
   return true;
 }
 
-// Everything integrateActiveBlocksKernel computes for one voxel before touching its layers (:849-899).
-// Returns the direction bin, or -1 when the voxel is not updated this frame.
-__device__ __forceinline__ int observe_voxel(const float* __restrict__ depth, const Params& p, const int4& bk,
-                                             int lx, int ly, int lz, const float gs[3], float& sc, f3& spw, f3& nw,
-                                             float& obs) {
+// First part of integrateActiveBlocksKernel for one voxel (:849-877): voxel centre, projection, bilinear
+// depth, truncation test.  Returns false when the reference returns before touching the voxel.
+__device__ __forceinline__ bool voxel_prefix(const float* __restrict__ depth, const Params& p, const int4& bk, int li,
+                                             f3& pc, float& u, float& v, float& d) {
+  const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
   const f3 pw = mk3((static_cast<float>(bk.x * kBlockSide + lx) + 0.5f) * p.voxel_size,
                     (static_cast<float>(bk.y * kBlockSide + ly) + 0.5f) * p.voxel_size,
                     (static_cast<float>(bk.z * kBlockSide + lz) + 0.5f) * p.voxel_size);
-  const f3 pc = xform_point(p.T_cw, pw);
-  if (pc.z <= 0.0f) return -1;
-  if (pc.z <= 1e-6f) return -1;
-  const float u = p.fx * pc.x / pc.z + p.cx;
-  const float v = p.fy * pc.y / pc.z + p.cy;
+  pc = xform_point(p.T_cw, pw);
+  if (pc.z <= 0.0f) return false;
+  if (pc.z <= 1e-6f) return false;
+  u = p.fx * pc.x / pc.z + p.cx;
+  v = p.fy * pc.y / pc.z + p.cy;
   if (!(u >= 0.0f && u <= static_cast<float>(p.width - 1) && v >= 0.0f && v <= static_cast<float>(p.height - 1))) {
-    return -1;
+    return false;
   }
-  float d;
-  if (!sample_bilinear(depth, p, u, v, d)) return -1;
+  if (!sample_bilinear(depth, p, u, v, d)) return false;
+  return !(d - pc.z <= -p.truncation);
+}
+
+// Rest of integrateActiveBlocksKernel (:879-899): bilateral normal, observation weight, surface point,
+// direction bin.  Returns the direction bin, or -1 when the reference skips the voxel.
+__device__ __forceinline__ int voxel_observation(const float* __restrict__ depth, const Params& p, f3 pc, float u,
+                                                 float v, float d, const float gs[3], float& sc, f3& spw, f3& nw,
+                                                 float& obs) {
   const float sd = d - pc.z;
-  if (sd <= -p.truncation) return -1;
   const f3 view = normalize3(pc);
   float view_w = 1.0f;
   f3 nc = mul3(view, -1.0f);
@@ -399,30 +408,61 @@ __device__ __forceinline__ int observe_voxel(const float* __restrict__ depth, co
   return dir;
 }
 
-__global__ void __launch_bounds__(kThreads, 2) integrate_kernel(const float* __restrict__ depth, const Volume V,
-                                                                const Params p) {
-  __shared__ uint32_t s_item;
+// Pass 1: every voxel of every visible block; the ones that reach the layer update in the reference are
+// appended to V.active (warp-aggregated: one atomic per warp).  Cheap and uniform per voxel.
+__global__ void __launch_bounds__(kThreads) classify_kernel(const float* __restrict__ depth, const Volume V,
+                                                            const Params p) {
   const uint32_t nvis = V.counters->visible_count;
-  const int tid = threadIdx.x, lane = tid & 31;
-  // spatial factor of the normal bilateral for du^2+dv^2 in {0,1,2}: depends on (du,dv) only
+  const unsigned long long total = static_cast<unsigned long long>(nvis) * kBlockVoxels;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  // every lane of a warp runs the same number of iterations (the total is a multiple of 512)
+  for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += stride) {
+    const uint32_t item = static_cast<uint32_t>(i >> 9);
+    const int li = static_cast<int>(i & 511U);
+    const uint32_t b = V.slot_block[V.visible[item]];
+    bool pass = false;
+    if (b != kInvalidBlock) {
+      const int4 bk = V.block_keys[b];
+      f3 pc;
+      float u, v, d;
+      pass = voxel_prefix(depth, p, bk, li, pc, u, v, d);
+    }
+    const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
+    if (ballot) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(&V.counters->active_voxels, static_cast<uint32_t>(__popc(ballot)));
+      base = __shfl_sync(0xffffffffU, base, 0);
+      if (pass) V.active[base + __popc(ballot & ((1U << lane) - 1U))] = (b << 9) | static_cast<uint32_t>(li);
+    }
+  }
+}
+
+// Pass 2: the layer update of the active voxels, one voxel per thread, no CTA barriers: the expensive
+// bilateral normal runs only where the reference runs it, and slow voxels no longer hold a whole block.
+__global__ void __launch_bounds__(kThreads, 2) update_kernel(const float* __restrict__ depth, const Volume V,
+                                                             const Params p) {
+  const uint32_t n = V.counters->active_voxels;
+  const uint32_t padded = (n + 31U) & ~31U;
+  const int lane = threadIdx.x & 31;
   const float gs[3] = {gaussian(0.0f, p.normal_k_spatial), gaussian(1.0f, p.normal_k_spatial),
                        gaussian(2.0f, p.normal_k_spatial)};
-  for (;;) {
-    if (tid == 0) s_item = atomicAdd(&V.counters->pad[0], 1U);
-    __syncthreads();
-    const uint32_t item = s_item;
-    __syncthreads();
-    if (item >= nvis) break;
-    const uint32_t b = V.slot_block[V.visible[item]];
-    if (b == kInvalidBlock) continue;
-    const int4 bk = V.block_keys[b];
-#pragma unroll 1
-    for (int half = 0; half < 2; ++half) {
-      const int li = tid + kThreads * half;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < padded; i += stride) {
+    bool updated = false;
+    uint32_t newly = 0U;
+    if (i < n) {
+      const uint32_t code = V.active[i];
+      const uint32_t b = code >> 9;
+      const int li = static_cast<int>(code & 511U);
+      const int4 bk = V.block_keys[b];
+      f3 pc;
+      float u, v, d;
+      voxel_prefix(depth, p, bk, li, pc, u, v, d);
       float sc = 0.0f, obs = 0.0f;
       f3 spw = mk3(0.0f, 0.0f, 0.0f), nw = spw;
-      const int dir = observe_voxel(depth, p, bk, li & 7, (li >> 3) & 7, li >> 6, gs, sc, spw, nw, obs);
-      bool updated = false;
+      const int dir = voxel_observation(depth, p, pc, u, v, d, gs, sc, spw, nw, obs);
       if (dir >= 0) {
         float4* base = V.layers + layer_index(b, dir, li, 0);
         float4 L0 = base[0], L1 = base[1], L2 = base[2];
@@ -431,39 +471,44 @@ __global__ void __launch_bounds__(kThreads, 2) integrate_kernel(const float* __r
           base[0] = L0;
           base[1] = L1;
           base[2] = L2;
+          const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
+          const uint32_t bit = 1U << (li & 31);
+          if (!(V.obs_mask[w] & bit)) newly = (atomicOr(&V.obs_mask[w], bit) & bit) ? 0U : 1U;
         }
       }
-      const uint32_t upd = __ballot_sync(0xffffffffU, updated);
-      if (lane == 0 && upd) {
-        const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
-        const uint32_t old = V.obs_mask[w];
-        const uint32_t now = old | upd;
-        if (now != old) {
-          V.obs_mask[w] = now;
-          atomicAdd(&V.counters->observed_voxels, static_cast<unsigned long long>(__popc(now & ~old)));
-        }
-        atomicAdd(&V.counters->integrated_voxels, static_cast<uint32_t>(__popc(upd)));
-      }
+    }
+    const uint32_t upd = __ballot_sync(0xffffffffU, updated);
+    const uint32_t nw_ = __ballot_sync(0xffffffffU, newly != 0U);
+    if (lane == 0) {
+      if (upd) atomicAdd(&V.counters->integrated_voxels, static_cast<uint32_t>(__popc(upd)));
+      if (nw_) atomicAdd(&V.counters->observed_voxels, static_cast<unsigned long long>(__popc(nw_)));
     }
   }
 }
 
 }  // namespace
 
+static int grid_for(const void* kernel, int threads) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0);
+  return (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
+}
+
 int integrate_grid_size() {
   static int grid = 0;
-  if (grid == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, integrate_kernel, kThreads, 0);
-    grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
-  }
+  if (grid == 0) grid = grid_for(reinterpret_cast<const void*>(update_kernel), kThreads);
   return grid;
 }
 
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s) {
-  integrate_kernel<<<grid > 0 ? grid : integrate_grid_size(), kThreads, 0, s>>>(depth, V, p);
+  static int classify_grid = 0;
+  if (classify_grid == 0) classify_grid = grid_for(reinterpret_cast<const void*>(classify_kernel), kThreads);
+  classify_kernel<<<classify_grid, kThreads, 0, s>>>(depth, V, p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  update_kernel<<<grid > 0 ? grid : integrate_grid_size(), kThreads, 0, s>>>(depth, V, p);
   return cudaGetLastError();
 }
 
