@@ -91,7 +91,7 @@ __device__ __forceinline__ bool sample_bilinear(const float* __restrict__ depth,
 }
 
 // estimateSurfaceNormalBaseCamera (cuda_tsdf_integrator.cu:727-752)
-__device__ bool base_normal_literal(const float* __restrict__ depth, const Params& p, float u, float v, f3& n) {
+__device__ __noinline__ bool base_normal_literal(const float* __restrict__ depth, const Params& p, float u, float v, f3& n) {
   float dl, dr, du, dd;
   if (!sample_bilinear(depth, p, u - 1.0f, v, dl) || !sample_bilinear(depth, p, u + 1.0f, v, dr) ||
       !sample_bilinear(depth, p, u, v - 1.0f, du) || !sample_bilinear(depth, p, u, v + 1.0f, dd)) {
@@ -148,76 +148,98 @@ __device__ __noinline__ bool surface_normal_literal(const float* __restrict__ de
   return norm3(n) > 1e-6f;
 }
 
-// Same function through the 21 distinct samples (valid when the shifted coordinates are exact).
-__device__ __forceinline__ bool surface_normal(const float* __restrict__ depth, const Params& p, float u, float v,
-                                               const float gs[3], f3& normal) {
+// The 21 distinct sample positions (i, j) of the fast path, i, j in [0, 4] (offsets i-2, j-2): row 0 and row 4
+// hold columns 1..3, rows 1..3 all five columns.
+__device__ __forceinline__ void sample_position(int s, int& i, int& j) {
+  if (s < 3) {
+    j = 0;
+    i = s + 1;
+  } else if (s < 18) {
+    j = 1 + (s - 3) / 5;
+    i = (s - 3) % 5;
+  } else {
+    j = 4;
+    i = s - 17;
+  }
+}
+__device__ __forceinline__ int sample_slot(int i, int j) {
+  return j == 0 ? i - 1 : (j == 4 ? 17 + i : 3 + (j - 1) * 5 + i);
+}
+__device__ __forceinline__ float pick5(int k, float a0, float a1, float a2, float a3, float a4) {
+  return k == 0 ? a0 : (k == 1 ? a1 : (k == 2 ? a2 : (k == 3 ? a3 : a4)));
+}
+
+constexpr int kSamples = 21;
+
+// Per-thread scratch of the fast path: backprojected sample points, [component][sample][thread] so a warp's
+// accesses hit 32 consecutive words.
+template <int kT>
+struct NormalScratch {
+  float x[kSamples][kT];
+  float y[kSamples][kT];
+  float z[kSamples][kT];
+};
+
+// estimateSurfaceNormalCamera through the 21 distinct samples, valid when the shifted coordinates are exact
+// (checked by the caller).  Rolled loops keep the code small; the samples live in shared memory.
+template <int kT>
+__device__ __forceinline__ bool surface_normal_fast(const float* __restrict__ depth, const Params& p, float u, float v,
+                                                    const float gs[3], NormalScratch<kT>& S, int t, f3& normal) {
   const float um1 = u - 1.0f, up1 = u + 1.0f, vm1 = v - 1.0f, vp1 = v + 1.0f;
-  if (!(um1 + 1.0f == u && up1 - 1.0f == u && vm1 + 1.0f == v && vp1 - 1.0f == v)) {
-    return surface_normal_literal(depth, p, u, v, gs, normal);
-  }
-  const float U[5] = {um1 - 1.0f, um1, u, up1, up1 + 1.0f};
-  const float V[5] = {vm1 - 1.0f, vm1, v, vp1, vp1 + 1.0f};
-  // backprojected sample points P[j][i] at (U[i], V[j]); the 4 corners are never used
-  f3 P[5][5];
+  const float U0 = um1 - 1.0f, U4 = up1 + 1.0f, V0 = vm1 - 1.0f, V4 = vp1 + 1.0f;
   uint32_t ok = 0U;
-#pragma unroll
-  for (int j = 0; j < 5; ++j) {
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-      if ((i == 0 || i == 4) && (j == 0 || j == 4)) continue;
-      float d;
-      if (sample_bilinear(depth, p, U[i], V[j], d)) {
-        ok |= 1U << (j * 5 + i);
-        P[j][i] = backproject(U[i], V[j], d, p);
-      } else {
-        P[j][i] = mk3(0.0f, 0.0f, 0.0f);
-      }
+#pragma unroll 1
+  for (int s = 0; s < kSamples; ++s) {
+    int i, j;
+    sample_position(s, i, j);
+    const float su = pick5(i, U0, um1, u, up1, U4);
+    const float sv = pick5(j, V0, vm1, v, vp1, V4);
+    float d;
+    if (sample_bilinear(depth, p, su, sv, d)) {
+      ok |= 1U << s;
+      const f3 q = backproject(su, sv, d, p);
+      S.x[s][t] = q.x;
+      S.y[s][t] = q.y;
+      S.z[s][t] = q.z;
     }
   }
-  // base normals at (i, j) in [1, 3]^2
-  f3 N[3][3];
-  uint32_t nok = 0U;
-#pragma unroll
-  for (int j = 1; j <= 3; ++j) {
-#pragma unroll
-    for (int i = 1; i <= 3; ++i) {
-      const uint32_t need = (1U << (j * 5 + i - 1)) | (1U << (j * 5 + i + 1)) | (1U << ((j - 1) * 5 + i)) |
-                            (1U << ((j + 1) * 5 + i));
-      N[j - 1][i - 1] = mk3(0.0f, 0.0f, 0.0f);
-      if ((ok & need) == need) {
-        const f3 n = normalize3(cross3(sub3(P[j + 1][i], P[j - 1][i]), sub3(P[j][i + 1], P[j][i - 1])));
-        if (norm3(n) > 1e-6f) {
-          N[j - 1][i - 1] = n;
-          nok |= 1U << ((j - 1) * 3 + (i - 1));
-        }
-      }
-    }
-  }
-  if (!(nok & (1U << 4))) return false;
-  if (!(ok & (1U << 12))) return false;
-  const f3 cp = P[2][2];
+  auto point = [&](int i, int j) {
+    const int s = sample_slot(i, j);
+    return mk3(S.x[s][t], S.y[s][t], S.z[s][t]);
+  };
+  auto valid = [&](int i, int j) { return (ok >> sample_slot(i, j)) & 1U; };
+  // base normal at (i, j): estimateSurfaceNormalBaseCamera on the cached samples
+  auto base = [&](int i, int j, f3& n) -> bool {
+    if (!(valid(i - 1, j) && valid(i + 1, j) && valid(i, j - 1) && valid(i, j + 1))) return false;
+    n = normalize3(cross3(sub3(point(i, j + 1), point(i, j - 1)), sub3(point(i + 1, j), point(i - 1, j))));
+    return norm3(n) > 1e-6f;
+  };
+  f3 cn;
+  if (!base(2, 2, cn)) return false;
+  if (!valid(2, 2)) return false;
+  const f3 cp = point(2, 2);
   const float cd = cp.z;
-  const f3 cn = orient_toward_camera(N[1][1], cp);
+  cn = orient_toward_camera(cn, cp);
   f3 wsum = mk3(0.0f, 0.0f, 0.0f);
   float ws = 0.0f;
-#pragma unroll
-  for (int j = 1; j <= 3; ++j) {
-#pragma unroll
-    for (int i = 1; i <= 3; ++i) {
-      if (!(nok & (1U << ((j - 1) * 3 + (i - 1))))) continue;
-      if (!(ok & (1U << (j * 5 + i)))) continue;
-      const f3 sp = P[j][i];
-      const f3 sn = orient_toward_camera(N[j - 1][i - 1], sp);
-      const float delta = sp.z - cd;
-      const float cosine = clampf(dot3(cn, sn), -1.0f, 1.0f);
-      const float ad = 1.0f - cosine;
-      const int r2 = (i - 2) * (i - 2) + (j - 2) * (j - 2);
-      const float w = gs[r2] * gaussian(delta * delta, p.normal_k_range) * gaussian(ad * ad, p.normal_k_angular);
-      wsum.x += sn.x * w;
-      wsum.y += sn.y * w;
-      wsum.z += sn.z * w;
-      ws += w;
-    }
+#pragma unroll 1
+  for (int k = 0; k < 9; ++k) {
+    const int i = 1 + k % 3, j = 1 + k / 3;
+    f3 sn;
+    if (!base(i, j, sn)) continue;
+    if (!valid(i, j)) continue;
+    const f3 sp = point(i, j);
+    sn = orient_toward_camera(sn, sp);
+    const float delta = sp.z - cd;
+    const float cosine = clampf(dot3(cn, sn), -1.0f, 1.0f);
+    const float ad = 1.0f - cosine;
+    const int r2 = (i - 2) * (i - 2) + (j - 2) * (j - 2);
+    const float w = pick5(r2, gs[0], gs[1], gs[2], 0.0f, 0.0f) * gaussian(delta * delta, p.normal_k_range) *
+                    gaussian(ad * ad, p.normal_k_angular);
+    wsum.x += sn.x * w;
+    wsum.y += sn.y * w;
+    wsum.z += sn.z * w;
+    ws += w;
   }
   if (ws <= 1e-6f) {
     normal = cn;
@@ -229,6 +251,16 @@ __device__ __forceinline__ bool surface_normal(const float* __restrict__ depth, 
   if (norm3(n) <= 1e-6f) n = cn;
   normal = n;
   return norm3(n) > 1e-6f;
+}
+
+template <int kT>
+__device__ __forceinline__ bool surface_normal(const float* __restrict__ depth, const Params& p, float u, float v,
+                                               const float gs[3], NormalScratch<kT>& S, int t, f3& normal) {
+  const float um1 = u - 1.0f, up1 = u + 1.0f, vm1 = v - 1.0f, vp1 = v + 1.0f;
+  if (!(um1 + 1.0f == u && up1 - 1.0f == u && vm1 + 1.0f == v && vp1 - 1.0f == v)) {
+    return surface_normal_literal(depth, p, u, v, gs, normal);
+  }
+  return surface_normal_fast<kT>(depth, p, u, v, gs, S, t, normal);
 }
 
 // computeObservationWeightGpu (cuda_tsdf_integrator.cu:429-450)
@@ -390,14 +422,15 @@ __device__ __forceinline__ bool voxel_prefix(const float* __restrict__ depth, co
 
 // Rest of integrateActiveBlocksKernel (:879-899): bilateral normal, observation weight, surface point,
 // direction bin.  Returns the direction bin, or -1 when the reference skips the voxel.
+template <int kT>
 __device__ __forceinline__ int voxel_observation(const float* __restrict__ depth, const Params& p, f3 pc, float u,
-                                                 float v, float d, const float gs[3], float& sc, f3& spw, f3& nw,
-                                                 float& obs) {
+                                                 float v, float d, const float gs[3], NormalScratch<kT>& S, int t,
+                                                 float& sc, f3& spw, f3& nw, float& obs) {
   const float sd = d - pc.z;
   const f3 view = normalize3(pc);
   float view_w = 1.0f;
   f3 nc = mul3(view, -1.0f);
-  if (surface_normal(depth, p, u, v, gs, nc)) view_w = fabsf(dot3(nc, view));
+  if (surface_normal<kT>(depth, p, u, v, gs, S, t, nc)) view_w = fabsf(dot3(nc, view));
   obs = observation_weight(p, d, sd, view_w);
   if (obs <= 0.0f) return -1;
   spw = xform_point(p.T_wc, backproject(u, v, d, p));
@@ -441,8 +474,11 @@ __global__ void __launch_bounds__(kThreads) classify_kernel(const float* __restr
 
 // Pass 2: the layer update of the active voxels, one voxel per thread, no CTA barriers: the expensive
 // bilateral normal runs only where the reference runs it, and slow voxels no longer hold a whole block.
-__global__ void __launch_bounds__(kThreads, 2) update_kernel(const float* __restrict__ depth, const Volume V,
-                                                             const Params p) {
+constexpr int kUpdateThreads = 128;
+
+__global__ void __launch_bounds__(kUpdateThreads) update_kernel(const float* __restrict__ depth, const Volume V,
+                                                                const Params p) {
+  __shared__ NormalScratch<kUpdateThreads> S;
   const uint32_t n = V.counters->active_voxels;
   const uint32_t padded = (n + 31U) & ~31U;
   const int lane = threadIdx.x & 31;
@@ -462,7 +498,7 @@ __global__ void __launch_bounds__(kThreads, 2) update_kernel(const float* __rest
       voxel_prefix(depth, p, bk, li, pc, u, v, d);
       float sc = 0.0f, obs = 0.0f;
       f3 spw = mk3(0.0f, 0.0f, 0.0f), nw = spw;
-      const int dir = voxel_observation(depth, p, pc, u, v, d, gs, sc, spw, nw, obs);
+      const int dir = voxel_observation<kUpdateThreads>(depth, p, pc, u, v, d, gs, S, threadIdx.x, sc, spw, nw, obs);
       if (dir >= 0) {
         float4* base = V.layers + layer_index(b, dir, li, 0);
         float4 L0 = base[0], L1 = base[1], L2 = base[2];
@@ -498,7 +534,7 @@ static int grid_for(const void* kernel, int threads) {
 
 int integrate_grid_size() {
   static int grid = 0;
-  if (grid == 0) grid = grid_for(reinterpret_cast<const void*>(update_kernel), kThreads);
+  if (grid == 0) grid = grid_for(reinterpret_cast<const void*>(update_kernel), kUpdateThreads);
   return grid;
 }
 
@@ -508,7 +544,7 @@ cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& 
   classify_kernel<<<classify_grid, kThreads, 0, s>>>(depth, V, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  update_kernel<<<grid > 0 ? grid : integrate_grid_size(), kThreads, 0, s>>>(depth, V, p);
+  update_kernel<<<grid > 0 ? grid : integrate_grid_size(), kUpdateThreads, 0, s>>>(depth, V, p);
   return cudaGetLastError();
 }
 
