@@ -48,7 +48,8 @@ typedef enum vh_status {
   VH_ERR_KEY_RANGE = 5,         /* a block coordinate left the 21-bit packed range (reference: CudaActiveBlockAllocationFallback) */
   VH_ERR_HASH_FULL = 6,         /* no free hash slot (reference: CudaActiveBlockAllocationFallback) */
   VH_ERR_POOL_FULL = 7,         /* more blocks than vh_params.max_blocks */
-  VH_ERR_BUFFER_TOO_SMALL = 8   /* caller's output buffer is smaller than the result; *count holds the size */
+  VH_ERR_BUFFER_TOO_SMALL = 8,  /* caller's output buffer is smaller than the result; *count holds the size */
+  VH_ERR_CAPACITY = 9           /* request larger than the fixed scratch of vh_allocate_static_scratch */
 } vh_status;
 
 typedef struct vh_volume vh_volume;
@@ -127,6 +128,20 @@ vh_status vh_allocate(vh_volume* volume, const float* depth, int32_t depth_on_de
 /* Unique block keys (3 int32 each, unordered, host memory) the last vh_integrate / vh_allocate frame touched
  * -- the reference's per-frame active block list.  *count receives the number of keys.  Synchronises. */
 vh_status vh_visible_block_keys(vh_volume* volume, int32_t* keys_out, size_t max_keys, size_t* count, void* stream);
+
+/* vh_allocate without any allocation -- no counterpart in the reference.  For callers that cannot call
+ * cudaMalloc once running (real-time tracking loops that forbid allocator calls, applications whose own pool
+ * owns the whole device): the same keys-only allocation as vh_allocate, with the hash table, visible list and
+ * counters in a fixed static device array of the library (20 MiB per GPU, held until the process exits).
+ * depth: device memory, width*height floats; keys_out: device memory, 3 int32 per key (NULL: count only).
+ * Limit: at most 32,768 sampled pixels per call (e.g. 640x480 at allocation_stride 4, 181x181 at stride 1);
+ * larger requests return VH_ERR_CAPACITY.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call before any stream capture.
+ * Every call clears the table it uses, so no state carries over, but all calls share the one array:
+ * calls that overlap on the same GPU race.  Synchronises the stream. */
+vh_status vh_allocate_static_scratch(const float* depth, const vh_intrinsics* K, const vh_pose* T_wc,
+                                     float voxel_size, float truncation_distance, int32_t allocation_stride,
+                                     int32_t* keys_out, size_t max_keys, size_t* count, void* stream);
 
 /* The depth bilateral filter alone (device buffers), with the volume's algorithm constants. */
 vh_status vh_filter_depth(vh_volume* volume, const float* depth_in, float* depth_out, const vh_intrinsics* K,

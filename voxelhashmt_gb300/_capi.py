@@ -23,6 +23,7 @@ VH_ERR_KEY_RANGE = 5
 VH_ERR_HASH_FULL = 6
 VH_ERR_POOL_FULL = 7
 VH_ERR_BUFFER_TOO_SMALL = 8
+VH_ERR_CAPACITY = 9
 
 BLOCK_BYTES = 512 * 6 * 3 * 16
 
@@ -70,7 +71,7 @@ class VhError(RuntimeError):
 def _status_name(status):
     names = {0: "VH_OK", 1: "VH_ERR_INVALID_ARGUMENT", 2: "VH_ERR_CUDA", 3: "VH_ERR_NO_DEVICE",
              4: "VH_ERR_OUT_OF_MEMORY", 5: "VH_ERR_KEY_RANGE", 6: "VH_ERR_HASH_FULL", 7: "VH_ERR_POOL_FULL",
-             8: "VH_ERR_BUFFER_TOO_SMALL"}
+             8: "VH_ERR_BUFFER_TOO_SMALL", 9: "VH_ERR_CAPACITY"}
     return names.get(status, "VH_STATUS_%d" % status)
 
 
@@ -104,6 +105,8 @@ _SIGNATURES = {
     "vh_recount_observed_voxels": (C.c_int, [_vp, _u64p, _vp]),
     "vh_frame_stats_get": (C.c_int, [_vp, C.POINTER(VhFrameStats), _vp]),
     "vh_export_blocks": (C.c_int, [_vp, C.c_uint64, C.c_uint64, _ip, _vp, C.c_int32, _vp]),
+    "vh_allocate_static_scratch": (C.c_int, [_vp, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_float, C.c_float,
+                                             C.c_int32, _vp, C.c_size_t, _szp, _vp]),
     "vh_profile_enable": (C.c_int, [_vp, C.c_int32]),
     "vh_profile_read": (C.c_int, [_vp, C.POINTER(C.c_double), _u64p]),
     "vh_render_depth": (C.c_int, [_vp, C.c_int32, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_uint32,

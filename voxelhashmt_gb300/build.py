@@ -19,7 +19,7 @@ LIB = os.path.join(LIBDIR, "libvoxelhash_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["vh_filter.cu", "vh_alloc.cu", "vh_integrate.cu", "vh_mesh.cu", "vh_misc.cu", "vh_render.cu",
-           "vh_capi.cpp"]
+           "vh_static_scratch.cu", "vh_capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
          "-I", CSRC, "-I", INCLUDE]

@@ -223,6 +223,7 @@ const char* vh_status_string(vh_status s) {
     case VH_ERR_HASH_FULL: return "block hash table full";
     case VH_ERR_POOL_FULL: return "block pool full";
     case VH_ERR_BUFFER_TOO_SMALL: return "output buffer too small";
+    case VH_ERR_CAPACITY: return "request larger than the fixed static scratch";
   }
   return "unknown status";
 }
