@@ -113,6 +113,20 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_throughput(pixels, ms, device="cpu"):
+    """Whole-job rate of independent replicas: the pixels of all ranks over the slowest rank's time.
+    Returns (Mpix/s, max ms).  Works on any initialised process group (NCCL on GPUs, gloo in tests)."""
+    import torch
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        mx = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        tot = torch.tensor([float(pixels)], dtype=torch.float64, device=device)
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        ms, pixels = float(mx.item()), float(tot.item())
+    return pixels / (ms / 1000.0) / 1e6, ms
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -267,12 +281,7 @@ def run_gb300(args):
     stage_ms, nprof = vol.read_profile()
     vol.profile(False)
     fstats = vol.frame_stats()
-    # updated voxels per frame for the roofline: re-run the last frame's counter read
-    t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    max_ms = float(t.item())
-    value = world * args.steps * px / (max_ms / 1000.0) / 1e6
+    value, max_ms = replica_throughput(args.steps * px, total_ms, device="cuda")
 
     # marching cubes over the whole volume
     nblocks = vol.block_count()

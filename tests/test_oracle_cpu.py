@@ -1,0 +1,180 @@
+"""CPU tests of the parity oracle: pinned against the reference's own outputs.
+
+* against the committed fixtures in tests/golden/ (made by tests/golden/make_golden.py from the reference
+  build): filtered depth, allocated block keys, every voxel byte (SHA-256), observed-voxel count and the
+  triangle soup, for the reference CUDA path (emulated on the host) and the reference CPU path;
+* against the live reference build (oracle/_ref/libref.so) where the reference tree is present, on more
+  frames and strides;
+* known-answer tests of the key hash, key packing, octahedral packing and the observation weight;
+* the product's exponential against float64 exp.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def O(oracle_lib):
+    return oracle_lib
+
+
+@pytest.fixture(scope="module")
+def golden_scene():
+    from voxelhashmt_gb300 import scenes
+    g = np.load(os.path.join(GOLDEN, "golden_scene.npz"))
+    w, h, fx, fy, cx, cy = g["intrinsics"]
+    K = scenes.Intrinsics(int(w), int(h), float(fx), float(fy), float(cx), float(cy))
+    poses = [scenes.Pose(p[:9].reshape(3, 3).copy(), p[9:].copy()) for p in g["poses"]]
+    return {"depth": g["depth"], "K": K, "poses": poses, "vs": float(g["voxel_size"]), "trunc": float(g["truncation"])}
+
+
+@pytest.mark.parametrize("flavor_name", ["gpu", "cpu"])
+def test_oracle_matches_reference_fixtures(O, golden_scene, flavor_name):
+    gs = golden_scene
+    ref = np.load(os.path.join(GOLDEN, "golden_%s.npz" % flavor_name))
+    flavor = O.FLAVOR_REF_GPU if flavor_name == "gpu" else O.FLAVOR_REF_CPU
+    cfg = O.config(flavor, O.EXP_LIBM, threads=4)
+    K = gs["K"]
+    d0 = gs["depth"][0]
+    assert np.array_equal(_bits(O.filter_depth(cfg, d0, K)), _bits(ref["filtered0"]))
+    for stride in (1, 2):
+        keys = O.collect_blocks(cfg, d0, K, gs["poses"][0], gs["vs"], gs["trunc"], stride)
+        assert np.array_equal(keys, ref["keys_stride%d" % stride])
+    vol = O.Volume(cfg, gs["vs"], gs["trunc"])
+    for d, P in zip(gs["depth"], gs["poses"]):
+        vol.integrate(d, K, P)
+    keys, vox = O.sort_blocks(*vol.blocks())
+    assert np.array_equal(keys, ref["block_keys"])
+    assert vol.observed_voxels() == int(ref["observed_voxels"])
+    assert hashlib.sha256(np.ascontiguousarray(vox).view(np.uint8).tobytes()).hexdigest() == str(ref["voxel_sha256"])
+    for k, v in zip(ref["fullest_keys"], ref["fullest_voxels"]):
+        i = int(np.nonzero((keys == k).all(axis=1))[0][0])
+        assert np.array_equal(vox[i].view(np.uint32), v)
+    tris = O.canonical_triangles(vol.extract_mesh())
+    assert np.array_equal(_bits(tris), _bits(ref["triangles"]))
+    vol.close()
+
+
+def test_known_answers(O):
+    import ctypes as C
+    kat = np.load(os.path.join(GOLDEN, "golden_kat.npz"))
+    L = O.lib()
+    for k, h, pk, ok in zip(kat["keys"], kat["hashes"], kat["packed"], kat["packable"]):
+        assert L.vo_hash_block_key(*map(int, k)) == int(h)
+        p = C.c_uint64()
+        assert L.vo_pack_block_key(*map(int, k), C.byref(p)) == int(ok)
+        if ok:
+            assert p.value == int(pk)
+    fp = C.POINTER(C.c_float)
+    for n, pg, pc in zip(kat["normals"], kat["pack_gpu"], kat["pack_cpu"]):
+        n = np.ascontiguousarray(n, np.float32)
+        assert O.lib().vo_pack_normal(O.FLAVOR_REF_GPU, n.ctypes.data_as(fp)) == int(pg)
+        assert O.lib().vo_pack_normal(O.FLAVOR_REF_CPU, n.ctypes.data_as(fp)) == int(pc)
+    out = np.zeros(3, np.float32)
+    for name, flavor, mesh in (("unpack_gpu", O.FLAVOR_REF_GPU, 0), ("unpack_gpu_mesh", O.FLAVOR_REF_GPU, 1),
+                               ("unpack_cpu", O.FLAVOR_REF_CPU, 0)):
+        for code, want in zip(kat["codes"], kat[name]):
+            O.lib().vo_unpack_normal(flavor, mesh, int(code), out.ctypes.data_as(fp))
+            assert np.array_equal(_bits(out), _bits(want)), (name, int(code))
+    cfg = O.config(O.FLAVOR_REF_GPU)
+    for a, w in zip(kat["weight_args"], kat["weights"]):
+        got = O.lib().vo_observation_weight(C.byref(cfg), *map(float, a))
+        assert np.float32(got).view(np.uint32) == np.float32(w).view(np.uint32)
+
+
+def test_own_exp_accuracy(O):
+    """vh_expf (product) == vo_expf_own (oracle): within 1 ulp of exp over the arguments the path uses."""
+    L = O.lib()
+    xs = np.concatenate([-np.logspace(-8, np.log10(103.0), 20000), np.linspace(-20.0, 0.0, 20001),
+                         np.linspace(0.0, 80.0, 2001)]).astype(np.float32)
+    got = np.array([L.vo_expf_own(float(x)) for x in xs], np.float32)
+    want = np.exp(xs.astype(np.float64))
+    normal = want > np.float64(np.finfo(np.float32).tiny)
+    ulp = np.spacing(want[normal].astype(np.float32)).astype(np.float64)
+    err = np.abs(got[normal].astype(np.float64) - want[normal]) / ulp
+    assert err.max() <= 1.0, float(err.max())
+    assert L.vo_expf_own(0.0) == 1.0
+    assert L.vo_expf_own(-200.0) == 0.0
+
+
+ref_only = pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libref.so")),
+                              reason="reference build (oracle/_ref) not present on this machine")
+
+
+@ref_only
+@pytest.mark.parametrize("gpu", [True, False])
+def test_oracle_matches_live_reference(O, gpu):
+    """Several frames, strides 1 and 3, both flavours, against the reference compiled from its sources."""
+    from voxelhashmt_gb300 import scenes
+    sc = scenes.orbit_scene(seed=77, frames=10, width=56, height=40, fx=48.5, fy=48.5, cx=27.5, cy=19.5)
+    sc.voxel_size, sc.truncation = 0.02, 0.06
+    K = sc.intrinsics
+    cfg = O.config(O.FLAVOR_REF_GPU if gpu else O.FLAVOR_REF_CPU, O.EXP_LIBM, threads=4)
+    for f, stride in ((1, 1), (6, 3)):
+        d = scenes.render_depth(sc, f)
+        assert np.array_equal(_bits(O.filter_depth(cfg, d, K)), _bits(O.ref_filter(d, K, gpu)))
+        ko = O.collect_blocks(cfg, d, K, sc.poses[f], sc.voxel_size, sc.truncation, stride)
+        kr = O.ref_collect(d, K, sc.poses[f], sc.voxel_size, sc.truncation, stride, gpu)
+        assert np.array_equal(ko, kr)
+    vo = O.Volume(cfg, sc.voxel_size, sc.truncation)
+    vr = O.RefVolume(gpu, sc.voxel_size, sc.truncation)
+    for f in (0, 3, 7):
+        d = scenes.render_depth(sc, f)
+        vo.integrate(d, K, sc.poses[f], 2)
+        vr.integrate(d, K, sc.poses[f], 2)
+    ko, xo = O.sort_blocks(*vo.blocks())
+    kr, xr = O.sort_blocks(*vr.blocks())
+    assert np.array_equal(ko, kr)
+    assert np.array_equal(xo.view(np.uint32), xr.view(np.uint32))
+    assert vo.observed_voxels() == vr.observed_voxels()
+    assert np.array_equal(_bits(O.canonical_triangles(vo.extract_mesh())),
+                          _bits(O.canonical_triangles(vr.extract_mesh())))
+    vr.close()
+    vo.close()
+
+
+@ref_only
+def test_mc_tables_match_reference_header():
+    import re
+    from oracle import build as ob
+    ref = os.path.join(ob.REFERENCE, "include", "tsdfmc", "marching_cubes_tables.h")
+    if not os.path.exists(ref):
+        pytest.skip("reference header not present")
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("gen", os.path.join(os.path.dirname(HERE), "oracle", "gen_mc_tables.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    edge, tri = gen.parse_reference(ref)
+    text = open(os.path.join(os.path.dirname(HERE), "voxelhashmt_gb300", "csrc", "vh_mc_tables.h")).read()
+    body_e = text[text.index("vh_mc_edge_table[256] = {"):text.index("};")]
+    ours_e = [int(x) for x in re.findall(r"-?\d+", body_e.split("{", 1)[1])]
+    body_t = text[text.index("vh_mc_tri_table[256][16] = {"):]
+    ours_t = [int(x) for x in re.findall(r"-?\d+", body_t.split("= {", 1)[1].split("};", 1)[0])]
+    assert ours_e == edge
+    assert ours_t == [v for row in tri for v in row]
+
+
+def test_oracle_parallel_equals_serial(O):
+    """threads > 1 (the CPU baseline's setting) gives the same volume as the literal serial order."""
+    from voxelhashmt_gb300 import scenes
+    sc = scenes.orbit_scene(seed=5, frames=4, width=40, height=30, fx=34.6, fy=34.6, cx=20.0, cy=15.0)
+    sc.voxel_size, sc.truncation = 0.02, 0.06
+    res = []
+    for threads in (1, 4):
+        v = O.Volume(O.config(O.FLAVOR_REF_CPU, O.EXP_LIBM, threads=threads), sc.voxel_size, sc.truncation)
+        for f in range(2):
+            v.integrate(scenes.render_depth(sc, f), sc.intrinsics, sc.poses[f])
+        k, x = O.sort_blocks(*v.blocks())
+        res.append((k, x.view(np.uint32), O.canonical_triangles(v.extract_mesh())))
+        v.close()
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+    assert np.array_equal(_bits(res[0][2]), _bits(res[1][2]))
