@@ -291,6 +291,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   step(cudaMalloc(reinterpret_cast<void**>(&V.layers), std::max<size_t>(nb, 1) * kBlockBytes));
   step(dalloc(&V.block_keys, nb));
   step(dalloc(&V.obs_mask, nb * (vh::kBlockVoxels / 32)));
+  step(dalloc(&V.dir_mask, nb));
   step(dalloc(&V.counters, 1));
   step(cudaMallocHost(reinterpret_cast<void**>(&v->h_counters), sizeof(vh::Counters)));
   step(dalloc(&v->d_scalar, 2));
@@ -300,6 +301,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
     step(cudaMemset(V.slot_stamp, 0, buckets * sizeof(uint32_t)));
     step(cudaMemset(V.layers, 0, std::max<size_t>(nb, 1) * kBlockBytes));
     step(cudaMemset(V.obs_mask, 0, nb * (vh::kBlockVoxels / 32) * sizeof(uint32_t)));
+    step(cudaMemset(V.dir_mask, 0, std::max<size_t>(nb, 1) * sizeof(uint32_t)));
     step(cudaMemset(V.counters, 0, sizeof(vh::Counters)));
     step(cudaDeviceSynchronize());
   }
@@ -326,6 +328,7 @@ void vh_destroy(vh_volume* v) {
   dfree(V.layers);
   dfree(V.block_keys);
   dfree(V.obs_mask);
+  dfree(V.dir_mask);
   dfree(V.counters);
   if (v->h_counters) cudaFreeHost(v->h_counters);
   dfree(v->d_depth_in);
@@ -358,6 +361,7 @@ vh_status vh_reset(vh_volume* v, void* stream) {
   VH_CUDA(v, cudaMemsetAsync(V.slot_stamp, 0, V.capacity * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.layers, 0, used * kBlockBytes, s));
   VH_CUDA(v, cudaMemsetAsync(V.obs_mask, 0, used * (vh::kBlockVoxels / 32) * sizeof(uint32_t), s));
+  VH_CUDA(v, cudaMemsetAsync(V.dir_mask, 0, used * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.counters, 0, sizeof(vh::Counters), s));
   VH_CUDA(v, cudaStreamSynchronize(s));
   v->mesh_triangles = 0;

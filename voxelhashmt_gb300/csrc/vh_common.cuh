@@ -52,6 +52,7 @@ static_assert(sizeof(Counters) == 64, "Counters is read back as one 64-byte copy
 //                                       same dominant direction reads/writes 32 x 48 contiguous bytes
 //   block_keys  int4[max_blocks]        {x, y, z, frame the block was allocated in}
 //   obs_mask    u32[max_blocks][16]     one bit per voxel: any layer observed
+//   dir_mask    u32[max_blocks]         bit d set once any voxel of the block has an observed layer in bin d
 //   visible     u32[capacity]           slots touched by the current frame (unordered)
 //   active      u32[max_blocks * 512]   (block << 9 | voxel) of the current frame's voxels that pass the
 //                                       projection / depth / truncation tests (unordered)
@@ -62,6 +63,7 @@ struct Volume {
   float4* layers;
   int4* block_keys;
   uint32_t* obs_mask;
+  uint32_t* dir_mask;
   uint32_t* visible;
   uint32_t* active;
   Counters* counters;

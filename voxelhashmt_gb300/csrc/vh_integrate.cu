@@ -510,6 +510,8 @@ __global__ void __launch_bounds__(kUpdateThreads) update_kernel(const float* __r
           const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
           const uint32_t bit = 1U << (li & 31);
           if (!(V.obs_mask[w] & bit)) newly = (atomicOr(&V.obs_mask[w], bit) & bit) ? 0U : 1U;
+          const uint32_t dbit = 1U << dir;
+          if (!(V.dir_mask[b] & dbit)) atomicOr(&V.dir_mask[b], dbit);
         }
       }
     }

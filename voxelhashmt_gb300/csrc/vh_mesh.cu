@@ -268,7 +268,7 @@ __device__ __forceinline__ uint32_t block_scan(Shared& S, uint32_t v, int tid) {
 }
 
 template <bool kEmit>
-__global__ void __launch_bounds__(kThreads) mc_kernel(const Volume V, const Params p, uint32_t* __restrict__ counts,
+__global__ void __launch_bounds__(kThreads, 2) mc_kernel(const Volume V, const Params p, uint32_t* __restrict__ counts,
                                                       const unsigned long long* __restrict__ offsets,
                                                       float* __restrict__ tris) {
   __shared__ Shared S;
@@ -285,9 +285,15 @@ __global__ void __launch_bounds__(kThreads) mc_kernel(const Volume V, const Para
     }
     __syncthreads();
     const int gx = bk.x * kBlockSide + lx, gy = bk.y * kBlockSide + ly, gz = bk.z * kBlockSide + lz;
+    // directions with an observed layer anywhere in the block or its +x/+y/+z neighbours; a cell of the
+    // block only has corners there, so in any other direction no cell has a candidate surface
+    uint32_t dirs = 0U;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) dirs |= S.nbr[k] != kInvalidBlock ? V.dir_mask[S.nbr[k]] : 0U;
     uint32_t run = 0U;
     const unsigned long long base = kEmit ? offsets[b] : 0ULL;
     for (int d = 0; d < kDirs; ++d) {
+      if (!(dirs & (1U << d))) continue;  // uniform across the CTA
       stage_direction(S, V, d, tid);
       __syncthreads();
       const uint32_t n = static_cast<uint32_t>(process_cell<false>(S, p, gx, gy, gz, lx, ly, lz, nullptr));
