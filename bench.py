@@ -36,6 +36,9 @@ sys.path.insert(0, ROOT)
 
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 VOXEL_LAYER_BIN_BYTES = 3 * 16  # one direction bin: 3 layers x 16 B
+# DRAM bytes (read + write) per active voxel of update_kernel, from the ncu capture summarised in
+# profiles/update_kernel_room640.md (one launch, 6.55 M active voxels); scaled by the active voxels of a launch
+UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL = (539.49e6 + 267.04e6) / 6.548e6
 
 
 def parse():
@@ -333,12 +336,13 @@ def run_gb300(args):
     integ_ms = stage_ms["integrate"] / max(1, nprof)
     integ_bytes = upd_mean * 2 * VOXEL_LAYER_BIN_BYTES + px * 4
     achieved = integ_bytes / (integ_ms / 1000.0) / 1e9
-    roofline = {"kernel": "integrate_kernel", "bound": "hbm", "achieved": round(achieved, 2),
+    roofline = {"kernel": "update_kernel", "bound": "hbm", "achieved": round(achieved, 2),
                 "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 5),
-                "traffic": None, "peak_source": pk["source"],
+                "traffic": int(UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL * act_mean), "peak_source": pk["source"],
                 "algorithmic_bytes_per_launch": int(integ_bytes),
-                "note": "updated voxels x 96 B (read+write of one 3-layer bin) + 4 B/px depth; the kernel is "
-                        "bound by FP32/ALU work of the per-voxel bilateral normal, not by HBM"}
+                "note": "integrate stage (classify + update kernels) time; algorithmic bytes = updated voxels x 96 B "
+                        "(read+write of one 3-layer bin) + 4 B/px depth; traffic = ncu DRAM bytes per active voxel x "
+                        "active voxels; bound by issue slots of the per-voxel bilateral normal, not by HBM"}
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_budget_s > 0:
@@ -364,7 +368,6 @@ def run_gb300(args):
             "mc_blocks_per_s": round(mc_blocks_per_s, 1), "mc_ms": round(mc_ms, 3), "mc_triangles": n_tri.value,
             "blocks": nblocks, "observed_voxels": observed,
             "stage_ms_per_frame": {k: round(v / max(1, nprof), 4) for k, v in stage_ms.items()},
-            "stream_mpix_per_s_no_flush": round(world * args.steps * px / wall / 1e6, 3),
             "e2e": {"value": round(e2e_value, 3), "unit": "Mpix/s", "h2d_bytes_per_step": px * 4,
                     "d2h_bytes_per_step": 64},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,

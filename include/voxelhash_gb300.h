@@ -14,6 +14,7 @@
  *   vh_block_count          gpuVolumeCacheBlockCount           src/cuda_tsdf_integrator.h:22
  *   vh_observed_voxel_count gpuVolumeCacheObservedVoxelCount   src/cuda_tsdf_integrator.h:23
  *   vh_export_blocks        gpuVolumeCacheBlockKeys / gpuVolumeCacheFlatBlocks  src/cuda_tsdf_integrator.h:24-25
+ *   vh_import_blocks        VoxelHashTSDF::applyFlatBlocks     include/tsdfmc/voxel_hash_tsdf.h:183-188
  *   vh_filter_depth         estimateDepthNormalsKernel + bilateralFilterDepthKernel (src/cuda_tsdf_integrator.cu:629-725)
  *
  * Conventions (include/tsdfmc/math_types.h:180-244): depth is row-major float32 metres, index v*width+u,
@@ -170,6 +171,13 @@ vh_status vh_frame_stats_get(vh_volume* volume, vh_frame_stats* stats, void* str
  * per block), into host memory (out_on_device = 0) or device memory (1).  Either pointer may be NULL. */
 vh_status vh_export_blocks(vh_volume* volume, uint64_t first, uint64_t count, int32_t* keys, void* voxels,
                            int32_t out_on_device, void* stream);
+
+/* applyFlatBlocks (include/tsdfmc/voxel_hash_tsdf.h:183-188): inserts or overwrites blocks given as keys
+ * (3 int32 each, unique within one call) and voxels in the reference Voxel layout (512 x 6 x 3 x 16 bytes per
+ * block), read from host (in_on_device = 0) or device memory (1): the inverse of vh_export_blocks, for
+ * checkpoint / resume and for meshing volumes built elsewhere.  Recounts the observed voxels.  Synchronises. */
+vh_status vh_import_blocks(vh_volume* volume, const int32_t* keys, const void* voxels, uint64_t count,
+                           int32_t in_on_device, void* stream);
 
 /* Stage timing with CUDA events (the reference times its stages with steady_clock, src/main.cpp:424-452).
  * While enabled, vh_integrate brackets its filter, allocation and update kernels with events on the call's

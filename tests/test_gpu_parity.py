@@ -285,3 +285,30 @@ def test_room_frame_full_resolution_properties(env):
     tris = backend.extract_mesh_cuda(vol)
     assert tris.shape[0] > 1000 and np.all(np.isfinite(tris))
     vol.close()
+
+
+def test_checkpoint_export_import_round_trip(env, small_orbit):
+    """applyFlatBlocks-style resume: export -> import into a fresh volume is the identity on blocks, counts
+    and mesh, and integrating the next frame on both volumes gives the same result."""
+    backend, O = env
+    from voxelhashmt_gb300 import scenes
+    sc = small_orbit
+    a = _volume(backend, sc)
+    for f in (0, 5, 10):
+        backend.integrate_depth_frame_cuda(a, backend.DepthFrame(sc.intrinsics, scenes.render_depth(sc, f)), sc.poses[f])
+    keys, vox = a.export_blocks()
+    b = _volume(backend, sc)
+    b.import_blocks(keys, vox)
+    kb, vb = b.export_blocks()
+    assert np.array_equal(keys, kb) and np.array_equal(vox, vb)
+    assert b.observed_voxel_count() == a.observed_voxel_count() == a.recount_observed_voxels()
+    assert np.array_equal(_bits(backend.extract_mesh_cuda(a)), _bits(backend.extract_mesh_cuda(b)))
+    d = scenes.render_depth(sc, 15)
+    for v in (a, b):
+        backend.integrate_depth_frame_cuda(v, backend.DepthFrame(sc.intrinsics, d), sc.poses[15])
+    ka, va = O.sort_blocks(*a.export_blocks())
+    kb, vb = O.sort_blocks(*b.export_blocks())
+    assert np.array_equal(ka, kb) and np.array_equal(va, vb)
+    assert a.observed_voxel_count() == b.observed_voxel_count()
+    a.close()
+    b.close()

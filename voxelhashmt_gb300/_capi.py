@@ -107,6 +107,7 @@ _SIGNATURES = {
     "vh_export_blocks": (C.c_int, [_vp, C.c_uint64, C.c_uint64, _ip, _vp, C.c_int32, _vp]),
     "vh_allocate_static_scratch": (C.c_int, [_vp, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_float, C.c_float,
                                              C.c_int32, _vp, C.c_size_t, _szp, _vp]),
+    "vh_import_blocks": (C.c_int, [_vp, _ip, _vp, C.c_uint64, C.c_int32, _vp]),
     "vh_profile_enable": (C.c_int, [_vp, C.c_int32]),
     "vh_profile_read": (C.c_int, [_vp, C.POINTER(C.c_double), _u64p]),
     "vh_render_depth": (C.c_int, [_vp, C.c_int32, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_uint32,

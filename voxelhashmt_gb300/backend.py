@@ -172,6 +172,15 @@ class VoxelHashTSDF:
         return keys, vox
 
 
+    def import_blocks(self, keys, voxels):
+        """applyFlatBlocks: insert/overwrite blocks from (keys (N,3) int32, voxels in the reference layout as
+        returned by export_blocks); keys must be unique.  Checkpoint / resume."""
+        k = np.ascontiguousarray(keys, np.int32).reshape(-1, 3)
+        v = np.ascontiguousarray(voxels).view(np.uint32).reshape(k.shape[0], -1)
+        _capi.check(_capi.lib().vh_import_blocks(self.handle, k.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                 C.c_void_p(v.ctypes.data), k.shape[0], 0, None), self.handle)
+
+
 class TsdfIntegrationBackend:
     """reconstruction_backend.h:18-42, GPU only."""
 

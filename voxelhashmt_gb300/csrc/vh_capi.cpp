@@ -32,6 +32,7 @@ struct vh_volume {
   int* d_keys = nullptr;
   float4* d_export = nullptr;
   int* d_export_keys = nullptr;
+  uint32_t* d_import_idx = nullptr;
   size_t export_capacity = 0;  // blocks
   bool profile = false;
   std::vector<cudaEvent_t> event_pool;
@@ -340,6 +341,7 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_keys);
   dfree(v->d_export);
   dfree(v->d_export_keys);
+  dfree(v->d_import_idx);
   for (auto& fr : v->profiled)
     for (cudaEvent_t e : fr) cudaEventDestroy(e);
   for (cudaEvent_t e : v->event_pool) cudaEventDestroy(e);
@@ -612,6 +614,32 @@ vh_status vh_export_blocks(vh_volume* v, uint64_t first, uint64_t count, int32_t
   }
   VH_CUDA(v, cudaStreamSynchronize(s));
   return VH_OK;
+}
+
+vh_status vh_import_blocks(vh_volume* v, const int32_t* keys, const void* voxels, uint64_t count, int32_t on_device,
+                           void* stream) {
+  if (!v || (count && (!keys || !voxels))) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_import_blocks: bad argument");
+  if (v->dev.max_blocks == 0) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_import_blocks: keys-only volume");
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  if (!v->d_export) {
+    VH_CUDA(v, cudaMalloc(reinterpret_cast<void**>(&v->d_export), kExportChunk * kBlockBytes));
+    VH_CUDA(v, dalloc(&v->d_export_keys, 3 * kExportChunk));
+    v->export_capacity = kExportChunk;
+  }
+  if (!v->d_import_idx) VH_CUDA(v, dalloc(&v->d_import_idx, kExportChunk));
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  for (uint64_t done = 0; done < count; done += kExportChunk) {
+    const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(kExportChunk, count - done));
+    VH_CUDA(v, cudaMemcpyAsync(v->d_export_keys, keys + 3 * done, 3 * n * sizeof(int32_t), kind, s));
+    VH_CUDA(v, cudaMemcpyAsync(v->d_export, static_cast<const char*>(voxels) + done * kBlockBytes, n * kBlockBytes,
+                               kind, s));
+    VH_CUDA(v, vh::launch_import(v->dev, v->d_export_keys, v->d_export, n, v->d_import_idx, s));
+  }
+  VH_CUDA(v, vh::launch_recount(v->dev, v->d_scalar + 1, s));
+  VH_CUDA(v, cudaMemcpyAsync(&v->dev.counters->observed_voxels, v->d_scalar + 1, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToDevice, s));
+  return vh_synchronize(v, stream);
 }
 
 vh_status vh_render_depth(const float* prims, int32_t n_prims, const vh_intrinsics* K, const vh_pose* T_wc,

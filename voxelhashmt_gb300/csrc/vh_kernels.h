@@ -36,6 +36,9 @@ cudaError_t launch_visible_keys(const Volume& V, int* keys, cudaStream_t s);
 cudaError_t launch_export(const Volume& V, uint32_t first, uint32_t count, int* keys, float4* voxels,
                           cudaStream_t s);
 
+// import blocks in the reference layout (insert or overwrite); idx: n scratch words
+cudaError_t launch_import(const Volume& V, const int* keys, const float4* voxels, uint32_t n, uint32_t* idx,
+                          cudaStream_t s);
 // synthetic depth for the analytic benchmark scenes (prims: n x 10 floats, device memory)
 cudaError_t launch_render(const float* prims, int n_prims, const Params& p, uint32_t seed, uint32_t frame,
                           float sigma_z2, float dropout, float max_depth, float* out, cudaStream_t s);

@@ -64,3 +64,87 @@ cudaError_t launch_export(const Volume& V, uint32_t first, uint32_t count, int* 
 }
 
 }  // namespace vh
+
+namespace vh {
+namespace {
+
+// Insert (or find) each imported key; idx[i] receives its pool block (kInvalidBlock when the pool is full).
+__global__ void import_keys_kernel(const Volume V, const int* __restrict__ keys, uint32_t n, uint32_t* __restrict__ idx) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int x = keys[3 * i], y = keys[3 * i + 1], z = keys[3 * i + 2];
+    unsigned long long key;
+    idx[i] = kInvalidBlock;
+    if (!pack_block_key(x, y, z, key)) {
+      atomicOr(&V.counters->error, kErrKeyRange);
+      continue;
+    }
+    uint32_t slot = hash_block_key(x, y, z) & V.mask;
+    bool done = false;
+    for (uint32_t probe = 0; probe < V.capacity && !done; ++probe) {
+      unsigned long long cur = atomicCAS(&V.slot_keys[slot], kEmptyKey, key);
+      if (cur == kEmptyKey) {
+        uint32_t b = atomicAdd(&V.counters->num_blocks, 1U);
+        if (b >= V.max_blocks) {
+          atomicOr(&V.counters->error, kErrPoolFull);
+          b = kInvalidBlock;
+        } else {
+          V.block_keys[b] = make_int4(x, y, z, 0);
+        }
+        V.slot_block[slot] = b;
+        idx[i] = b;
+        done = true;
+      } else if (cur == key) {
+        idx[i] = V.slot_block[slot];
+        done = true;
+      } else {
+        slot = (slot + 1U) & V.mask;
+      }
+    }
+    if (!done) atomicOr(&V.counters->error, kErrHashFull);
+  }
+}
+
+// reference Voxel layout [i][li][d][l] -> pool (direction-major); rebuilds the observed and direction masks
+__global__ void __launch_bounds__(256) import_voxels_kernel(const Volume V, const float4* __restrict__ voxels,
+                                                            uint32_t n, const uint32_t* __restrict__ idx) {
+  for (size_t t = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; t < static_cast<size_t>(n) * kBlockVoxels;
+       t += static_cast<size_t>(gridDim.x) * blockDim.x) {
+    const uint32_t i = static_cast<uint32_t>(t / kBlockVoxels);
+    const int li = static_cast<int>(t % kBlockVoxels);
+    const uint32_t b = idx[i];
+    bool obs = false;
+    uint32_t dirs = 0U;
+    if (b != kInvalidBlock) {
+      const float4* src = voxels + t * kDirs * kLayers;
+      for (int d = 0; d < kDirs; ++d) {
+        for (int l = 0; l < kLayers; ++l) {
+          const float4 L = src[d * kLayers + l];
+          V.layers[layer_index(b, d, li, l)] = L;
+          if (L.x > 0.0f) {
+            obs = true;
+            dirs |= 1U << d;
+          }
+        }
+      }
+    }
+    const unsigned ballot = __ballot_sync(__activemask(), obs);
+    if (b != kInvalidBlock) {
+      if ((li & 31) == 0) V.obs_mask[static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5)] = ballot;
+      if (dirs) atomicOr(&V.dir_mask[b], dirs);
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_import(const Volume& V, const int* keys, const float4* voxels, uint32_t n, uint32_t* idx,
+                          cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  import_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(V, keys, n, idx);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  import_voxels_kernel<<<152 * 8, 256, 0, s>>>(V, voxels, n, idx);
+  return cudaGetLastError();
+}
+
+}  // namespace vh
