@@ -24,6 +24,8 @@ struct vh_volume {
   float* d_depth_filtered = nullptr;
   size_t depth_capacity = 0;  // pixels
   uint32_t* d_mc_counts = nullptr;
+  uint32_t* d_mc_dir_totals = nullptr;
+  uint8_t* d_mc_cell_counts = nullptr;
   unsigned long long* d_mc_offsets = nullptr;
   unsigned long long* d_scalar = nullptr;  // [0] mesh total, [1] recount
   float* d_tris = nullptr;
@@ -335,6 +337,8 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_depth_in);
   dfree(v->d_depth_filtered);
   dfree(v->d_mc_counts);
+  dfree(v->d_mc_dir_totals);
+  dfree(v->d_mc_cell_counts);
   dfree(v->d_mc_offsets);
   dfree(v->d_scalar);
   dfree(v->d_tris);
@@ -508,11 +512,13 @@ vh_status vh_extract_mesh(vh_volume* v, float iso, size_t* triangle_count, void*
   if (!v->d_mc_counts) {
     VH_CUDA(v, dalloc(&v->d_mc_counts, v->dev.max_blocks));
     VH_CUDA(v, dalloc(&v->d_mc_offsets, v->dev.max_blocks));
+    VH_CUDA(v, dalloc(&v->d_mc_dir_totals, static_cast<size_t>(v->dev.max_blocks) * vh::kDirs));
+    VH_CUDA(v, dalloc(&v->d_mc_cell_counts, static_cast<size_t>(v->dev.max_blocks) * vh::kDirs * vh::kBlockVoxels));
   }
   vh_intrinsics K{1, 1, 1.0f, 1.0f, 0.0f, 0.0f};
   vh::Params p = make_params(v, &K, nullptr, 1);
   p.iso = iso;
-  VH_CUDA(v, vh::launch_mc_count(v->dev, p, v->d_mc_counts, s));
+  VH_CUDA(v, vh::launch_mc_count(v->dev, p, v->d_mc_counts, v->d_mc_dir_totals, v->d_mc_cell_counts, s));
   VH_CUDA(v, vh::launch_mc_scan(v->dev, v->d_mc_counts, v->d_mc_offsets, v->d_scalar, s));
   unsigned long long total = 0;
   VH_CUDA(v, cudaMemcpyAsync(&total, v->d_scalar, sizeof(total), cudaMemcpyDeviceToHost, s));
@@ -524,7 +530,10 @@ vh_status vh_extract_mesh(vh_volume* v, float iso, size_t* triangle_count, void*
     VH_CUDA(v, dalloc(&v->d_tris, cap * 9));
     v->tri_capacity = cap;
   }
-  if (total > 0) VH_CUDA(v, vh::launch_mc_emit(v->dev, p, v->d_mc_offsets, v->d_tris, s));
+  if (total > 0) {
+    VH_CUDA(v, vh::launch_mc_emit(v->dev, p, v->d_mc_counts, v->d_mc_dir_totals, v->d_mc_cell_counts,
+                                  v->d_mc_offsets, v->d_tris, s));
+  }
   VH_CUDA(v, cudaStreamSynchronize(s));
   v->mesh_triangles = static_cast<size_t>(total);
   *triangle_count = v->mesh_triangles;

@@ -219,7 +219,7 @@ __device__ __forceinline__ bool surface_normal_fast(const float* __restrict__ de
   if (!valid(2, 2)) return false;
   const f3 cp = point(2, 2);
   const float cd = cp.z;
-  cn = orient_toward_camera(cn, cp);
+  cn = orient_unit_toward_camera(cn, cp);
   f3 wsum = mk3(0.0f, 0.0f, 0.0f);
   float ws = 0.0f;
 #pragma unroll 1
@@ -229,7 +229,7 @@ __device__ __forceinline__ bool surface_normal_fast(const float* __restrict__ de
     if (!base(i, j, sn)) continue;
     if (!valid(i, j)) continue;
     const f3 sp = point(i, j);
-    sn = orient_toward_camera(sn, sp);
+    sn = orient_unit_toward_camera(sn, sp);
     const float delta = sp.z - cd;
     const float cosine = clampf(dot3(cn, sn), -1.0f, 1.0f);
     const float ad = 1.0f - cosine;
@@ -320,8 +320,8 @@ __device__ __forceinline__ uint32_t pack_normal(f3 raw) {
 
 // unpackNormalOctahedralGpu (:258-294)
 __device__ __forceinline__ f3 unpack_normal(uint32_t packed) {
-  f3 n = mk3(static_cast<float>(packed & 0xffffU) / 65535.0f * 2.0f - 1.0f,
-             static_cast<float>((packed >> 16U) & 0xffffU) / 65535.0f * 2.0f - 1.0f, 0.0f);
+  f3 n = mk3(div65535(static_cast<float>(packed & 0xffffU)) * 2.0f - 1.0f,
+             div65535(static_cast<float>((packed >> 16U) & 0xffffU)) * 2.0f - 1.0f, 0.0f);
   n.z = 1.0f - fabsf(n.x) - fabsf(n.y);
   if (n.z < 0.0f) {
     const float fx = (1.0f - fabsf(n.y)) * sign_not_zero(n.x);

@@ -19,12 +19,14 @@ cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, c
 // directional multi-layer update of every visible block; grid = persistent CTAs
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s);
 int integrate_grid_size();
-// marching cubes over all allocated blocks: pass 1 writes per-block triangle counts,
-// the scan turns them into offsets (+ total), pass 2 writes triangles (9 floats each)
-cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, cudaStream_t s);
+// marching cubes over all allocated blocks: pass 1 writes per-block, per-direction and per-cell triangle
+// counts, the scan turns the block counts into offsets (+ total), pass 2 writes triangles (9 floats each)
+cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, uint32_t* dir_totals,
+                            uint8_t* cell_counts, cudaStream_t s);
 cudaError_t launch_mc_scan(const Volume& V, const uint32_t* counts, unsigned long long* offsets,
                            unsigned long long* total, cudaStream_t s);
-cudaError_t launch_mc_emit(const Volume& V, const Params& p, const unsigned long long* offsets, float* tris,
+cudaError_t launch_mc_emit(const Volume& V, const Params& p, const uint32_t* counts, const uint32_t* dir_totals,
+                           const uint8_t* cell_counts, const unsigned long long* offsets, float* tris,
                            cudaStream_t s);
 int mc_grid_size();
 // full recount of observed voxels (any layer weight > 0) over the pool

@@ -6,8 +6,9 @@
 // it resolves its 7 (+x, +y, +z) neighbour blocks once through the persistent hash, then for each of the 6
 // directions stages that direction's bin of the 9x9x9 voxel region (block + one-voxel halo) in shared
 // memory with the octahedral normals decoded once per layer, and every thread processes one cell from shared
-// memory.  Pass 1 writes the per-block triangle count, a scan turns counts into offsets, pass 2 recomputes
-// and writes each block's triangles at its offset: the output is deterministic (block, direction, cell,
+// memory.  Pass 1 records every cell's triangle count, a scan turns the block totals into offsets, and pass 2
+// re-stages only the blocks and directions that produce triangles and evaluates only the cells with a non-zero
+// count, writing each block's triangles at its offset: the output is deterministic (block, direction, cell,
 // cluster, table order) and needs no atomics.
 //
 // Per cell the arithmetic is the reference's collectSurfaceClusters / loadCubeForSurface /
@@ -43,8 +44,8 @@ struct Shared {
 
 // unpackNormalOctahedralGpu of the mesh extractor (:237-257): degenerate -> (0,0,1)
 __device__ __forceinline__ f3 unpack_normal_mesh(uint32_t packed) {
-  f3 n = mk3(static_cast<float>(packed & 0xffffU) / 65535.0f * 2.0f - 1.0f,
-             static_cast<float>((packed >> 16U) & 0xffffU) / 65535.0f * 2.0f - 1.0f, 0.0f);
+  f3 n = mk3(div65535(static_cast<float>(packed & 0xffffU)) * 2.0f - 1.0f,
+             div65535(static_cast<float>((packed >> 16U) & 0xffffU)) * 2.0f - 1.0f, 0.0f);
   n.z = 1.0f - fabsf(n.x) - fabsf(n.y);
   if (n.z < 0.0f) {
     const float fx = (1.0f - fabsf(n.y)) * (n.x >= 0.0f ? 1.0f : -1.0f);
@@ -267,10 +268,36 @@ __device__ __forceinline__ uint32_t block_scan(Shared& S, uint32_t v, int tid) {
   return r;
 }
 
-template <bool kEmit>
-__global__ void __launch_bounds__(kThreads, 2) mc_kernel(const Volume V, const Params p, uint32_t* __restrict__ counts,
-                                                      const unsigned long long* __restrict__ offsets,
-                                                      float* __restrict__ tris) {
+// sum of one value per thread over the CTA (S.total)
+__device__ __forceinline__ void block_sum(Shared& S, uint32_t v, int tid) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffU, v, o);
+  if ((tid & 31) == 0) S.warp_sums[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) {
+    uint32_t w = tid < kThreads / 32 ? S.warp_sums[tid] : 0U;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffU, w, o);
+    if (tid == 0) S.total = w;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void load_neighbours(Shared& S, const Volume& V, uint32_t b, const int4& bk, int tid) {
+  __syncthreads();  // previous block's readers are done with S.nbr / S.plane
+  if (tid < 8) {
+    S.nbr[tid] = tid == 0 ? b : lookup_block(V, bk.x + (tid & 1), bk.y + ((tid >> 1) & 1), bk.z + (tid >> 2));
+  }
+  __syncthreads();
+}
+
+// Pass 1: every cell of every direction with an observed layer in the block's neighbourhood; stores the
+// cell's triangle count (cell_counts, one byte: at most 5 triangles x 24 clusters), the per-direction totals
+// and the block total.
+__global__ void __launch_bounds__(kThreads, 2) mc_count_kernel(const Volume V, const Params p,
+                                                               uint32_t* __restrict__ counts,
+                                                               uint32_t* __restrict__ dir_totals,
+                                                               uint8_t* __restrict__ cell_counts) {
   __shared__ Shared S;
   const int tid = threadIdx.x;
   for (int i = tid; i < 256 * 16; i += kThreads) S.tri[i / 16][i % 16] = vh_mc_tri_table[i / 16][i % 16];
@@ -279,32 +306,62 @@ __global__ void __launch_bounds__(kThreads, 2) mc_kernel(const Volume V, const P
   const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
   for (uint32_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
     const int4 bk = V.block_keys[b];
-    __syncthreads();  // previous block's readers are done with S.nbr / S.plane
-    if (tid < 8) {
-      S.nbr[tid] = tid == 0 ? b : lookup_block(V, bk.x + (tid & 1), bk.y + ((tid >> 1) & 1), bk.z + (tid >> 2));
-    }
-    __syncthreads();
-    const int gx = bk.x * kBlockSide + lx, gy = bk.y * kBlockSide + ly, gz = bk.z * kBlockSide + lz;
+    load_neighbours(S, V, b, bk, tid);
     // directions with an observed layer anywhere in the block or its +x/+y/+z neighbours; a cell of the
     // block only has corners there, so in any other direction no cell has a candidate surface
     uint32_t dirs = 0U;
 #pragma unroll
     for (int k = 0; k < 8; ++k) dirs |= S.nbr[k] != kInvalidBlock ? V.dir_mask[S.nbr[k]] : 0U;
+    const int gx = bk.x * kBlockSide + lx, gy = bk.y * kBlockSide + ly, gz = bk.z * kBlockSide + lz;
     uint32_t run = 0U;
-    const unsigned long long base = kEmit ? offsets[b] : 0ULL;
     for (int d = 0; d < kDirs; ++d) {
-      if (!(dirs & (1U << d))) continue;  // uniform across the CTA
-      stage_direction(S, V, d, tid);
-      __syncthreads();
-      const uint32_t n = static_cast<uint32_t>(process_cell<false>(S, p, gx, gy, gz, lx, ly, lz, nullptr));
-      const uint32_t prefix = block_scan(S, n, tid);
-      if (kEmit && n > 0U) {
-        process_cell<true>(S, p, gx, gy, gz, lx, ly, lz, tris + (base + run + prefix) * 9ULL);
+      uint32_t total = 0U;
+      if (dirs & (1U << d)) {  // uniform across the CTA
+        stage_direction(S, V, d, tid);
+        __syncthreads();
+        const uint32_t n = static_cast<uint32_t>(process_cell<false>(S, p, gx, gy, gz, lx, ly, lz, nullptr));
+        cell_counts[(static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + tid] = static_cast<uint8_t>(n);
+        block_sum(S, n, tid);
+        total = S.total;
+        __syncthreads();  // S.total / S.plane reused by the next direction
       }
-      run += S.total;
-      __syncthreads();  // S.total / S.plane reused by the next direction
+      if (tid == 0) dir_totals[static_cast<size_t>(b) * kDirs + d] = total;
+      run += total;
     }
-    if (!kEmit && tid == 0) counts[b] = run;
+    if (tid == 0) counts[b] = run;
+  }
+}
+
+// Pass 2: only blocks and directions that produce triangles are staged again, and only the cells whose
+// pass-1 count is non-zero are evaluated, writing at offset + direction run + exclusive scan of the counts.
+__global__ void __launch_bounds__(kThreads, 2) mc_emit_kernel(const Volume V, const Params p,
+                                                              const uint32_t* __restrict__ counts,
+                                                              const uint32_t* __restrict__ dir_totals,
+                                                              const uint8_t* __restrict__ cell_counts,
+                                                              const unsigned long long* __restrict__ offsets,
+                                                              float* __restrict__ tris) {
+  __shared__ Shared S;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 256 * 16; i += kThreads) S.tri[i / 16][i % 16] = vh_mc_tri_table[i / 16][i % 16];
+  for (int i = tid; i < 256; i += kThreads) S.edge[i] = vh_mc_edge_table[i];
+  const uint32_t nblocks = min(V.counters->num_blocks, V.max_blocks);
+  const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
+  for (uint32_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+    if (counts[b] == 0U) continue;  // uniform
+    const int4 bk = V.block_keys[b];
+    load_neighbours(S, V, b, bk, tid);
+    const int gx = bk.x * kBlockSide + lx, gy = bk.y * kBlockSide + ly, gz = bk.z * kBlockSide + lz;
+    unsigned long long run = offsets[b];
+    for (int d = 0; d < kDirs; ++d) {
+      const uint32_t total = dir_totals[static_cast<size_t>(b) * kDirs + d];
+      if (total == 0U) continue;  // uniform
+      stage_direction(S, V, d, tid);
+      const uint32_t n = cell_counts[(static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + tid];
+      const uint32_t prefix = block_scan(S, n, tid);  // its barriers also publish the staged direction
+      if (n > 0U) process_cell<true>(S, p, gx, gy, gz, lx, ly, lz, tris + (run + prefix) * 9ULL);
+      run += total;
+      __syncthreads();  // S.plane / S.warp_sums reused by the next direction
+    }
   }
 }
 
@@ -357,14 +414,15 @@ int mc_grid_size() {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_kernel<true>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_count_kernel, kThreads, 0);
     grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
   }
   return grid;
 }
 
-cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, cudaStream_t s) {
-  mc_kernel<false><<<mc_grid_size(), kThreads, 0, s>>>(V, p, counts, nullptr, nullptr);
+cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, uint32_t* dir_totals,
+                            uint8_t* cell_counts, cudaStream_t s) {
+  mc_count_kernel<<<mc_grid_size(), kThreads, 0, s>>>(V, p, counts, dir_totals, cell_counts);
   return cudaGetLastError();
 }
 
@@ -374,9 +432,10 @@ cudaError_t launch_mc_scan(const Volume& V, const uint32_t* counts, unsigned lon
   return cudaGetLastError();
 }
 
-cudaError_t launch_mc_emit(const Volume& V, const Params& p, const unsigned long long* offsets, float* tris,
+cudaError_t launch_mc_emit(const Volume& V, const Params& p, const uint32_t* counts, const uint32_t* dir_totals,
+                           const uint8_t* cell_counts, const unsigned long long* offsets, float* tris,
                            cudaStream_t s) {
-  mc_kernel<true><<<mc_grid_size(), kThreads, 0, s>>>(V, p, nullptr, offsets, tris);
+  mc_emit_kernel<<<mc_grid_size(), kThreads, 0, s>>>(V, p, counts, dir_totals, cell_counts, offsets, tris);
   return cudaGetLastError();
 }
 
