@@ -175,7 +175,9 @@ vh_status vh_export_blocks(vh_volume* volume, uint64_t first, uint64_t count, in
 /* applyFlatBlocks (include/tsdfmc/voxel_hash_tsdf.h:183-188): inserts or overwrites blocks given as keys
  * (3 int32 each, unique within one call) and voxels in the reference Voxel layout (512 x 6 x 3 x 16 bytes per
  * block), read from host (in_on_device = 0) or device memory (1): the inverse of vh_export_blocks, for
- * checkpoint / resume and for meshing volumes built elsewhere.  Recounts the observed voxels.  Synchronises. */
+ * checkpoint / resume and for meshing volumes built elsewhere.  New blocks take pool slots in no particular
+ * order (the export order of the result may differ from the input order).  Recounts the observed voxels.
+ * Synchronises. */
 vh_status vh_import_blocks(vh_volume* volume, const int32_t* keys, const void* voxels, uint64_t count,
                            int32_t in_on_device, void* stream);
 
