@@ -34,6 +34,7 @@ __constant__ int c_edge_corners[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}
 
 struct Shared {
   float4 plane[3][kStaged];  // {n.x, n.y, n.z, plane_offset} per layer
+  float cand[kMaxCand][kThreads];  // per-thread candidate keys, then cluster centres (thread = fast index)
   uint8_t valid[3][kStaged];
   int8_t tri[256][16];
   uint16_t edge[256];
@@ -98,7 +99,7 @@ __device__ __forceinline__ f3 interp(f3 p0, f3 p1, float v0, float v1, float iso
 
 // One cell of one direction: returns its triangle count; with kEmit writes them to out (9 floats each).
 template <bool kEmit>
-__device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, int gz, int lx, int ly, int lz,
+__device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, int gz, int lx, int ly, int lz, int t,
                             float* __restrict__ out) {
   const float vs = p.voxel_size;
   const f3 cc = mk3((static_cast<float>(gx) + 1.0f) * vs, (static_cast<float>(gy) + 1.0f) * vs,
@@ -107,42 +108,46 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
 #pragma unroll
   for (int k = 0; k < 8; ++k) si[k] = staged_index(lx + c_corner[k][0], ly + c_corner[k][1], lz + c_corner[k][2]);
 
-  // collectSurfaceClusters (:439-507)
-  float cand[kMaxCand];
+  // collectSurfaceClusters (:439-507); candidates in shared memory, column `t` of S.cand
+  float* cand = const_cast<float*>(&S.cand[0][0]) + t;
   int nc = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
 #pragma unroll
     for (int l = 0; l < kLayers; ++l) {
-      if (S.valid[l][si[k]]) cand[nc++] = plane_sd(S.plane[l][si[k]], cc);
+      if (S.valid[l][si[k]]) {
+        cand[nc * kThreads] = plane_sd(S.plane[l][si[k]], cc);
+        ++nc;
+      }
     }
   }
   if (nc == 0) return 0;
-  for (int i = 1; i < nc; ++i) {
-    const float x = cand[i];
+  for (int i = 1; i < nc; ++i) {  // insertion sort (:264-274)
+    const float x = cand[i * kThreads];
     int j = i - 1;
-    while (j >= 0 && cand[j] > x) {
-      cand[j + 1] = cand[j];
+    while (j >= 0 && cand[j * kThreads] > x) {
+      cand[(j + 1) * kThreads] = cand[j * kThreads];
       --j;
     }
-    cand[j + 1] = x;
+    cand[(j + 1) * kThreads] = x;
   }
+  // greedy clustering with running means; centre c is written to slot c <= i after slot i has been read,
+  // and only the last cluster's size is ever used
   const float tol = p.extract_tol;
-  float centers[kMaxCand];
-  int sizes[kMaxCand];
   int ncl = 0;
+  int last_size = 0;
   for (int i = 0; i < nc; ++i) {
-    const float key = cand[i];
-    if (ncl == 0 || fabsf(key - centers[ncl - 1]) > tol) {
-      centers[ncl] = key;
-      sizes[ncl] = 1;
+    const float key = cand[i * kThreads];
+    if (ncl == 0 || fabsf(key - cand[(ncl - 1) * kThreads]) > tol) {
+      cand[ncl * kThreads] = key;
+      last_size = 1;
       ++ncl;
       continue;
     }
     const int last = ncl - 1;
-    const int cnt = sizes[last];
-    centers[last] = (centers[last] * static_cast<float>(cnt) + key) / static_cast<float>(cnt + 1);
-    sizes[last] = cnt + 1;
+    cand[last * kThreads] = (cand[last * kThreads] * static_cast<float>(last_size) + key) /
+                            static_cast<float>(last_size + 1);
+    last_size += 1;
   }
 
   f3 pos[8];
@@ -154,7 +159,7 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
   }
   int total = 0;
   for (int ci = 0; ci < ncl; ++ci) {
-    const float key = centers[ci];
+    const float key = cand[ci * kThreads];
     // loadCubeForSurface + selectClosestLayerForSurfaceGpu (:276-303, :509-551)
     float val[8];
     uint32_t mask = 0U;
@@ -298,7 +303,8 @@ __global__ void __launch_bounds__(kThreads, 2) mc_count_kernel(const Volume V, c
                                                                uint32_t* __restrict__ counts,
                                                                uint32_t* __restrict__ dir_totals,
                                                                uint8_t* __restrict__ cell_counts) {
-  __shared__ Shared S;
+  extern __shared__ __align__(16) unsigned char mc_smem[];
+  Shared& S = *reinterpret_cast<Shared*>(mc_smem);
   const int tid = threadIdx.x;
   for (int i = tid; i < 256 * 16; i += kThreads) S.tri[i / 16][i % 16] = vh_mc_tri_table[i / 16][i % 16];
   for (int i = tid; i < 256; i += kThreads) S.edge[i] = vh_mc_edge_table[i];
@@ -319,7 +325,7 @@ __global__ void __launch_bounds__(kThreads, 2) mc_count_kernel(const Volume V, c
       if (dirs & (1U << d)) {  // uniform across the CTA
         stage_direction(S, V, d, tid);
         __syncthreads();
-        const uint32_t n = static_cast<uint32_t>(process_cell<false>(S, p, gx, gy, gz, lx, ly, lz, nullptr));
+        const uint32_t n = static_cast<uint32_t>(process_cell<false>(S, p, gx, gy, gz, lx, ly, lz, tid, nullptr));
         cell_counts[(static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + tid] = static_cast<uint8_t>(n);
         block_sum(S, n, tid);
         total = S.total;
@@ -340,7 +346,8 @@ __global__ void __launch_bounds__(kThreads, 2) mc_emit_kernel(const Volume V, co
                                                               const uint8_t* __restrict__ cell_counts,
                                                               const unsigned long long* __restrict__ offsets,
                                                               float* __restrict__ tris) {
-  __shared__ Shared S;
+  extern __shared__ __align__(16) unsigned char mc_smem[];
+  Shared& S = *reinterpret_cast<Shared*>(mc_smem);
   const int tid = threadIdx.x;
   for (int i = tid; i < 256 * 16; i += kThreads) S.tri[i / 16][i % 16] = vh_mc_tri_table[i / 16][i % 16];
   for (int i = tid; i < 256; i += kThreads) S.edge[i] = vh_mc_edge_table[i];
@@ -358,7 +365,7 @@ __global__ void __launch_bounds__(kThreads, 2) mc_emit_kernel(const Volume V, co
       stage_direction(S, V, d, tid);
       const uint32_t n = cell_counts[(static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + tid];
       const uint32_t prefix = block_scan(S, n, tid);  // its barriers also publish the staged direction
-      if (n > 0U) process_cell<true>(S, p, gx, gy, gz, lx, ly, lz, tris + (run + prefix) * 9ULL);
+      if (n > 0U) process_cell<true>(S, p, gx, gy, gz, lx, ly, lz, tid, tris + (run + prefix) * 9ULL);
       run += total;
       __syncthreads();  // S.plane / S.warp_sums reused by the next direction
     }
@@ -414,7 +421,9 @@ int mc_grid_size() {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_count_kernel, kThreads, 0);
+    cudaFuncSetAttribute(mc_count_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(Shared));
+    cudaFuncSetAttribute(mc_emit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, sizeof(Shared));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_count_kernel, kThreads, sizeof(Shared));
     grid = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
   }
   return grid;
@@ -422,7 +431,7 @@ int mc_grid_size() {
 
 cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, uint32_t* dir_totals,
                             uint8_t* cell_counts, cudaStream_t s) {
-  mc_count_kernel<<<mc_grid_size(), kThreads, 0, s>>>(V, p, counts, dir_totals, cell_counts);
+  mc_count_kernel<<<mc_grid_size(), kThreads, sizeof(Shared), s>>>(V, p, counts, dir_totals, cell_counts);
   return cudaGetLastError();
 }
 
@@ -435,7 +444,8 @@ cudaError_t launch_mc_scan(const Volume& V, const uint32_t* counts, unsigned lon
 cudaError_t launch_mc_emit(const Volume& V, const Params& p, const uint32_t* counts, const uint32_t* dir_totals,
                            const uint8_t* cell_counts, const unsigned long long* offsets, float* tris,
                            cudaStream_t s) {
-  mc_emit_kernel<<<mc_grid_size(), kThreads, 0, s>>>(V, p, counts, dir_totals, cell_counts, offsets, tris);
+  mc_emit_kernel<<<mc_grid_size(), kThreads, sizeof(Shared), s>>>(V, p, counts, dir_totals, cell_counts, offsets,
+                                                                  tris);
   return cudaGetLastError();
 }
 
