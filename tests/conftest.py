@@ -41,3 +41,26 @@ def small_orbit():
                             cx=32.0, cy=24.0)
     sc.voxel_size, sc.truncation = 0.02, 0.06
     return sc
+
+
+@pytest.fixture(scope="session")
+def reference_demo(product_lib):
+    """The reference's main.cpp + reconstruction_backend.cpp, unchanged, linked with the adapter
+    (voxelhashmt_gb300/adapter) and libvoxelhash_gb300.so; built where the reference tree is present."""
+    import subprocess
+    from oracle import build as ob
+    if not ob.reference_available():
+        pytest.skip("reference tree not present")
+    ref = ob.REFERENCE
+    out_dir = os.path.join(ROOT, "oracle", "_ref")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "tsdf_demo_gb300")
+    libdir = os.path.join(ROOT, "voxelhashmt_gb300", "_lib")
+    cmd = ["g++", "-std=c++17", "-O1", "-w", "-DTSDFMC_HAVE_CUDA=1",
+           "-I", os.path.join(ref, "include"), "-I", os.path.join(ref, "src"), "-I", os.path.join(ROOT, "include"),
+           os.path.join(ref, "src", "main.cpp"), os.path.join(ref, "src", "reconstruction_backend.cpp"),
+           os.path.join(ROOT, "voxelhashmt_gb300", "adapter", "tsdfmc_gb300_adapter.cpp"),
+           "-L", libdir, "-lvoxelhash_gb300", "-Wl,-rpath," + libdir, "-o", exe]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-3000:]
+    return exe

@@ -10,28 +10,9 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _reference_root():
-    from oracle import build as ob
-    return ob.REFERENCE if ob.reference_available() else None
-
-
 @pytest.fixture(scope="module")
-def demo(product_lib):
-    ref = _reference_root()
-    if ref is None:
-        pytest.skip("reference tree not present")
-    out_dir = os.path.join(ROOT, "oracle", "_ref")
-    os.makedirs(out_dir, exist_ok=True)
-    exe = os.path.join(out_dir, "tsdf_demo_gb300")
-    libdir = os.path.join(ROOT, "voxelhashmt_gb300", "_lib")
-    cmd = ["g++", "-std=c++17", "-O1", "-w", "-DTSDFMC_HAVE_CUDA=1",
-           "-I", os.path.join(ref, "include"), "-I", os.path.join(ref, "src"), "-I", os.path.join(ROOT, "include"),
-           os.path.join(ref, "src", "main.cpp"), os.path.join(ref, "src", "reconstruction_backend.cpp"),
-           os.path.join(ROOT, "voxelhashmt_gb300", "adapter", "tsdfmc_gb300_adapter.cpp"),
-           "-L", libdir, "-lvoxelhash_gb300", "-Wl,-rpath," + libdir, "-o", exe]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    assert res.returncode == 0, res.stderr[-3000:]
-    return exe
+def demo(reference_demo):
+    return reference_demo
 
 
 def test_reference_demo_links_against_the_gb300_library(demo):

@@ -162,6 +162,9 @@ def test_mesh_bit_exact_and_deterministic(env, small_orbit):
     assert np.array_equal(_bits(again), _bits(got)), "two extractions of the same volume differ"
     dev = backend.extract_mesh_cuda(vol, device_out="cuda")
     assert np.array_equal(_bits(dev.cpu().numpy()), _bits(got))
+    from voxelhashmt_gb300 import mesh_io
+    verts, faces = mesh_io.weld(got)
+    assert 0 < verts.shape[0] < 3 * got.shape[0] and 0 < faces.shape[0] <= got.shape[0]
     vol.close()
 
 
