@@ -49,6 +49,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--form", default="chosen", choices=["chosen", "plain"],
+                    help="form reported as the headline value (the other is measured beside it)")
+    ap.add_argument("--no-chamfer", action="store_true", help="skip the Chamfer distances of the fused meshes")
     return ap.parse_args()
 
 
@@ -226,31 +229,41 @@ def run_reference(args):
     return 0
 
 
-def run_gb300(args):
+# The opt-in "chosen form" (vh_algorithm fields); the plain form is the reference-exact FP32 path.
+CHOSEN_FORM = {"allocation_mode": 1, "fast_math": 1}
+FORM_NOTE = {"plain": "reference allocation rule (3 points x 27 neighbours), exact FP32 update",
+             "chosen": "truncation-band allocation, fast-math FP32 update"}
+
+
+def surface_points(sc, torch, capi, stride=4, every=20, max_points=200_000):
+    """Points of the analytic surface seen by every `every`-th frame: noise-free device renders."""
+    from voxelhashmt_gb300 import metrics
     import ctypes as C
+    K = sc.intrinsics
+    prims = torch.from_numpy(np.ascontiguousarray(sc.prims, np.float32)).cuda()
+    sel = list(range(0, len(sc.poses), every))
+    out = torch.empty((K.height, K.width), dtype=torch.float32, device="cuda")
+    Kc = capi.intrinsics(K)
+    maps = []
+    for f in sel:
+        P = capi.pose(sc.poses[f])
+        capi.check(capi.lib().vh_render_depth(C.c_void_p(prims.data_ptr()), prims.shape[0], C.byref(Kc), C.byref(P),
+                                              sc.seed, f, 0.0, 0.0, sc.max_depth, C.c_void_p(out.data_ptr()),
+                                              C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        maps.append(out.cpu().numpy())
+    return metrics.observed_surface_points(sc, sel, depth_maps=maps, stride=stride, max_points=max_points)
 
-    import torch
 
-    world, rank, local = dist_setup()
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-        torch.cuda.set_device(local)
-    else:
-        torch.cuda.set_device(0)
-    from voxelhashmt_gb300 import _capi, backend
-    from voxelhashmt_gb300 import build as pbuild
-    pbuild.build()
-    sc = make_scene(args.seed + rank, args.warmup + args.steps)
+def fuse_form(args, torch, backend, capi, sc, frames, algo_kw, flush, world):
+    """Time K frames of one form (after W warm-up frames) and extract the mesh; returns the measurements."""
+    import ctypes as C
     K = sc.intrinsics
     px = K.width * K.height
-    frames = render_all(sc, torch, None, _capi)
     stream = torch.cuda.current_stream()
     max_blocks = int(os.environ.get("VH_BENCH_MAX_BLOCKS", "900000"))
     vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=max_blocks,
-                                device=torch.cuda.current_device())
+                                device=torch.cuda.current_device(), algorithm=capi.default_algorithm(**algo_kw))
     bk = backend.TsdfIntegrationBackend("gpu")
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def step(f, sync=False):
         bk.integrate(vol, backend.DepthFrame(K, frames[f].view(-1)), sc.poses[f], 1, stream=stream,
@@ -265,22 +278,18 @@ def run_gb300(args):
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     vol.profile(True)
     vol.read_profile()
-    stats = []
     clocks = ClockSampler(torch.cuda.current_device())
     clocks.start()
     torch.cuda.synchronize()
-    wall0 = time.perf_counter()
     for i in range(args.steps):
         flush.fill_(float(i))
         ev0[i].record(stream)
         step(args.warmup + i)
         ev1[i].record(stream)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
     clock_info = clocks.stop()
     vol.synchronize(stream)
-    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    total_ms = sum(step_ms)
+    total_ms = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1))
     stage_ms, nprof = vol.read_profile()
     vol.profile(False)
     fstats = vol.frame_stats()
@@ -294,15 +303,15 @@ def run_gb300(args):
     m1 = torch.cuda.Event(enable_timing=True)
     m0.record(stream)
     n_tri = C.c_size_t()
-    _capi.check(_capi.lib().vh_extract_mesh(vol.handle, 0.0, C.byref(n_tri), C.c_void_p(stream.cuda_stream)),
-                vol.handle)
+    capi.check(capi.lib().vh_extract_mesh(vol.handle, 0.0, C.byref(n_tri), C.c_void_p(stream.cuda_stream)),
+               vol.handle)
     m1.record(stream)
     torch.cuda.synchronize()
     mc_ms = m0.elapsed_time(m1)
-    mc_blocks_per_s = nblocks / (mc_ms / 1000.0)
+    tris = backend.extract_mesh_cuda(vol)
     observed = vol.observed_voxel_count()
 
-    # per-frame updated voxels (for algorithmic bytes): measure on a replay of the last 8 frames
+    # per-frame updated / active voxels of the last 16 frames (algorithmic bytes), on a replay
     vol.reset(stream)
     upd, act = [], []
     for f in range(args.warmup + args.steps):
@@ -311,8 +320,6 @@ def run_gb300(args):
             st = vol.frame_stats()
             upd.append(st["updated_voxels"])
             act.append(st["active_voxels"])
-    upd_mean = float(np.mean(upd))
-    act_mean = float(np.mean(act))
 
     # end to end through the public API from pinned host memory
     host = torch.empty((len(sc.poses), K.height, K.width), dtype=torch.float32, pin_memory=True)
@@ -330,16 +337,51 @@ def run_gb300(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - e0
     vol.synchronize(stream)
-    e2e_value = world * args.steps * px / e2e_s / 1e6
+    vol.close()
+    return {"value": value, "max_ms": max_ms, "stage_ms": stage_ms, "nprof": nprof, "fstats": fstats,
+            "nblocks": nblocks, "mc_ms": mc_ms, "mc_blocks_per_s": nblocks / (mc_ms / 1000.0),
+            "triangles": n_tri.value, "tris": tris, "observed": observed, "upd_mean": float(np.mean(upd)),
+            "act_mean": float(np.mean(act)), "e2e_value": world * args.steps * px / e2e_s / 1e6,
+            "clocks": clock_info}
+
+
+def run_gb300(args):
+    import torch
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    else:
+        torch.cuda.set_device(0)
+    from voxelhashmt_gb300 import _capi, backend, metrics
+    from voxelhashmt_gb300 import build as pbuild
+    pbuild.build()
+    sc = make_scene(args.seed + rank, args.warmup + args.steps)
+    K = sc.intrinsics
+    px = K.width * K.height
+    frames = render_all(sc, torch, None, _capi)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    forms = {"chosen": CHOSEN_FORM, "plain": {}}
+    res = {name: fuse_form(args, torch, backend, _capi, sc, frames, kw, flush, world) for name, kw in forms.items()}
+    quality = {}
+    if rank == 0 and not args.no_chamfer:
+        pts = surface_points(sc, torch, _capi)
+        for name, r in res.items():
+            quality[name] = {k: (round(v, 4) if isinstance(v, float) else v)
+                             for k, v in metrics.chamfer(r["tris"], sc, pts).items()}
+    head = res[args.form]
+    other = "plain" if args.form == "chosen" else "chosen"
 
     pk = peaks()
-    integ_ms = stage_ms["integrate"] / max(1, nprof)
-    integ_bytes = upd_mean * 2 * VOXEL_LAYER_BIN_BYTES + px * 4
+    integ_ms = head["stage_ms"]["integrate"] / max(1, head["nprof"])
+    integ_bytes = head["upd_mean"] * 2 * VOXEL_LAYER_BIN_BYTES + px * 4
     achieved = integ_bytes / (integ_ms / 1000.0) / 1e9
     roofline = {"kernel": "update_kernel", "bound": "hbm", "achieved": round(achieved, 2),
                 "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 5),
-                "traffic": int(UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL * act_mean), "peak_source": pk["source"],
-                "algorithmic_bytes_per_launch": int(integ_bytes),
+                "traffic": int(UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL * head["act_mean"]),
+                "peak_source": pk["source"], "algorithmic_bytes_per_launch": int(integ_bytes),
                 "note": "integrate stage (classify + update kernels) time; algorithmic bytes = updated voxels x 96 B "
                         "(read+write of one 3-layer bin) + 4 B/px depth; traffic = ncu DRAM bytes per active voxel x "
                         "active voxels; bound by issue slots of the per-voxel bilateral normal, not by HBM"}
@@ -359,24 +401,31 @@ def run_gb300(args):
         except Exception as e:  # the baseline is reported, never the target
             cpu = {"value": None, "unit": "Mpix/s", "cores": 0, "kind": "port", "sample": "failed: %s" % e}
 
+    def summary(r, name):
+        return {"form": FORM_NOTE[name], "integrated_mpix_per_s": round(r["value"], 3),
+                "ms_per_step": round(r["max_ms"] / args.steps, 4), "mc_blocks_per_s": round(r["mc_blocks_per_s"], 1),
+                "mc_ms": round(r["mc_ms"], 3), "mc_triangles": r["triangles"], "blocks": r["nblocks"],
+                "observed_voxels": r["observed"], "e2e_mpix_per_s": round(r["e2e_value"], 3),
+                "stage_ms_per_frame": {k: round(v / max(1, r["nprof"]), 4) for k, v in r["stage_ms"].items()},
+                "visible_blocks_last_frame": r["fstats"]["visible_blocks"],
+                "updated_voxels_per_frame": round(r["upd_mean"]), "active_voxels_per_frame": round(r["act_mean"]),
+                "chamfer": quality.get(name)}
+
     if rank == 0:
         line = {
-            "metric": "integrated_mpix_per_s", "value": round(value, 3), "unit": "Mpix/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(max_ms / args.steps, 4),
+            "metric": "integrated_mpix_per_s", "value": round(head["value"], 3), "unit": "Mpix/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(head["max_ms"] / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_config(sc, args.steps, args.warmup),
-            "mc_blocks_per_s": round(mc_blocks_per_s, 1), "mc_ms": round(mc_ms, 3), "mc_triangles": n_tri.value,
-            "blocks": nblocks, "observed_voxels": observed,
-            "stage_ms_per_frame": {k: round(v / max(1, nprof), 4) for k, v in stage_ms.items()},
-            "e2e": {"value": round(e2e_value, 3), "unit": "Mpix/s", "h2d_bytes_per_step": px * 4,
+            "config": dict(workload_config(sc, args.steps, args.warmup), form=FORM_NOTE[args.form]),
+            "mc_blocks_per_s": round(head["mc_blocks_per_s"], 1),
+            "e2e": {"value": round(head["e2e_value"], 3), "unit": "Mpix/s", "h2d_bytes_per_step": px * 4,
                     "d2h_bytes_per_step": 64},
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
-            "gpu_launches": args.steps * 3,
-            "visible_blocks_last_frame": fstats["visible_blocks"], "updated_voxels_per_frame": round(upd_mean),
-            "active_voxels_per_frame": round(act_mean),
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": head["clocks"],
+            "gpu_launches": args.steps * 4,
+            args.form: summary(head, args.form), other: summary(res[other], other),
+            "speedup_vs_plain": round(res["chosen"]["value"] / res["plain"]["value"], 3),
         }
         print(json.dumps(line))
-    vol.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

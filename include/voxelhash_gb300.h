@@ -87,6 +87,12 @@ typedef struct vh_algorithm {
   float normal_sigma_spatial, normal_sigma_range, normal_sigma_angular;
   float layer_merge_voxel_scale, layer_normal_cosine, layer_extract_voxel_scale;
   float max_voxel_weight, depth_sigma, huber_delta, min_observation_weight, min_view_angle_weight;
+  /* 0 (default): the reference's allocation rule, 3 points x 27-block neighbourhood per pixel;
+   * 1: truncation band, the blocks crossed by each pixel's [depth - trunc, depth + trunc] ray segment. */
+  int32_t allocation_mode;
+  /* 0 (default): plain FP32, bit-reproducible; 1: the update pass with fused multiply-adds and hardware
+   * approximations of exp, division and square root (results differ in the last bits). */
+  int32_t fast_math;
 } vh_algorithm;
 
 /* per-frame statistics of the last integrated/allocated frame */

@@ -44,6 +44,7 @@ class VhAlgorithm(C.Structure):
         ("layer_extract_voxel_scale", C.c_float),
         ("max_voxel_weight", C.c_float), ("depth_sigma", C.c_float), ("huber_delta", C.c_float),
         ("min_observation_weight", C.c_float), ("min_view_angle_weight", C.c_float),
+        ("allocation_mode", C.c_int32), ("fast_math", C.c_int32),
     ]
 
 

@@ -3,7 +3,8 @@
 One nvcc invocation per translation unit (run in parallel), one -gencode (sm_103a), then a shared link.
 Device code is compiled with -fmad=false and host code with -ffp-contract=off so that every a*b+c of
 the reference algorithm rounds twice, as the reference source is written; -prec-div / -prec-sqrt keep
-their IEEE defaults (no --use_fast_math).
+their IEEE defaults.  The one exception is the second compile of vh_integrate.cu (VARIANTS): the opt-in
+fast-math update pass, namespace vh::fast, built with -use_fast_math.
 
 usage: python -m voxelhashmt_gb300.build [--force]
 """
@@ -20,6 +21,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["vh_filter.cu", "vh_alloc.cu", "vh_integrate.cu", "vh_mesh.cu", "vh_misc.cu", "vh_render.cu",
            "vh_static_scratch.cu", "vh_capi.cpp"]
+# second compile of the update pass: the fast-math form (vh::fast), object name and extra device flags
+VARIANTS = [("vh_integrate.cu", "vh_integrate_fast", ["-DVH_FAST_MATH", "-use_fast_math", "-fmad=true"])]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2",
          "-I", CSRC, "-I", INCLUDE]
@@ -52,9 +55,11 @@ def build(force=False, verbose=False):
     os.makedirs(LIBDIR, exist_ok=True)
     objs = []
 
-    def compile_one(src):
-        obj = os.path.join(LIBDIR, os.path.splitext(src)[0] + ".o")
-        cmd = [nvcc(), *ARCH, *FLAGS, "-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj]
+    def compile_one(unit):
+        src, name, extra = unit
+        obj = os.path.join(LIBDIR, name + ".o")
+        flags = [f for f in FLAGS if not (extra and f == "-fmad=false")]
+        cmd = [nvcc(), *ARCH, *flags, *extra, "-x", "cu", "-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         r = _run(cmd)
@@ -62,8 +67,9 @@ def build(force=False, verbose=False):
             sys.stderr.write(r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(compile_one, SOURCES))
+    units = [(src, os.path.splitext(src)[0], []) for src in SOURCES] + VARIANTS
+    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+        objs = list(ex.map(compile_one, units))
     _run([nvcc(), *ARCH, "-shared", "-o", LIB + ".tmp", *objs])
     os.replace(LIB + ".tmp", LIB)
     for o in objs:

@@ -12,7 +12,8 @@
 //      first, atomicCAS only on an empty slot) and, the first time a frame touches a slot (atomicExch on
 //      the slot's frame stamp), appended to the visible list.  New keys take the next pool index.
 // Key packing, the slot hash and linear probing follow cuda_block_allocator.cu:153-196, so the table's
-// key words are the reference's.
+// key words are the reference's.  Params::alloc_mode 1 replaces the 3 x 27-neighbourhood rule by the blocks the
+// +-truncation segment of each pixel's ray crosses (a 3-D DDA): the truncation band only.
 #include "vh_common.cuh"
 #include "vh_kernels.h"
 
@@ -86,6 +87,38 @@ __device__ __forceinline__ int smem_insert(unsigned long long* set, int bits, un
   return -1;
 }
 
+// Blocks crossed by the segment a -> b (3-D DDA over the block grid, Amanatides & Woo 1987), each inserted into
+// the tile set; returns false when a block leaves the packed key range.
+__device__ bool insert_band_blocks(const Volume& V, unsigned long long* s_nset, f3 a, f3 b, float bws, uint32_t frame) {
+  int c[3] = {static_cast<int>(floorf(a.x / bws)), static_cast<int>(floorf(a.y / bws)), static_cast<int>(floorf(a.z / bws))};
+  const int e[3] = {static_cast<int>(floorf(b.x / bws)), static_cast<int>(floorf(b.y / bws)),
+                    static_cast<int>(floorf(b.z / bws))};
+  const float o[3] = {a.x, a.y, a.z};
+  const float d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
+  int st[3];
+  float tmax[3], tdel[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    st[k] = d[k] > 0.0f ? 1 : (d[k] < 0.0f ? -1 : 0);
+    tmax[k] = st[k] != 0 ? ((static_cast<float>(c[k] + (st[k] > 0 ? 1 : 0)) * bws - o[k]) / d[k]) : 3.0e38f;
+    tdel[k] = st[k] != 0 ? bws / fabsf(d[k]) : 3.0e38f;
+  }
+  for (int it = 0; it < 64; ++it) {
+    unsigned long long key;
+    if (!pack_block_key(c[0], c[1], c[2], key)) return false;
+    if (smem_insert(s_nset, 12, key) < 0) insert_global(V, key, frame);
+    if (c[0] == e[0] && c[1] == e[1] && c[2] == e[2]) break;
+    const int k = (tmax[0] < tmax[1]) ? (tmax[0] < tmax[2] ? 0 : 2) : (tmax[1] < tmax[2] ? 1 : 2);
+    if (tmax[k] > 1.0f) break;  // rounding ended the walk one cell short of the end block
+    c[k] += st[k];
+    tmax[k] += tdel[k];
+  }
+  unsigned long long key;  // the end block always belongs to the band (the set drops the duplicate)
+  if (!pack_block_key(e[0], e[1], e[2], key)) return false;
+  if (smem_insert(s_nset, 12, key) < 0) insert_global(V, key, frame);
+  return true;
+}
+
 __global__ void __launch_bounds__(kThreads) alloc_kernel(const float* __restrict__ depth, const Volume V,
                                                          const Params p) {
   __shared__ unsigned long long s_cset[kCenterSlots];
@@ -115,6 +148,11 @@ __global__ void __launch_bounds__(kThreads) alloc_kernel(const float* __restrict
             mk3(pw.x - ray.x * p.truncation, pw.y - ray.y * p.truncation, pw.z - ray.z * p.truncation),
             mk3(pw.x + ray.x * p.truncation, pw.y + ray.y * p.truncation, pw.z + ray.z * p.truncation),
         };
+        if (p.alloc_mode == 1) {
+          if (!insert_band_blocks(V, s_nset, pts[1], pts[2], p.block_world_size, frame)) {
+            atomicOr(&V.counters->error, kErrKeyRange);
+          }
+        } else
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           const int bx = static_cast<int>(floorf(pts[k].x / p.block_world_size));

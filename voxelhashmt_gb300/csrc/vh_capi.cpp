@@ -140,6 +140,7 @@ vh::Params make_params(const vh_volume* v, const vh_intrinsics* K, const vh_pose
   p.min_obs_weight = a.min_observation_weight;
   p.min_view_weight = a.min_view_angle_weight;
   p.iso = 0.0f;
+  p.alloc_mode = a.allocation_mode;
   return p;
 }
 
@@ -213,6 +214,8 @@ void vh_algorithm_default(vh_algorithm* a) {
   a->huber_delta = 0.35f;                   // :20
   a->min_observation_weight = 0.05f;        // :21
   a->min_view_angle_weight = 0.15f;         // :22
+  a->allocation_mode = 0;
+  a->fast_math = 0;
 }
 
 const char* vh_status_string(vh_status s) {
@@ -272,7 +275,8 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   } else {
     vh_algorithm_default(&v->algo);
   }
-  if (v->algo.filter_radius < 0 || v->algo.filter_radius > 2 || v->algo.normal_radius != 1) {
+  if (v->algo.filter_radius < 0 || v->algo.filter_radius > 2 || v->algo.normal_radius != 1 ||
+      v->algo.allocation_mode < 0 || v->algo.allocation_mode > 1 || v->algo.fast_math < 0 || v->algo.fast_math > 1) {
     delete v;
     return VH_ERR_INVALID_ARGUMENT;
   }
@@ -402,7 +406,8 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[2], s));
-  VH_CUDA(v, vh::launch_integrate(v->d_depth_filtered, v->dev, p, 0, s));
+  VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_integrate(v->d_depth_filtered, v->dev, p, 0, s)
+                                : vh::exact::launch_integrate(v->d_depth_filtered, v->dev, p, 0, s));
   if (v->profile) {
     VH_CUDA(v, cudaEventRecord(ev[3], s));
     v->profiled.push_back(std::move(ev));

@@ -98,6 +98,7 @@ struct Params {
   float merge_tol, layer_normal_cos, extract_tol;
   float max_weight, depth_sigma, huber_delta, min_obs_weight, min_view_weight;
   float iso;
+  int alloc_mode;  // 0: reference rule (3 points x 27 neighbours), 1: truncation band (blocks crossed by the band)
 };
 
 struct f3 {
@@ -167,8 +168,13 @@ __device__ __forceinline__ float div65535(float x) {
   return __fmaf_rn(__fmaf_rn(-q, 65535.0f, x), inv, q);
 }
 
-// cuda_tsdf_integrator.cu:173-179
+// cuda_tsdf_integrator.cu:173-179.  The fast-math build of the update pass (VH_FAST_MATH) uses the hardware
+// exponential instead.
+#ifdef VH_FAST_MATH
+__device__ __forceinline__ float gaussian(float sq, float k) { return __expf(-sq * k); }
+#else
 __device__ __forceinline__ float gaussian(float sq, float k) { return vh_expf(-sq * k); }
+#endif
 __device__ __forceinline__ float disc_threshold(const Params& p, float ref) {
   return fmaxf(p.disc_base, p.disc_rel * fmaxf(ref, 0.0f));
 }

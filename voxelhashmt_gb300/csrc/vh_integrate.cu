@@ -16,10 +16,21 @@
 // same for v, which the kernel checks -- the reference evaluates every one of those samples at the same
 // float coordinates, so the 21 distinct samples are computed once and reused; the result is bit-identical.
 // Otherwise (u or v within 2 of a power of two, or below 1) the literal 50-sample sequence runs.
+//
+// The file is compiled twice: as vh::exact (the bit-reproducible FP32 form: -fmad=false, IEEE division and
+// square root, vh_expf) and, with VH_FAST_MATH, as vh::fast (fused multiply-adds, approximate division, square
+// root and exponential; selected per volume by vh_algorithm.fast_math).
 #include "vh_common.cuh"
 #include "vh_kernels.h"
 
+#ifdef VH_FAST_MATH
+#define VH_INTEGRATE_NS fast
+#else
+#define VH_INTEGRATE_NS exact
+#endif
+
 namespace vh {
+namespace VH_INTEGRATE_NS {
 namespace {
 
 constexpr int kThreads = 256;
@@ -550,4 +561,5 @@ cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& 
   return cudaGetLastError();
 }
 
+}  // namespace VH_INTEGRATE_NS
 }  // namespace vh

@@ -16,9 +16,16 @@ cudaError_t launch_depth_normals(const float* in, float* normals, unsigned char*
 cudaError_t launch_begin_frame(Counters* c, cudaStream_t s);
 // allocation: 3 points x 27-neighbourhood per sampled pixel -> persistent hash + visible list
 cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, cudaStream_t s);
-// directional multi-layer update of every visible block; grid = persistent CTAs
+// directional multi-layer update of every visible block; grid = persistent CTAs.  exact: the bit-reproducible
+// FP32 form; fast: the same source compiled with fused multiply-adds and hardware approximations.
+namespace exact {
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s);
 int integrate_grid_size();
+}  // namespace exact
+namespace fast {
+cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s);
+int integrate_grid_size();
+}  // namespace fast
 // marching cubes over all allocated blocks: pass 1 writes per-block, per-direction and per-cell triangle
 // counts, the scan turns the block counts into offsets (+ total), pass 2 writes triangles (9 floats each)
 cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, uint32_t* dir_totals,
