@@ -230,9 +230,9 @@ def run_reference(args):
 
 
 # The opt-in "chosen form" (vh_algorithm fields); the plain form is the reference-exact FP32 path.
-CHOSEN_FORM = {"allocation_mode": 1, "fast_math": 1}
+CHOSEN_FORM = {"allocation_mode": 1, "fast_math": 1, "normal_mode": 1}
 FORM_NOTE = {"plain": "reference allocation rule (3 points x 27 neighbours), exact FP32 update",
-             "chosen": "truncation-band allocation, fast-math FP32 update"}
+             "chosen": "truncation-band allocation, per-pixel normal map, fast-math FP32 update"}
 
 
 def surface_points(sc, torch, capi, stride=4, every=20, max_points=200_000):

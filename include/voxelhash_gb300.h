@@ -93,6 +93,9 @@ typedef struct vh_algorithm {
   /* 0 (default): plain FP32, bit-reproducible; 1: the update pass with fused multiply-adds and hardware
    * approximations of exp, division and square root (results differ in the last bits). */
   int32_t fast_math;
+  /* 0 (default): the reference's bilateral surface normal evaluated at each voxel's projection (50 subpixel
+   * depth samples); 1: the same normal evaluated once per pixel, bilinearly interpolated per voxel. */
+  int32_t normal_mode;
 } vh_algorithm;
 
 /* per-frame statistics of the last integrated/allocated frame */
@@ -156,6 +159,13 @@ vh_status vh_filter_depth(vh_volume* volume, const float* depth_in, float* depth
 /* The filter's per-pixel normals (device buffers): normals 3*W*H floats, valid W*H bytes. */
 vh_status vh_depth_normals(vh_volume* volume, const float* depth_in, float* normals, uint8_t* valid,
                            const vh_intrinsics* K, void* stream);
+
+/* The per-pixel normal map of vh_algorithm.normal_mode 1 (device buffers): estimateSurfaceNormalCamera
+ * (cuda_tsdf_integrator.cu:754-832) at every pixel centre of depth_in, camera frame, as normals[4*W*H] =
+ * (nx, ny, nz, valid 1/0) per pixel; normals 16-byte aligned.  No reference counterpart (the reference
+ * evaluates the normal per voxel). */
+vh_status vh_pixel_normals(vh_volume* volume, const float* depth_in, float* normals, const vh_intrinsics* K,
+                           void* stream);
 
 /* Waits for the stream and returns (then clears) the device-side errors accumulated since the last call. */
 vh_status vh_synchronize(vh_volume* volume, void* stream);

@@ -75,6 +75,9 @@ def lib():
         L.vo_filter_depth.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp]
         L.vo_depth_normals.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp,
                                        C.POINTER(C.c_uint8)]
+        L.vo_surface_normal.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.c_float, C.c_float,
+                                        _fp]
+        L.vo_surface_normal.restype = C.c_int32
         L.vo_collect_blocks.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose),
                                         C.c_float, C.c_float, C.c_int32, _ip, C.c_int64]
         L.vo_collect_blocks.restype = C.c_int64
@@ -152,6 +155,21 @@ def depth_normals(cfg, depth, K):
     lib().vo_depth_normals(C.byref(cfg), dp, C.byref(intrinsics(K)), n.ctypes.data_as(_fp),
                            v.ctypes.data_as(C.POINTER(C.c_uint8)))
     return n, v
+
+
+def pixel_normals(cfg, depth, K):
+    """estimateSurfaceNormalCamera at every pixel centre: normals (H, W, 3) float32, valid (H, W) uint8."""
+    d, dp = _f32(depth)
+    n = np.zeros(d.shape + (3,), np.float32)
+    ok = np.zeros(d.shape, np.uint8)
+    out = np.zeros(3, np.float32)
+    Ki = intrinsics(K)
+    for y in range(d.shape[0]):
+        for x in range(d.shape[1]):
+            if lib().vo_surface_normal(C.byref(cfg), dp, C.byref(Ki), float(x), float(y), out.ctypes.data_as(_fp)):
+                ok[y, x] = 1
+                n[y, x] = out
+    return n, ok
 
 
 def collect_blocks(cfg, depth, K, P, voxel_size, truncation, stride=1):

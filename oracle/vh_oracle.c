@@ -1219,3 +1219,15 @@ int64_t vo_volume_extract_mesh(const vo_volume* vol, float iso, vo_triangle** ou
   *out = all.t;
   return all.n;
 }
+
+/* estimateSurfaceNormalCamera (cuda_tsdf_integrator.cu:754-832) at one image position, for the per-pixel
+ * normal map's parity test: returns 1 and the camera-frame normal, or 0 where the reference fails. */
+int32_t vo_surface_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, float u, float v,
+                          float n[3]) {
+  v3 r = mk(0.0f, 0.0f, 0.0f);
+  const int ok = surface_normal(c, depth, K, u, v, &r);
+  n[0] = r.x;
+  n[1] = r.y;
+  n[2] = r.z;
+  return ok;
+}

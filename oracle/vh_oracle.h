@@ -137,6 +137,8 @@ int64_t vo_volume_extract_mesh(const vo_volume* vol, float iso, vo_triangle** ou
 void vo_free(void* p);
 
 /* small kernels exposed for known-answer tests */
+int32_t vo_surface_normal(const vo_config* cfg, const float* depth, const vo_intrinsics* K, float u, float v,
+                          float n[3]);
 uint32_t vo_pack_normal(int32_t flavor, const float n[3]);
 void vo_unpack_normal(int32_t flavor, int32_t mesh_variant, uint32_t packed, float n[3]);
 uint32_t vo_hash_block_key(int32_t x, int32_t y, int32_t z);

@@ -44,7 +44,7 @@ class VhAlgorithm(C.Structure):
         ("layer_extract_voxel_scale", C.c_float),
         ("max_voxel_weight", C.c_float), ("depth_sigma", C.c_float), ("huber_delta", C.c_float),
         ("min_observation_weight", C.c_float), ("min_view_angle_weight", C.c_float),
-        ("allocation_mode", C.c_int32), ("fast_math", C.c_int32),
+        ("allocation_mode", C.c_int32), ("fast_math", C.c_int32), ("normal_mode", C.c_int32),
     ]
 
 
@@ -98,6 +98,7 @@ _SIGNATURES = {
     "vh_visible_block_keys": (C.c_int, [_vp, _ip, C.c_size_t, _szp, _vp]),
     "vh_filter_depth": (C.c_int, [_vp, _vp, _vp, C.POINTER(VhIntrinsics), _vp]),
     "vh_depth_normals": (C.c_int, [_vp, _vp, _vp, _vp, C.POINTER(VhIntrinsics), _vp]),
+    "vh_pixel_normals": (C.c_int, [_vp, _vp, _vp, C.POINTER(VhIntrinsics), _vp]),
     "vh_synchronize": (C.c_int, [_vp, _vp]),
     "vh_extract_mesh": (C.c_int, [_vp, C.c_float, _szp, _vp]),
     "vh_copy_mesh": (C.c_int, [_vp, _vp, C.c_size_t, C.c_int32, _vp]),

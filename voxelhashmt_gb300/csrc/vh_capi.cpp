@@ -22,6 +22,7 @@ struct vh_volume {
   vh::Counters* h_counters = nullptr;  // pinned mirror for read-back
   float* d_depth_in = nullptr;
   float* d_depth_filtered = nullptr;
+  float4* d_normal_map = nullptr;  // per-pixel normals (vh_algorithm.normal_mode 1)
   size_t depth_capacity = 0;  // pixels
   uint32_t* d_mc_counts = nullptr;
   uint32_t* d_mc_dir_totals = nullptr;
@@ -141,6 +142,7 @@ vh::Params make_params(const vh_volume* v, const vh_intrinsics* K, const vh_pose
   p.min_view_weight = a.min_view_angle_weight;
   p.iso = 0.0f;
   p.alloc_mode = a.allocation_mode;
+  p.normal_mode = a.normal_mode;
   return p;
 }
 
@@ -148,9 +150,11 @@ vh_status ensure_depth(vh_volume* v, size_t pixels) {
   if (pixels <= v->depth_capacity) return VH_OK;
   dfree(v->d_depth_in);
   dfree(v->d_depth_filtered);
+  dfree(v->d_normal_map);
   v->depth_capacity = 0;
   VH_CUDA(v, dalloc(&v->d_depth_in, pixels));
   VH_CUDA(v, dalloc(&v->d_depth_filtered, pixels));
+  if (v->algo.normal_mode == 1) VH_CUDA(v, dalloc(&v->d_normal_map, pixels));
   v->depth_capacity = pixels;
   return VH_OK;
 }
@@ -216,6 +220,7 @@ void vh_algorithm_default(vh_algorithm* a) {
   a->min_view_angle_weight = 0.15f;         // :22
   a->allocation_mode = 0;
   a->fast_math = 0;
+  a->normal_mode = 0;
 }
 
 const char* vh_status_string(vh_status s) {
@@ -276,7 +281,8 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
     vh_algorithm_default(&v->algo);
   }
   if (v->algo.filter_radius < 0 || v->algo.filter_radius > 2 || v->algo.normal_radius != 1 ||
-      v->algo.allocation_mode < 0 || v->algo.allocation_mode > 1 || v->algo.fast_math < 0 || v->algo.fast_math > 1) {
+      v->algo.allocation_mode < 0 || v->algo.allocation_mode > 1 || v->algo.fast_math < 0 || v->algo.fast_math > 1 ||
+      v->algo.normal_mode < 0 || v->algo.normal_mode > 1) {
     delete v;
     return VH_ERR_INVALID_ARGUMENT;
   }
@@ -340,6 +346,7 @@ void vh_destroy(vh_volume* v) {
   if (v->h_counters) cudaFreeHost(v->h_counters);
   dfree(v->d_depth_in);
   dfree(v->d_depth_filtered);
+  dfree(v->d_normal_map);
   dfree(v->d_mc_counts);
   dfree(v->d_mc_dir_totals);
   dfree(v->d_mc_cell_counts);
@@ -406,8 +413,9 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[2], s));
-  VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_integrate(v->d_depth_filtered, v->dev, p, 0, s)
-                                : vh::exact::launch_integrate(v->d_depth_filtered, v->dev, p, 0, s));
+  VH_CUDA(v, v->algo.fast_math
+                 ? vh::fast::launch_integrate(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s)
+                 : vh::exact::launch_integrate(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s));
   if (v->profile) {
     VH_CUDA(v, cudaEventRecord(ev[3], s));
     v->profiled.push_back(std::move(ev));
@@ -492,6 +500,21 @@ vh_status vh_depth_normals(vh_volume* v, const float* in, float* normals, uint8_
   DeviceGuard guard(v->params.device);
   const vh::Params p = make_params(v, K, nullptr, 1);
   VH_CUDA(v, vh::launch_depth_normals(in, normals, valid, p, as_stream(stream)));
+  return VH_OK;
+}
+
+vh_status vh_pixel_normals(vh_volume* v, const float* in, float* normals, const vh_intrinsics* K, void* stream) {
+  if (!v || !in || !normals || !valid_intrinsics(K)) {
+    return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_pixel_normals: bad argument");
+  }
+  if ((reinterpret_cast<uintptr_t>(normals) & 15U) != 0U) {
+    return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_pixel_normals: normals must be 16-byte aligned");
+  }
+  DeviceGuard guard(v->params.device);
+  const vh::Params p = make_params(v, K, nullptr, 1);
+  float4* out = reinterpret_cast<float4*>(normals);
+  VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_pixel_normals(in, p, out, as_stream(stream))
+                                : vh::exact::launch_pixel_normals(in, p, out, as_stream(stream)));
   return VH_OK;
 }
 

@@ -99,6 +99,7 @@ struct Params {
   float max_weight, depth_sigma, huber_delta, min_obs_weight, min_view_weight;
   float iso;
   int alloc_mode;  // 0: reference rule (3 points x 27 neighbours), 1: truncation band (blocks crossed by the band)
+  int normal_mode;  // 0: bilateral normal per voxel (reference), 1: per-pixel normal map, interpolated per voxel
 };
 
 struct f3 {

@@ -535,6 +535,171 @@ __global__ void __launch_bounds__(kUpdateThreads) update_kernel(const float* __r
   }
 }
 
+// ---- per-pixel normal map (Params::normal_mode 1) ----
+//
+// At integer pixel coordinates sample_bilinear returns the pixel's own depth (weight 1 on d00, or the nearest
+// tap), so estimateSurfaceNormalCamera evaluated at every pixel centre is a 5x5 stencil over the depth image:
+// computed once per pixel here from a shared-memory tile, then bilinearly interpolated at each voxel's
+// projection.  This replaces the reference's 50 subpixel samples per voxel by 4 map taps; the normal differs
+// from the reference's at subpixel positions, which is why the mode is opt-in (results are judged by the
+// Chamfer distance of the fused surface, not bit parity).
+constexpr int kMapTX = 32, kMapTY = 8, kMapHalo = 2;
+constexpr int kMapW = kMapTX + 2 * kMapHalo, kMapH = kMapTY + 2 * kMapHalo;
+
+__global__ void __launch_bounds__(kMapTX * kMapTY) pixel_normal_kernel(const float* __restrict__ depth, const Params p,
+                                                                       float4* __restrict__ nmap) {
+  __shared__ float s_px[kMapH][kMapW], s_py[kMapH][kMapW], s_pz[kMapH][kMapW];
+  __shared__ float s_nx[kMapH][kMapW], s_ny[kMapH][kMapW], s_nz[kMapH][kMapW];
+  __shared__ unsigned char s_pv[kMapH][kMapW], s_nv[kMapH][kMapW];
+  const int tid = threadIdx.y * kMapTX + threadIdx.x;
+  const int x0 = blockIdx.x * kMapTX - kMapHalo, y0 = blockIdx.y * kMapTY - kMapHalo;
+  // 1. backprojected points of the tile + halo (invalid outside the image or where depth <= 0)
+  for (int k = tid; k < kMapW * kMapH; k += kMapTX * kMapTY) {
+    const int ty = k / kMapW, tx = k - ty * kMapW;
+    const int x = x0 + tx, y = y0 + ty;
+    float d = 0.0f;
+    if (x >= 0 && x < p.width && y >= 0 && y < p.height) d = __ldg(&depth[static_cast<size_t>(y) * p.width + x]);
+    const bool ok = d > 0.0f;
+    const f3 q = ok ? backproject(static_cast<float>(x), static_cast<float>(y), d, p) : mk3(0.0f, 0.0f, 0.0f);
+    s_px[ty][tx] = q.x;
+    s_py[ty][tx] = q.y;
+    s_pz[ty][tx] = q.z;
+    s_pv[ty][tx] = ok ? 1 : 0;
+  }
+  __syncthreads();
+  // 2. base normals (estimateSurfaceNormalBaseCamera) of the tile + 1-pixel ring, oriented toward the camera
+  for (int k = tid; k < kMapW * kMapH; k += kMapTX * kMapTY) {
+    const int ty = k / kMapW, tx = k - ty * kMapW;
+    bool ok = tx >= 1 && tx < kMapW - 1 && ty >= 1 && ty < kMapH - 1 && s_pv[ty][tx] && s_pv[ty][tx - 1] &&
+              s_pv[ty][tx + 1] && s_pv[ty - 1][tx] && s_pv[ty + 1][tx];
+    f3 n = mk3(0.0f, 0.0f, 0.0f);
+    if (ok) {
+      const f3 dv = mk3(s_px[ty + 1][tx] - s_px[ty - 1][tx], s_py[ty + 1][tx] - s_py[ty - 1][tx],
+                        s_pz[ty + 1][tx] - s_pz[ty - 1][tx]);
+      const f3 du = mk3(s_px[ty][tx + 1] - s_px[ty][tx - 1], s_py[ty][tx + 1] - s_py[ty][tx - 1],
+                        s_pz[ty][tx + 1] - s_pz[ty][tx - 1]);
+      n = normalize3(cross3(dv, du));
+      ok = norm3(n) > 1e-6f;
+      if (ok) n = orient_unit_toward_camera(n, mk3(s_px[ty][tx], s_py[ty][tx], s_pz[ty][tx]));
+    }
+    s_nx[ty][tx] = n.x;
+    s_ny[ty][tx] = n.y;
+    s_nz[ty][tx] = n.z;
+    s_nv[ty][tx] = ok ? 1 : 0;
+  }
+  __syncthreads();
+  // 3. the bilateral combination of the 3x3 base normals (estimateSurfaceNormalCamera)
+  const int x = blockIdx.x * kMapTX + threadIdx.x, y = blockIdx.y * kMapTY + threadIdx.y;
+  if (x >= p.width || y >= p.height) return;
+  const int cx = threadIdx.x + kMapHalo, cy = threadIdx.y + kMapHalo;
+  float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (s_nv[cy][cx]) {
+    const f3 cn = mk3(s_nx[cy][cx], s_ny[cy][cx], s_nz[cy][cx]);
+    const f3 cp = mk3(s_px[cy][cx], s_py[cy][cx], s_pz[cy][cx]);
+    const float g1 = gaussian(1.0f, p.normal_k_spatial), g2 = gaussian(2.0f, p.normal_k_spatial);
+    f3 wsum = mk3(0.0f, 0.0f, 0.0f);
+    float ws = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const int dx = k % 3 - 1, dy = k / 3 - 1;
+      if (!s_nv[cy + dy][cx + dx]) continue;
+      const f3 sn = mk3(s_nx[cy + dy][cx + dx], s_ny[cy + dy][cx + dx], s_nz[cy + dy][cx + dx]);
+      const float delta = s_pz[cy + dy][cx + dx] - cp.z;
+      const float ad = 1.0f - clampf(dot3(cn, sn), -1.0f, 1.0f);
+      const int r2 = dx * dx + dy * dy;
+      const float w = (r2 == 0 ? 1.0f : (r2 == 1 ? g1 : g2)) * gaussian(delta * delta, p.normal_k_range) *
+                      gaussian(ad * ad, p.normal_k_angular);
+      wsum = add3(wsum, mul3(sn, w));
+      ws += w;
+    }
+    f3 n = cn;
+    if (ws > 1e-6f) {
+      n = orient_toward_camera(normalize3(mul3(wsum, 1.0f / ws)), cp);
+      if (norm3(n) <= 1e-6f) n = cn;
+    }
+    out = make_float4(n.x, n.y, n.z, 1.0f);
+  }
+  nmap[static_cast<size_t>(y) * p.width + x] = out;
+}
+
+// Normal at a voxel's projection (u, v): bilinear blend of the valid map taps around it, renormalised.
+__device__ __forceinline__ bool map_normal(const float4* __restrict__ nmap, const Params& p, float u, float v, f3& n) {
+  const int x0 = static_cast<int>(floorf(u)), y0 = static_cast<int>(floorf(v));
+  const int x1 = min(x0 + 1, p.width - 1), y1 = min(y0 + 1, p.height - 1);
+  const float tx = u - static_cast<float>(x0), ty = v - static_cast<float>(y0);
+  const float4 a = __ldg(&nmap[static_cast<size_t>(y0) * p.width + x0]);
+  const float4 b = __ldg(&nmap[static_cast<size_t>(y0) * p.width + x1]);
+  const float4 c = __ldg(&nmap[static_cast<size_t>(y1) * p.width + x0]);
+  const float4 d = __ldg(&nmap[static_cast<size_t>(y1) * p.width + x1]);
+  const float wa = (1.0f - tx) * (1.0f - ty) * a.w, wb = tx * (1.0f - ty) * b.w;
+  const float wc = (1.0f - tx) * ty * c.w, wd = tx * ty * d.w;
+  const f3 s = mk3(wa * a.x + wb * b.x + wc * c.x + wd * d.x, wa * a.y + wb * b.y + wc * c.y + wd * d.y,
+                   wa * a.z + wb * b.z + wc * c.z + wd * d.z);
+  if (wa + wb + wc + wd <= 1e-6f || norm3(s) <= 1e-6f) return false;
+  n = normalize3(s);
+  return true;
+}
+
+// One pass over every voxel of the visible blocks with the normal from the map: prefix, observation and
+// layer update in the same thread (the per-voxel cost is uniform, so no active list is needed).
+__global__ void __launch_bounds__(kThreads) fused_update_kernel(const float* __restrict__ depth,
+                                                                const float4* __restrict__ nmap, const Volume V,
+                                                                const Params p) {
+  const uint32_t nvis = V.counters->visible_count;
+  const unsigned long long total = static_cast<unsigned long long>(nvis) * kBlockVoxels;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
+  for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
+       i += stride) {
+    const uint32_t item = static_cast<uint32_t>(i >> 9);
+    const int li = static_cast<int>(i & 511U);
+    const uint32_t b = V.slot_block[V.visible[item]];
+    bool pass = false, updated = false;
+    uint32_t newly = 0U;
+    if (b != kInvalidBlock) {
+      const int4 bk = V.block_keys[b];
+      f3 pc;
+      float u, v, d;
+      pass = voxel_prefix(depth, p, bk, li, pc, u, v, d);
+      if (pass) {
+        const float sd = d - pc.z;
+        const f3 view = normalize3(pc);
+        float view_w = 1.0f;
+        f3 nc = mul3(view, -1.0f);
+        if (map_normal(nmap, p, u, v, nc)) view_w = fabsf(dot3(nc, view));
+        const float obs = observation_weight(p, d, sd, view_w);
+        const f3 nw = normalize3(xform_vector(p.T_wc, nc));
+        const int dir = obs > 0.0f ? dominant_direction(nw) : -1;
+        if (dir >= 0 && dir < kDirs) {
+          const f3 spw = xform_point(p.T_wc, backproject(u, v, d, p));
+          const float sc = coordinate_along(spw, dir);
+          float4* base = V.layers + layer_index(b, dir, li, 0);
+          float4 L0 = base[0], L1 = base[1], L2 = base[2];
+          updated = integrate_sample(p, L0, L1, L2, sc, spw, nw, obs);
+          if (updated) {
+            base[0] = L0;
+            base[1] = L1;
+            base[2] = L2;
+            const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
+            const uint32_t bit = 1U << (li & 31);
+            if (!(V.obs_mask[w] & bit)) newly = (atomicOr(&V.obs_mask[w], bit) & bit) ? 0U : 1U;
+            const uint32_t dbit = 1U << dir;
+            if (!(V.dir_mask[b] & dbit)) atomicOr(&V.dir_mask[b], dbit);
+          }
+        }
+      }
+    }
+    const uint32_t act = __ballot_sync(0xffffffffU, pass);
+    const uint32_t upd = __ballot_sync(0xffffffffU, updated);
+    const uint32_t nw_ = __ballot_sync(0xffffffffU, newly != 0U);
+    if (lane == 0) {
+      if (act) atomicAdd(&V.counters->active_voxels, static_cast<uint32_t>(__popc(act)));
+      if (upd) atomicAdd(&V.counters->integrated_voxels, static_cast<uint32_t>(__popc(upd)));
+      if (nw_) atomicAdd(&V.counters->observed_voxels, static_cast<unsigned long long>(__popc(nw_)));
+    }
+  }
+}
+
 }  // namespace
 
 static int grid_for(const void* kernel, int threads) {
@@ -551,7 +716,23 @@ int integrate_grid_size() {
   return grid;
 }
 
-cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s) {
+cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s) {
+  const dim3 mb(kMapTX, kMapTY), mg((p.width + kMapTX - 1) / kMapTX, (p.height + kMapTY - 1) / kMapTY);
+  pixel_normal_kernel<<<mg, mb, 0, s>>>(depth, p, nmap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
+                             cudaStream_t s) {
+  if (p.normal_mode == 1) {
+    if (nmap == nullptr) return cudaErrorInvalidValue;
+    static int fused_grid = 0;
+    if (fused_grid == 0) fused_grid = grid_for(reinterpret_cast<const void*>(fused_update_kernel), kThreads);
+    cudaError_t e = launch_pixel_normals(depth, p, nmap, s);
+    if (e != cudaSuccess) return e;
+    fused_update_kernel<<<grid > 0 ? grid : fused_grid, kThreads, 0, s>>>(depth, nmap, V, p);
+    return cudaGetLastError();
+  }
   static int classify_grid = 0;
   if (classify_grid == 0) classify_grid = grid_for(reinterpret_cast<const void*>(classify_kernel), kThreads);
   classify_kernel<<<classify_grid, kThreads, 0, s>>>(depth, V, p);

@@ -17,13 +17,18 @@ cudaError_t launch_begin_frame(Counters* c, cudaStream_t s);
 // allocation: 3 points x 27-neighbourhood per sampled pixel -> persistent hash + visible list
 cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, cudaStream_t s);
 // directional multi-layer update of every visible block; grid = persistent CTAs.  exact: the bit-reproducible
-// FP32 form; fast: the same source compiled with fused multiply-adds and hardware approximations.
+// FP32 form; fast: the same source compiled with fused multiply-adds and hardware approximations.  With
+// Params::normal_mode 1, nmap (width x height float4) receives the per-pixel normal map.
 namespace exact {
-cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s);
+cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
+                             cudaStream_t s);
+cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s);
 int integrate_grid_size();
 }  // namespace exact
 namespace fast {
-cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, cudaStream_t s);
+cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
+                             cudaStream_t s);
+cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s);
 int integrate_grid_size();
 }  // namespace fast
 // marching cubes over all allocated blocks: pass 1 writes per-block, per-direction and per-cell triangle
