@@ -35,10 +35,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
-VOXEL_LAYER_BIN_BYTES = 3 * 16  # one direction bin: 3 layers x 16 B
-# DRAM bytes (read + write) per active voxel of update_kernel, from the ncu capture summarised in
-# profiles/update_kernel_room640.md (one launch, 6.55 M active voxels); scaled by the active voxels of a launch
-UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL = (539.49e6 + 267.04e6) / 6.548e6
+# DRAM bytes (read + write) per active voxel of the layer-update kernel of each form, from the ncu captures
+# summarised in profiles/ (plain: update_kernel_room640.md, one launch over 6.55 M active voxels); scaled by
+# the active voxels of a launch.  None until a capture of that kernel exists.
+UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL = {"plain": (539.49e6 + 267.04e6) / 6.548e6, "chosen": None}
 
 
 def parse():
@@ -230,9 +230,15 @@ def run_reference(args):
 
 
 # The opt-in "chosen form" (vh_algorithm fields); the plain form is the reference-exact FP32 path.
-CHOSEN_FORM = {"allocation_mode": 1, "fast_math": 1, "normal_mode": 1}
-FORM_NOTE = {"plain": "reference allocation rule (3 points x 27 neighbours), exact FP32 update",
-             "chosen": "truncation-band allocation, per-pixel normal map, fast-math FP32 update"}
+# forms: vh_algorithm fields + vh_params.layer_format
+FORMS = {
+    "chosen": ({"allocation_mode": 1, "fast_math": 1, "normal_mode": 1}, 1),
+    "plain": ({}, 0),
+}
+FORM_NOTE = {"plain": "reference allocation rule (3 points x 27 neighbours), exact FP32 update, FP32 layers",
+             "chosen": "truncation-band allocation, per-pixel normal map, fast-math FP32 update, FP16 layers"}
+BIN_BYTES = {0: 3 * 16, 1: 32}  # one direction bin (3 layers) in FP32 / FP16 storage
+UPDATE_KERNEL = {"plain": "update_kernel", "chosen": "fused_update_kernel"}
 
 
 def surface_points(sc, torch, capi, stride=4, every=20, max_points=200_000):
@@ -254,15 +260,17 @@ def surface_points(sc, torch, capi, stride=4, every=20, max_points=200_000):
     return metrics.observed_surface_points(sc, sel, depth_maps=maps, stride=stride, max_points=max_points)
 
 
-def fuse_form(args, torch, backend, capi, sc, frames, algo_kw, flush, world):
+def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
     """Time K frames of one form (after W warm-up frames) and extract the mesh; returns the measurements."""
     import ctypes as C
     K = sc.intrinsics
     px = K.width * K.height
     stream = torch.cuda.current_stream()
     max_blocks = int(os.environ.get("VH_BENCH_MAX_BLOCKS", "900000"))
+    algo_kw, layer_format = form
     vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=max_blocks,
-                                device=torch.cuda.current_device(), algorithm=capi.default_algorithm(**algo_kw))
+                                device=torch.cuda.current_device(), algorithm=capi.default_algorithm(**algo_kw),
+                                layer_format=layer_format)
     bk = backend.TsdfIntegrationBackend("gpu")
 
     def step(f, sync=False):
@@ -363,8 +371,8 @@ def run_gb300(args):
     px = K.width * K.height
     frames = render_all(sc, torch, None, _capi)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    forms = {"chosen": CHOSEN_FORM, "plain": {}}
-    res = {name: fuse_form(args, torch, backend, _capi, sc, frames, kw, flush, world) for name, kw in forms.items()}
+    res = {name: fuse_form(args, torch, backend, _capi, sc, frames, form, flush, world)
+           for name, form in FORMS.items()}
     quality = {}
     if rank == 0 and not args.no_chamfer:
         pts = surface_points(sc, torch, _capi)
@@ -375,16 +383,19 @@ def run_gb300(args):
     other = "plain" if args.form == "chosen" else "chosen"
 
     pk = peaks()
-    integ_ms = head["stage_ms"]["integrate"] / max(1, head["nprof"])
-    integ_bytes = head["upd_mean"] * 2 * VOXEL_LAYER_BIN_BYTES + px * 4
-    achieved = integ_bytes / (integ_ms / 1000.0) / 1e9
-    roofline = {"kernel": "update_kernel", "bound": "hbm", "achieved": round(achieved, 2),
+    upd_ms = head["stage_ms"]["update"] / max(1, head["nprof"])
+    bin_bytes = BIN_BYTES[FORMS[args.form][1]]
+    upd_bytes = head["upd_mean"] * 2 * bin_bytes + px * 4
+    achieved = upd_bytes / (upd_ms / 1000.0) / 1e9
+    traffic_per_active = UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL.get(args.form)
+    roofline = {"kernel": UPDATE_KERNEL[args.form], "bound": "hbm", "achieved": round(achieved, 2),
                 "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 5),
-                "traffic": int(UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL * head["act_mean"]),
-                "peak_source": pk["source"], "algorithmic_bytes_per_launch": int(integ_bytes),
-                "note": "integrate stage (classify + update kernels) time; algorithmic bytes = updated voxels x 96 B "
-                        "(read+write of one 3-layer bin) + 4 B/px depth; traffic = ncu DRAM bytes per active voxel x "
-                        "active voxels; bound by issue slots of the per-voxel bilateral normal, not by HBM"}
+                "traffic": int(traffic_per_active * head["act_mean"]) if traffic_per_active else None,
+                "peak_source": pk["source"], "algorithmic_bytes_per_launch": int(upd_bytes),
+                "ms_per_launch": round(upd_ms, 5),
+                "note": "layer-update kernel alone (CUDA events around its launch); algorithmic bytes = updated "
+                        "voxels x 2 x %d B (read + write of one 3-layer bin) + 4 B/px depth; traffic = ncu DRAM "
+                        "bytes per active voxel x active voxels" % bin_bytes}
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_budget_s > 0:

@@ -72,9 +72,13 @@ typedef struct vh_params {
   float voxel_size;
   float truncation_distance;
   uint32_t hash_buckets; /* power of two; slots of the persistent block hash */
-  uint32_t max_blocks;   /* pool capacity in blocks (<= 2^23), 147,456 bytes each; 0 = keys-only volume (vh_allocate only) */
+  uint32_t max_blocks;   /* pool capacity in blocks (<= 2^23); 0 = keys-only volume (vh_allocate only) */
   int32_t device;        /* CUDA device ordinal */
-  int32_t reserved;
+  /* 0 (default): FP32 layer records, 147,456 bytes per block, bit-identical to the reference;
+   * 1: FP16 storage, 98,304 bytes per block: weight, surface coordinate and plane offset in binary16 (the two
+   * coordinates relative to the voxel centre, in voxel units), normal word unchanged; FP32 update arithmetic.
+   * Export and import always use the reference's FP32 Voxel layout. */
+  int32_t layer_format;
 } vh_params;
 
 /* Algorithm constants; defaults are the reference CUDA path's (src/cuda_tsdf_integrator.cu:18-35,
@@ -198,11 +202,12 @@ vh_status vh_import_blocks(vh_volume* volume, const int32_t* keys, const void* v
                            int32_t in_on_device, void* stream);
 
 /* Stage timing with CUDA events (the reference times its stages with steady_clock, src/main.cpp:424-452).
- * While enabled, vh_integrate brackets its filter, allocation and update kernels with events on the call's
- * stream.  vh_profile_read waits for the recorded frames and returns the milliseconds spent in each stage
- * (ms[0] filter, ms[1] allocation, ms[2] update) since the last read, and how many frames they cover. */
+ * While enabled, vh_integrate brackets each of its kernels with events on the call's stream.
+ * vh_profile_read waits for the recorded frames and returns the milliseconds spent in each stage since the
+ * last read -- ms[0] filter, ms[1] allocation, ms[2] update preparation (the active-voxel list, or the
+ * per-pixel normal map with normal_mode 1), ms[3] layer update -- and how many frames they cover. */
 vh_status vh_profile_enable(vh_volume* volume, int32_t enable);
-vh_status vh_profile_read(vh_volume* volume, double ms[3], uint64_t* frames);
+vh_status vh_profile_read(vh_volume* volume, double ms[4], uint64_t* frames);
 
 /* Workload generator, not a reference interface: ray-casts the analytic benchmark scenes the way the
  * reference's demo renders its synthetic frames (src/main.cpp:189-335) -- primitives `prims` (device memory,

@@ -215,3 +215,72 @@ def test_pixel_normal_map_matches_reference_normal(backend, oracle_lib, fast_mat
             cosang = np.clip(np.sum(got[ok, :3].astype(np.float64) * want_n[ok], axis=1), -1.0, 1.0)
             assert np.quantile(np.arccos(cosang), 0.999) <= 1e-3
     vol.close()
+
+
+@pytest.mark.parametrize("chosen", [False, True])
+def test_fp16_storage_matches_fp32(backend, orbit_half, chosen):
+    """FP16 layer storage (vh_params.layer_format 1) against FP32 storage, same frames, same algorithm.
+    Stated per-field errors, for layers observed in both, at the 99th percentile: weight within 1e-3
+    relative (binary16 rounding of the accumulated weight, 2^-11 per update); surface coordinate and plane
+    offset within 0.03 voxel (binary16 step of the voxel-relative value, <= 1/64 voxel below 16 voxels, plus
+    the slightly different blending weights).  Beyond that percentile the differences are layer-assignment
+    flips: a rounded coordinate crosses the merge tolerance or the layer order, and the observation lands
+    in another layer of the bin, so both the weight and the coordinates of that slot differ by whole
+    observations; at most 1% of layers.  Block keys identical, layer occupancy equal on 99.9% of bins,
+    incremental observed count equal to the recount, Chamfer within 2% of the FP32 form's."""
+    sc, depths, clean = orbit_half
+    frames = list(range(0, 16, 2))
+    from oracle import oracle as O
+    algo = dict(allocation_mode=1, fast_math=1, normal_mode=1) if chosen else {}
+    from voxelhashmt_gb300 import _capi
+    vols = []
+    for fmt in (0, 1):
+        vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=1 << 18, max_blocks=60000,
+                                    algorithm=_capi.default_algorithm(**algo), layer_format=fmt)
+        bk = backend.TsdfIntegrationBackend("gpu")
+        for f in frames:
+            bk.integrate(vol, backend.DepthFrame(sc.intrinsics, depths[f]), sc.poses[f], 1)
+        vols.append(vol)
+    k32, v32 = O.sort_blocks(*vols[0].export_blocks())
+    k16, v16 = O.sort_blocks(*vols[1].export_blocks())
+    assert np.array_equal(k32, k16)
+    a = v32.view(np.float32).reshape(-1, 4)
+    b = v16.view(np.float32).reshape(-1, 4)
+    occ_a, occ_b = a[:, 0] > 0, b[:, 0] > 0
+    assert occ_a.sum() > 10000
+    assert np.mean(occ_a == occ_b) >= 0.999
+    both = occ_a & occ_b
+    w_err = np.abs(b[both, 0] - a[both, 0]) / a[both, 0]
+    errs = {"weight_rel": w_err}
+    for col, name in ((1, "surface_coord_vox"), (2, "plane_offset_vox")):
+        errs[name] = np.abs(b[both, col].astype(np.float64) - a[both, col]) / sc.voxel_size
+    for name, e in errs.items():
+        print("fp16-vs-fp32 %-18s q50 %.3g q90 %.3g q99 %.3g q999 %.3g max %.3g" % (
+            name, *(float(np.quantile(e, q)) for q in (0.5, 0.9, 0.99, 0.999)), float(e.max())))
+    assert np.quantile(w_err, 0.99) <= 1e-3, float(np.quantile(w_err, 0.99))
+    for name in ("surface_coord_vox", "plane_offset_vox"):
+        assert np.quantile(errs[name], 0.99) <= 0.03, (name, float(np.quantile(errs[name], 0.99)))
+    flipped = (w_err > 1e-2) | (errs["surface_coord_vox"] > 0.25) | (errs["plane_offset_vox"] > 0.25)
+    print("fp16-vs-fp32 layer-assignment flips: %.4f%% of layers" % (100.0 * float(np.mean(flipped))))
+    assert np.mean(flipped) <= 0.01
+    assert vols[1].observed_voxel_count() == vols[1].recount_observed_voxels()
+    c32, _ = _chamfer(backend, vols[0], sc, clean, frames)
+    c16, _ = _chamfer(backend, vols[1], sc, clean, frames)
+    print("fp32", c32)
+    print("fp16", c16)
+    assert abs(c16["chamfer_mm"] - c32["chamfer_mm"]) <= 0.02 * c32["chamfer_mm"], (c16, c32)
+    # checkpoint round trip through the reference FP32 layout into a fresh FP16 volume
+    keys, vox = vols[1].export_blocks()
+    fresh = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=1 << 18, max_blocks=60000,
+                                  layer_format=1)
+    fresh.import_blocks(keys, vox)
+    k2, v2 = O.sort_blocks(*fresh.export_blocks())
+    assert np.array_equal(k2, k16)
+    x2 = v2.view(np.float32).reshape(-1, 4)
+    assert np.array_equal(x2[:, 0] > 0, b[:, 0] > 0)
+    assert np.array_equal(x2[:, 3].view(np.uint32), b[:, 3].view(np.uint32))
+    assert np.array_equal(x2[:, 0], b[:, 0])
+    assert np.max(np.abs(x2[:, 1:3].astype(np.float64) - b[:, 1:3])) <= 1e-3 * sc.voxel_size
+    assert fresh.observed_voxel_count() == vols[1].observed_voxel_count()
+    for v in vols + [fresh]:
+        v.close()

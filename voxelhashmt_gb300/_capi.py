@@ -30,7 +30,7 @@ BLOCK_BYTES = 512 * 6 * 3 * 16
 
 class VhParams(C.Structure):
     _fields_ = [("voxel_size", C.c_float), ("truncation_distance", C.c_float), ("hash_buckets", C.c_uint32),
-                ("max_blocks", C.c_uint32), ("device", C.c_int32), ("reserved", C.c_int32)]
+                ("max_blocks", C.c_uint32), ("device", C.c_int32), ("layer_format", C.c_int32)]
 
 
 class VhAlgorithm(C.Structure):

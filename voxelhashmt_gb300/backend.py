@@ -81,17 +81,21 @@ class VoxelHashTSDF:
     """A voxel-hashed directional multi-layer volume resident on one GPU."""
 
     def __init__(self, voxel_size, truncation_distance, hash_buckets=1 << 16, max_blocks=1 << 14, device=0,
-                 algorithm: _capi.VhAlgorithm | None = None):
+                 algorithm: _capi.VhAlgorithm | None = None, layer_format=0):
+        """layer_format 0: FP32 layer records (the reference's); 1: FP16 storage (weight, and surface
+        coordinate / plane offset relative to the voxel centre, in binary16) with FP32 update arithmetic."""
         self._voxel_size = float(voxel_size)
         self._truncation = float(truncation_distance)
         params = _capi.default_params(voxel_size=self._voxel_size, truncation_distance=self._truncation,
-                                      hash_buckets=int(hash_buckets), max_blocks=int(max_blocks), device=int(device))
+                                      hash_buckets=int(hash_buckets), max_blocks=int(max_blocks), device=int(device),
+                                      layer_format=int(layer_format))
         self.algorithm = algorithm if algorithm is not None else _capi.default_algorithm()
         h = C.c_void_p()
         _capi.check(_capi.lib().vh_create(C.byref(params), C.byref(self.algorithm), C.byref(h)))
         self.handle = h
         self.max_blocks = int(max_blocks)
         self.hash_buckets = int(hash_buckets)
+        self.layer_format = int(layer_format)
         self.device = int(device)
 
     def close(self):
@@ -143,11 +147,13 @@ class VoxelHashTSDF:
         _capi.check(_capi.lib().vh_profile_enable(self.handle, 1 if enable else 0), self.handle)
 
     def read_profile(self):
-        """({'filter': ms, 'allocate': ms, 'integrate': ms}, frames) accumulated since the last read."""
-        ms = (C.c_double * 3)()
+        """({'filter', 'allocate', 'prepare', 'update', 'integrate': ms}, frames) accumulated since the last
+        read; prepare = active-voxel list or normal map, update = layer update, integrate = their sum."""
+        ms = (C.c_double * 4)()
         n = C.c_uint64()
         _capi.check(_capi.lib().vh_profile_read(self.handle, ms, C.byref(n)), self.handle)
-        return {"filter": ms[0], "allocate": ms[1], "integrate": ms[2]}, n.value
+        return {"filter": ms[0], "allocate": ms[1], "prepare": ms[2], "update": ms[3],
+                "integrate": ms[2] + ms[3]}, n.value
 
     def block_keys(self):
         """gpuVolumeCacheBlockKeys: (N, 3) int32 in allocation order."""

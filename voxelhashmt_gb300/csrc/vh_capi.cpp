@@ -45,7 +45,10 @@ struct vh_volume {
 
 namespace {
 
+// one block in the reference Voxel layout / the FP32 pool (16-byte layer records)
 constexpr size_t kBlockBytes = static_cast<size_t>(vh::kDirs) * vh::kBlockVoxels * vh::kLayers * sizeof(float4);
+// one block of the FP16 pool (32-byte bins)
+constexpr size_t kBlockBytes16 = static_cast<size_t>(vh::kDirs) * vh::kBlockVoxels * vh::kBinWords16 * sizeof(uint4);
 constexpr size_t kExportChunk = 1024;  // blocks per export staging pass
 
 class DeviceGuard {
@@ -146,6 +149,11 @@ vh::Params make_params(const vh_volume* v, const vh_intrinsics* K, const vh_pose
   return p;
 }
 
+size_t pool_block_bytes(const vh_volume* v) { return v->dev.layers16 ? kBlockBytes16 : kBlockBytes; }
+void* pool_base(const vh_volume* v) {
+  return v->dev.layers16 ? static_cast<void*>(v->dev.layers16) : static_cast<void*>(v->dev.layers);
+}
+
 vh_status ensure_depth(vh_volume* v, size_t pixels) {
   if (pixels <= v->depth_capacity) return VH_OK;
   dfree(v->d_depth_in);
@@ -194,7 +202,7 @@ void vh_params_default(vh_params* p) {
   p->hash_buckets = 1u << 16;
   p->max_blocks = 1u << 14;
   p->device = 0;
-  p->reserved = 0;
+  p->layer_format = 0;
 }
 
 void vh_algorithm_default(vh_algorithm* a) {
@@ -265,7 +273,8 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   *out = nullptr;
   const uint32_t buckets = params->hash_buckets;
   if (!(params->voxel_size > 0.0f) || !(params->truncation_distance > 0.0f) || buckets < 2 ||
-      (buckets & (buckets - 1)) != 0 || params->max_blocks > (1u << 23)) {
+      (buckets & (buckets - 1)) != 0 || params->max_blocks > (1u << 23) || params->layer_format < 0 ||
+      params->layer_format > 1) {
     return VH_ERR_INVALID_ARGUMENT;  // pool indices are packed with the voxel index in 32 bits
   }
   int count = 0;
@@ -301,7 +310,12 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   step(dalloc(&V.slot_stamp, buckets));
   step(dalloc(&V.visible, buckets));
   step(dalloc(&V.active, nb * vh::kBlockVoxels));
-  step(cudaMalloc(reinterpret_cast<void**>(&V.layers), std::max<size_t>(nb, 1) * kBlockBytes));
+  V.voxel_size = params->voxel_size;
+  if (params->layer_format == 1) {
+    step(cudaMalloc(reinterpret_cast<void**>(&V.layers16), std::max<size_t>(nb, 1) * kBlockBytes16));
+  } else {
+    step(cudaMalloc(reinterpret_cast<void**>(&V.layers), std::max<size_t>(nb, 1) * kBlockBytes));
+  }
   step(dalloc(&V.block_keys, nb));
   step(dalloc(&V.obs_mask, nb * (vh::kBlockVoxels / 32)));
   step(dalloc(&V.dir_mask, nb));
@@ -312,7 +326,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
     step(cudaMemset(V.slot_keys, 0xFF, buckets * sizeof(unsigned long long)));
     step(cudaMemset(V.slot_block, 0xFF, buckets * sizeof(uint32_t)));
     step(cudaMemset(V.slot_stamp, 0, buckets * sizeof(uint32_t)));
-    step(cudaMemset(V.layers, 0, std::max<size_t>(nb, 1) * kBlockBytes));
+    step(cudaMemset(pool_base(v), 0, std::max<size_t>(nb, 1) * pool_block_bytes(v)));
     step(cudaMemset(V.obs_mask, 0, nb * (vh::kBlockVoxels / 32) * sizeof(uint32_t)));
     step(cudaMemset(V.dir_mask, 0, std::max<size_t>(nb, 1) * sizeof(uint32_t)));
     step(cudaMemset(V.counters, 0, sizeof(vh::Counters)));
@@ -339,6 +353,7 @@ void vh_destroy(vh_volume* v) {
   dfree(V.visible);
   dfree(V.active);
   dfree(V.layers);
+  dfree(V.layers16);
   dfree(V.block_keys);
   dfree(V.obs_mask);
   dfree(V.dir_mask);
@@ -376,7 +391,7 @@ vh_status vh_reset(vh_volume* v, void* stream) {
   VH_CUDA(v, cudaMemsetAsync(V.slot_keys, 0xFF, V.capacity * sizeof(unsigned long long), s));
   VH_CUDA(v, cudaMemsetAsync(V.slot_block, 0xFF, V.capacity * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.slot_stamp, 0, V.capacity * sizeof(uint32_t), s));
-  VH_CUDA(v, cudaMemsetAsync(V.layers, 0, used * kBlockBytes, s));
+  VH_CUDA(v, cudaMemsetAsync(pool_base(v), 0, used * pool_block_bytes(v), s));
   VH_CUDA(v, cudaMemsetAsync(V.obs_mask, 0, used * (vh::kBlockVoxels / 32) * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.dir_mask, 0, used * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.counters, 0, sizeof(vh::Counters), s));
@@ -397,7 +412,7 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
   const vh::Params p = make_params(v, K, T_wc, stride);
   std::vector<cudaEvent_t> ev;
   if (v->profile) {
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < 5; ++i) {
       cudaEvent_t e = nullptr;
       if (!v->event_pool.empty()) {
         e = v->event_pool.back();
@@ -413,11 +428,14 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[2], s));
+  VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_integrate_prepare(v->d_depth_filtered, v->dev, p, v->d_normal_map, s)
+                                : vh::exact::launch_integrate_prepare(v->d_depth_filtered, v->dev, p, v->d_normal_map, s));
+  if (v->profile) VH_CUDA(v, cudaEventRecord(ev[3], s));
   VH_CUDA(v, v->algo.fast_math
-                 ? vh::fast::launch_integrate(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s)
-                 : vh::exact::launch_integrate(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s));
+                 ? vh::fast::launch_integrate_update(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s)
+                 : vh::exact::launch_integrate_update(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s));
   if (v->profile) {
-    VH_CUDA(v, cudaEventRecord(ev[3], s));
+    VH_CUDA(v, cudaEventRecord(ev[4], s));
     v->profiled.push_back(std::move(ev));
   }
   return VH_OK;
@@ -429,14 +447,14 @@ vh_status vh_profile_enable(vh_volume* v, int32_t enable) {
   return VH_OK;
 }
 
-vh_status vh_profile_read(vh_volume* v, double ms[3], uint64_t* frames) {
+vh_status vh_profile_read(vh_volume* v, double ms[4], uint64_t* frames) {
   if (!v || !ms) return VH_ERR_INVALID_ARGUMENT;
   DeviceGuard guard(v->params.device);
-  ms[0] = ms[1] = ms[2] = 0.0;
+  ms[0] = ms[1] = ms[2] = ms[3] = 0.0;
   const uint64_t n = v->profiled.size();
   for (auto& fr : v->profiled) {
-    VH_CUDA(v, cudaEventSynchronize(fr[3]));
-    for (int k = 0; k < 3; ++k) {
+    VH_CUDA(v, cudaEventSynchronize(fr[4]));
+    for (int k = 0; k < 4; ++k) {
       float t = 0.0f;
       VH_CUDA(v, cudaEventElapsedTime(&t, fr[k], fr[k + 1]));
       ms[k] += t;

@@ -10,6 +10,7 @@
 
 #include <cstdint>
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace vh {
@@ -60,7 +61,8 @@ struct Volume {
   unsigned long long* slot_keys;
   uint32_t* slot_block;
   uint32_t* slot_stamp;
-  float4* layers;
+  float4* layers;    // FP32 layer records (layer_format 0), nullptr otherwise
+  uint4* layers16;   // FP16 bins (layer_format 1), nullptr otherwise
   int4* block_keys;
   uint32_t* obs_mask;
   uint32_t* dir_mask;
@@ -70,7 +72,7 @@ struct Volume {
   uint32_t capacity;
   uint32_t mask;
   uint32_t max_blocks;
-  uint32_t pad;
+  float voxel_size;  // metres (the FP16 codec's unit)
 };
 
 struct Mat34 {
@@ -235,6 +237,140 @@ __device__ __forceinline__ uint32_t lookup_block(const Volume& V, int x, int y, 
 // float4 index of layer l of voxel li, direction d, block b
 __device__ __forceinline__ size_t layer_index(uint32_t b, int d, int li, int l) {
   return ((static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + li) * kLayers + l;
+}
+
+// ---- FP16 layer storage (vh_params.layer_format 1) ----
+//
+// One (block, direction, voxel) bin is 32 bytes, two uint4 words:
+//   A = {w0 | s0 << 16, p0 | w1 << 16, s1 | p1 << 16, w2 | s2 << 16},  B = {p2, n0, n1, n2}
+// per layer l: w = weight (binary16), n = the octahedral normal word of the FP32 record (unchanged),
+// s = (surface_coord - c_d) / voxel_size and p = (plane_offset - dot(bin_normal(n), c)) / voxel_size
+// (binary16), c the voxel centre and c_d its coordinate along the bin's direction.  Coordinates are stored
+// relative to the voxel they belong to because absolute world metres would have a 4 mm binary16 step at
+// 4 m; relative to the voxel, |s|, |p| stay below a few truncation distances and the step is <= 1/64 voxel.
+// Empty layers are all-zero.  The update arithmetic stays FP32: a bin is decoded to three FP32 records,
+// updated, and encoded back.  Every operation of the codec is an IEEE round-to-nearest intrinsic, so the
+// fast-math and the exact compiles encode and decode identically.
+constexpr int kBinWords16 = 2;
+
+__device__ __forceinline__ size_t bin16_index(uint32_t b, int d, int li) {
+  return ((static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + li) * kBinWords16;
+}
+
+// voxel centre in world coordinates, ((block * 8 + local) + 0.5) * voxel_size per axis
+__device__ __forceinline__ f3 voxel_centre(const int4& bk, int li, float vs) {
+  const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
+  return mk3(__fmul_rn(__fadd_rn(static_cast<float>(bk.x * kBlockSide + lx), 0.5f), vs),
+             __fmul_rn(__fadd_rn(static_cast<float>(bk.y * kBlockSide + ly), 0.5f), vs),
+             __fmul_rn(__fadd_rn(static_cast<float>(bk.z * kBlockSide + lz), 0.5f), vs));
+}
+
+__device__ __forceinline__ float axis_coordinate(f3 p, int d) {
+  const float a = (d >> 1) == 0 ? p.x : ((d >> 1) == 1 ? p.y : p.z);
+  return (d & 1) ? -a : a;
+}
+
+// octahedral decode of a packed normal word, normalised (the codec's reference direction for p)
+__device__ __forceinline__ f3 bin_normal(uint32_t packed) {
+  float x = __fadd_rn(__fmul_rn(div65535(static_cast<float>(packed & 0xffffU)), 2.0f), -1.0f);
+  float y = __fadd_rn(__fmul_rn(div65535(static_cast<float>(packed >> 16U)), 2.0f), -1.0f);
+  const float z = __fadd_rn(__fadd_rn(1.0f, -fabsf(x)), -fabsf(y));
+  if (z < 0.0f) {
+    const float fx = __fmul_rn(__fadd_rn(1.0f, -fabsf(y)), x >= 0.0f ? 1.0f : -1.0f);
+    const float fy = __fmul_rn(__fadd_rn(1.0f, -fabsf(x)), y >= 0.0f ? 1.0f : -1.0f);
+    x = fx;
+    y = fy;
+  }
+  const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+  if (len <= 1e-6f) return mk3(0.0f, 0.0f, 1.0f);
+  return mk3(__fdiv_rn(x, len), __fdiv_rn(y, len), __fdiv_rn(z, len));
+}
+
+__device__ __forceinline__ float dot_rn(f3 a, f3 b) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+
+__device__ __forceinline__ float4 decode_layer16(uint16_t w, uint16_t s, uint16_t p, uint32_t n, f3 c, float cd,
+                                                 float vs) {
+  const float wf = __half2float(__ushort_as_half(w));
+  if (!(wf > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  const float sc = __fadd_rn(cd, __fmul_rn(__half2float(__ushort_as_half(s)), vs));
+  const float po = __fadd_rn(dot_rn(bin_normal(n), c), __fmul_rn(__half2float(__ushort_as_half(p)), vs));
+  return make_float4(wf, sc, po, __uint_as_float(n));
+}
+
+__device__ __forceinline__ void encode_layer16(const float4& L, f3 c, float cd, float vs, uint16_t& w, uint16_t& s,
+                                               uint16_t& p) {
+  if (!(L.x > 0.0f)) {
+    w = s = p = 0;
+    return;
+  }
+  const uint32_t n = __float_as_uint(L.w);
+  w = __half_as_ushort(__float2half_rn(L.x));
+  if (w == 0) w = 1;  // a positive weight below the binary16 range keeps the layer observed
+  s = __half_as_ushort(__float2half_rn(__fdiv_rn(__fadd_rn(L.y, -cd), vs)));
+  p = __half_as_ushort(__float2half_rn(__fdiv_rn(__fadd_rn(L.z, -dot_rn(bin_normal(n), c)), vs)));
+}
+
+__device__ __forceinline__ void decode_bin16(const uint4& A, const uint4& B, f3 c, int d, float vs, float4& L0,
+                                             float4& L1, float4& L2) {
+  const float cd = axis_coordinate(c, d);
+  L0 = decode_layer16(A.x & 0xffffU, A.x >> 16, A.y & 0xffffU, B.y, c, cd, vs);
+  L1 = decode_layer16(A.y >> 16, A.z & 0xffffU, A.z >> 16, B.z, c, cd, vs);
+  L2 = decode_layer16(A.w & 0xffffU, A.w >> 16, B.x & 0xffffU, B.w, c, cd, vs);
+}
+
+__device__ __forceinline__ void encode_bin16(const float4& L0, const float4& L1, const float4& L2, f3 c, int d,
+                                             float vs, uint4& A, uint4& B) {
+  const float cd = axis_coordinate(c, d);
+  uint16_t w0, s0, p0, w1, s1, p1, w2, s2, p2;
+  encode_layer16(L0, c, cd, vs, w0, s0, p0);
+  encode_layer16(L1, c, cd, vs, w1, s1, p1);
+  encode_layer16(L2, c, cd, vs, w2, s2, p2);
+  A = make_uint4(w0 | (static_cast<uint32_t>(s0) << 16), p0 | (static_cast<uint32_t>(w1) << 16),
+                 s1 | (static_cast<uint32_t>(p1) << 16), w2 | (static_cast<uint32_t>(s2) << 16));
+  B = make_uint4(p2, L0.x > 0.0f ? __float_as_uint(L0.w) : 0U, L1.x > 0.0f ? __float_as_uint(L1.w) : 0U,
+                 L2.x > 0.0f ? __float_as_uint(L2.w) : 0U);
+}
+
+// the three layer records of one bin, in the FP32 record form, whichever storage the volume uses
+__device__ __forceinline__ void load_bin(const Volume& V, uint32_t b, int d, int li, const int4& bk, float vs,
+                                         float4& L0, float4& L1, float4& L2) {
+  if (V.layers16 == nullptr) {
+    const float4* base = V.layers + layer_index(b, d, li, 0);
+    L0 = base[0];
+    L1 = base[1];
+    L2 = base[2];
+    return;
+  }
+  const uint4* q = V.layers16 + bin16_index(b, d, li);
+  decode_bin16(q[0], q[1], voxel_centre(bk, li, vs), d, vs, L0, L1, L2);
+}
+
+__device__ __forceinline__ void store_bin(const Volume& V, uint32_t b, int d, int li, const int4& bk, float vs,
+                                          const float4& L0, const float4& L1, const float4& L2) {
+  if (V.layers16 == nullptr) {
+    float4* base = V.layers + layer_index(b, d, li, 0);
+    base[0] = L0;
+    base[1] = L1;
+    base[2] = L2;
+    return;
+  }
+  uint4 A, B;
+  encode_bin16(L0, L1, L2, voxel_centre(bk, li, vs), d, vs, A, B);
+  uint4* q = V.layers16 + bin16_index(b, d, li);
+  q[0] = A;
+  q[1] = B;
+}
+
+// any layer of the bin observed (weight > 0)
+__device__ __forceinline__ bool bin_observed(const Volume& V, uint32_t b, int d, int li) {
+  if (V.layers16 == nullptr) {
+    const float4* L = V.layers + layer_index(b, d, li, 0);
+    return L[0].x > 0.0f || L[1].x > 0.0f || L[2].x > 0.0f;
+  }
+  const uint4 A = V.layers16[bin16_index(b, d, li)];
+  return (A.x & 0xffffU) != 0U || (A.y >> 16) != 0U || (A.w & 0xffffU) != 0U;
 }
 
 }  // namespace vh

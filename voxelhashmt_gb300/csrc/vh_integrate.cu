@@ -511,13 +511,11 @@ __global__ void __launch_bounds__(kUpdateThreads) update_kernel(const float* __r
       f3 spw = mk3(0.0f, 0.0f, 0.0f), nw = spw;
       const int dir = voxel_observation<kUpdateThreads>(depth, p, pc, u, v, d, gs, S, threadIdx.x, sc, spw, nw, obs);
       if (dir >= 0) {
-        float4* base = V.layers + layer_index(b, dir, li, 0);
-        float4 L0 = base[0], L1 = base[1], L2 = base[2];
+        float4 L0, L1, L2;
+        load_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
         updated = integrate_sample(p, L0, L1, L2, sc, spw, nw, obs);
         if (updated) {
-          base[0] = L0;
-          base[1] = L1;
-          base[2] = L2;
+          store_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
           const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
           const uint32_t bit = 1U << (li & 31);
           if (!(V.obs_mask[w] & bit)) newly = (atomicOr(&V.obs_mask[w], bit) & bit) ? 0U : 1U;
@@ -673,13 +671,11 @@ __global__ void __launch_bounds__(kThreads) fused_update_kernel(const float* __r
         if (dir >= 0 && dir < kDirs) {
           const f3 spw = xform_point(p.T_wc, backproject(u, v, d, p));
           const float sc = coordinate_along(spw, dir);
-          float4* base = V.layers + layer_index(b, dir, li, 0);
-          float4 L0 = base[0], L1 = base[1], L2 = base[2];
+          float4 L0, L1, L2;
+          load_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
           updated = integrate_sample(p, L0, L1, L2, sc, spw, nw, obs);
           if (updated) {
-            base[0] = L0;
-            base[1] = L1;
-            base[2] = L2;
+            store_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
             const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
             const uint32_t bit = 1U << (li & 31);
             if (!(V.obs_mask[w] & bit)) newly = (atomicOr(&V.obs_mask[w], bit) & bit) ? 0U : 1U;
@@ -722,24 +718,39 @@ cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nm
   return cudaGetLastError();
 }
 
-cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
-                             cudaStream_t s) {
+// first kernel of the update: the active-voxel list (classify_kernel) or the per-pixel normal map
+cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
+                                     cudaStream_t s) {
   if (p.normal_mode == 1) {
     if (nmap == nullptr) return cudaErrorInvalidValue;
-    static int fused_grid = 0;
-    if (fused_grid == 0) fused_grid = grid_for(reinterpret_cast<const void*>(fused_update_kernel), kThreads);
-    cudaError_t e = launch_pixel_normals(depth, p, nmap, s);
-    if (e != cudaSuccess) return e;
-    fused_update_kernel<<<grid > 0 ? grid : fused_grid, kThreads, 0, s>>>(depth, nmap, V, p);
-    return cudaGetLastError();
+    return launch_pixel_normals(depth, p, nmap, s);
   }
   static int classify_grid = 0;
   if (classify_grid == 0) classify_grid = grid_for(reinterpret_cast<const void*>(classify_kernel), kThreads);
   classify_kernel<<<classify_grid, kThreads, 0, s>>>(depth, V, p);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+// second kernel: the layer update over the active list (update_kernel) or over every visible voxel with the
+// map normal (fused_update_kernel)
+cudaError_t launch_integrate_update(const float* depth, const Volume& V, const Params& p, int grid,
+                                    const float4* nmap, cudaStream_t s) {
+  if (p.normal_mode == 1) {
+    if (nmap == nullptr) return cudaErrorInvalidValue;
+    static int fused_grid = 0;
+    if (fused_grid == 0) fused_grid = grid_for(reinterpret_cast<const void*>(fused_update_kernel), kThreads);
+    fused_update_kernel<<<grid > 0 ? grid : fused_grid, kThreads, 0, s>>>(depth, nmap, V, p);
+    return cudaGetLastError();
+  }
   update_kernel<<<grid > 0 ? grid : integrate_grid_size(), kUpdateThreads, 0, s>>>(depth, V, p);
   return cudaGetLastError();
+}
+
+cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
+                             cudaStream_t s) {
+  const cudaError_t e = launch_integrate_prepare(depth, V, p, nmap, s);
+  if (e != cudaSuccess) return e;
+  return launch_integrate_update(depth, V, p, grid, nmap, s);
 }
 
 }  // namespace VH_INTEGRATE_NS

@@ -22,12 +22,20 @@ cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, c
 namespace exact {
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
+cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
+                                     cudaStream_t s);
+cudaError_t launch_integrate_update(const float* depth, const Volume& V, const Params& p, int grid,
+                                    const float4* nmap, cudaStream_t s);
 cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s);
 int integrate_grid_size();
 }  // namespace exact
 namespace fast {
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
+cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
+                                     cudaStream_t s);
+cudaError_t launch_integrate_update(const float* depth, const Volume& V, const Params& p, int grid,
+                                    const float4* nmap, cudaStream_t s);
 cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s);
 int integrate_grid_size();
 }  // namespace fast

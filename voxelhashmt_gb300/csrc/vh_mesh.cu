@@ -67,7 +67,37 @@ __device__ __forceinline__ float plane_sd(const float4& pl, f3 p) {
 
 __device__ __forceinline__ int staged_index(int x, int y, int z) { return (z * kSide + y) * kSide + x; }
 
-__device__ void stage_direction(Shared& S, const Volume& V, int d, int tid) {
+// FP16 bins: one thread decodes the three layers of a voxel.  Kept out of line so the codec's registers do
+// not add to the marching-cubes body's.
+__device__ __noinline__ void stage_direction16(Shared& S, const Volume& V, float vs, int d, int tid) {
+  for (int vi = tid; vi < kStaged; vi += kThreads) {
+    const int sx = vi % kSide, sy = (vi / kSide) % kSide, sz = vi / (kSide * kSide);
+    const uint32_t nb = S.nbr[(sx >> 3) | ((sy >> 3) << 1) | ((sz >> 3) << 2)];
+    float4 L[kLayers] = {make_float4(0.0f, 0.0f, 0.0f, 0.0f), make_float4(0.0f, 0.0f, 0.0f, 0.0f),
+                         make_float4(0.0f, 0.0f, 0.0f, 0.0f)};
+    if (nb != kInvalidBlock) {
+      const int li = (sx & 7) + kBlockSide * ((sy & 7) + kBlockSide * (sz & 7));
+      load_bin(V, nb, d, li, V.block_keys[nb], vs, L[0], L[1], L[2]);
+    }
+#pragma unroll
+    for (int l = 0; l < kLayers; ++l) {
+      float4 pl = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      const bool ok = L[l].x > 0.0f;
+      if (ok) {
+        const f3 n = unpack_normal_mesh(__float_as_uint(L[l].w));
+        pl = make_float4(n.x, n.y, n.z, L[l].z);
+      }
+      S.plane[l][vi] = pl;
+      S.valid[l][vi] = ok ? 1 : 0;
+    }
+  }
+}
+
+__device__ void stage_direction(Shared& S, const Volume& V, const Params& p, int d, int tid) {
+  if (V.layers16 != nullptr) {
+    stage_direction16(S, V, p.voxel_size, d, tid);
+    return;
+  }
   for (int i = tid; i < kStaged * kLayers; i += kThreads) {
     const int l = i % kLayers;
     const int vi = i / kLayers;
@@ -323,7 +353,7 @@ __global__ void __launch_bounds__(kThreads, 2) mc_count_kernel(const Volume V, c
     for (int d = 0; d < kDirs; ++d) {
       uint32_t total = 0U;
       if (dirs & (1U << d)) {  // uniform across the CTA
-        stage_direction(S, V, d, tid);
+        stage_direction(S, V, p, d, tid);
         __syncthreads();
         const uint32_t n = static_cast<uint32_t>(process_cell<false>(S, p, gx, gy, gz, lx, ly, lz, tid, nullptr));
         cell_counts[(static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + tid] = static_cast<uint8_t>(n);
@@ -362,7 +392,7 @@ __global__ void __launch_bounds__(kThreads, 2) mc_emit_kernel(const Volume V, co
     for (int d = 0; d < kDirs; ++d) {
       const uint32_t total = dir_totals[static_cast<size_t>(b) * kDirs + d];
       if (total == 0U) continue;  // uniform
-      stage_direction(S, V, d, tid);
+      stage_direction(S, V, p, d, tid);
       const uint32_t n = cell_counts[(static_cast<size_t>(b) * kDirs + d) * kBlockVoxels + tid];
       const uint32_t prefix = block_scan(S, n, tid);  // its barriers also publish the staged direction
       if (n > 0U) process_cell<true>(S, p, gx, gy, gz, lx, ly, lz, tid, tris + (run + prefix) * 9ULL);

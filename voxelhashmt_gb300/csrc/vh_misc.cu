@@ -16,10 +16,7 @@ __global__ void __launch_bounds__(256) recount_kernel(const Volume V, unsigned l
     const uint32_t b = static_cast<uint32_t>(i / kBlockVoxels);
     const int li = static_cast<int>(i % kBlockVoxels);
     bool obs = false;
-    for (int d = 0; d < kDirs && !obs; ++d) {
-      const float4* L = V.layers + layer_index(b, d, li, 0);
-      obs = L[0].x > 0.0f || L[1].x > 0.0f || L[2].x > 0.0f;
-    }
+    for (int d = 0; d < kDirs && !obs; ++d) obs = bin_observed(V, b, d, li);
     local += obs ? 1ULL : 0ULL;
   }
 #pragma unroll
@@ -37,7 +34,13 @@ __global__ void __launch_bounds__(256) export_kernel(const Volume V, uint32_t fi
     const int d = static_cast<int>((i / kLayers) % kDirs);
     const int li = static_cast<int>((i / (kLayers * kDirs)) % kBlockVoxels);
     const uint32_t bo = static_cast<uint32_t>(i / (static_cast<size_t>(kLayers) * kDirs * kBlockVoxels));
-    voxels[i] = V.layers[layer_index(first + bo, d, li, l)];
+    if (V.layers16 == nullptr) {
+      voxels[i] = V.layers[layer_index(first + bo, d, li, l)];
+    } else {
+      float4 L[kLayers];
+      load_bin(V, first + bo, d, li, V.block_keys[first + bo], V.voxel_size, L[0], L[1], L[2]);
+      voxels[i] = L[l];
+    }
     if (keys && d == 0 && l == 0 && li == 0) {
       const int4 k = V.block_keys[first + bo];
       keys[3 * bo] = k.x;
@@ -116,14 +119,13 @@ __global__ void __launch_bounds__(256) import_voxels_kernel(const Volume V, cons
     uint32_t dirs = 0U;
     if (b != kInvalidBlock) {
       const float4* src = voxels + t * kDirs * kLayers;
+      const int4 bk = V.block_keys[b];
       for (int d = 0; d < kDirs; ++d) {
-        for (int l = 0; l < kLayers; ++l) {
-          const float4 L = src[d * kLayers + l];
-          V.layers[layer_index(b, d, li, l)] = L;
-          if (L.x > 0.0f) {
-            obs = true;
-            dirs |= 1U << d;
-          }
+        const float4 L0 = src[d * kLayers], L1 = src[d * kLayers + 1], L2 = src[d * kLayers + 2];
+        store_bin(V, b, d, li, bk, V.voxel_size, L0, L1, L2);
+        if (L0.x > 0.0f || L1.x > 0.0f || L2.x > 0.0f) {
+          obs = true;
+          dirs |= 1U << d;
         }
       }
     }
