@@ -311,6 +311,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   step(dalloc(&V.visible, buckets));
   step(dalloc(&V.active, nb * vh::kBlockVoxels));
   V.voxel_size = params->voxel_size;
+  V.inv_voxel_size = 1.0f / params->voxel_size;
   if (params->layer_format == 1) {
     step(cudaMalloc(reinterpret_cast<void**>(&V.layers16), std::max<size_t>(nb, 1) * kBlockBytes16));
   } else {

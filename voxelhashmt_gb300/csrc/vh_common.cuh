@@ -72,7 +72,9 @@ struct Volume {
   uint32_t capacity;
   uint32_t mask;
   uint32_t max_blocks;
-  float voxel_size;  // metres (the FP16 codec's unit)
+  float voxel_size;      // metres (the FP16 codec's unit)
+  float inv_voxel_size;  // 1 / voxel_size, rounded once on the host
+  uint32_t pad[3];
 };
 
 struct Mat34 {
@@ -249,8 +251,9 @@ __device__ __forceinline__ size_t layer_index(uint32_t b, int d, int li, int l) 
 // relative to the voxel they belong to because absolute world metres would have a 4 mm binary16 step at
 // 4 m; relative to the voxel, |s|, |p| stay below a few truncation distances and the step is <= 1/64 voxel.
 // Empty layers are all-zero.  The update arithmetic stays FP32: a bin is decoded to three FP32 records,
-// updated, and encoded back.  Every operation of the codec is an IEEE round-to-nearest intrinsic, so the
-// fast-math and the exact compiles encode and decode identically.
+// updated, and encoded back.  The codec's products and sums are explicit round-to-nearest intrinsics and
+// its one approximation is the hardware reciprocal square root, so the exact and the fast-math compiles
+// encode and decode alike.
 constexpr int kBinWords16 = 2;
 
 __device__ __forceinline__ size_t bin16_index(uint32_t b, int d, int li) {
@@ -276,61 +279,62 @@ __device__ __forceinline__ f3 bin_normal(uint32_t packed) {
   float y = __fadd_rn(__fmul_rn(div65535(static_cast<float>(packed >> 16U)), 2.0f), -1.0f);
   const float z = __fadd_rn(__fadd_rn(1.0f, -fabsf(x)), -fabsf(y));
   if (z < 0.0f) {
-    const float fx = __fmul_rn(__fadd_rn(1.0f, -fabsf(y)), x >= 0.0f ? 1.0f : -1.0f);
-    const float fy = __fmul_rn(__fadd_rn(1.0f, -fabsf(x)), y >= 0.0f ? 1.0f : -1.0f);
+    const float fx = copysignf(__fadd_rn(1.0f, -fabsf(y)), x >= 0.0f ? 1.0f : -1.0f);
+    const float fy = copysignf(__fadd_rn(1.0f, -fabsf(x)), y >= 0.0f ? 1.0f : -1.0f);
     x = fx;
     y = fy;
   }
-  const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
-  if (len <= 1e-6f) return mk3(0.0f, 0.0f, 1.0f);
-  return mk3(__fdiv_rn(x, len), __fdiv_rn(y, len), __fdiv_rn(z, len));
+  // |(x, y, z)|_1 = 1, so the squared length is in [1/3, 1]: no degenerate case
+  const float inv = rsqrtf(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+  return mk3(__fmul_rn(x, inv), __fmul_rn(y, inv), __fmul_rn(z, inv));
 }
 
 __device__ __forceinline__ float dot_rn(f3 a, f3 b) {
   return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
 }
 
-__device__ __forceinline__ float4 decode_layer16(uint16_t w, uint16_t s, uint16_t p, uint32_t n, f3 c, float cd,
-                                                 float vs) {
-  const float wf = __half2float(__ushort_as_half(w));
-  if (!(wf > 0.0f)) return make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  const float sc = __fadd_rn(cd, __fmul_rn(__half2float(__ushort_as_half(s)), vs));
-  const float po = __fadd_rn(dot_rn(bin_normal(n), c), __fmul_rn(__half2float(__ushort_as_half(p)), vs));
-  return make_float4(wf, sc, po, __uint_as_float(n));
+__device__ __forceinline__ float h2f(uint32_t h) { return __half2float(__ushort_as_half(static_cast<uint16_t>(h))); }
+__device__ __forceinline__ uint32_t f2h(float x) { return __half_as_ushort(__float2half_rn(x)); }
+
+// layer record from its binary16 triplet (n: unit normal of the packed word, from bin_normal)
+__device__ __forceinline__ float4 decode_layer16(uint32_t w, uint32_t s, uint32_t p, uint32_t packed, f3 n, f3 c,
+                                                 float cd, float vs) {
+  return make_float4(h2f(w), __fadd_rn(cd, __fmul_rn(h2f(s), vs)), __fadd_rn(dot_rn(n, c), __fmul_rn(h2f(p), vs)),
+                     __uint_as_float(packed));
 }
 
-__device__ __forceinline__ void encode_layer16(const float4& L, f3 c, float cd, float vs, uint16_t& w, uint16_t& s,
-                                               uint16_t& p) {
-  if (!(L.x > 0.0f)) {
-    w = s = p = 0;
-    return;
-  }
-  const uint32_t n = __float_as_uint(L.w);
-  w = __half_as_ushort(__float2half_rn(L.x));
-  if (w == 0) w = 1;  // a positive weight below the binary16 range keeps the layer observed
-  s = __half_as_ushort(__float2half_rn(__fdiv_rn(__fadd_rn(L.y, -cd), vs)));
-  p = __half_as_ushort(__float2half_rn(__fdiv_rn(__fadd_rn(L.z, -dot_rn(bin_normal(n), c)), vs)));
+// binary16 triplet of an observed layer record, packed as w | s << 16 and p
+__device__ __forceinline__ void encode_layer16(const float4& L, f3 n, f3 c, float cd, float inv_vs, uint32_t& ws,
+                                               uint32_t& p) {
+  uint32_t w = f2h(L.x);
+  if (w == 0U) w = 1U;  // a positive weight below the binary16 range keeps the layer observed
+  ws = w | (f2h(__fmul_rn(__fadd_rn(L.y, -cd), inv_vs)) << 16);
+  p = f2h(__fmul_rn(__fadd_rn(L.z, -dot_rn(n, c)), inv_vs));
 }
 
 __device__ __forceinline__ void decode_bin16(const uint4& A, const uint4& B, f3 c, int d, float vs, float4& L0,
                                              float4& L1, float4& L2) {
   const float cd = axis_coordinate(c, d);
-  L0 = decode_layer16(A.x & 0xffffU, A.x >> 16, A.y & 0xffffU, B.y, c, cd, vs);
-  L1 = decode_layer16(A.y >> 16, A.z & 0xffffU, A.z >> 16, B.z, c, cd, vs);
-  L2 = decode_layer16(A.w & 0xffffU, A.w >> 16, B.x & 0xffffU, B.w, c, cd, vs);
+  const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  L0 = (A.x & 0xffffU) ? decode_layer16(A.x & 0xffffU, A.x >> 16, A.y & 0xffffU, B.y, bin_normal(B.y), c, cd, vs) : z;
+  L1 = (A.y >> 16) ? decode_layer16(A.y >> 16, A.z & 0xffffU, A.z >> 16, B.z, bin_normal(B.z), c, cd, vs) : z;
+  L2 = (A.w & 0xffffU) ? decode_layer16(A.w & 0xffffU, A.w >> 16, B.x & 0xffffU, B.w, bin_normal(B.w), c, cd, vs) : z;
 }
 
 __device__ __forceinline__ void encode_bin16(const float4& L0, const float4& L1, const float4& L2, f3 c, int d,
-                                             float vs, uint4& A, uint4& B) {
+                                             float inv_vs, uint4& A, uint4& B) {
   const float cd = axis_coordinate(c, d);
-  uint16_t w0, s0, p0, w1, s1, p1, w2, s2, p2;
-  encode_layer16(L0, c, cd, vs, w0, s0, p0);
-  encode_layer16(L1, c, cd, vs, w1, s1, p1);
-  encode_layer16(L2, c, cd, vs, w2, s2, p2);
-  A = make_uint4(w0 | (static_cast<uint32_t>(s0) << 16), p0 | (static_cast<uint32_t>(w1) << 16),
-                 s1 | (static_cast<uint32_t>(p1) << 16), w2 | (static_cast<uint32_t>(s2) << 16));
-  B = make_uint4(p2, L0.x > 0.0f ? __float_as_uint(L0.w) : 0U, L1.x > 0.0f ? __float_as_uint(L1.w) : 0U,
-                 L2.x > 0.0f ? __float_as_uint(L2.w) : 0U);
+  uint32_t ws[3] = {0U, 0U, 0U}, pp[3] = {0U, 0U, 0U}, nn[3] = {0U, 0U, 0U};
+  const float4* L[3] = {&L0, &L1, &L2};
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    if (L[l]->x > 0.0f) {
+      nn[l] = __float_as_uint(L[l]->w);
+      encode_layer16(*L[l], bin_normal(nn[l]), c, cd, inv_vs, ws[l], pp[l]);
+    }
+  }
+  A = make_uint4(ws[0], pp[0] | ((ws[1] & 0xffffU) << 16), (ws[1] >> 16) | (pp[1] << 16), ws[2]);
+  B = make_uint4(pp[2], nn[0], nn[1], nn[2]);
 }
 
 // the three layer records of one bin, in the FP32 record form, whichever storage the volume uses
@@ -357,7 +361,7 @@ __device__ __forceinline__ void store_bin(const Volume& V, uint32_t b, int d, in
     return;
   }
   uint4 A, B;
-  encode_bin16(L0, L1, L2, voxel_centre(bk, li, vs), d, vs, A, B);
+  encode_bin16(L0, L1, L2, voxel_centre(bk, li, vs), d, V.inv_voxel_size, A, B);
   uint4* q = V.layers16 + bin16_index(b, d, li);
   q[0] = A;
   q[1] = B;

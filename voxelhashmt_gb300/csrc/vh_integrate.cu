@@ -411,6 +411,102 @@ __device__ __forceinline__ bool integrate_sample(const Params& p, float4& L0, fl
   return true;
 }
 
+// integrate_sample on an FP16 bin (A, B): each observed layer's normal is unpacked once (for the match and
+// for its plane offset), only the updated layer is re-encoded, and the three layers are re-sorted as raw
+// binary16 triplets.  Same decisions and blending formulas as integrate_sample on the decoded records.
+// Returns true when a layer was updated (A, B then hold the new bin).
+__device__ __forceinline__ uint32_t cswap_u32(uint32_t& a, uint32_t& b, bool c) {
+  const uint32_t t = a;
+  a = c ? b : a;
+  b = c ? t : b;
+  return 0U;
+}
+
+__device__ __forceinline__ bool integrate_bin16(const Params& p, const Volume& V, uint4& A, uint4& B, f3 c, int dir,
+                                                float sc, f3 sp, f3 nw, float obs) {
+  if (obs <= 0.0f) return false;
+  const f3 n = normalize3(nw);
+  if (norm3(n) <= 1e-6f) return false;
+  const float vs = V.voxel_size, inv_vs = V.inv_voxel_size;
+  const float cd = axis_coordinate(c, dir);
+  uint32_t w16[3] = {A.x & 0xffffU, A.y >> 16, A.w & 0xffffU};
+  uint32_t s16[3] = {A.x >> 16, A.z & 0xffffU, A.w >> 16};
+  uint32_t p16[3] = {A.y & 0xffffU, A.z >> 16, B.x & 0xffffU};
+  uint32_t nk[3] = {B.y, B.z, B.w};
+  float ls[3];
+  f3 ln[3];
+  int empty = -1, best = -1;
+  float best_delta = 1e30f;
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    ls[l] = __fadd_rn(cd, __fmul_rn(h2f(s16[l]), vs));
+    ln[l] = mk3(0.0f, 0.0f, 1.0f);
+    if (w16[l] == 0U) {
+      if (empty < 0) empty = l;
+      continue;
+    }
+    ln[l] = bin_normal(nk[l]);
+    if (dot3(ln[l], n) < p.layer_normal_cos) continue;
+    const float delta = fabsf(ls[l] - sc);
+    if (delta < best_delta) {
+      best_delta = delta;
+      best = l;
+    }
+  }
+  const int li = (best >= 0 && best_delta <= p.merge_tol) ? best : empty;
+  if (li < 0) return false;
+  const bool had = w16[li] != 0U;
+  const float pw = had ? h2f(w16[li]) : 0.0f;
+  const float ew = fminf(obs, fmaxf(0.0f, p.max_weight - pw));
+  if (ew <= 0.0f) return false;
+  const float nwt = pw + ew;
+  const float plane_offset = dot3(n, sp);
+  const f3 pn = li == 0 ? ln[0] : (li == 1 ? ln[1] : ln[2]);
+  float new_s = sc, new_p = plane_offset;
+  f3 blended = n;
+  if (had) {
+    const float old_s = li == 0 ? ls[0] : (li == 1 ? ls[1] : ls[2]);
+    const float old_p = __fadd_rn(dot_rn(pn, c), __fmul_rn(h2f(p16[li]), vs));
+    new_s = (old_s * pw + sc * ew) / nwt;
+    new_p = (old_p * pw + plane_offset * ew) / nwt;
+    blended = normalize3(mul3(add3(mul3(pn, pw), mul3(n, ew)), 1.0f / nwt));
+    if (norm3(blended) <= 1e-6f) blended = n;
+  }
+  const uint32_t packed = pack_normal(blended);
+  uint32_t nwt16 = f2h(nwt);
+  if (nwt16 == 0U) nwt16 = 1U;
+  const uint32_t ns16 = f2h(__fmul_rn(__fadd_rn(new_s, -cd), inv_vs));
+  const uint32_t np16 = f2h(__fmul_rn(__fadd_rn(new_p, -dot_rn(bin_normal(packed), c)), inv_vs));
+#pragma unroll
+  for (int l = 0; l < 3; ++l) {
+    if (l == li) {
+      w16[l] = nwt16;
+      s16[l] = ns16;
+      p16[l] = np16;
+      nk[l] = packed;
+      ls[l] = new_s;
+    }
+  }
+  // sortDirectionalLayersGpu's bubble network: observed layers first, ascending surface coordinate
+  auto step = [&](int a, int b) {
+    const bool av = w16[a] != 0U, bv = w16[b] != 0U;
+    const bool sw = (!av && bv) || (av && bv && ls[a] > ls[b]);
+    cswap_u32(w16[a], w16[b], sw);
+    cswap_u32(s16[a], s16[b], sw);
+    cswap_u32(p16[a], p16[b], sw);
+    cswap_u32(nk[a], nk[b], sw);
+    const float t = ls[a];
+    ls[a] = sw ? ls[b] : ls[a];
+    ls[b] = sw ? t : ls[b];
+  };
+  step(0, 1);
+  step(1, 2);
+  step(0, 1);
+  A = make_uint4(w16[0] | (s16[0] << 16), p16[0] | (w16[1] << 16), s16[1] | (p16[1] << 16), w16[2] | (s16[2] << 16));
+  B = make_uint4(p16[2], w16[0] ? nk[0] : 0U, w16[1] ? nk[1] : 0U, w16[2] ? nk[2] : 0U);
+  return true;
+}
+
 // First part of integrateActiveBlocksKernel for one voxel (:849-877): voxel centre, projection, bilinear
 // depth, truncation test.  Returns false when the reference returns before touching the voxel.
 __device__ __forceinline__ bool voxel_prefix(const float* __restrict__ depth, const Params& p, const int4& bk, int li,
@@ -638,62 +734,135 @@ __device__ __forceinline__ bool map_normal(const float4* __restrict__ nmap, cons
   return true;
 }
 
-// One pass over every voxel of the visible blocks with the normal from the map: prefix, observation and
-// layer update in the same thread (the per-voxel cost is uniform, so no active list is needed).
+// The layer update of one voxel that passed voxel_prefix, with the normal from the map.  Returns true when a
+// layer was updated; newly = the voxel was observed for the first time.
+__device__ __forceinline__ bool map_update_voxel(const float* __restrict__ depth, const float4* __restrict__ nmap,
+                                                 const Volume& V, const Params& p, uint32_t b, int li, f3 pc, float u,
+                                                 float v, float d, bool& newly) {
+  newly = false;
+  const int4 bk = V.block_keys[b];
+  const float sd = d - pc.z;
+  const f3 view = normalize3(pc);
+  float view_w = 1.0f;
+  f3 nc = mul3(view, -1.0f);
+  if (map_normal(nmap, p, u, v, nc)) view_w = fabsf(dot3(nc, view));
+  const float obs = observation_weight(p, d, sd, view_w);
+  const f3 nw = normalize3(xform_vector(p.T_wc, nc));
+  const int dir = obs > 0.0f ? dominant_direction(nw) : -1;
+  if (dir < 0 || dir >= kDirs) return false;
+  const f3 spw = xform_point(p.T_wc, backproject(u, v, d, p));
+  const float sc = coordinate_along(spw, dir);
+  bool updated;
+  if (V.layers16 != nullptr) {
+    uint4* q = V.layers16 + bin16_index(b, dir, li);
+    uint4 A = q[0], B = q[1];
+    updated = integrate_bin16(p, V, A, B, voxel_centre(bk, li, p.voxel_size), dir, sc, spw, nw, obs);
+    if (updated) {
+      q[0] = A;
+      q[1] = B;
+    }
+  } else {
+    float4 L0, L1, L2;
+    load_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
+    updated = integrate_sample(p, L0, L1, L2, sc, spw, nw, obs);
+    if (updated) store_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
+  }
+  if (updated) {
+    const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
+    const uint32_t bit = 1U << (li & 31);
+    if (!(V.obs_mask[w] & bit)) newly = !(atomicOr(&V.obs_mask[w], bit) & bit);
+    const uint32_t dbit = 1U << dir;
+    if (!(V.dir_mask[b] & dbit)) atomicOr(&V.dir_mask[b], dbit);
+  }
+  return updated;
+}
+
+// One pass over every voxel of the visible blocks with the normal from the map.  Each CTA walks chunks of
+// kThreads voxel slots; the slots that pass voxel_prefix are appended (warp-aggregated) to a shared-memory
+// queue together with their projection, and whenever the queue holds kThreads entries the CTA updates one
+// full batch, one entry per thread.  The expensive part therefore runs on full warps whatever the pass
+// rate, and the survivors of one chunk wait at most one chunk for their batch.
+constexpr int kQueue = 2 * kThreads;
+
+struct MapQueue {
+  uint32_t code[kQueue];  // (pool block << 9) | voxel
+  float u[kQueue], v[kQueue], d[kQueue], x[kQueue], y[kQueue], z[kQueue];
+  uint32_t count;
+};
+
+__device__ __forceinline__ void map_update_entry(const float* __restrict__ depth, const float4* __restrict__ nmap,
+                                                 const Volume& V, const Params& p, const MapQueue& Q, int e,
+                                                 bool& updated, bool& newly) {
+  const uint32_t code = Q.code[e];
+  updated = map_update_voxel(depth, nmap, V, p, code >> 9, static_cast<int>(code & 511U), mk3(Q.x[e], Q.y[e], Q.z[e]),
+                             Q.u[e], Q.v[e], Q.d[e], newly);
+}
+
+__device__ __forceinline__ void count_updates(const Volume& V, bool updated, bool newly, int lane) {
+  const uint32_t upd = __ballot_sync(0xffffffffU, updated);
+  const uint32_t nw_ = __ballot_sync(0xffffffffU, newly);
+  if (lane == 0) {
+    if (upd) atomicAdd(&V.counters->integrated_voxels, static_cast<uint32_t>(__popc(upd)));
+    if (nw_) atomicAdd(&V.counters->observed_voxels, static_cast<unsigned long long>(__popc(nw_)));
+  }
+}
+
 __global__ void __launch_bounds__(kThreads) fused_update_kernel(const float* __restrict__ depth,
                                                                 const float4* __restrict__ nmap, const Volume V,
                                                                 const Params p) {
+  __shared__ MapQueue Q;
   const uint32_t nvis = V.counters->visible_count;
   const unsigned long long total = static_cast<unsigned long long>(nvis) * kBlockVoxels;
+  const unsigned long long nchunks = total / kThreads;  // kThreads divides 512
   const int lane = threadIdx.x & 31;
-  const unsigned long long stride = static_cast<unsigned long long>(gridDim.x) * blockDim.x;
-  for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; i < total;
-       i += stride) {
+  if (threadIdx.x == 0) Q.count = 0U;
+  __syncthreads();
+  for (unsigned long long chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+    // 1. prefix of one slot per thread, survivors appended to the queue
+    const unsigned long long i = chunk * kThreads + threadIdx.x;
     const uint32_t item = static_cast<uint32_t>(i >> 9);
     const int li = static_cast<int>(i & 511U);
     const uint32_t b = V.slot_block[V.visible[item]];
-    bool pass = false, updated = false;
-    uint32_t newly = 0U;
-    if (b != kInvalidBlock) {
-      const int4 bk = V.block_keys[b];
-      f3 pc;
-      float u, v, d;
-      pass = voxel_prefix(depth, p, bk, li, pc, u, v, d);
-      if (pass) {
-        const float sd = d - pc.z;
-        const f3 view = normalize3(pc);
-        float view_w = 1.0f;
-        f3 nc = mul3(view, -1.0f);
-        if (map_normal(nmap, p, u, v, nc)) view_w = fabsf(dot3(nc, view));
-        const float obs = observation_weight(p, d, sd, view_w);
-        const f3 nw = normalize3(xform_vector(p.T_wc, nc));
-        const int dir = obs > 0.0f ? dominant_direction(nw) : -1;
-        if (dir >= 0 && dir < kDirs) {
-          const f3 spw = xform_point(p.T_wc, backproject(u, v, d, p));
-          const float sc = coordinate_along(spw, dir);
-          float4 L0, L1, L2;
-          load_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
-          updated = integrate_sample(p, L0, L1, L2, sc, spw, nw, obs);
-          if (updated) {
-            store_bin(V, b, dir, li, bk, p.voxel_size, L0, L1, L2);
-            const size_t w = static_cast<size_t>(b) * (kBlockVoxels / 32) + (li >> 5);
-            const uint32_t bit = 1U << (li & 31);
-            if (!(V.obs_mask[w] & bit)) newly = (atomicOr(&V.obs_mask[w], bit) & bit) ? 0U : 1U;
-            const uint32_t dbit = 1U << dir;
-            if (!(V.dir_mask[b] & dbit)) atomicOr(&V.dir_mask[b], dbit);
-          }
-        }
-      }
+    bool pass = false;
+    f3 pc = mk3(0.0f, 0.0f, 0.0f);
+    float u = 0.0f, v = 0.0f, d = 0.0f;
+    if (b != kInvalidBlock) pass = voxel_prefix(depth, p, V.block_keys[b], li, pc, u, v, d);
+    const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
+    uint32_t base = 0U;
+    if (lane == 0 && ballot) {
+      base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
+      atomicAdd(&V.counters->active_voxels, static_cast<uint32_t>(__popc(ballot)));
     }
-    const uint32_t act = __ballot_sync(0xffffffffU, pass);
-    const uint32_t upd = __ballot_sync(0xffffffffU, updated);
-    const uint32_t nw_ = __ballot_sync(0xffffffffU, newly != 0U);
-    if (lane == 0) {
-      if (act) atomicAdd(&V.counters->active_voxels, static_cast<uint32_t>(__popc(act)));
-      if (upd) atomicAdd(&V.counters->integrated_voxels, static_cast<uint32_t>(__popc(upd)));
-      if (nw_) atomicAdd(&V.counters->observed_voxels, static_cast<unsigned long long>(__popc(nw_)));
+    base = __shfl_sync(0xffffffffU, base, 0);
+    if (pass) {
+      const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
+      Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
+      Q.u[e] = u;
+      Q.v[e] = v;
+      Q.d[e] = d;
+      Q.x[e] = pc.x;
+      Q.y[e] = pc.y;
+      Q.z[e] = pc.z;
+    }
+    __syncthreads();
+    // 2. a full batch: the last kThreads entries, one per thread.  Every thread reads the count before any
+    // thread appends again, so the branch below is uniform across the CTA.
+    const uint32_t n = Q.count;
+    __syncthreads();
+    if (n >= static_cast<uint32_t>(kThreads)) {
+      bool updated, newly;
+      map_update_entry(depth, nmap, V, p, Q, static_cast<int>(n) - kThreads + threadIdx.x, updated, newly);
+      count_updates(V, updated, newly, lane);
+      __syncthreads();
+      if (threadIdx.x == 0) Q.count = n - kThreads;
+      __syncthreads();
     }
   }
+  // 3. the remainder (< kThreads entries)
+  const uint32_t n = Q.count;
+  bool updated = false, newly = false;
+  if (threadIdx.x < n) map_update_entry(depth, nmap, V, p, Q, threadIdx.x, updated, newly);
+  count_updates(V, updated, newly, lane);
 }
 
 }  // namespace
