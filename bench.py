@@ -318,6 +318,7 @@ def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
     mc_ms = m0.elapsed_time(m1)
     tris = backend.extract_mesh_cuda(vol)
     observed = vol.observed_voxel_count()
+    tuned = vol.autotune_result()
 
     # per-frame updated / active voxels of the last 16 frames (algorithmic bytes), on a replay
     vol.reset(stream)
@@ -350,7 +351,7 @@ def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
             "nblocks": nblocks, "mc_ms": mc_ms, "mc_blocks_per_s": nblocks / (mc_ms / 1000.0),
             "triangles": n_tri.value, "tris": tris, "observed": observed, "upd_mean": float(np.mean(upd)),
             "act_mean": float(np.mean(act)), "e2e_value": world * args.steps * px / e2e_s / 1e6,
-            "clocks": clock_info}
+            "clocks": clock_info, "autotune": tuned}
 
 
 def run_gb300(args):
@@ -420,6 +421,7 @@ def run_gb300(args):
                 "stage_ms_per_frame": {k: round(v / max(1, r["nprof"]), 4) for k, v in r["stage_ms"].items()},
                 "visible_blocks_last_frame": r["fstats"]["visible_blocks"],
                 "updated_voxels_per_frame": round(r["upd_mean"]), "active_voxels_per_frame": round(r["act_mean"]),
+                "update_launch_shape": r["autotune"] if r["autotune"]["variant"] >= 0 else None,
                 "chamfer": quality.get(name)}
 
     if rank == 0:

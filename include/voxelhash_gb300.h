@@ -100,6 +100,11 @@ typedef struct vh_algorithm {
   /* 0 (default): the reference's bilateral surface normal evaluated at each voxel's projection (50 subpixel
    * depth samples); 1: the same normal evaluated once per pixel, bilinearly interpolated per voxel. */
   int32_t normal_mode;
+  /* 1 (default): with normal_mode 1, the first frames cycle the layer-update kernel through its launch shapes
+   * (threads per CTA x minimum resident CTAs per SM), time each with CUDA events and keep the fastest
+   * (results do not depend on the shape); 0: the shape launch_variant. */
+  int32_t autotune;
+  int32_t launch_variant; /* the layer-update launch shape used without autotuning (0..5, default 0) */
 } vh_algorithm;
 
 /* per-frame statistics of the last integrated/allocated frame */
@@ -200,6 +205,12 @@ vh_status vh_export_blocks(vh_volume* volume, uint64_t first, uint64_t count, in
  * Synchronises. */
 vh_status vh_import_blocks(vh_volume* volume, const int32_t* keys, const void* voxels, uint64_t count,
                            int32_t in_on_device, void* stream);
+
+/* The launch shape the autotuner chose for the layer update (vh_algorithm.autotune): variant index (-1 while
+ * still tuning or when not tuned), threads per CTA, minimum resident CTAs per SM, and the chosen shape's median
+ * time in ms.  No reference counterpart. */
+vh_status vh_autotune_result(vh_volume* volume, int32_t* variant, int32_t* threads_per_cta,
+                             int32_t* min_ctas_per_sm, float* ms);
 
 /* Stage timing with CUDA events (the reference times its stages with steady_clock, src/main.cpp:424-452).
  * While enabled, vh_integrate brackets each of its kernels with events on the call's stream.

@@ -284,3 +284,40 @@ def test_fp16_storage_matches_fp32(backend, orbit_half, chosen):
     assert fresh.observed_voxel_count() == vols[1].observed_voxel_count()
     for v in vols + [fresh]:
         v.close()
+
+
+@pytest.mark.parametrize("fast_math", [0, 1])
+def test_autotuned_launch_shapes_give_identical_volumes(backend, orbit_half, fast_math):
+    """The autotuner cycles the layer update through its launch shapes on the first frames; every shape runs
+    the same per-voxel update.  In the exact compile (no contraction, IEEE division and square root) the
+    volume is bit-identical to one fused with a fixed shape.  In the fast-math compile each shape is a
+    separate instantiation whose multiply-add contraction the compiler decides on its own, so fields may
+    differ in the last bits: identical keys and occupancy on 99.9% of bins, fields within 1e-3 voxel
+    (99.9%)."""
+    sc, depths, _ = orbit_half
+    frames = list(range(16)) + list(range(16)) + list(range(4))  # 36 frames: tuning (18) and after
+    from oracle import oracle as O
+    algo = dict(allocation_mode=1, fast_math=fast_math, normal_mode=1)
+    tuned, _ = _fuse(backend, sc, frames, depths, **algo)
+    fixed, _ = _fuse(backend, sc, frames, depths, autotune=0, **algo)
+    res = tuned.autotune_result()
+    print("autotune", fast_math, res)
+    assert res["variant"] >= 0 and res["threads_per_cta"] in (64, 128, 256, 512) and res["ms"] > 0
+    assert fixed.autotune_result()["variant"] == -1
+    k1, v1 = O.sort_blocks(*tuned.export_blocks())
+    k2, v2 = O.sort_blocks(*fixed.export_blocks())
+    assert np.array_equal(k1, k2)
+    print("differing words", int(np.sum(v1 != v2)), "of", v1.size)
+    if fast_math == 0:
+        assert np.array_equal(v1, v2)
+        assert tuned.observed_voxel_count() == fixed.observed_voxel_count()
+    else:
+        a = v1.view(np.float32).reshape(-1, 4)
+        b = v2.view(np.float32).reshape(-1, 4)
+        assert np.mean((a[:, 0] > 0) == (b[:, 0] > 0)) >= 0.999
+        both = (a[:, 0] > 0) & (b[:, 0] > 0)
+        for col in (1, 2):
+            e = np.abs(a[both, col].astype(np.float64) - b[both, col]) / sc.voxel_size
+            assert np.quantile(e, 0.999) <= 1e-3, (col, float(np.quantile(e, 0.999)))
+    tuned.close()
+    fixed.close()

@@ -45,6 +45,7 @@ class VhAlgorithm(C.Structure):
         ("max_voxel_weight", C.c_float), ("depth_sigma", C.c_float), ("huber_delta", C.c_float),
         ("min_observation_weight", C.c_float), ("min_view_angle_weight", C.c_float),
         ("allocation_mode", C.c_int32), ("fast_math", C.c_int32), ("normal_mode", C.c_int32),
+        ("autotune", C.c_int32), ("launch_variant", C.c_int32),
     ]
 
 
@@ -110,6 +111,8 @@ _SIGNATURES = {
     "vh_allocate_static_scratch": (C.c_int, [_vp, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_float, C.c_float,
                                              C.c_int32, _vp, C.c_size_t, _szp, _vp]),
     "vh_import_blocks": (C.c_int, [_vp, _ip, _vp, C.c_uint64, C.c_int32, _vp]),
+    "vh_autotune_result": (C.c_int, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_float)]),
     "vh_profile_enable": (C.c_int, [_vp, C.c_int32]),
     "vh_profile_read": (C.c_int, [_vp, C.POINTER(C.c_double), _u64p]),
     "vh_render_depth": (C.c_int, [_vp, C.c_int32, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_uint32,

@@ -142,6 +142,15 @@ class VoxelHashTSDF:
         _capi.check(_capi.lib().vh_frame_stats_get(self.handle, C.byref(s), _stream_handle(stream)), self.handle)
         return {f: getattr(s, f) for f, _ in s._fields_}
 
+    def autotune_result(self):
+        """{'variant', 'threads_per_cta', 'min_ctas_per_sm', 'ms'} of the layer-update launch shape the
+        autotuner kept (variant -1 while tuning)."""
+        v, t, b = C.c_int32(), C.c_int32(), C.c_int32()
+        ms = C.c_float()
+        _capi.check(_capi.lib().vh_autotune_result(self.handle, C.byref(v), C.byref(t), C.byref(b), C.byref(ms)),
+                    self.handle)
+        return {"variant": v.value, "threads_per_cta": t.value, "min_ctas_per_sm": b.value, "ms": ms.value}
+
     def profile(self, enable=True):
         """Stage timing of vh_integrate with CUDA events (see read_profile)."""
         _capi.check(_capi.lib().vh_profile_enable(self.handle, 1 if enable else 0), self.handle)

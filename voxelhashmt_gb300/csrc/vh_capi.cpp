@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -23,6 +24,13 @@ struct vh_volume {
   float* d_depth_in = nullptr;
   float* d_depth_filtered = nullptr;
   float4* d_normal_map = nullptr;  // per-pixel normals (vh_algorithm.normal_mode 1)
+  // launch-shape autotuner of the fused update (vh_algorithm.autotune): frames cycle through the variants,
+  // each timed with a pair of events, until every variant has kTuneRounds samples; then the fastest is kept
+  int tuned_variant = -1;
+  int tune_frames = 0;
+  std::vector<std::array<cudaEvent_t, 2>> tune_events;
+  std::vector<int> tune_variant_of;
+  float tune_best_ms = 0.0f;
   size_t depth_capacity = 0;  // pixels
   uint32_t* d_mc_counts = nullptr;
   uint32_t* d_mc_dir_totals = nullptr;
@@ -191,6 +199,67 @@ uint64_t block_total(const vh_volume* v) {
   return std::min<uint64_t>(v->h_counters->num_blocks, v->dev.max_blocks);
 }
 
+constexpr int kTuneStart = 24;  // frames before tuning starts: the first frames of a volume update far more
+                                // voxels (everything is new) than the steady state the choice is for
+constexpr int kTuneRounds = 4;
+
+// Chooses the fused-update variant of this frame.  Until kTuneStart frames have run, the first variant; then,
+// while tuning, the next variant in the cycle and a pair of events to record around its launch; once every
+// variant has kTuneRounds samples, waits for the last one, keeps the variant with the smallest median time
+// and frees the events.
+vh_status autotune_step(vh_volume* v, int* variant, cudaEvent_t ev[2]) {
+  ev[0] = ev[1] = nullptr;
+  if (v->tuned_variant >= 0) {
+    *variant = v->tuned_variant;
+    return VH_OK;
+  }
+  const int nvar = v->algo.fast_math ? vh::fast::fused_variant_count() : vh::exact::fused_variant_count();
+  if (v->tune_frames < kTuneStart) {
+    *variant = 0;
+    ++v->tune_frames;
+    return VH_OK;
+  }
+  if (v->tune_frames < kTuneStart + nvar * kTuneRounds) {
+    *variant = (v->tune_frames - kTuneStart) % nvar;
+    std::array<cudaEvent_t, 2> pair{};
+    VH_CUDA(v, cudaEventCreate(&pair[0]));
+    VH_CUDA(v, cudaEventCreate(&pair[1]));
+    v->tune_events.push_back(pair);
+    v->tune_variant_of.push_back(*variant);
+    ev[0] = pair[0];
+    ev[1] = pair[1];
+    ++v->tune_frames;
+    return VH_OK;
+  }
+  VH_CUDA(v, cudaEventSynchronize(v->tune_events.back()[1]));
+  std::vector<std::vector<float>> times(nvar);
+  for (size_t i = 0; i < v->tune_events.size(); ++i) {
+    float ms = 0.0f;
+    VH_CUDA(v, cudaEventElapsedTime(&ms, v->tune_events[i][0], v->tune_events[i][1]));
+    times[v->tune_variant_of[i]].push_back(ms);
+  }
+  int best = 0;
+  float best_ms = 0.0f;
+  for (int k = 0; k < nvar; ++k) {
+    std::sort(times[k].begin(), times[k].end());
+    const float med = times[k][times[k].size() / 2];
+    if (k == 0 || med < best_ms) {
+      best = k;
+      best_ms = med;
+    }
+  }
+  for (auto& pair : v->tune_events) {
+    cudaEventDestroy(pair[0]);
+    cudaEventDestroy(pair[1]);
+  }
+  v->tune_events.clear();
+  v->tune_variant_of.clear();
+  v->tuned_variant = best;
+  v->tune_best_ms = best_ms;
+  *variant = best;
+  return VH_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -229,6 +298,8 @@ void vh_algorithm_default(vh_algorithm* a) {
   a->allocation_mode = 0;
   a->fast_math = 0;
   a->normal_mode = 0;
+  a->autotune = 1;
+  a->launch_variant = 0;
 }
 
 const char* vh_status_string(vh_status s) {
@@ -291,7 +362,8 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   }
   if (v->algo.filter_radius < 0 || v->algo.filter_radius > 2 || v->algo.normal_radius != 1 ||
       v->algo.allocation_mode < 0 || v->algo.allocation_mode > 1 || v->algo.fast_math < 0 || v->algo.fast_math > 1 ||
-      v->algo.normal_mode < 0 || v->algo.normal_mode > 1) {
+      v->algo.normal_mode < 0 || v->algo.normal_mode > 1 || v->algo.autotune < 0 || v->algo.autotune > 1 ||
+      v->algo.launch_variant < 0 || v->algo.launch_variant >= vh::exact::fused_variant_count()) {
     delete v;
     return VH_ERR_INVALID_ARGUMENT;
   }
@@ -363,6 +435,10 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_depth_in);
   dfree(v->d_depth_filtered);
   dfree(v->d_normal_map);
+  for (auto& pair : v->tune_events) {
+    cudaEventDestroy(pair[0]);
+    cudaEventDestroy(pair[1]);
+  }
   dfree(v->d_mc_counts);
   dfree(v->d_mc_dir_totals);
   dfree(v->d_mc_cell_counts);
@@ -432,13 +508,33 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
   VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_integrate_prepare(v->d_depth_filtered, v->dev, p, v->d_normal_map, s)
                                 : vh::exact::launch_integrate_prepare(v->d_depth_filtered, v->dev, p, v->d_normal_map, s));
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[3], s));
+  int variant = v->algo.launch_variant;
+  cudaEvent_t tune[2] = {nullptr, nullptr};
+  if (v->algo.normal_mode == 1 && v->algo.autotune) {
+    st = autotune_step(v, &variant, tune);
+    if (st != VH_OK) return st;
+    if (tune[0]) VH_CUDA(v, cudaEventRecord(tune[0], s));
+  }
   VH_CUDA(v, v->algo.fast_math
-                 ? vh::fast::launch_integrate_update(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s)
-                 : vh::exact::launch_integrate_update(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s));
+                 ? vh::fast::launch_integrate_update(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s, variant)
+                 : vh::exact::launch_integrate_update(v->d_depth_filtered, v->dev, p, 0, v->d_normal_map, s, variant));
+  if (tune[1]) VH_CUDA(v, cudaEventRecord(tune[1], s));
   if (v->profile) {
     VH_CUDA(v, cudaEventRecord(ev[4], s));
     v->profiled.push_back(std::move(ev));
   }
+  return VH_OK;
+}
+
+vh_status vh_autotune_result(vh_volume* v, int32_t* variant, int32_t* threads_per_cta, int32_t* min_ctas_per_sm,
+                             float* ms) {
+  if (!v) return VH_ERR_INVALID_ARGUMENT;
+  int t = 0, b = 0;
+  vh::exact::fused_variant_shape(v->tuned_variant, &t, &b);
+  if (variant) *variant = v->tuned_variant;
+  if (threads_per_cta) *threads_per_cta = v->tuned_variant >= 0 ? t : 0;
+  if (min_ctas_per_sm) *min_ctas_per_sm = v->tuned_variant >= 0 ? b : 0;
+  if (ms) *ms = v->tune_best_ms;
   return VH_OK;
 }
 

@@ -455,8 +455,10 @@ __device__ __forceinline__ bool integrate_bin16(const Params& p, const Volume& V
   }
   const int li = (best >= 0 && best_delta <= p.merge_tol) ? best : empty;
   if (li < 0) return false;
-  const bool had = w16[li] != 0U;
-  const float pw = had ? h2f(w16[li]) : 0.0f;
+  const uint32_t wli = li == 0 ? w16[0] : (li == 1 ? w16[1] : w16[2]);
+  const uint32_t pli = li == 0 ? p16[0] : (li == 1 ? p16[1] : p16[2]);
+  const bool had = wli != 0U;
+  const float pw = had ? h2f(wli) : 0.0f;
   const float ew = fminf(obs, fmaxf(0.0f, p.max_weight - pw));
   if (ew <= 0.0f) return false;
   const float nwt = pw + ew;
@@ -466,7 +468,7 @@ __device__ __forceinline__ bool integrate_bin16(const Params& p, const Volume& V
   f3 blended = n;
   if (had) {
     const float old_s = li == 0 ? ls[0] : (li == 1 ? ls[1] : ls[2]);
-    const float old_p = __fadd_rn(dot_rn(pn, c), __fmul_rn(h2f(p16[li]), vs));
+    const float old_p = __fadd_rn(dot_rn(pn, c), __fmul_rn(h2f(pli), vs));
     new_s = (old_s * pw + sc * ew) / nwt;
     new_p = (old_p * pw + plane_offset * ew) / nwt;
     blended = normalize3(mul3(add3(mul3(pn, pw), mul3(n, ew)), 1.0f / nwt));
@@ -782,16 +784,17 @@ __device__ __forceinline__ bool map_update_voxel(const float* __restrict__ depth
 // queue together with their projection, and whenever the queue holds kThreads entries the CTA updates one
 // full batch, one entry per thread.  The expensive part therefore runs on full warps whatever the pass
 // rate, and the survivors of one chunk wait at most one chunk for their batch.
-constexpr int kQueue = 2 * kThreads;
-
+template <int kT>
 struct MapQueue {
+  static constexpr int kQueue = 2 * kT;
   uint32_t code[kQueue];  // (pool block << 9) | voxel
   float u[kQueue], v[kQueue], d[kQueue], x[kQueue], y[kQueue], z[kQueue];
   uint32_t count;
 };
 
+template <int kT>
 __device__ __forceinline__ void map_update_entry(const float* __restrict__ depth, const float4* __restrict__ nmap,
-                                                 const Volume& V, const Params& p, const MapQueue& Q, int e,
+                                                 const Volume& V, const Params& p, const MapQueue<kT>& Q, int e,
                                                  bool& updated, bool& newly) {
   const uint32_t code = Q.code[e];
   updated = map_update_voxel(depth, nmap, V, p, code >> 9, static_cast<int>(code & 511U), mk3(Q.x[e], Q.y[e], Q.z[e]),
@@ -807,13 +810,17 @@ __device__ __forceinline__ void count_updates(const Volume& V, bool updated, boo
   }
 }
 
-__global__ void __launch_bounds__(kThreads) fused_update_kernel(const float* __restrict__ depth,
-                                                                const float4* __restrict__ nmap, const Volume V,
-                                                                const Params p) {
-  __shared__ MapQueue Q;
+// kT threads per CTA (a divisor of 512), at least kMinBlocks resident CTAs per SM (which caps the registers)
+template <int kT, int kMinBlocks>
+__global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const float* __restrict__ depth,
+                                                                     const float4* __restrict__ nmap, const Volume V,
+                                                                     const Params p) {
+  constexpr int kThreads = kT;
+  static_assert(kBlockVoxels % kT == 0, "CTA size must divide the block's voxel count");
+  __shared__ MapQueue<kT> Q;
   const uint32_t nvis = V.counters->visible_count;
   const unsigned long long total = static_cast<unsigned long long>(nvis) * kBlockVoxels;
-  const unsigned long long nchunks = total / kThreads;  // kThreads divides 512
+  const unsigned long long nchunks = total / kThreads;
   const int lane = threadIdx.x & 31;
   if (threadIdx.x == 0) Q.count = 0U;
   __syncthreads();
@@ -902,13 +909,48 @@ cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const 
 
 // second kernel: the layer update over the active list (update_kernel) or over every visible voxel with the
 // map normal (fused_update_kernel)
+// Launch shapes of fused_update_kernel the autotuner chooses from: (threads per CTA, minimum resident CTAs per
+// SM).  The grid is always the number of CTAs that fit on the device at once.
+struct FusedVariant {
+  const void* fn;
+  void (*launch)(int grid, cudaStream_t s, const float* depth, const float4* nmap, const Volume& V, const Params& p);
+  int threads;
+};
+
+template <int kT, int kMinB>
+void launch_fused_variant(int grid, cudaStream_t s, const float* depth, const float4* nmap, const Volume& V,
+                          const Params& p) {
+  fused_update_kernel<kT, kMinB><<<grid, kT, 0, s>>>(depth, nmap, V, p);
+}
+
+#define VH_FUSED_VARIANT(T, B) \
+  FusedVariant { reinterpret_cast<const void*>(fused_update_kernel<T, B>), launch_fused_variant<T, B>, T }
+static const FusedVariant kFusedVariants[] = {
+    VH_FUSED_VARIANT(256, 4), VH_FUSED_VARIANT(128, 8),  VH_FUSED_VARIANT(256, 6),
+    VH_FUSED_VARIANT(128, 12), VH_FUSED_VARIANT(512, 2), VH_FUSED_VARIANT(64, 16),
+};
+#undef VH_FUSED_VARIANT
+constexpr int kNumFusedVariants = static_cast<int>(sizeof(kFusedVariants) / sizeof(kFusedVariants[0]));
+
+int fused_variant_count() { return kNumFusedVariants; }
+
+void fused_variant_shape(int variant, int* threads, int* min_blocks) {
+  static const int kMin[] = {4, 8, 6, 12, 2, 16};
+  static_assert(sizeof(kMin) / sizeof(kMin[0]) == kNumFusedVariants, "one entry per variant");
+  const int v = (variant >= 0 && variant < kNumFusedVariants) ? variant : 0;
+  *threads = kFusedVariants[v].threads;
+  *min_blocks = kMin[v];
+}
+
 cudaError_t launch_integrate_update(const float* depth, const Volume& V, const Params& p, int grid,
-                                    const float4* nmap, cudaStream_t s) {
+                                    const float4* nmap, cudaStream_t s, int variant) {
   if (p.normal_mode == 1) {
     if (nmap == nullptr) return cudaErrorInvalidValue;
-    static int fused_grid = 0;
-    if (fused_grid == 0) fused_grid = grid_for(reinterpret_cast<const void*>(fused_update_kernel), kThreads);
-    fused_update_kernel<<<grid > 0 ? grid : fused_grid, kThreads, 0, s>>>(depth, nmap, V, p);
+    if (variant < 0 || variant >= kNumFusedVariants) variant = 0;
+    static int fused_grid[kNumFusedVariants] = {};
+    const FusedVariant& fv = kFusedVariants[variant];
+    if (fused_grid[variant] == 0) fused_grid[variant] = grid_for(fv.fn, fv.threads);
+    fv.launch(grid > 0 ? grid : fused_grid[variant], s, depth, nmap, V, p);
     return cudaGetLastError();
   }
   update_kernel<<<grid > 0 ? grid : integrate_grid_size(), kUpdateThreads, 0, s>>>(depth, V, p);
@@ -919,7 +961,7 @@ cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& 
                              cudaStream_t s) {
   const cudaError_t e = launch_integrate_prepare(depth, V, p, nmap, s);
   if (e != cudaSuccess) return e;
-  return launch_integrate_update(depth, V, p, grid, nmap, s);
+  return launch_integrate_update(depth, V, p, grid, nmap, s, 0);
 }
 
 }  // namespace VH_INTEGRATE_NS

@@ -25,7 +25,9 @@ cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& 
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
                                      cudaStream_t s);
 cudaError_t launch_integrate_update(const float* depth, const Volume& V, const Params& p, int grid,
-                                    const float4* nmap, cudaStream_t s);
+                                    const float4* nmap, cudaStream_t s, int variant);
+int fused_variant_count();
+void fused_variant_shape(int variant, int* threads, int* min_blocks);
 cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s);
 int integrate_grid_size();
 }  // namespace exact
@@ -35,7 +37,9 @@ cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& 
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
                                      cudaStream_t s);
 cudaError_t launch_integrate_update(const float* depth, const Volume& V, const Params& p, int grid,
-                                    const float4* nmap, cudaStream_t s);
+                                    const float4* nmap, cudaStream_t s, int variant);
+int fused_variant_count();
+void fused_variant_shape(int variant, int* threads, int* min_blocks);
 cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s);
 int integrate_grid_size();
 }  // namespace fast
