@@ -1,18 +1,25 @@
 #!/usr/bin/env python
-"""bench.py -- depth-fusion throughput of the GB300 path (integrated Mpix/s, MC blocks/s).
+"""bench.py -- depth-fusion throughput of the GB300 path (integrated Mpix/s, MC blocks/s), two forms.
 
 Workload: the room-scale configuration -- 640x480 float32 depth (fx=fy=525, cx=319.5, cy=239.5) ray-cast
 from a seeded 4x5x3 m room holding 40 primitives, hand-held random walk (1 cm/frame, 1 degree/frame
 yaw/pitch jitter), noise N(0, (0.0012 z^2)^2) + 1 % dropouts, 5 mm voxels, 2 cm truncation, 2^20 hash
-buckets, plain FP32 directional multi-layer storage, mesh extracted at the end.  Frames are synthetic
-(voxelhashmt_gb300/scenes.py, rendered on the device by vh_render_depth).
+buckets, mesh extracted at the end.  Frames are synthetic (voxelhashmt_gb300/scenes.py, rendered on the
+device by vh_render_depth).
+
+Forms: "plain" is the reference's algorithm, bit-identical to the oracle (FP32 layers, exact arithmetic);
+"chosen" is the opt-in form (truncation-band allocation, per-pixel normal map, fast-math update, FP16
+layers).  Both run on the same frames; --form picks the one reported as the headline value, the other is
+reported beside it, with the Chamfer distance of each fused mesh to the analytic surface
+(voxelhashmt_gb300/metrics.py; surface points from noise-free renders of every 20th frame).
 
 A step is one frame through filter -> allocate -> integrate.  W warm-up frames, then K timed frames,
 each bracketed by CUDA events on the stream the kernels run on; between timed frames a 512 MB buffer is
 written to flush L2 (outside the events).  value = W*H*K / sum(step times).  e2e = the same frames
 again on a reset volume through the public API (TsdfIntegrationBackend.integrate) from pinned host
 memory, with the host->device copy of the frame and a device->host read of the frame statistics inside
-each step, wall clock.  MC blocks/s = allocated blocks / full 6-direction extraction time.
+each step, wall clock.  MC blocks/s = allocated blocks / full 6-direction extraction time.  The roofline
+is the layer-update kernel's own time (CUDA events around its launch).
 
 --impl reference times the reference's CPU implementation of the same path (the oracle port of
 TsdfIntegrationBackend(kCpu): CPU filter constants and allocation rule, every host thread) on a bounded
@@ -36,9 +43,10 @@ sys.path.insert(0, ROOT)
 
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # DRAM bytes (read + write) per active voxel of the layer-update kernel of each form, from the ncu captures
-# summarised in profiles/ (plain: update_kernel_room640.md, one launch over 6.55 M active voxels); scaled by
-# the active voxels of a launch.  None until a capture of that kernel exists.
-UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL = {"plain": (539.49e6 + 267.04e6) / 6.548e6, "chosen": None}
+# summarised in profiles/ (plain: update_kernel_room640.md, one launch over 6.55 M active voxels; opt-in form:
+# fused_update_room640.md, one launch over 3.16 M active voxels); scaled by the active voxels of a launch.
+UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL = {"plain": (539.49e6 + 267.04e6) / 6.548e6,
+                                         "chosen": (190.369e6 + 57.800e6) / 3.163e6}
 
 
 def parse():
@@ -148,7 +156,7 @@ def make_scene(seed, frames):
 def workload_config(sc, steps, warmup):
     K = sc.intrinsics
     return {"workload": "room %dx%d, 40 primitives, %d-frame random walk, voxel %.0f mm, trunc %.0f mm, %d hash "
-                        "buckets, FP32 directional layers" % (K.width, K.height, len(sc.poses),
+                        "buckets, directional multi-layer volume" % (K.width, K.height, len(sc.poses),
                                                             sc.voxel_size * 1000, sc.truncation * 1000,
                                                             sc.hash_buckets),
             "width": K.width, "height": K.height, "frames": len(sc.poses), "voxel_size_m": sc.voxel_size,

@@ -19,7 +19,8 @@
 //     (src/cuda_mesh_extractor.cu:640-653).
 // Differences: gpuVolumeCacheFlatBlocks returns host memory (the reference returns device memory; its only
 // caller is the mesh extractor this file replaces).  Device sizing comes from the environment:
-// VH_HASH_BUCKETS (default 2^22) and VH_MAX_BLOCKS (default 2^17 blocks = 19 GB).
+// VH_HASH_BUCKETS (default 2^22) and VH_MAX_BLOCKS (default 2^17 blocks = 19 GB); the opt-in forms too:
+// VH_LAYER_FORMAT, VH_ALLOCATION_MODE, VH_NORMAL_MODE, VH_FAST_MATH (all default 0, the reference's form).
 #include <algorithm>
 #include <cstdint>
 #include <cstdlib>
@@ -86,8 +87,14 @@ vh_volume* create_volume(float voxel_size, float truncation, uint32_t buckets, u
   p.truncation_distance = truncation;
   p.hash_buckets = buckets;
   p.max_blocks = max_blocks;
+  p.layer_format = static_cast<int32_t>(env_u32("VH_LAYER_FORMAT", 0));
+  vh_algorithm a;
+  vh_algorithm_default(&a);  // the reference's constants; the opt-in switches default off
+  a.allocation_mode = static_cast<int32_t>(env_u32("VH_ALLOCATION_MODE", 0));
+  a.normal_mode = static_cast<int32_t>(env_u32("VH_NORMAL_MODE", 0));
+  a.fast_math = static_cast<int32_t>(env_u32("VH_FAST_MATH", 0));
   vh_volume* v = nullptr;
-  check(vh_create(&p, nullptr, &v), nullptr, "vh_create");
+  check(vh_create(&p, &a, &v), nullptr, "vh_create");
   return v;
 }
 
