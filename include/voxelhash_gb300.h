@@ -176,6 +176,16 @@ vh_status vh_depth_normals(vh_volume* volume, const float* depth_in, float* norm
 vh_status vh_pixel_normals(vh_volume* volume, const float* depth_in, float* normals, const vh_intrinsics* K,
                            void* stream);
 
+/* Depth ray-cast of the fused volume (no reference counterpart: the reference renders only its analytic
+ * scenes).  For every pixel of K seen from T_wc, the ray is sampled every step_voxels voxels of path length
+ * between camera depths min_depth and max_depth; the surface is the one marching cubes extracts, a voxel's
+ * observed layers as planes (cuda_mesh_extractor.cu:237-262): at each sample, the signed plane distance of
+ * the camera-facing layer closest to the sample; the first crossing from positive to non-positive (a drop
+ * of at most the truncation distance) is the hit, interpolated linearly.  depth_out: W*H floats in device
+ * memory, camera depth in metres, 0 where no surface is hit.  Asynchronous on the stream. */
+vh_status vh_raycast_depth(vh_volume* volume, const vh_intrinsics* K, const vh_pose* T_wc, float min_depth,
+                           float max_depth, float step_voxels, float* depth_out, void* stream);
+
 /* Waits for the stream and returns (then clears) the device-side errors accumulated since the last call. */
 vh_status vh_synchronize(vh_volume* volume, void* stream);
 

@@ -75,6 +75,8 @@ def lib():
         L.vo_filter_depth.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp]
         L.vo_depth_normals.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp,
                                        C.POINTER(C.c_uint8)]
+        L.vo_raycast_depth.argtypes = [C.c_void_p, C.POINTER(VoIntrinsics), C.POINTER(VoPose), C.c_float, C.c_float,
+                                       C.c_float, _fp]
         L.vo_surface_normal.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.c_float, C.c_float,
                                         _fp]
         L.vo_surface_normal.restype = C.c_int32
@@ -207,6 +209,13 @@ class Volume:
         d, dp = _f32(depth)
         lib().vo_volume_integrate_blocks(self.h, k.ctypes.data_as(_ip), k.shape[0], dp, C.byref(intrinsics(K)),
                                          C.byref(pose(P)))
+
+    def raycast_depth(self, K, P, min_depth=0.1, max_depth=8.0, step_voxels=0.5):
+        """Depth (H, W) float32 of the product's ray-cast definition on this volume; 0 = no hit."""
+        out = np.zeros((K.height, K.width), np.float32)
+        lib().vo_raycast_depth(self.h, C.byref(intrinsics(K)), C.byref(pose(P)), float(min_depth), float(max_depth),
+                               float(step_voxels), out.ctypes.data_as(_fp))
+        return out
 
     def block_count(self):
         return lib().vo_volume_block_count(self.h)

@@ -1231,3 +1231,93 @@ int32_t vo_surface_normal(const vo_config* c, const float* depth, const vo_intri
   n[2] = r.z;
   return ok;
 }
+
+/* ------------------------------------------------------------- ray-cast */
+/* Restatement of the product's depth ray-cast (voxelhashmt_gb300/csrc/vh_raycast.cu), which has no reference
+ * counterpart; it uses the reference's marching-cubes surface (planeSignedDistanceGpu with the mesh unpack,
+ * cuda_mesh_extractor.cu:237-262) on the GPU flavour's voxels. */
+typedef struct {
+  const vo_volume* v;
+  const vo_intrinsics* K;
+  const vo_pose* T;
+  float min_depth, max_depth, step;
+  float* out;
+} raycast_ctx;
+
+static int ray_plane_distance(const vo_voxel* vox, v3 x, v3 dw, float* sdf) {
+  int any = 0;
+  float best = 0.0f, best_abs = 0.0f;
+  for (int d = 0; d < DIRS; ++d) {
+    for (int l = 0; l < LAYERS; ++l) {
+      const vo_layer* L = &vox->layers[d][l];
+      if (!(L->weight > 0.0f)) continue;
+      const v3 n = unpack_normal(GPU, 1, L->packed_normal);
+      if (!(vdot(n, dw) < 0.0f)) continue;
+      const float s = n.x * x.x + n.y * x.y + n.z * x.z - L->plane_offset;
+      const float a = fabsf(s);
+      if (!any || a < best_abs) {
+        any = 1;
+        best = s;
+        best_abs = a;
+      }
+    }
+  }
+  *sdf = best;
+  return any;
+}
+
+static void raycast_row(void* p, int64_t row) {
+  const raycast_ctx* c = (const raycast_ctx*)p;
+  const vo_volume* v = c->v;
+  const vo_intrinsics* K = c->K;
+  const float vs = v->vs;
+  for (int u = 0; u < K->width; ++u) {
+    const v3 dc = mk(((float)u - K->cx) / K->fx, ((float)row - K->cy) / K->fy, 1.0f);
+    const v3 dw = pose_vector(c->T, dc);
+    const v3 o = mk(c->T->t[0], c->T->t[1], c->T->t[2]);
+    const float dz = c->step * vs / vnorm(dc);
+    float z = c->min_depth, prev_sdf = 0.0f, prev_z = 0.0f, result = 0.0f;
+    int prev_ok = 0;
+    for (int it = 0; it < (1 << 16) && z <= c->max_depth; ++it) {
+      const v3 x = mk(o.x + dw.x * z, o.y + dw.y * z, o.z + dw.z * z);
+      const int gx = (int)floorf(x.x / vs), gy = (int)floorf(x.y / vs), gz = (int)floorf(x.z / vs);
+      const int bx = floor_div(gx, BLOCK), by = floor_div(gy, BLOCK), bz = floor_div(gz, BLOCK);
+      const vo_key k = {bx, by, bz};
+      const int64_t bi = keymap_find(&v->map, k);
+      if (bi < 0) {
+        prev_ok = 0;
+        float zexit = 3.0e38f;
+        const int bb[3] = {bx, by, bz};
+        const float oo[3] = {o.x, o.y, o.z}, dd[3] = {dw.x, dw.y, dw.z};
+        for (int a = 0; a < 3; ++a) {
+          if (dd[a] > 0.0f) zexit = fminf(zexit, ((float)((bb[a] + 1) * BLOCK) * vs - oo[a]) / dd[a]);
+          if (dd[a] < 0.0f) zexit = fminf(zexit, ((float)(bb[a] * BLOCK) * vs - oo[a]) / dd[a]);
+        }
+        z = fmaxf(z + dz, zexit + 0.25f * dz);
+        continue;
+      }
+      const int li = positive_mod(gx, BLOCK) + BLOCK * (positive_mod(gy, BLOCK) + BLOCK * positive_mod(gz, BLOCK));
+      float sdf = 0.0f;
+      if (!ray_plane_distance(&v->voxels[bi * BLOCK_VOLUME + li], x, dw, &sdf)) {
+        prev_ok = 0;
+        z += dz;
+        continue;
+      }
+      if (prev_ok && prev_sdf > 0.0f && sdf <= 0.0f && prev_sdf - sdf <= v->trunc) {
+        result = prev_z + (z - prev_z) * (prev_sdf / (prev_sdf - sdf));
+        break;
+      }
+      prev_ok = 1;
+      prev_sdf = sdf;
+      prev_z = z;
+      z += dz;
+    }
+    c->out[(size_t)row * (size_t)K->width + (size_t)u] = result;
+  }
+}
+
+void vo_raycast_depth(const vo_volume* v, const vo_intrinsics* K, const vo_pose* T_wc, float min_depth, float max_depth,
+                      float step_voxels, float* out) {
+  raycast_ctx c = {v, K, T_wc, min_depth, max_depth, step_voxels, out};
+  parallel_for(v->cfg.threads, K->height, raycast_row, &c);
+}

@@ -137,6 +137,9 @@ int64_t vo_volume_extract_mesh(const vo_volume* vol, float iso, vo_triangle** ou
 void vo_free(void* p);
 
 /* small kernels exposed for known-answer tests */
+/* depth ray-cast of the fused volume (restates voxelhashmt_gb300/csrc/vh_raycast.cu): out[W*H], 0 = no hit */
+void vo_raycast_depth(const vo_volume* vol, const vo_intrinsics* K, const vo_pose* T_wc, float min_depth,
+                      float max_depth, float step_voxels, float* out);
 int32_t vo_surface_normal(const vo_config* cfg, const float* depth, const vo_intrinsics* K, float u, float v,
                           float n[3]);
 uint32_t vo_pack_normal(int32_t flavor, const float n[3]);

@@ -317,3 +317,21 @@ def test_checkpoint_export_import_round_trip(env, small_orbit):
     assert a.observed_voxel_count() == b.observed_voxel_count()
     a.close()
     b.close()
+
+
+def test_raycast_bit_exact_and_close_to_scene(env, small_orbit):
+    """Depth ray-cast of the fused plain volume: bit-identical to the oracle's restatement, and within a
+    voxel of the analytic depth where both see the surface."""
+    backend, O = env
+    from voxelhashmt_gb300 import scenes
+    sc = small_orbit
+    vol, ora = _integrate_both(backend, O, sc, frames=[0, 3, 6, 9, 12])
+    for f in (0, 4, 9):
+        got = backend.raycast_depth(vol, sc.intrinsics, sc.poses[f], 0.1, 4.0, 0.5)
+        want = ora.raycast_depth(sc.intrinsics, sc.poses[f], 0.1, 4.0, 0.5)
+        assert np.array_equal(_bits(got), _bits(want)), int(np.sum(_bits(got) != _bits(want)))
+        clean = scenes.render_depth(sc, f, noise=False)
+        both = (got > 0) & (clean > 0)
+        assert both.sum() > 0.5 * (clean > 0).sum()
+        assert np.median(np.abs(got[both] - clean[both])) <= sc.voxel_size
+    vol.close()

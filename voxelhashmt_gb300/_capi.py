@@ -100,6 +100,8 @@ _SIGNATURES = {
     "vh_filter_depth": (C.c_int, [_vp, _vp, _vp, C.POINTER(VhIntrinsics), _vp]),
     "vh_depth_normals": (C.c_int, [_vp, _vp, _vp, _vp, C.POINTER(VhIntrinsics), _vp]),
     "vh_pixel_normals": (C.c_int, [_vp, _vp, _vp, C.POINTER(VhIntrinsics), _vp]),
+    "vh_raycast_depth": (C.c_int, [_vp, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_float, C.c_float, C.c_float,
+                                   _vp, _vp]),
     "vh_synchronize": (C.c_int, [_vp, _vp]),
     "vh_extract_mesh": (C.c_int, [_vp, C.c_float, _szp, _vp]),
     "vh_copy_mesh": (C.c_int, [_vp, _vp, C.c_size_t, C.c_int32, _vp]),

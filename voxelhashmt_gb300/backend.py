@@ -297,6 +297,23 @@ def visible_block_keys(volume: VoxelHashTSDF, stream=None):
     return keys[:n.value].copy()
 
 
+def raycast_depth(volume: VoxelHashTSDF, intrinsics, T_wc, min_depth=0.1, max_depth=8.0, step_voxels=0.5, stream=None,
+                  device_out=None):
+    """Depth map (H, W) float32 of the fused surface seen from T_wc (vh_raycast_depth); 0 = no hit.  With
+    device_out (a torch device), a CUDA tensor is returned instead of a numpy array."""
+    import torch
+    K = _capi.intrinsics(intrinsics)
+    out = torch.empty((intrinsics.height, intrinsics.width), dtype=torch.float32, device="cuda")
+    s = _stream_handle(stream)
+    _capi.check(_capi.lib().vh_raycast_depth(volume.handle, C.byref(K), C.byref(_capi.pose(T_wc)), float(min_depth),
+                                             float(max_depth), float(step_voxels), C.c_void_p(out.data_ptr()), s),
+                volume.handle)
+    if device_out is not None:
+        return out
+    volume.synchronize(stream)
+    return out.cpu().numpy()
+
+
 def extract_mesh_cuda(volume: VoxelHashTSDF, iso_level=0.0, stream=None, device_out=None):
     """Triangle soup (N, 9) float32 (v0, v1, v2).  With device_out (a torch tensor factory device), the soup
     is returned as a CUDA tensor instead of a host array."""

@@ -633,6 +633,18 @@ vh_status vh_pixel_normals(vh_volume* v, const float* in, float* normals, const 
   return VH_OK;
 }
 
+vh_status vh_raycast_depth(vh_volume* v, const vh_intrinsics* K, const vh_pose* T_wc, float min_depth, float max_depth,
+                           float step_voxels, float* depth_out, void* stream) {
+  if (!v || !valid_intrinsics(K) || !T_wc || !depth_out || !(min_depth >= 0.0f) || !(max_depth > min_depth) ||
+      !(step_voxels > 0.0f) || v->dev.max_blocks == 0) {
+    return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_raycast_depth: bad argument");
+  }
+  DeviceGuard guard(v->params.device);
+  const vh::Params p = make_params(v, K, T_wc, 1);
+  VH_CUDA(v, vh::launch_raycast(v->dev, p, min_depth, max_depth, step_voxels, depth_out, as_stream(stream)));
+  return VH_OK;
+}
+
 vh_status vh_synchronize(vh_volume* v, void* stream) {
   if (!v) return VH_ERR_INVALID_ARGUMENT;
   DeviceGuard guard(v->params.device);

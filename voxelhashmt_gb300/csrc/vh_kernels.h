@@ -65,6 +65,9 @@ cudaError_t launch_export(const Volume& V, uint32_t first, uint32_t count, int* 
 // import blocks in the reference layout (insert or overwrite); idx: n scratch words
 cudaError_t launch_import(const Volume& V, const int* keys, const float4* voxels, uint32_t n, uint32_t* idx,
                           cudaStream_t s);
+// depth ray-cast of the fused volume from pose p.T_wc: out[W*H] camera depth of the first plane crossing, 0 = none
+cudaError_t launch_raycast(const Volume& V, const Params& p, float min_depth, float max_depth, float step, float* out,
+                           cudaStream_t s);
 // synthetic depth for the analytic benchmark scenes (prims: n x 10 floats, device memory)
 cudaError_t launch_render(const float* prims, int n_prims, const Params& p, uint32_t seed, uint32_t frame,
                           float sigma_z2, float dropout, float max_depth, float* out, cudaStream_t s);

@@ -43,23 +43,6 @@ struct Shared {
   uint32_t total;
 };
 
-// unpackNormalOctahedralGpu of the mesh extractor (:237-257): degenerate -> (0,0,1)
-__device__ __forceinline__ f3 unpack_normal_mesh(uint32_t packed) {
-  f3 n = mk3(div65535(static_cast<float>(packed & 0xffffU)) * 2.0f - 1.0f,
-             div65535(static_cast<float>((packed >> 16U) & 0xffffU)) * 2.0f - 1.0f, 0.0f);
-  n.z = 1.0f - fabsf(n.x) - fabsf(n.y);
-  if (n.z < 0.0f) {
-    const float fx = (1.0f - fabsf(n.y)) * (n.x >= 0.0f ? 1.0f : -1.0f);
-    const float fy = (1.0f - fabsf(n.x)) * (n.y >= 0.0f ? 1.0f : -1.0f);
-    n.x = fx;
-    n.y = fy;
-  }
-  const float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
-  if (len <= 1e-6f) return mk3(0.0f, 0.0f, 1.0f);
-  const float inv = 1.0f / len;
-  return mk3(n.x * inv, n.y * inv, n.z * inv);
-}
-
 // planeSignedDistanceGpu (:259-262)
 __device__ __forceinline__ float plane_sd(const float4& pl, f3 p) {
   return pl.x * p.x + pl.y * p.y + pl.z * p.z - pl.w;
