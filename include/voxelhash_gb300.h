@@ -50,7 +50,9 @@ typedef enum vh_status {
   VH_ERR_HASH_FULL = 6,         /* no free hash slot (reference: CudaActiveBlockAllocationFallback) */
   VH_ERR_POOL_FULL = 7,         /* more blocks than vh_params.max_blocks */
   VH_ERR_BUFFER_TOO_SMALL = 8,  /* caller's output buffer is smaller than the result; *count holds the size */
-  VH_ERR_CAPACITY = 9           /* request larger than the fixed scratch of vh_allocate_static_scratch */
+  VH_ERR_CAPACITY = 9,          /* request larger than the fixed scratch of vh_allocate_static_scratch */
+  VH_ERR_IO = 10,               /* dataset file missing, unreadable or unparsable (vh_dataset_last_error) */
+  VH_ERR_FORMAT = 11            /* unsupported or corrupt PNG / metadata layout (vh_dataset_last_error) */
 } vh_status;
 
 typedef struct vh_volume vh_volume;
@@ -239,6 +241,28 @@ vh_status vh_profile_read(vh_volume* volume, double ms[4], uint64_t* frames);
 vh_status vh_render_depth(const float* prims, int32_t n_prims, const vh_intrinsics* K, const vh_pose* T_wc,
                           uint32_t seed, uint32_t frame, float sigma_z2, float dropout, float max_depth,
                           float* depth_out, void* stream);
+
+/* ---- Dataset reader: include/tsdfmc/dataset_io.h, portable ----
+ * Layout: <root>/<frame id>/depth.png and <root>/<frame id>/<pose file>; the frame ids are the all-digit
+ * directory names, ascending (listDatasetFrameIds, :135-152).  These calls touch no GPU.  On failure they
+ * return VH_ERR_IO / VH_ERR_FORMAT / VH_ERR_INVALID_ARGUMENT and vh_dataset_last_error() holds the message
+ * the reference would throw (thread-local). */
+const char* vh_dataset_last_error(void);
+/* listDatasetFrameIds: ids may be NULL (count only); VH_ERR_BUFFER_TOO_SMALL when max_ids < *count. */
+vh_status vh_dataset_list_frames(const char* root, int32_t* ids, size_t max_ids, size_t* count);
+/* loadDatasetIntrinsics (:382-395): metadata of 5 (fx fy cx cy depth_scale), 6 (fx fy cx cy width height) or
+ * 7 (fx fy cx cy width height depth_scale) numbers; a missing file falls back to the first
+ * <root>/<frame>/params.txt; without a resolution, the size of the first depth.png completes it. */
+vh_status vh_dataset_load_intrinsics(const char* metadata_path, vh_intrinsics* K, float* depth_scale);
+/* loadPoseFromFile (:154-188): 7 numbers (quaternion w x y z, translation) or 12/16 (row-major 3x4 / 4x4). */
+vh_status vh_dataset_load_pose(const char* path, vh_pose* T_wc);
+/* Any grayscale PNG (bit depth 1-16, optional alpha, optional Adam7) as 16-bit gray, the conversion the
+ * reference requests from WIC (:321-330).  pixels may be NULL (size probe); else max_pixels >= W*H. */
+vh_status vh_png_read_gray16(const char* path, uint16_t* pixels, size_t max_pixels, int32_t* width, int32_t* height);
+/* loadDepthPng (:276-361): depth[i] = raw[i] * depth_scale where raw != 0 and the product > 0, else 0 (host
+ * buffer of K->width * K->height floats); the PNG size must equal K's.  *valid_samples = nonzero depths. */
+vh_status vh_dataset_load_depth_png(const char* path, const vh_intrinsics* K, float depth_scale, float* depth,
+                                    uint64_t* valid_samples);
 
 #ifdef __cplusplus
 }

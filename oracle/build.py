@@ -141,7 +141,28 @@ def build_ref(force=False):
     return REF_SO
 
 
+REF_DATASET = os.path.join(REF_DIR, "ref_dataset_driver")
+
+
+def build_ref_dataset(force=False):
+    """oracle/ref_dataset_driver.cpp against the reference's include/tsdfmc/dataset_io.h (read in place)."""
+    if not reference_available():
+        return None
+    os.makedirs(REF_DIR, exist_ok=True)
+    src = os.path.join(HERE, "ref_dataset_driver.cpp")
+    inputs = [src, os.path.join(REFERENCE, "include", "tsdfmc", "dataset_io.h"),
+              os.path.join(REFERENCE, "include", "tsdfmc", "math_types.h"), os.path.abspath(__file__)]
+    if not force and os.path.exists(REF_DATASET) and \
+            os.path.getmtime(REF_DATASET) >= max(os.path.getmtime(p) for p in inputs):
+        return REF_DATASET
+    _run(["g++", "-std=c++17", "-O2", *FP_FLAGS, "-I", os.path.join(REFERENCE, "include"), src, "-o",
+          REF_DATASET + ".tmp"])
+    os.replace(REF_DATASET + ".tmp", REF_DATASET)
+    return REF_DATASET
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     if "--ref" in sys.argv:
         print(build_ref(force=True))
+        print(build_ref_dataset(force=True))

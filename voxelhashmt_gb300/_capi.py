@@ -24,6 +24,8 @@ VH_ERR_HASH_FULL = 6
 VH_ERR_POOL_FULL = 7
 VH_ERR_BUFFER_TOO_SMALL = 8
 VH_ERR_CAPACITY = 9
+VH_ERR_IO = 10
+VH_ERR_FORMAT = 11
 
 BLOCK_BYTES = 512 * 6 * 3 * 16
 
@@ -73,7 +75,7 @@ class VhError(RuntimeError):
 def _status_name(status):
     names = {0: "VH_OK", 1: "VH_ERR_INVALID_ARGUMENT", 2: "VH_ERR_CUDA", 3: "VH_ERR_NO_DEVICE",
              4: "VH_ERR_OUT_OF_MEMORY", 5: "VH_ERR_KEY_RANGE", 6: "VH_ERR_HASH_FULL", 7: "VH_ERR_POOL_FULL",
-             8: "VH_ERR_BUFFER_TOO_SMALL", 9: "VH_ERR_CAPACITY"}
+             8: "VH_ERR_BUFFER_TOO_SMALL", 9: "VH_ERR_CAPACITY", 10: "VH_ERR_IO", 11: "VH_ERR_FORMAT"}
     return names.get(status, "VH_STATUS_%d" % status)
 
 
@@ -116,6 +118,14 @@ _SIGNATURES = {
     "vh_autotune_result": (C.c_int, [_vp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                      C.POINTER(C.c_float)]),
     "vh_profile_enable": (C.c_int, [_vp, C.c_int32]),
+    "vh_dataset_last_error": (C.c_char_p, []),
+    "vh_dataset_list_frames": (C.c_int, [C.c_char_p, _ip, C.c_size_t, _szp]),
+    "vh_dataset_load_intrinsics": (C.c_int, [C.c_char_p, C.POINTER(VhIntrinsics), C.POINTER(C.c_float)]),
+    "vh_dataset_load_pose": (C.c_int, [C.c_char_p, C.POINTER(VhPose)]),
+    "vh_png_read_gray16": (C.c_int, [C.c_char_p, C.POINTER(C.c_uint16), C.c_size_t, C.POINTER(C.c_int32),
+                                     C.POINTER(C.c_int32)]),
+    "vh_dataset_load_depth_png": (C.c_int, [C.c_char_p, C.POINTER(VhIntrinsics), C.c_float, C.POINTER(C.c_float),
+                                            _u64p]),
     "vh_profile_read": (C.c_int, [_vp, C.POINTER(C.c_double), _u64p]),
     "vh_render_depth": (C.c_int, [_vp, C.c_int32, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_uint32,
                                   C.c_uint32, C.c_float, C.c_float, C.c_float, _vp, _vp]),

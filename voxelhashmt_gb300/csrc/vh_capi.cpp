@@ -314,6 +314,8 @@ const char* vh_status_string(vh_status s) {
     case VH_ERR_POOL_FULL: return "block pool full";
     case VH_ERR_BUFFER_TOO_SMALL: return "output buffer too small";
     case VH_ERR_CAPACITY: return "request larger than the fixed static scratch";
+    case VH_ERR_IO: return "dataset file missing, unreadable or unparsable";
+    case VH_ERR_FORMAT: return "unsupported or corrupt PNG or metadata layout";
   }
   return "unknown status";
 }
