@@ -242,6 +242,22 @@ vh_status vh_render_depth(const float* prims, int32_t n_prims, const vh_intrinsi
                           uint32_t seed, uint32_t frame, float sigma_z2, float dropout, float max_depth,
                           float* depth_out, void* stream);
 
+/* ---- Multi-scene batch (no reference counterpart) ----
+ * Many independent volumes fused together: each vh_batch_integrate call is one step in which every active
+ * scene integrates one depth frame.  The step runs as three work-queue kernels over all scenes' work (filter
+ * tiles; allocation and normal-map tiles; chunks of visible voxels), so small and large scenes share the GPU
+ * without per-scene launches; with use_graph the step (descriptor upload, queue reset, three kernels) is one
+ * CUDA graph launch.  Volumes: same device, vh_algorithm.normal_mode 1 (the per-pixel normal map) and the same
+ * fast_math setting; at most 256 per batch; a volume keeps its own counters and statistics
+ * (vh_frame_stats_get, vh_synchronize).  Results equal integrating each scene alone with the same settings. */
+typedef struct vh_batch vh_batch;
+vh_status vh_batch_create(vh_volume* const* volumes, int32_t count, int32_t use_graph, vh_batch** out);
+void vh_batch_destroy(vh_batch* batch);
+/* depth_device[i]: device pointer of scene i's depth (K[i].width x K[i].height floats); active may be NULL (all
+ * active), else scenes with active[i] == 0 skip the step.  Asynchronous on the stream. */
+vh_status vh_batch_integrate(vh_batch* batch, const float* const* depth_device, const vh_intrinsics* K,
+                             const vh_pose* T_wc, const int32_t* active, int32_t stride, void* stream);
+
 /* ---- Dataset reader: include/tsdfmc/dataset_io.h, portable ----
  * Layout: <root>/<frame id>/depth.png and <root>/<frame id>/<pose file>; the frame ids are the all-digit
  * directory names, ascending (listDatasetFrameIds, :135-152).  These calls touch no GPU.  On failure they

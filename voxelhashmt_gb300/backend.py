@@ -297,6 +297,52 @@ def visible_block_keys(volume: VoxelHashTSDF, stream=None):
     return keys[:n.value].copy()
 
 
+class VolumeBatch:
+    """Many volumes fused together (vh_batch_*): each integrate() is one step in which every active scene
+    integrates one device-resident depth frame, as three work-queue kernels over all scenes (one CUDA graph
+    launch with use_graph).  Volumes need algorithm.normal_mode 1 and the same fast_math setting."""
+
+    def __init__(self, volumes, use_graph=True):
+        self.volumes = list(volumes)
+        handles = (C.c_void_p * len(self.volumes))(*[v.handle.value for v in self.volumes])
+        h = C.c_void_p()
+        _capi.check(_capi.lib().vh_batch_create(handles, len(self.volumes), 1 if use_graph else 0, C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _capi.lib().vh_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def integrate(self, depths, intrinsics, poses, stride=1, stream=None):
+        """depths[i]: contiguous float32 CUDA tensor of scene i's frame, or None to skip scene i this step."""
+        n = len(self.volumes)
+        ptrs = (C.c_void_p * n)()
+        Ks = (_capi.VhIntrinsics * n)()
+        Ps = (_capi.VhPose * n)()
+        act = (C.c_int32 * n)()
+        for i in range(n):
+            if depths[i] is None:
+                continue
+            d = depths[i]
+            if not (hasattr(d, "is_cuda") and d.is_cuda and d.is_contiguous()):
+                raise ValueError("batch depth must be a contiguous CUDA tensor")
+            if d.numel() != intrinsics[i].width * intrinsics[i].height:
+                raise ValueError("depth size does not match the intrinsics of scene %d" % i)
+            ptrs[i] = d.data_ptr()
+            Ks[i] = _capi.intrinsics(intrinsics[i])
+            Ps[i] = _capi.pose(poses[i])
+            act[i] = 1
+        self._keep = depths  # the kernels read the tensors asynchronously
+        _capi.check(_capi.lib().vh_batch_integrate(self.handle, ptrs, Ks, Ps, act, int(stride), _stream_handle(stream)))
+
+
 def raycast_depth(volume: VoxelHashTSDF, intrinsics, T_wc, min_depth=0.1, max_depth=8.0, step_voxels=0.5, stream=None,
                   device_out=None):
     """Depth map (H, W) float32 of the fused surface seen from T_wc (vh_raycast_depth); 0 = no hit.  With

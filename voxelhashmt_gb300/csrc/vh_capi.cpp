@@ -828,4 +828,154 @@ vh_status vh_render_depth(const float* prims, int32_t n_prims, const vh_intrinsi
   return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
 }
 
+// ---- multi-scene batch ----
+
+struct vh_batch {
+  std::vector<vh_volume*> vols;
+  int device = 0;
+  int fast = 0;
+  bool use_graph = false;
+  size_t bytes = 0;                 // header + descriptors
+  unsigned char* d_buf = nullptr;   // [BatchHeader][SceneDesc x n]
+  uint32_t* d_queue = nullptr;      // 3 work-queue counters
+  unsigned char* h_stage[2] = {nullptr, nullptr};  // pinned, alternate steps
+  cudaEvent_t done[2] = {nullptr, nullptr};         // step that last used h_stage[k] has finished
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  cudaStream_t capture = nullptr;
+  int next = 0;
+};
+
+static uint32_t tiles(int w, int h, int tx, int ty) {
+  if (w <= 0 || h <= 0) return 0U;
+  return static_cast<uint32_t>(((w + tx - 1) / tx) * ((h + ty - 1) / ty));
+}
+
+static cudaError_t batch_launch(vh_batch* b, int slot, cudaStream_t s) {
+  cudaError_t e = cudaMemcpyAsync(b->d_buf, b->h_stage[slot], b->bytes, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return e;
+  const auto* hdr = reinterpret_cast<const vh::BatchHeader*>(b->d_buf);
+  const auto* desc = reinterpret_cast<const vh::SceneDesc*>(b->d_buf + sizeof(vh::BatchHeader));
+  return b->fast ? vh::fast::launch_batch(desc, hdr, b->d_queue, s) : vh::exact::launch_batch(desc, hdr, b->d_queue, s);
+}
+
+void vh_batch_destroy(vh_batch* b) {
+  if (!b) return;
+  DeviceGuard guard(b->device);
+  cudaDeviceSynchronize();
+  for (int k = 0; k < 2; ++k) {
+    if (b->exec[k]) cudaGraphExecDestroy(b->exec[k]);
+    if (b->done[k]) cudaEventDestroy(b->done[k]);
+    if (b->h_stage[k]) cudaFreeHost(b->h_stage[k]);
+  }
+  if (b->capture) cudaStreamDestroy(b->capture);
+  if (b->d_buf) cudaFree(b->d_buf);
+  if (b->d_queue) cudaFree(b->d_queue);
+  delete b;
+}
+
+vh_status vh_batch_create(vh_volume* const* volumes, int32_t count, int32_t use_graph, vh_batch** out) {
+  if (!volumes || !out || count <= 0 || count > vh::kMaxBatchScenes) return VH_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  for (int i = 0; i < count; ++i) {
+    const vh_volume* v = volumes[i];
+    if (!v || v->dev.max_blocks == 0 || v->algo.normal_mode != 1 || v->params.device != volumes[0]->params.device ||
+        v->algo.fast_math != volumes[0]->algo.fast_math) {
+      return VH_ERR_INVALID_ARGUMENT;
+    }
+  }
+  vh_batch* b = new (std::nothrow) vh_batch();
+  if (!b) return VH_ERR_OUT_OF_MEMORY;
+  b->vols.assign(volumes, volumes + count);
+  b->device = volumes[0]->params.device;
+  b->fast = volumes[0]->algo.fast_math;
+  b->use_graph = use_graph != 0;
+  b->bytes = sizeof(vh::BatchHeader) + static_cast<size_t>(count) * sizeof(vh::SceneDesc);
+  DeviceGuard guard(b->device);
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&b->d_buf), b->bytes);
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_queue), 4 * sizeof(uint32_t));
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+    e = cudaMallocHost(reinterpret_cast<void**>(&b->h_stage[k]), b->bytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done[k], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess && b->use_graph) e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    vh_batch_destroy(b);
+    return e == cudaErrorMemoryAllocation ? VH_ERR_OUT_OF_MEMORY : VH_ERR_CUDA;
+  }
+  *out = b;
+  return VH_OK;
+}
+
+vh_status vh_batch_integrate(vh_batch* b, const float* const* depth_device, const vh_intrinsics* K, const vh_pose* T_wc,
+                             const int32_t* active, int32_t stride, void* stream) {
+  if (!b || !depth_device || !K || !T_wc || stride < 1) return VH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(b->device);
+  const cudaStream_t s = as_stream(stream);
+  const int slot = b->next;
+  b->next ^= 1;
+  // the step two calls ago read this staging buffer: wait until it has finished
+  if (cudaEventSynchronize(b->done[slot]) != cudaSuccess) return VH_ERR_CUDA;
+  auto* hdr = reinterpret_cast<vh::BatchHeader*>(b->h_stage[slot]);
+  auto* desc = reinterpret_cast<vh::SceneDesc*>(b->h_stage[slot] + sizeof(vh::BatchHeader));
+  const int n = static_cast<int>(b->vols.size());
+  uint32_t filter_total = 0, alloc_total = 0, map_total = 0;
+  for (int i = 0; i < n; ++i) {
+    vh_volume* v = b->vols[i];
+    vh::SceneDesc& d = desc[i];
+    std::memset(&d, 0, sizeof(d));
+    d.V = v->dev;
+    const bool on = !active || active[i] != 0;
+    if (on) {
+      if (!valid_intrinsics(&K[i]) || !depth_device[i]) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_batch_integrate: bad scene");
+      const vh_status st = ensure_depth(v, static_cast<size_t>(K[i].width) * K[i].height);
+      if (st != VH_OK) return st;
+      d.V = v->dev;
+      d.p = make_params(v, &K[i], &T_wc[i], stride);
+      d.depth_in = depth_device[i];
+      d.depth = v->d_depth_filtered;
+      d.nmap = v->d_normal_map;
+      d.filter_items = tiles(K[i].width, K[i].height, 32, 8);
+      d.alloc_items = tiles(d.p.sample_width, d.p.sample_height, 32, 8);
+      d.map_items = tiles(K[i].width, K[i].height, 32, 8);
+      d.active = 1U;
+    }
+    d.filter_first = filter_total;
+    d.alloc_first = alloc_total;
+    filter_total += d.filter_items;
+    alloc_total += d.alloc_items;
+  }
+  for (int i = 0; i < n; ++i) {
+    desc[i].map_first = alloc_total + map_total;
+    map_total += desc[i].map_items;
+  }
+  hdr->nscenes = static_cast<uint32_t>(n);
+  hdr->filter_total = filter_total;
+  hdr->alloc_total = alloc_total;
+  hdr->stage2_total = alloc_total + map_total;
+  cudaError_t e = cudaSuccess;
+  if (b->use_graph) {
+    if (!b->exec[slot]) {
+      cudaGraph_t g = nullptr;
+      e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeRelaxed);
+      if (e == cudaSuccess) {
+        const cudaError_t le = batch_launch(b, slot, b->capture);
+        e = cudaStreamEndCapture(b->capture, &g);
+        if (le != cudaSuccess) e = le;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec[slot], g, 0);
+      if (g) cudaGraphDestroy(g);
+    }
+    if (e == cudaSuccess) e = cudaGraphLaunch(b->exec[slot], s);
+  } else {
+    e = batch_launch(b, slot, s);
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(b->done[slot], s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return VH_ERR_CUDA;
+  }
+  return VH_OK;
+}
+
 }  // extern "C"

@@ -106,6 +106,30 @@ struct Params {
   int normal_mode;  // 0: bilateral normal per voxel (reference), 1: per-pixel normal map, interpolated per voxel
 };
 
+// One scene of a multi-scene batch step (device memory, rewritten by the host every step).  Items are the
+// work-queue units of the three batch kernels: filter tiles, allocation tiles, normal-map tiles (32x8 each).
+struct SceneDesc {
+  Volume V;
+  Params p;
+  const float* depth_in;  // raw depth, device
+  float* depth;           // filtered depth, device
+  float4* nmap;           // per-pixel normal map, device
+  uint32_t filter_first, filter_items;  // [first, first + items) in the filter kernel's item space
+  uint32_t alloc_first, alloc_items;    // in the allocation + normal-map kernel's item space
+  uint32_t map_first, map_items;        // (allocation items of all scenes come first)
+  uint32_t active, pad;
+};
+
+// Step header of a batch (device memory): scene count and item totals.
+struct BatchHeader {
+  uint32_t nscenes;
+  uint32_t filter_total;
+  uint32_t stage2_total;  // allocation + normal-map items
+  uint32_t alloc_total;   // allocation items (they precede the normal-map items)
+};
+
+constexpr int kMaxBatchScenes = 256;
+
 struct f3 {
   float x, y, z;
 };

@@ -2,125 +2,29 @@
 //
 // Reference: src/cuda_tsdf_integrator.cu:581-648 (estimateSurfaceNormalAtPixel / estimateDepthNormalsKernel)
 // and :650-725 (bilateralFilterDepthKernel), two kernels with a float3 + u8 normal map round trip through
-// global memory.  Here one CTA stages a 32x8 output tile of depth plus a 3-pixel halo in shared memory,
-// computes the normals of the tile plus a 2-pixel halo into shared memory, and runs the 5x5 joint bilateral
-// from shared memory: HBM traffic is one read and one write of the depth image.
-#include "vh_common.cuh"
+// global memory.  Here one kernel (device code in vh_filter.cuh): HBM traffic is one read and one write of
+// the depth image.
+#include "vh_filter.cuh"
 #include "vh_kernels.h"
 
 namespace vh {
 namespace {
 
-constexpr int kTX = 32;
-constexpr int kTY = 8;
-constexpr int kR = 2;                    // largest filter radius the tile supports
-constexpr int kDW = kTX + 2 * (kR + 1);  // depth tile incl. halo
-constexpr int kDH = kTY + 2 * (kR + 1);
-constexpr int kNW = kTX + 2 * kR;        // normal tile incl. halo
-constexpr int kNH = kTY + 2 * kR;
-
-// estimateSurfaceNormalAtPixel (cuda_tsdf_integrator.cu:581-627) on the staged tile; (sx, sy) = tile coords
-// of pixel (u, v) in s_depth.
-__device__ __forceinline__ float4 pixel_normal(const float (*s_depth)[kDW], int sx, int sy, int u, int v,
-                                               const Params& p) {
-  const float4 none = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (u <= 0 || v <= 0 || u + 1 >= p.width || v + 1 >= p.height) return none;
-  const float dc = s_depth[sy][sx];
-  const float dl = s_depth[sy][sx - 1];
-  const float dr = s_depth[sy][sx + 1];
-  const float du = s_depth[sy - 1][sx];
-  const float dd = s_depth[sy + 1][sx];
-  if (!(dc > 0.0f) || !(dl > 0.0f) || !(dr > 0.0f) || !(du > 0.0f) || !(dd > 0.0f)) return none;
-  const float thr = disc_threshold(p, dc);
-  if (fabsf(dl - dc) > thr || fabsf(dr - dc) > thr || fabsf(du - dc) > thr || fabsf(dd - dc) > thr) return none;
-  const f3 pl = backproject(static_cast<float>(u - 1), static_cast<float>(v), dl, p);
-  const f3 pr = backproject(static_cast<float>(u + 1), static_cast<float>(v), dr, p);
-  const f3 pu = backproject(static_cast<float>(u), static_cast<float>(v - 1), du, p);
-  const f3 pd = backproject(static_cast<float>(u), static_cast<float>(v + 1), dd, p);
-  f3 n = normalize3(cross3(sub3(pd, pu), sub3(pr, pl)));
-  if (norm3(n) <= 1e-6f) return none;
-  n = orient_toward_camera(n, backproject(static_cast<float>(u), static_cast<float>(v), dc, p));
-  if (!(norm3(n) > 1e-6f)) return none;
-  return make_float4(n.x, n.y, n.z, 1.0f);
-}
-
-__device__ __forceinline__ void stage_tile(const float* __restrict__ in, float (*s_depth)[kDW],
-                                           float4 (*s_normal)[kNW], int u0, int v0, const Params& p, int tid) {
-  for (int i = tid; i < kDW * kDH; i += kTX * kTY) {
-    const int dy = i / kDW, dx = i - dy * kDW;
-    const int gu = u0 + dx - (kR + 1), gv = v0 + dy - (kR + 1);
-    s_depth[dy][dx] = (gu >= 0 && gu < p.width && gv >= 0 && gv < p.height)
-                          ? __ldg(&in[static_cast<size_t>(gv) * p.width + gu])
-                          : 0.0f;
-  }
-  __syncthreads();
-  for (int i = tid; i < kNW * kNH; i += kTX * kTY) {
-    const int ny = i / kNW, nx = i - ny * kNW;
-    s_normal[ny][nx] = pixel_normal(s_depth, nx + 1, ny + 1, u0 + nx - kR, v0 + ny - kR, p);
-  }
-  __syncthreads();
-}
+using filt::kDH;
+using filt::kDW;
+using filt::kNH;
+using filt::kNW;
+using filt::kR;
+using filt::kTX;
+using filt::kTY;
 
 template <bool kBeginFrame>
 __global__ void __launch_bounds__(kTX* kTY) filter_kernel(const float* __restrict__ in, float* __restrict__ out,
                                                           const Params p, Counters* counters) {
-  __shared__ float s_depth[kDH][kDW];
-  __shared__ float4 s_normal[kNH][kNW];
-  __shared__ float s_spatial[(2 * kR + 1) * (2 * kR + 1)];
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
-  const int u0 = blockIdx.x * kTX, v0 = blockIdx.y * kTY;
-  if (kBeginFrame && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) {
-    counters->frame += 1U;
-    counters->visible_count = 0U;
-    counters->new_blocks = 0U;
-    counters->integrated_voxels = 0U;
-    counters->active_voxels = 0U;
-  }
-  const int R = p.filter_radius;
-  if (tid < (2 * kR + 1) * (2 * kR + 1)) {
-    const int du = tid % (2 * kR + 1) - kR, dv = tid / (2 * kR + 1) - kR;
-    // exp of the spatial term depends only on (du, dv): evaluated once per tile, same value as per tap
-    s_spatial[tid] = gaussian(static_cast<float>(du * du + dv * dv), p.filter_k_spatial);
-  }
-  stage_tile(in, s_depth, s_normal, u0, v0, p, tid);
-
-  const int u = u0 + tx, v = v0 + ty;
-  if (u >= p.width || v >= p.height) return;
-  const size_t ci = static_cast<size_t>(v) * p.width + u;
-  const float center = s_depth[ty + kR + 1][tx + kR + 1];
-  if (center <= 0.0f) {
-    out[ci] = 0.0f;
-    return;
-  }
-  const float4 cn4 = s_normal[ty + kR][tx + kR];
-  const bool has_cn = cn4.w != 0.0f;
-  const f3 cn = has_cn ? mk3(cn4.x, cn4.y, cn4.z) : mk3(0.0f, 0.0f, 0.0f);
-  const float thr = disc_threshold(p, center);
-  float wds = 0.0f, ws = 0.0f;
-  for (int dv = -R; dv <= R; ++dv) {
-    const int sv = v + dv;
-    if (sv < 0 || sv >= p.height) continue;
-    for (int du = -R; du <= R; ++du) {
-      const int su = u + du;
-      if (su < 0 || su >= p.width) continue;
-      const float sd = s_depth[ty + kR + 1 + dv][tx + kR + 1 + du];
-      if (sd <= 0.0f || fabsf(sd - center) > thr) continue;
-      const float delta = sd - center;
-      const float range = delta * delta;
-      float w = s_spatial[(dv + kR) * (2 * kR + 1) + (du + kR)] * gaussian(range, p.filter_k_range);
-      if (has_cn) {
-        const float4 sn = s_normal[ty + kR + dv][tx + kR + du];
-        if (sn.w == 0.0f) continue;
-        const float cosine = clampf(dot3(cn, mk3(sn.x, sn.y, sn.z)), -1.0f, 1.0f);
-        if (cosine < p.filter_min_cos) continue;
-        const float ad = 1.0f - cosine;
-        w *= gaussian(ad * ad, p.filter_k_angular);
-      }
-      wds += w * sd;
-      ws += w;
-    }
-  }
-  out[ci] = ws > 1e-6f ? (wds / ws) : center;
+  __shared__ filt::Smem S;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  if (kBeginFrame && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) filt::begin_frame(counters);
+  filt::filter_tile(in, out, p, blockIdx.x * kTX, blockIdx.y * kTY, tid, S);
 }
 
 __global__ void __launch_bounds__(kTX* kTY) normals_kernel(const float* __restrict__ in, float* __restrict__ normals,
@@ -129,7 +33,7 @@ __global__ void __launch_bounds__(kTX* kTY) normals_kernel(const float* __restri
   __shared__ float4 s_normal[kNH][kNW];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTX + tx;
   const int u0 = blockIdx.x * kTX, v0 = blockIdx.y * kTY;
-  stage_tile(in, s_depth, s_normal, u0, v0, p, tid);
+  filt::stage_tile(in, s_depth, s_normal, u0, v0, p, tid);
   const int u = u0 + tx, v = v0 + ty;
   if (u >= p.width || v >= p.height) return;
   const size_t ci = static_cast<size_t>(v) * p.width + u;
@@ -140,13 +44,7 @@ __global__ void __launch_bounds__(kTX* kTY) normals_kernel(const float* __restri
   valid[ci] = n.w != 0.0f ? 1 : 0;
 }
 
-__global__ void begin_frame_kernel(Counters* counters) {
-  counters->frame += 1U;
-  counters->visible_count = 0U;
-  counters->new_blocks = 0U;
-  counters->integrated_voxels = 0U;
-  counters->active_voxels = 0U;
-}
+__global__ void begin_frame_kernel(Counters* counters) { filt::begin_frame(counters); }
 
 }  // namespace
 

@@ -20,7 +20,9 @@
 // The file is compiled twice: as vh::exact (the bit-reproducible FP32 form: -fmad=false, IEEE division and
 // square root, vh_expf) and, with VH_FAST_MATH, as vh::fast (fused multiply-adds, approximate division, square
 // root and exponential; selected per volume by vh_algorithm.fast_math).
+#include "vh_alloc.cuh"
 #include "vh_common.cuh"
+#include "vh_filter.cuh"
 #include "vh_kernels.h"
 
 #ifdef VH_FAST_MATH
@@ -642,13 +644,16 @@ __global__ void __launch_bounds__(kUpdateThreads) update_kernel(const float* __r
 constexpr int kMapTX = 32, kMapTY = 8, kMapHalo = 2;
 constexpr int kMapW = kMapTX + 2 * kMapHalo, kMapH = kMapTY + 2 * kMapHalo;
 
-__global__ void __launch_bounds__(kMapTX * kMapTY) pixel_normal_kernel(const float* __restrict__ depth, const Params p,
-                                                                       float4* __restrict__ nmap) {
-  __shared__ float s_px[kMapH][kMapW], s_py[kMapH][kMapW], s_pz[kMapH][kMapW];
-  __shared__ float s_nx[kMapH][kMapW], s_ny[kMapH][kMapW], s_nz[kMapH][kMapW];
-  __shared__ unsigned char s_pv[kMapH][kMapW], s_nv[kMapH][kMapW];
-  const int tid = threadIdx.y * kMapTX + threadIdx.x;
-  const int x0 = blockIdx.x * kMapTX - kMapHalo, y0 = blockIdx.y * kMapTY - kMapHalo;
+struct MapSmem {
+  float px[kMapH][kMapW], py[kMapH][kMapW], pz[kMapH][kMapW];
+  float nx[kMapH][kMapW], ny[kMapH][kMapW], nz[kMapH][kMapW];
+  unsigned char pv[kMapH][kMapW], nv[kMapH][kMapW];
+};
+
+// the normal map of the 32x8 pixel tile at (x0, y0); every thread of the CTA calls it (it synchronises)
+__device__ __forceinline__ void map_tile(const float* __restrict__ depth, const Params& p, float4* __restrict__ nmap,
+                                         int x0t, int y0t, int tid, MapSmem& S) {
+  const int x0 = x0t - kMapHalo, y0 = y0t - kMapHalo;
   // 1. backprojected points of the tile + halo (invalid outside the image or where depth <= 0)
   for (int k = tid; k < kMapW * kMapH; k += kMapTX * kMapTY) {
     const int ty = k / kMapW, tx = k - ty * kMapW;
@@ -657,50 +662,51 @@ __global__ void __launch_bounds__(kMapTX * kMapTY) pixel_normal_kernel(const flo
     if (x >= 0 && x < p.width && y >= 0 && y < p.height) d = __ldg(&depth[static_cast<size_t>(y) * p.width + x]);
     const bool ok = d > 0.0f;
     const f3 q = ok ? backproject(static_cast<float>(x), static_cast<float>(y), d, p) : mk3(0.0f, 0.0f, 0.0f);
-    s_px[ty][tx] = q.x;
-    s_py[ty][tx] = q.y;
-    s_pz[ty][tx] = q.z;
-    s_pv[ty][tx] = ok ? 1 : 0;
+    S.px[ty][tx] = q.x;
+    S.py[ty][tx] = q.y;
+    S.pz[ty][tx] = q.z;
+    S.pv[ty][tx] = ok ? 1 : 0;
   }
   __syncthreads();
   // 2. base normals (estimateSurfaceNormalBaseCamera) of the tile + 1-pixel ring, oriented toward the camera
   for (int k = tid; k < kMapW * kMapH; k += kMapTX * kMapTY) {
     const int ty = k / kMapW, tx = k - ty * kMapW;
-    bool ok = tx >= 1 && tx < kMapW - 1 && ty >= 1 && ty < kMapH - 1 && s_pv[ty][tx] && s_pv[ty][tx - 1] &&
-              s_pv[ty][tx + 1] && s_pv[ty - 1][tx] && s_pv[ty + 1][tx];
+    bool ok = tx >= 1 && tx < kMapW - 1 && ty >= 1 && ty < kMapH - 1 && S.pv[ty][tx] && S.pv[ty][tx - 1] &&
+              S.pv[ty][tx + 1] && S.pv[ty - 1][tx] && S.pv[ty + 1][tx];
     f3 n = mk3(0.0f, 0.0f, 0.0f);
     if (ok) {
-      const f3 dv = mk3(s_px[ty + 1][tx] - s_px[ty - 1][tx], s_py[ty + 1][tx] - s_py[ty - 1][tx],
-                        s_pz[ty + 1][tx] - s_pz[ty - 1][tx]);
-      const f3 du = mk3(s_px[ty][tx + 1] - s_px[ty][tx - 1], s_py[ty][tx + 1] - s_py[ty][tx - 1],
-                        s_pz[ty][tx + 1] - s_pz[ty][tx - 1]);
+      const f3 dv = mk3(S.px[ty + 1][tx] - S.px[ty - 1][tx], S.py[ty + 1][tx] - S.py[ty - 1][tx],
+                        S.pz[ty + 1][tx] - S.pz[ty - 1][tx]);
+      const f3 du = mk3(S.px[ty][tx + 1] - S.px[ty][tx - 1], S.py[ty][tx + 1] - S.py[ty][tx - 1],
+                        S.pz[ty][tx + 1] - S.pz[ty][tx - 1]);
       n = normalize3(cross3(dv, du));
       ok = norm3(n) > 1e-6f;
-      if (ok) n = orient_unit_toward_camera(n, mk3(s_px[ty][tx], s_py[ty][tx], s_pz[ty][tx]));
+      if (ok) n = orient_unit_toward_camera(n, mk3(S.px[ty][tx], S.py[ty][tx], S.pz[ty][tx]));
     }
-    s_nx[ty][tx] = n.x;
-    s_ny[ty][tx] = n.y;
-    s_nz[ty][tx] = n.z;
-    s_nv[ty][tx] = ok ? 1 : 0;
+    S.nx[ty][tx] = n.x;
+    S.ny[ty][tx] = n.y;
+    S.nz[ty][tx] = n.z;
+    S.nv[ty][tx] = ok ? 1 : 0;
   }
   __syncthreads();
   // 3. the bilateral combination of the 3x3 base normals (estimateSurfaceNormalCamera)
-  const int x = blockIdx.x * kMapTX + threadIdx.x, y = blockIdx.y * kMapTY + threadIdx.y;
+  const int lx = tid % kMapTX, ly = tid / kMapTX;
+  const int x = x0t + lx, y = y0t + ly;
   if (x >= p.width || y >= p.height) return;
-  const int cx = threadIdx.x + kMapHalo, cy = threadIdx.y + kMapHalo;
+  const int cx = lx + kMapHalo, cy = ly + kMapHalo;
   float4 out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (s_nv[cy][cx]) {
-    const f3 cn = mk3(s_nx[cy][cx], s_ny[cy][cx], s_nz[cy][cx]);
-    const f3 cp = mk3(s_px[cy][cx], s_py[cy][cx], s_pz[cy][cx]);
+  if (S.nv[cy][cx]) {
+    const f3 cn = mk3(S.nx[cy][cx], S.ny[cy][cx], S.nz[cy][cx]);
+    const f3 cp = mk3(S.px[cy][cx], S.py[cy][cx], S.pz[cy][cx]);
     const float g1 = gaussian(1.0f, p.normal_k_spatial), g2 = gaussian(2.0f, p.normal_k_spatial);
     f3 wsum = mk3(0.0f, 0.0f, 0.0f);
     float ws = 0.0f;
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
       const int dx = k % 3 - 1, dy = k / 3 - 1;
-      if (!s_nv[cy + dy][cx + dx]) continue;
-      const f3 sn = mk3(s_nx[cy + dy][cx + dx], s_ny[cy + dy][cx + dx], s_nz[cy + dy][cx + dx]);
-      const float delta = s_pz[cy + dy][cx + dx] - cp.z;
+      if (!S.nv[cy + dy][cx + dx]) continue;
+      const f3 sn = mk3(S.nx[cy + dy][cx + dx], S.ny[cy + dy][cx + dx], S.nz[cy + dy][cx + dx]);
+      const float delta = S.pz[cy + dy][cx + dx] - cp.z;
       const float ad = 1.0f - clampf(dot3(cn, sn), -1.0f, 1.0f);
       const int r2 = dx * dx + dy * dy;
       const float w = (r2 == 0 ? 1.0f : (r2 == 1 ? g1 : g2)) * gaussian(delta * delta, p.normal_k_range) *
@@ -716,6 +722,12 @@ __global__ void __launch_bounds__(kMapTX * kMapTY) pixel_normal_kernel(const flo
     out = make_float4(n.x, n.y, n.z, 1.0f);
   }
   nmap[static_cast<size_t>(y) * p.width + x] = out;
+}
+
+__global__ void __launch_bounds__(kMapTX * kMapTY) pixel_normal_kernel(const float* __restrict__ depth, const Params p,
+                                                                       float4* __restrict__ nmap) {
+  __shared__ MapSmem S;
+  map_tile(depth, p, nmap, blockIdx.x * kMapTX, blockIdx.y * kMapTY, threadIdx.y * kMapTX + threadIdx.x, S);
 }
 
 // Normal at a voxel's projection (u, v): bilinear blend of the valid map taps around it, renormalised.
@@ -872,6 +884,201 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
   count_updates(V, updated, newly, lane);
 }
 
+// ---- multi-scene batch: three work-queue kernels over the items of every scene of the step ----
+//
+// 1. batch_filter_kernel: the filter tiles of all scenes (the first tile of a scene also starts its frame);
+// 2. batch_stage2_kernel: the allocation tiles, then the normal-map tiles, of all scenes;
+// 3. batch_update_kernel: chunks of kThreads voxel slots of every scene's visible blocks (the per-scene
+//    visible counts are final after kernel 2; every CTA derives the chunk prefix from them).
+// Each CTA takes the next item from a global counter (a device work queue), so scenes of very different
+// sizes share the GPU without idle tails; the scene of an item is found by binary search over the
+// per-scene first items, and its descriptor is copied to shared memory when it changes.
+
+// last scene whose first item <= item (firsts ascending; empty scenes share the next scene's first)
+template <typename F>
+__device__ __forceinline__ int find_scene(int n, uint32_t item, F first) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first(mid) <= item) {
+      lo = mid;
+    } else {
+      hi = mid - 1;
+    }
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void copy_desc(SceneDesc& dst, const SceneDesc* __restrict__ src, int tid, int nthreads) {
+  static_assert(sizeof(SceneDesc) % 4 == 0, "descriptor copied as words");
+  const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
+  uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
+  for (int i = tid; i < static_cast<int>(sizeof(SceneDesc) / 4); i += nthreads) d[i] = s[i];
+}
+
+__global__ void __launch_bounds__(filt::kTX * filt::kTY) batch_filter_kernel(const SceneDesc* __restrict__ descs,
+                                                                             const BatchHeader* __restrict__ hdr,
+                                                                             uint32_t* __restrict__ queue) {
+  constexpr int kT = filt::kTX * filt::kTY;
+  __shared__ filt::Smem S;
+  __shared__ SceneDesc D;
+  __shared__ uint32_t s_item;
+  __shared__ int s_scene;
+  const int tid = threadIdx.x;
+  const int nsc = static_cast<int>(hdr->nscenes);
+  const uint32_t total = hdr->filter_total;
+  int cur = -1;
+  for (;;) {
+    if (tid == 0) {
+      const uint32_t it = atomicAdd(&queue[0], 1U);
+      s_item = it;
+      s_scene = it < total ? find_scene(nsc, it, [&](int k) { return descs[k].filter_first; }) : -1;
+    }
+    __syncthreads();
+    const uint32_t item = s_item;
+    const int sc = s_scene;
+    if (item >= total) break;
+    if (sc != cur) {
+      copy_desc(D, descs + sc, tid, kT);
+      cur = sc;
+      __syncthreads();
+    }
+    const uint32_t local = item - D.filter_first;
+    const uint32_t tiles_x = (static_cast<uint32_t>(D.p.width) + filt::kTX - 1) / filt::kTX;
+    if (local == 0U && tid == 0) filt::begin_frame(D.V.counters);
+    filt::filter_tile(D.depth_in, D.depth, D.p, static_cast<int>(local % tiles_x) * filt::kTX,
+                      static_cast<int>(local / tiles_x) * filt::kTY, tid, S);
+    __syncthreads();
+  }
+}
+
+union Stage2Smem {
+  alloc::Smem a;
+  MapSmem m;
+};
+
+__global__ void __launch_bounds__(alloc::kThreads) batch_stage2_kernel(const SceneDesc* __restrict__ descs,
+                                                                       const BatchHeader* __restrict__ hdr,
+                                                                       uint32_t* __restrict__ queue) {
+  static_assert(alloc::kThreads == kMapTX * kMapTY, "one CTA shape for both stages");
+  __shared__ Stage2Smem U;
+  __shared__ SceneDesc D;
+  __shared__ uint32_t s_item;
+  __shared__ int s_scene;
+  const int tid = threadIdx.x;
+  const int nsc = static_cast<int>(hdr->nscenes);
+  const uint32_t total = hdr->stage2_total, alloc_total = hdr->alloc_total;
+  int cur = -1;
+  for (;;) {
+    if (tid == 0) {
+      const uint32_t it = atomicAdd(&queue[1], 1U);
+      s_item = it;
+      int scn = -1;
+      if (it < alloc_total) {
+        scn = find_scene(nsc, it, [&](int k) { return descs[k].alloc_first; });
+      } else if (it < total) {
+        scn = find_scene(nsc, it, [&](int k) { return descs[k].map_first; });
+      }
+      s_scene = scn;
+    }
+    __syncthreads();
+    const uint32_t item = s_item;
+    const int sc = s_scene;
+    if (item >= total) break;
+    if (sc != cur) {
+      copy_desc(D, descs + sc, tid, alloc::kThreads);
+      cur = sc;
+      __syncthreads();
+    }
+    if (item < alloc_total) {
+      const uint32_t local = item - D.alloc_first;
+      const uint32_t tiles_x = (static_cast<uint32_t>(D.p.sample_width) + alloc::kTX - 1) / alloc::kTX;
+      alloc::alloc_tile(D.depth, D.V, D.p, static_cast<int>(local % tiles_x) * alloc::kTX,
+                        static_cast<int>(local / tiles_x) * alloc::kTY, tid, U.a);
+    } else {
+      const uint32_t local = item - D.map_first;
+      const uint32_t tiles_x = (static_cast<uint32_t>(D.p.width) + kMapTX - 1) / kMapTX;
+      map_tile(D.depth, D.p, D.nmap, static_cast<int>(local % tiles_x) * kMapTX,
+               static_cast<int>(local / tiles_x) * kMapTY, tid, U.m);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) batch_update_kernel(const SceneDesc* __restrict__ descs,
+                                                                const BatchHeader* __restrict__ hdr,
+                                                                uint32_t* __restrict__ queue) {
+  __shared__ MapQueue<kThreads> Q;
+  __shared__ SceneDesc D;
+  __shared__ uint32_t s_first[kMaxBatchScenes + 1];
+  __shared__ uint32_t s_item;
+  __shared__ int s_scene;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nsc = static_cast<int>(hdr->nscenes);
+  constexpr uint32_t kChunksPerBlock = kBlockVoxels / kThreads;
+  if (tid == 0) {
+    uint32_t run = 0U;
+    for (int k = 0; k < nsc; ++k) {
+      s_first[k] = run;
+      if (descs[k].active) run += descs[k].V.counters->visible_count * kChunksPerBlock;
+    }
+    s_first[nsc] = run;
+    Q.count = 0U;
+  }
+  __syncthreads();
+  const uint32_t total = s_first[nsc];
+  int cur = -1;
+  for (;;) {
+    if (tid == 0) {
+      const uint32_t it = atomicAdd(&queue[2], 1U);
+      s_item = it;
+      s_scene = it < total ? find_scene(nsc, it, [&](int k) { return s_first[k]; }) : -1;
+    }
+    __syncthreads();
+    const uint32_t item = s_item;
+    const int sc = s_scene;
+    if (item >= total) break;
+    if (sc != cur) {
+      copy_desc(D, descs + sc, tid, kThreads);
+      cur = sc;
+      __syncthreads();
+    }
+    // 1. prefix of one slot per thread, survivors appended to the queue
+    const unsigned long long i = static_cast<unsigned long long>(item - s_first[sc]) * kThreads + tid;
+    const uint32_t b = D.V.slot_block[D.V.visible[static_cast<uint32_t>(i >> 9)]];
+    const int li = static_cast<int>(i & 511U);
+    bool pass = false;
+    f3 pc = mk3(0.0f, 0.0f, 0.0f);
+    float u = 0.0f, v = 0.0f, d = 0.0f;
+    if (b != kInvalidBlock) pass = voxel_prefix(D.depth, D.p, D.V.block_keys[b], li, pc, u, v, d);
+    const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
+    uint32_t base = 0U;
+    if (lane == 0 && ballot) {
+      base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
+      atomicAdd(&D.V.counters->active_voxels, static_cast<uint32_t>(__popc(ballot)));
+    }
+    base = __shfl_sync(0xffffffffU, base, 0);
+    if (pass) {
+      const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
+      Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
+      Q.u[e] = u;
+      Q.v[e] = v;
+      Q.d[e] = d;
+      Q.x[e] = pc.x;
+      Q.y[e] = pc.y;
+      Q.z[e] = pc.z;
+    }
+    __syncthreads();
+    // 2. the survivors of the chunk, one per thread
+    const uint32_t n = Q.count;
+    bool updated = false, newly = false;
+    if (static_cast<uint32_t>(tid) < n) map_update_entry(D.depth, D.nmap, D.V, D.p, Q, tid, updated, newly);
+    count_updates(D.V, updated, newly, lane);
+    __syncthreads();
+    if (tid == 0) Q.count = 0U;
+  }
+}
+
 }  // namespace
 
 static int grid_for(const void* kernel, int threads) {
@@ -954,6 +1161,21 @@ cudaError_t launch_integrate_update(const float* depth, const Volume& V, const P
     return cudaGetLastError();
   }
   update_kernel<<<grid > 0 ? grid : integrate_grid_size(), kUpdateThreads, 0, s>>>(depth, V, p);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s) {
+  static int grids[3] = {0, 0, 0};
+  if (grids[0] == 0) {
+    grids[0] = grid_for(reinterpret_cast<const void*>(batch_filter_kernel), filt::kTX * filt::kTY);
+    grids[1] = grid_for(reinterpret_cast<const void*>(batch_stage2_kernel), alloc::kThreads);
+    grids[2] = grid_for(reinterpret_cast<const void*>(batch_update_kernel), kThreads);
+  }
+  cudaError_t e = cudaMemsetAsync(queue, 0, 3 * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  batch_filter_kernel<<<grids[0], filt::kTX * filt::kTY, 0, s>>>(descs, hdr, queue);
+  batch_stage2_kernel<<<grids[1], alloc::kThreads, 0, s>>>(descs, hdr, queue);
+  batch_update_kernel<<<grids[2], kThreads, 0, s>>>(descs, hdr, queue);
   return cudaGetLastError();
 }
 

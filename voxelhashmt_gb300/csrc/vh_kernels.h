@@ -20,6 +20,9 @@ cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, c
 // FP32 form; fast: the same source compiled with fused multiply-adds and hardware approximations.  With
 // Params::normal_mode 1, nmap (width x height float4) receives the per-pixel normal map.
 namespace exact {
+// one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
+// scenes (queue: 3 counters, cleared here)
+cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
@@ -32,6 +35,9 @@ cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nm
 int integrate_grid_size();
 }  // namespace exact
 namespace fast {
+// one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
+// scenes (queue: 3 counters, cleared here)
+cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
