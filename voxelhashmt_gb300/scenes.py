@@ -113,6 +113,45 @@ def orbit_scene(seed=0, frames=64, width=320, height=240, fx=277.0, fy=277.0, cx
                  voxel_size=0.01, truncation=0.04, hash_buckets=1 << 16, max_depth=4.0)
 
 
+def object_scan_scene(seed=0, frames=None, resolution=None, voxel_size=None) -> Scene:
+    """One object scan of the batched multi-scene workload: a seeded cluster of 3-8 primitives (spheres r
+    0.1-0.3 E, boxes 0.15-0.5 E sides, cylinders) within an extent E drawn from 0.5-2 m, resting on nothing
+    (background returns no depth), seen by a camera orbiting once at 1.6 E + 0.4 m, 0.6 E above the cluster
+    centre.  Frame count uniform in 20-300, resolution one of 160x120, 320x240, 640x480 (fx = fy = 0.866 W,
+    a 60 degree horizontal field of view), voxel size uniform in 2-8 mm, truncation 4 voxels; each drawn from
+    the seed unless given."""
+    rng = np.random.default_rng(10_000 + seed)
+    extent = float(rng.uniform(0.5, 2.0))
+    n = int(rng.integers(3, 9))
+    prims = []
+    for _ in range(n):
+        kind = int(rng.integers(0, 3))
+        c = rng.uniform(-0.35, 0.35, size=3) * extent
+        if kind == 0:
+            prims.append(_prim(SPHERE, c, r=float(rng.uniform(0.1, 0.3) * extent)))
+        elif kind == 1:
+            half = rng.uniform(0.075, 0.25, size=3) * extent
+            prims.append(_prim(BOX, c - half, c + half))
+        else:
+            r = float(rng.uniform(0.05, 0.2) * extent)
+            h = float(rng.uniform(0.2, 0.7) * extent)
+            prims.append(_prim(CYLINDER, (c[0], c[1], c[2] - h / 2), r=r, h=h))
+    n_frames = int(rng.integers(20, 301)) if frames is None else int(frames)
+    w, h = [(160, 120), (320, 240), (640, 480)][int(rng.integers(0, 3))] if resolution is None else resolution
+    vs = float(rng.uniform(0.002, 0.008)) if voxel_size is None else float(voxel_size)
+    K = Intrinsics(w, h, 0.866 * w, 0.866 * w, (w - 1) / 2.0, (h - 1) / 2.0)
+    radius, height = 1.6 * extent + 0.4, 0.6 * extent
+    phase = float(rng.uniform(0, 2 * math.pi))
+    poses = []
+    for i in range(n_frames):
+        a = phase + 2.0 * math.pi * i / n_frames
+        poses.append(look_at((radius * math.cos(a), radius * math.sin(a), height), (0.0, 0.0, 0.0)))
+    sc = Scene(np.asarray(prims, np.float32), K, poses, seed, name="object_scan", voxel_size=vs, truncation=4 * vs,
+               hash_buckets=1 << 18, max_depth=radius + 2 * extent)
+    sc.extent = extent
+    return sc
+
+
 def room_scene(seed=0, frames=1000, width=640, height=480, fx=525.0, fy=525.0, cx=319.5, cy=239.5,
                n_prims=40, room=(4.0, 5.0, 3.0)) -> Scene:
     rng = np.random.default_rng(seed)
