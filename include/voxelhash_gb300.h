@@ -258,6 +258,18 @@ void vh_batch_destroy(vh_batch* batch);
 vh_status vh_batch_integrate(vh_batch* batch, const float* const* depth_device, const vh_intrinsics* K,
                              const vh_pose* T_wc, const int32_t* active, int32_t stride, void* stream);
 
+/* ---- Learned depth denoiser: building blocks (no reference counterpart) ----
+ * Activations are NHWC BF16 with 32 channels (64 bytes per pixel), device memory, 16-byte aligned.
+ * vh_nn_pack_conv32_weights: FP32 weights w[co][ci][3][3] (32 x 32) -> the packed BF16 tensor-core operand
+ * (18,432 bytes); transpose_flip packs w[ci][co][2-ky][2-kx], the weights of the input gradient.
+ * vh_nn_conv32: 3x3 convolution with zero padding on the tensor cores (tcgen05, FP32 accumulation); mode 0:
+ * out = conv(in) + bias, then ReLU if relu; mode 1: out = conv(in) where mask > 0, else 0.  *error becomes
+ * nonzero if the tensor cores did not signal completion within a bounded wait. */
+vh_status vh_nn_pack_conv32_weights(const float* w, void* packed, int32_t transpose_flip, void* stream);
+vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, const void* mask, void* out,
+                       int32_t batch, int32_t width, int32_t height, int32_t mode, int32_t relu, uint32_t* error,
+                       void* stream);
+
 /* ---- Dataset reader: include/tsdfmc/dataset_io.h, portable ----
  * Layout: <root>/<frame id>/depth.png and <root>/<frame id>/<pose file>; the frame ids are the all-digit
  * directory names, ascending (listDatasetFrameIds, :135-152).  These calls touch no GPU.  On failure they

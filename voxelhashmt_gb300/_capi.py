@@ -122,6 +122,9 @@ _SIGNATURES = {
     "vh_batch_destroy": (None, [_vp]),
     "vh_batch_integrate": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(VhIntrinsics), C.POINTER(VhPose), _ip, C.c_int32,
                                      _vp]),
+    "vh_nn_pack_conv32_weights": (C.c_int, [_vp, _vp, C.c_int32, _vp]),
+    "vh_nn_conv32": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                               C.POINTER(C.c_uint32), _vp]),
     "vh_dataset_last_error": (C.c_char_p, []),
     "vh_dataset_list_frames": (C.c_int, [C.c_char_p, _ip, C.c_size_t, _szp]),
     "vh_dataset_load_intrinsics": (C.c_int, [C.c_char_p, C.POINTER(VhIntrinsics), C.POINTER(C.c_float)]),

@@ -15,6 +15,7 @@
 #include "../../include/voxelhash_gb300.h"
 #include "vh_common.cuh"
 #include "vh_kernels.h"
+#include "vh_nn.h"
 
 struct vh_volume {
   vh_params params{};
@@ -976,6 +977,28 @@ vh_status vh_batch_integrate(vh_batch* b, const float* const* depth_device, cons
     return VH_ERR_CUDA;
   }
   return VH_OK;
+}
+
+// ---- denoiser building blocks (device pointers; no reference counterpart) ----
+
+vh_status vh_nn_pack_conv32_weights(const float* w, void* packed, int32_t transpose_flip, void* stream) {
+  if (!w || !packed) return VH_ERR_INVALID_ARGUMENT;
+  return vh::nn::launch_pack_w32(w, static_cast<__nv_bfloat16*>(packed), transpose_flip, as_stream(stream)) == cudaSuccess
+             ? VH_OK
+             : VH_ERR_CUDA;
+}
+
+vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, const void* mask, void* out, int32_t batch,
+                       int32_t width, int32_t height, int32_t mode, int32_t relu, uint32_t* error, void* stream) {
+  if (!in || !packed_w || !out || !error || batch <= 0 || width <= 0 || height <= 0 || (mode != 0 && mode != 1) ||
+      (mode == 1 && !mask)) {
+    return VH_ERR_INVALID_ARGUMENT;
+  }
+  const cudaError_t e = vh::nn::launch_conv32(static_cast<const __nv_bfloat16*>(in),
+                                              static_cast<const __nv_bfloat16*>(packed_w), bias,
+                                              static_cast<const __nv_bfloat16*>(mask), static_cast<__nv_bfloat16*>(out),
+                                              batch, width, height, mode, relu, error, as_stream(stream));
+  return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
 }
 
 }  // extern "C"
