@@ -52,7 +52,8 @@ typedef enum vh_status {
   VH_ERR_BUFFER_TOO_SMALL = 8,  /* caller's output buffer is smaller than the result; *count holds the size */
   VH_ERR_CAPACITY = 9,          /* request larger than the fixed scratch of vh_allocate_static_scratch */
   VH_ERR_IO = 10,               /* dataset file missing, unreadable or unparsable (vh_dataset_last_error) */
-  VH_ERR_FORMAT = 11            /* unsupported or corrupt PNG / metadata layout (vh_dataset_last_error) */
+  VH_ERR_FORMAT = 11,           /* unsupported or corrupt PNG / metadata layout (vh_dataset_last_error) */
+  VH_ERR_TIMEOUT = 12           /* a bounded device-side wait gave up (the denoiser's tensor-core convolution) */
 } vh_status;
 
 typedef struct vh_volume vh_volume;
@@ -107,6 +108,9 @@ typedef struct vh_algorithm {
    * (results do not depend on the shape); 0: the shape launch_variant. */
   int32_t autotune;
   int32_t launch_variant; /* the layer-update launch shape used without autotuning (0..5, default 0) */
+  /* 0 (default): the reference's bilateral depth filter; 1: the learned depth denoiser set with
+   * vh_set_depth_denoiser (the bilateral filter until weights are set). */
+  int32_t depth_filter;
 } vh_algorithm;
 
 /* per-frame statistics of the last integrated/allocated frame */
@@ -269,6 +273,28 @@ vh_status vh_nn_pack_conv32_weights(const float* w, void* packed, int32_t transp
 vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, const void* mask, void* out,
                        int32_t batch, int32_t width, int32_t height, int32_t mode, int32_t relu, uint32_t* error,
                        void* stream);
+
+/* The whole denoiser (3x3 convolutions 4 -> 32 -> 32 -> 32 -> 1, ReLU, residual output; the two 32 -> 32 layers
+ * on the tensor cores).  params: FP32 [vh_nn_param_count()] = w1[32][4][3][3] b1[32] w2[32][32][3][3] b2[32]
+ * w3[32][32][3][3] b3[32] w4[32][3][3] b4; packed: 73,728 bytes (vh_nn_pack); workspace: vh_nn_workspace_bytes;
+ * depth, out, target: batch x height x width FP32, device memory.  vh_nn_backward reads the activations
+ * vh_nn_forward left in the same workspace and writes the FP32 gradients of the loss
+ * sum((out - target)^2) / (batch * height * width) over pixels valid in depth, target and out, and
+ * loss[0..1] = (sum of squared errors, pixel count).  error: as vh_nn_conv32. */
+int32_t vh_nn_param_count(void);
+uint64_t vh_nn_workspace_bytes(int32_t batch, int32_t width, int32_t height);
+vh_status vh_nn_pack(const float* params, void* packed, void* stream);
+vh_status vh_nn_forward(const float* params, const void* packed, const float* depth, float* out, int32_t batch,
+                        int32_t width, int32_t height, void* workspace, uint32_t* error, void* stream);
+vh_status vh_nn_backward(const float* params, const void* packed, const float* depth, const float* target,
+                         const float* out, int32_t batch, int32_t width, int32_t height, void* workspace, float* grads,
+                         float* loss, uint32_t* error, void* stream);
+/* one Adam step (FP32 moments m, v; step counts from 1) */
+vh_status vh_nn_adam(float* params, const float* grads, float* m, float* v, float lr, float beta1, float beta2,
+                     float eps, int32_t step, void* stream);
+/* Uses the denoiser with these parameters (host memory, vh_nn_param_count() floats) in place of the bilateral
+ * filter in vh_integrate when vh_algorithm.depth_filter is 1; params NULL clears it. */
+vh_status vh_set_depth_denoiser(vh_volume* volume, const float* params);
 
 /* ---- Dataset reader: include/tsdfmc/dataset_io.h, portable ----
  * Layout: <root>/<frame id>/depth.png and <root>/<frame id>/<pose file>; the frame ids are the all-digit

@@ -84,3 +84,97 @@ def test_conv32_input_gradient_matches_reference(capi):
     ref = torch.where(act.double() > 0, ref, torch.zeros_like(ref))
     nbad, worst = _close(out, ref)
     assert nbad == 0, (nbad, worst)
+
+
+def _bf(t):
+    """BF16 rounding in the forward pass, identity in the backward (straight-through)."""
+    return t + (t.to(torch.bfloat16).double() - t).detach()
+
+
+def _round_grad(t):
+    t.register_hook(lambda g: g.to(torch.bfloat16).double())
+    return t
+
+
+def _ref_loss(params, depth, target):
+    """The net in float64 on the CPU, BF16 rounding where the kernels store BF16: weights of the two 32 -> 32
+    layers, the activations, and the activation gradients."""
+    import torch.nn.functional as F
+    sizes = [32 * 4 * 9, 32, 32 * 32 * 9, 32, 32 * 32 * 9, 32, 32 * 9, 1]
+    w1, b1, w2, b2, w3, b3, w4, b4 = torch.split(params, sizes)
+    d = depth.unsqueeze(1)
+    valid = (d > 0).double()
+    ones = torch.ones(1, 1, 3, 3, dtype=torch.float64)
+    s = F.conv2d(d * valid, ones, padding=1)
+    c = F.conv2d(valid, ones, padding=1)
+    m = torch.where(c > 0, s / torch.clamp(c, min=1), torch.zeros_like(s))
+    X = torch.cat([(d - m) * 100 * valid, valid, m * 0.25 * valid, torch.zeros_like(d)], 1)
+    z1 = _round_grad(F.conv2d(X, w1.view(32, 4, 3, 3), b1, padding=1))
+    a1 = _bf(torch.relu(z1))
+    z2 = _round_grad(F.conv2d(a1, _bf(w2.view(32, 32, 3, 3)), b2, padding=1))
+    a2 = _bf(torch.relu(z2))
+    z3 = _round_grad(F.conv2d(a2, _bf(w3.view(32, 32, 3, 3)), b3, padding=1))
+    a3 = _bf(torch.relu(z3))
+    r = F.conv2d(a3, w4.view(1, 32, 3, 3), b4, padding=1)
+    out = torch.where(valid > 0, torch.clamp(d + 0.01 * r, min=0.0), torch.zeros_like(d)).squeeze(1)
+    mask = (depth > 0) & (target > 0) & (out > 0)
+    loss = torch.where(mask, (out - target) ** 2, torch.zeros_like(out)).sum() / out.numel()
+    return loss, out
+
+
+def test_denoiser_forward_and_gradients_match_reference(capi):
+    """Forward output within 0.1 mm and every parameter group's gradient within 2 % (relative L2) of the
+    float64 reference on the same BF16-rounded operands, on a batch of two 150 x 24 rooms crops (two tensor-
+    core tiles per row, one partial)."""
+    from voxelhashmt_gb300 import denoiser, scenes
+    sc = scenes.room_scene(seed=3, frames=2, width=150, height=24, fx=120.0, fy=120.0, cx=75.0, cy=12.0)
+    raw = np.stack([scenes.render_depth(sc, f) for f in range(2)]).astype(np.float32)
+    tgt = np.stack([scenes.render_depth(sc, f, noise=False) for f in range(2)]).astype(np.float32)
+    p0 = denoiser.init_params(seed=5)
+    p0[-289:] = np.random.default_rng(6).normal(0, 0.05, 289).astype(np.float32)  # a non-trivial output layer
+    net = denoiser.DepthDenoiser(p0)
+    g_gpu, loss_gpu, out_gpu = net.gradients(torch.from_numpy(raw).cuda(), torch.from_numpy(tgt).cuda())
+    params = torch.from_numpy(p0.astype(np.float64)).requires_grad_(True)
+    loss_ref, out_ref = _ref_loss(params, torch.from_numpy(raw).double(), torch.from_numpy(tgt).double())
+    loss_ref.backward()
+    g_ref = params.grad.numpy()
+    assert np.max(np.abs(out_gpu.cpu().numpy() - out_ref.detach().numpy())) <= 1e-4
+    assert abs(loss_gpu - float(loss_ref)) <= 1e-3 * float(loss_ref) + 1e-12
+    sizes = [32 * 4 * 9, 32, 32 * 32 * 9, 32, 32 * 32 * 9, 32, 32 * 9, 1]
+    names = ["w1", "b1", "w2", "b2", "w3", "b3", "w4", "b4"]
+    off = 0
+    for name, n in zip(names, sizes):
+        a, b = g_gpu[off:off + n].astype(np.float64), g_ref[off:off + n]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        assert rel <= 2e-2, (name, rel)
+        off += n
+
+
+def test_denoiser_training_and_gain(capi):
+    """Trains on raw / ray-cast pairs of two rooms (new seeds) and evaluates on a held-out room: the RMSE to
+    the ray-cast target of raw depth, of the bilateral filter and of the trained net (printed); the net
+    must beat raw depth, and its training loss must fall."""
+    from voxelhashmt_gb300 import _capi, backend, denoiser, scenes
+    raws, tgts = denoiser.make_training_pairs([101, 102], frames_per_scene=40, crops_per_frame=8)
+    net = denoiser.DepthDenoiser(seed=1)
+    hist = denoiser.train(net, raws, tgts, steps=300, batch=16)
+    assert np.mean(hist[-30:]) < 0.85 * np.mean(hist[:5]), (hist[:5], hist[-30:])
+    ev_raw, ev_tgt = denoiser.make_training_pairs([203], frames_per_scene=12, crops_per_frame=4, rng_seed=9)
+    out = net.forward(ev_raw)
+    vol = backend.VoxelHashTSDF(0.005, 0.02, max_blocks=1)
+    K = scenes.Intrinsics(128, 128, 105.0, 105.0, 63.5, 63.5)
+    bil = torch.empty_like(ev_raw)
+    for i in range(ev_raw.shape[0]):
+        _capi.check(_capi.lib().vh_filter_depth(vol.handle, C.c_void_p(ev_raw[i].data_ptr()),
+                                                C.c_void_p(bil[i].data_ptr()), C.byref(_capi.intrinsics(K)), None),
+                    vol.handle)
+    torch.cuda.synchronize()
+    m = (ev_raw > 0) & (ev_tgt > 0) & (out > 0) & (bil > 0)
+
+    def rmse(x):
+        return float(torch.sqrt(((x - ev_tgt)[m] ** 2).mean()))
+
+    print("held-out RMSE to the ray-cast target (mm): raw %.3f, bilateral %.3f, learned %.3f"
+          % (1000 * rmse(ev_raw), 1000 * rmse(bil), 1000 * rmse(out)))
+    assert rmse(out) < rmse(ev_raw)
+    vol.close()

@@ -26,6 +26,7 @@ VH_ERR_BUFFER_TOO_SMALL = 8
 VH_ERR_CAPACITY = 9
 VH_ERR_IO = 10
 VH_ERR_FORMAT = 11
+VH_ERR_TIMEOUT = 12
 
 BLOCK_BYTES = 512 * 6 * 3 * 16
 
@@ -47,7 +48,7 @@ class VhAlgorithm(C.Structure):
         ("max_voxel_weight", C.c_float), ("depth_sigma", C.c_float), ("huber_delta", C.c_float),
         ("min_observation_weight", C.c_float), ("min_view_angle_weight", C.c_float),
         ("allocation_mode", C.c_int32), ("fast_math", C.c_int32), ("normal_mode", C.c_int32),
-        ("autotune", C.c_int32), ("launch_variant", C.c_int32),
+        ("autotune", C.c_int32), ("launch_variant", C.c_int32), ("depth_filter", C.c_int32),
     ]
 
 
@@ -75,7 +76,7 @@ class VhError(RuntimeError):
 def _status_name(status):
     names = {0: "VH_OK", 1: "VH_ERR_INVALID_ARGUMENT", 2: "VH_ERR_CUDA", 3: "VH_ERR_NO_DEVICE",
              4: "VH_ERR_OUT_OF_MEMORY", 5: "VH_ERR_KEY_RANGE", 6: "VH_ERR_HASH_FULL", 7: "VH_ERR_POOL_FULL",
-             8: "VH_ERR_BUFFER_TOO_SMALL", 9: "VH_ERR_CAPACITY", 10: "VH_ERR_IO", 11: "VH_ERR_FORMAT"}
+             8: "VH_ERR_BUFFER_TOO_SMALL", 9: "VH_ERR_CAPACITY", 10: "VH_ERR_IO", 11: "VH_ERR_FORMAT", 12: "VH_ERR_TIMEOUT"}
     return names.get(status, "VH_STATUS_%d" % status)
 
 
@@ -125,6 +126,14 @@ _SIGNATURES = {
     "vh_nn_pack_conv32_weights": (C.c_int, [_vp, _vp, C.c_int32, _vp]),
     "vh_nn_conv32": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                C.POINTER(C.c_uint32), _vp]),
+    "vh_nn_param_count": (C.c_int32, []),
+    "vh_nn_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32]),
+    "vh_nn_pack": (C.c_int, [_vp, _vp, _vp]),
+    "vh_nn_forward": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, _vp, C.POINTER(C.c_uint32), _vp]),
+    "vh_nn_backward": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, _vp, _vp, _vp,
+                                 C.POINTER(C.c_uint32), _vp]),
+    "vh_nn_adam": (C.c_int, [_vp, _vp, _vp, _vp, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, _vp]),
+    "vh_set_depth_denoiser": (C.c_int, [_vp, C.POINTER(C.c_float)]),
     "vh_dataset_last_error": (C.c_char_p, []),
     "vh_dataset_list_frames": (C.c_int, [C.c_char_p, _ip, C.c_size_t, _szp]),
     "vh_dataset_load_intrinsics": (C.c_int, [C.c_char_p, C.POINTER(VhIntrinsics), C.POINTER(C.c_float)]),

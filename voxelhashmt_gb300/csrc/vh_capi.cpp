@@ -25,6 +25,11 @@ struct vh_volume {
   float* d_depth_in = nullptr;
   float* d_depth_filtered = nullptr;
   float4* d_normal_map = nullptr;  // per-pixel normals (vh_algorithm.normal_mode 1)
+  // learned depth denoiser (vh_algorithm.depth_filter 1)
+  float* d_nn_params = nullptr;
+  __nv_bfloat16* d_nn_packed = nullptr;
+  unsigned char* d_nn_ws = nullptr;
+  size_t nn_ws_bytes = 0;
   // launch-shape autotuner of the fused update (vh_algorithm.autotune): frames cycle through the variants,
   // each timed with a pair of events, until every variant has kTuneRounds samples; then the fastest is kept
   int tuned_variant = -1;
@@ -301,6 +306,7 @@ void vh_algorithm_default(vh_algorithm* a) {
   a->normal_mode = 0;
   a->autotune = 1;
   a->launch_variant = 0;
+  a->depth_filter = 0;
 }
 
 const char* vh_status_string(vh_status s) {
@@ -317,6 +323,7 @@ const char* vh_status_string(vh_status s) {
     case VH_ERR_CAPACITY: return "request larger than the fixed static scratch";
     case VH_ERR_IO: return "dataset file missing, unreadable or unparsable";
     case VH_ERR_FORMAT: return "unsupported or corrupt PNG or metadata layout";
+    case VH_ERR_TIMEOUT: return "a bounded device-side wait gave up";
   }
   return "unknown status";
 }
@@ -366,7 +373,8 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   if (v->algo.filter_radius < 0 || v->algo.filter_radius > 2 || v->algo.normal_radius != 1 ||
       v->algo.allocation_mode < 0 || v->algo.allocation_mode > 1 || v->algo.fast_math < 0 || v->algo.fast_math > 1 ||
       v->algo.normal_mode < 0 || v->algo.normal_mode > 1 || v->algo.autotune < 0 || v->algo.autotune > 1 ||
-      v->algo.launch_variant < 0 || v->algo.launch_variant >= vh::exact::fused_variant_count()) {
+      v->algo.launch_variant < 0 || v->algo.launch_variant >= vh::exact::fused_variant_count() ||
+      v->algo.depth_filter < 0 || v->algo.depth_filter > 1) {
     delete v;
     return VH_ERR_INVALID_ARGUMENT;
   }
@@ -438,6 +446,9 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_depth_in);
   dfree(v->d_depth_filtered);
   dfree(v->d_normal_map);
+  dfree(v->d_nn_params);
+  dfree(v->d_nn_packed);
+  dfree(v->d_nn_ws);
   for (auto& pair : v->tune_events) {
     cudaEventDestroy(pair[0]);
     cudaEventDestroy(pair[1]);
@@ -504,7 +515,20 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
     }
     VH_CUDA(v, cudaEventRecord(ev[0], s));
   }
-  VH_CUDA(v, vh::launch_filter(src, v->d_depth_filtered, p, v->dev.counters, s));
+  if (v->algo.depth_filter == 1 && v->d_nn_params) {
+    const size_t need = vh::nn::workspace_bytes(1, K->width, K->height);
+    if (need > v->nn_ws_bytes) {
+      dfree(v->d_nn_ws);
+      v->nn_ws_bytes = 0;
+      VH_CUDA(v, cudaMalloc(reinterpret_cast<void**>(&v->d_nn_ws), need));
+      v->nn_ws_bytes = need;
+    }
+    VH_CUDA(v, vh::launch_begin_frame(v->dev.counters, s));
+    VH_CUDA(v, vh::nn::forward(v->d_nn_params, v->d_nn_packed, src, v->d_depth_filtered, 1, K->width, K->height,
+                               v->d_nn_ws, &v->dev.counters->error, s));
+  } else {
+    VH_CUDA(v, vh::launch_filter(src, v->d_depth_filtered, p, v->dev.counters, s));
+  }
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[2], s));
@@ -659,6 +683,7 @@ vh_status vh_synchronize(vh_volume* v, void* stream) {
   VH_CUDA(v, cudaMemsetAsync(&v->dev.counters->error, 0, sizeof(uint32_t), s));
   VH_CUDA(v, cudaStreamSynchronize(s));
   if (err & vh::kErrKeyRange) return fail(v, VH_ERR_KEY_RANGE, "block coordinate outside the 21-bit packed key range");
+  if (err & vh::kErrTimeout) return fail(v, VH_ERR_TIMEOUT, "the tensor cores did not signal completion in time");
   if (err & vh::kErrHashFull) return fail(v, VH_ERR_HASH_FULL, "block hash table full (raise hash_buckets)");
   return fail(v, VH_ERR_POOL_FULL, "block pool full (raise max_blocks)");
 }
@@ -999,6 +1024,67 @@ vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, 
                                               static_cast<const __nv_bfloat16*>(mask), static_cast<__nv_bfloat16*>(out),
                                               batch, width, height, mode, relu, error, as_stream(stream));
   return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
+}
+
+int32_t vh_nn_param_count(void) { return vh::nn::param_count(); }
+
+uint64_t vh_nn_workspace_bytes(int32_t batch, int32_t width, int32_t height) {
+  if (batch <= 0 || width <= 0 || height <= 0) return 0;
+  return vh::nn::workspace_bytes(batch, width, height);
+}
+
+vh_status vh_nn_pack(const float* params, void* packed, void* stream) {
+  if (!params || !packed) return VH_ERR_INVALID_ARGUMENT;
+  return vh::nn::pack_weights(params, static_cast<__nv_bfloat16*>(packed), as_stream(stream)) == cudaSuccess ? VH_OK
+                                                                                                            : VH_ERR_CUDA;
+}
+
+vh_status vh_nn_forward(const float* params, const void* packed, const float* depth, float* out, int32_t batch,
+                        int32_t width, int32_t height, void* workspace, uint32_t* error, void* stream) {
+  if (!params || !packed || !depth || !out || !workspace || !error || batch <= 0 || width <= 0 || height <= 0) {
+    return VH_ERR_INVALID_ARGUMENT;
+  }
+  return vh::nn::forward(params, static_cast<const __nv_bfloat16*>(packed), depth, out, batch, width, height,
+                         static_cast<unsigned char*>(workspace), error, as_stream(stream)) == cudaSuccess
+             ? VH_OK
+             : VH_ERR_CUDA;
+}
+
+vh_status vh_nn_backward(const float* params, const void* packed, const float* depth, const float* target,
+                         const float* out, int32_t batch, int32_t width, int32_t height, void* workspace, float* grads,
+                         float* loss, uint32_t* error, void* stream) {
+  if (!params || !packed || !depth || !target || !out || !workspace || !grads || !loss || !error || batch <= 0 ||
+      width <= 0 || height <= 0) {
+    return VH_ERR_INVALID_ARGUMENT;
+  }
+  return vh::nn::backward(params, static_cast<const __nv_bfloat16*>(packed), depth, target, out, batch, width, height,
+                          static_cast<unsigned char*>(workspace), grads, loss, error, as_stream(stream)) == cudaSuccess
+             ? VH_OK
+             : VH_ERR_CUDA;
+}
+
+vh_status vh_nn_adam(float* params, const float* grads, float* m, float* v, float lr, float beta1, float beta2, float eps,
+                     int32_t step, void* stream) {
+  if (!params || !grads || !m || !v || step < 1) return VH_ERR_INVALID_ARGUMENT;
+  return vh::nn::adam(params, grads, m, v, lr, beta1, beta2, eps, step, as_stream(stream)) == cudaSuccess ? VH_OK
+                                                                                                          : VH_ERR_CUDA;
+}
+
+vh_status vh_set_depth_denoiser(vh_volume* v, const float* params) {
+  if (!v) return VH_ERR_INVALID_ARGUMENT;
+  DeviceGuard guard(v->params.device);
+  if (!params) {
+    dfree(v->d_nn_params);
+    dfree(v->d_nn_packed);
+    return VH_OK;
+  }
+  const size_t n = static_cast<size_t>(vh::nn::param_count());
+  if (!v->d_nn_params) VH_CUDA(v, dalloc(&v->d_nn_params, n));
+  if (!v->d_nn_packed) VH_CUDA(v, cudaMalloc(reinterpret_cast<void**>(&v->d_nn_packed), 4 * 9 * 32 * 32 * sizeof(__nv_bfloat16)));
+  VH_CUDA(v, cudaMemcpy(v->d_nn_params, params, n * sizeof(float), cudaMemcpyHostToDevice));
+  VH_CUDA(v, vh::nn::pack_weights(v->d_nn_params, v->d_nn_packed, nullptr));
+  VH_CUDA(v, cudaDeviceSynchronize());
+  return VH_OK;
 }
 
 }  // extern "C"

@@ -29,6 +29,7 @@ constexpr unsigned long long kKeyMask = (1ULL << kKeyBits) - 1ULL;
 constexpr uint32_t kErrKeyRange = 1u;  // block coordinate outside the 21-bit packed range
 constexpr uint32_t kErrHashFull = 2u;  // no free slot within `capacity` probes
 constexpr uint32_t kErrPoolFull = 4u;  // more blocks than the pool holds
+constexpr uint32_t kErrTimeout = 8u;   // a bounded wait on the tensor cores gave up (the denoiser's convolution)
 
 // Device-resident counters of one volume (64 bytes; read back with one D2H copy).
 struct Counters {

@@ -44,6 +44,7 @@ constexpr int kBPad = kBBytes + 8192;
 constexpr int kThreads = 128;              // 4 warps: one per 32 TMEM lanes
 constexpr int kSmem = kAPad + kBPad + 64;  // + mbarrier and TMEM address
 constexpr uint32_t kMaxPolls = 1u << 24;
+constexpr unsigned int kErrorBit = 8u;  // the volume error word's timeout bit
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) conv32_tc_kernel(const __nv_bfloat16
     __syncthreads();
   }
   if (!ok) {
-    if (tid == 0) atomicOr(error, 1u);
+    if (tid == 0) atomicOr(error, kErrorBit);
     mbar_wait(bar_addr, phase ^ 1u);  // the MMAs in flight, bounded
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -265,6 +266,364 @@ __global__ void pack_w32_kernel(const float* __restrict__ w, __nv_bfloat16* __re
 
 cudaError_t launch_pack_w32(const float* w, __nv_bfloat16* out, int transpose_flip, cudaStream_t s) {
   pack_w32_kernel<<<(9 * kC * kC + 255) / 256, 256, 0, s>>>(w, out, transpose_flip);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- the rest of the net (CUDA cores)
+//
+// Parameters, one FP32 array (kParamCount): w1[32][4][3][3] b1[32] w2[32][32][3][3] b2[32] w3[32][32][3][3] b3[32]
+// w4[32][3][3] b4.  Input channels per pixel (FP32): the depth's local high-pass (d - m) * 100 (centimetres;
+// m = mean of the valid depths of the 3x3 neighbourhood), the validity mask, and m / 4 (the depth level); the
+// output is the residual r in centimetres, depth' = d + r / 100 on valid pixels (clamped at 0).  The
+// high-pass keeps the BF16 activations' 8 significant bits on the noise rather than on metres of depth.
+namespace {
+
+constexpr int kCin = 4;
+constexpr float kScale = 100.0f, kInvScale = 0.01f;
+constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kC * kCin * 9, kOffW2 = kOffB1 + kC, kOffB2 = kOffW2 + kC * kC * 9;
+constexpr int kOffW3 = kOffB2 + kC, kOffB3 = kOffW3 + kC * kC * 9, kOffW4 = kOffB3 + kC, kOffB4 = kOffW4 + kC * 9;
+constexpr int kParams = kOffB4 + 1;
+
+__device__ __forceinline__ bool inside(int x, int y, int w, int h) { return x >= 0 && x < w && y >= 0 && y < h; }
+
+__global__ void pack_input_kernel(const float* __restrict__ depth, float4* __restrict__ X, int batch, int w, int h) {
+  const long long n = static_cast<long long>(batch) * w * h;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
+    const long long img = i / (static_cast<long long>(w) * h);
+    const float d = depth[i];
+    float sum = 0.0f;
+    int cnt = 0;
+    for (int dy = -1; dy <= 1; ++dy) {
+      for (int dx = -1; dx <= 1; ++dx) {
+        if (!inside(x + dx, y + dy, w, h)) continue;
+        const float v = depth[(img * h + y + dy) * w + x + dx];
+        if (v > 0.0f) {
+          sum += v;
+          ++cnt;
+        }
+      }
+    }
+    const bool valid = d > 0.0f;
+    const float m = cnt ? sum / static_cast<float>(cnt) : 0.0f;
+    X[i] = valid ? make_float4((d - m) * kScale, 1.0f, m * 0.25f, 0.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+// layer 1: 4 -> 32, ReLU, one thread per pixel
+__global__ void __launch_bounds__(256) conv_in_kernel(const float4* __restrict__ X, const float* __restrict__ params,
+                                                      __nv_bfloat16* __restrict__ A1, int batch, int w, int h) {
+  __shared__ float sw[kC * kCin * 9 + kC];
+  for (int i = threadIdx.x; i < kC * kCin * 9 + kC; i += blockDim.x) sw[i] = params[kOffW1 + i];
+  __syncthreads();
+  const long long n = static_cast<long long>(batch) * w * h;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
+    const long long img = i / (static_cast<long long>(w) * h);
+    float4 in[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
+      in[t] = inside(sx, sy, w, h) ? X[(img * h + sy) * w + sx] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+    __align__(16) __nv_bfloat16 res[kC];
+    for (int co = 0; co < kC; ++co) {
+      float acc = sw[kC * kCin * 9 + co];
+      const float* wc = sw + co * kCin * 9;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        acc += wc[0 * 9 + t] * in[t].x + wc[1 * 9 + t] * in[t].y + wc[2 * 9 + t] * in[t].z + wc[3 * 9 + t] * in[t].w;
+      }
+      res[co] = __float2bfloat16_rn(fmaxf(acc, 0.0f));
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(A1 + i * kC)[q] = reinterpret_cast<const uint4*>(res)[q];
+  }
+}
+
+__device__ __forceinline__ void load32(const __nv_bfloat16* p, float* v) {
+  __align__(16) __nv_bfloat16 b[kC];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(b)[q] = reinterpret_cast<const uint4*>(p)[q];
+#pragma unroll
+  for (int c = 0; c < kC; ++c) v[c] = __bfloat162float(b[c]);
+}
+
+// layer 4: 32 -> 1 residual, depth' = d + r / 100 on valid pixels
+__global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __restrict__ A3,
+                                                       const float* __restrict__ params,
+                                                       const float* __restrict__ depth, float* __restrict__ out,
+                                                       int batch, int w, int h) {
+  __shared__ float sw[kC * 9 + 1];
+  for (int i = threadIdx.x; i < kC * 9 + 1; i += blockDim.x) sw[i] = params[kOffW4 + i];
+  __syncthreads();
+  const long long n = static_cast<long long>(batch) * w * h;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const float d = depth[i];
+    if (!(d > 0.0f)) {
+      out[i] = 0.0f;
+      continue;
+    }
+    const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
+    const long long img = i / (static_cast<long long>(w) * h);
+    float r = sw[kC * 9];
+    for (int t = 0; t < 9; ++t) {
+      const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
+      if (!inside(sx, sy, w, h)) continue;
+      float a[kC];
+      load32(A3 + ((img * h + sy) * w + sx) * kC, a);
+#pragma unroll
+      for (int c = 0; c < kC; ++c) r += sw[c * 9 + t] * a[c];
+    }
+    out[i] = fmaxf(d + r * kInvScale, 0.0f);
+  }
+}
+
+// loss = sum over pixels valid in input and target of (out - target)^2 / n_pixels; dr = dloss/dr
+__global__ void loss_grad_kernel(const float* __restrict__ out, const float* __restrict__ target,
+                                 const float* __restrict__ depth, float* __restrict__ dr, long long n,
+                                 float* __restrict__ loss) {
+  float se = 0.0f, cnt = 0.0f;
+  const float inv_n = 1.0f / static_cast<float>(n);
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const bool m = depth[i] > 0.0f && target[i] > 0.0f && out[i] > 0.0f;
+    const float diff = m ? out[i] - target[i] : 0.0f;
+    dr[i] = 2.0f * diff * kInvScale * inv_n;
+    se += diff * diff;
+    cnt += m ? 1.0f : 0.0f;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    se += __shfl_down_sync(0xffffffffU, se, o);
+    cnt += __shfl_down_sync(0xffffffffU, cnt, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&loss[0], se);
+    atomicAdd(&loss[1], cnt);
+  }
+}
+
+// dA3[q][c] = (A3[q][c] > 0) * sum_t w4[c][t] dr[q - off(t)]
+__global__ void __launch_bounds__(256) dgrad_out_kernel(const float* __restrict__ dr, const float* __restrict__ params,
+                                                        const __nv_bfloat16* __restrict__ A3,
+                                                        __nv_bfloat16* __restrict__ dA3, int batch, int w, int h) {
+  __shared__ float sw[kC * 9];
+  for (int i = threadIdx.x; i < kC * 9; i += blockDim.x) sw[i] = params[kOffW4 + i];
+  __syncthreads();
+  const long long n = static_cast<long long>(batch) * w * h;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
+    const long long img = i / (static_cast<long long>(w) * h);
+    float g[9];
+#pragma unroll
+    for (int t = 0; t < 9; ++t) {
+      const int sx = x - (t % 3 - 1), sy = y - (t / 3 - 1);
+      g[t] = inside(sx, sy, w, h) ? dr[(img * h + sy) * w + sx] : 0.0f;
+    }
+    float a[kC];
+    load32(A3 + i * kC, a);
+    __align__(16) __nv_bfloat16 res[kC];
+#pragma unroll
+    for (int c = 0; c < kC; ++c) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) acc += sw[c * 9 + t] * g[t];
+      res[c] = __float2bfloat16_rn(a[c] > 0.0f ? acc : 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(dA3 + i * kC)[q] = reinterpret_cast<const uint4*>(res)[q];
+  }
+}
+
+// Weight gradients of a 3x3 convolution: dW[co][ci][t] = sum_p dY[p][co] X[p + off(t)][ci], db[co] = sum_p dY[p][co].
+// Thread (co, ci) keeps 9 accumulators over the CTA's row segments of kSeg pixels, staged in shared memory as
+// floats; one atomic flush per CTA.  X: BF16 with CI channels or FP32 float4 (CI = 4); dY: BF16 32 channels or
+// FP32 1 channel.
+constexpr int kSeg = 64;
+
+template <int CI, int CO, bool kXBf16, bool kDyBf16>
+__global__ void __launch_bounds__(CI * CO) wgrad_kernel(const void* __restrict__ Xv, const void* __restrict__ dYv,
+                                                        float* __restrict__ dW, float* __restrict__ db, int batch,
+                                                        int w, int h) {
+  __shared__ float sX[3][kSeg + 2][CI];
+  __shared__ float sG[kSeg][CO];
+  const int tid = threadIdx.x;
+  const int co = tid / CI, ci = tid % CI;
+  float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float bacc = 0.0f;
+  const int segs_x = (w + kSeg - 1) / kSeg;
+  const long long nseg = static_cast<long long>(batch) * h * segs_x;
+  for (long long sgi = blockIdx.x; sgi < nseg; sgi += gridDim.x) {
+    const int x0 = static_cast<int>(sgi % segs_x) * kSeg;
+    const int y = static_cast<int>((sgi / segs_x) % h);
+    const long long img = sgi / (static_cast<long long>(segs_x) * h);
+    for (int i = tid; i < 3 * (kSeg + 2) * CI; i += CI * CO) {
+      const int c = i % CI, px = (i / CI) % (kSeg + 2), r = i / (CI * (kSeg + 2));
+      const int sx = x0 - 1 + px, sy = y - 1 + r;
+      float v = 0.0f;
+      if (inside(sx, sy, w, h)) {
+        const long long p = (img * h + sy) * w + sx;
+        if (kXBf16) {
+          v = __bfloat162float(static_cast<const __nv_bfloat16*>(Xv)[p * CI + c]);
+        } else {
+          v = reinterpret_cast<const float*>(static_cast<const float4*>(Xv) + p)[c];
+        }
+      }
+      sX[r][px][c] = v;
+    }
+    for (int i = tid; i < kSeg * CO; i += CI * CO) {
+      const int c = i % CO, px = i / CO;
+      const int sx = x0 + px;
+      float v = 0.0f;
+      if (sx < w) {
+        const long long p = (img * h + y) * w + sx;
+        v = kDyBf16 ? __bfloat162float(static_cast<const __nv_bfloat16*>(dYv)[p * CO + c])
+                    : static_cast<const float*>(dYv)[p * CO + c];
+      }
+      sG[px][c] = v;
+    }
+    __syncthreads();
+    for (int px = 0; px < kSeg; ++px) {
+      const float g = sG[px][co];
+#pragma unroll
+      for (int t = 0; t < 9; ++t) acc[t] += g * sX[t / 3][px + t % 3][ci];
+      bacc += g;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int t = 0; t < 9; ++t) atomicAdd(&dW[(co * CI + ci) * 9 + t], acc[t]);
+  if (ci == 0) atomicAdd(&db[co], bacc);
+}
+
+__global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                            float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+  }
+}
+
+int grid_for_elems(long long n) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (n + 255) / 256;
+  const long long cap = 8LL * (sms > 0 ? sms : 152);
+  return static_cast<int>(want < cap ? (want > 0 ? want : 1) : cap);
+}
+
+int sm_count() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 152;
+}
+
+}  // namespace
+
+int param_count() { return kParams; }
+
+size_t workspace_bytes(int batch, int width, int height) {
+  const size_t n = static_cast<size_t>(batch) * width * height;
+  // X (float4), A1, A2, A3 (32 x BF16), r / dr (float), dA x 2 (32 x BF16)
+  return n * (16 + 3 * 64 + 4 + 2 * 64) + 4096;
+}
+
+static void carve(unsigned char* ws, size_t n, float4** X, __nv_bfloat16** A1, __nv_bfloat16** A2,
+                  __nv_bfloat16** A3, float** r, __nv_bfloat16** G1, __nv_bfloat16** G2) {
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char* p = ws + o;
+    o += (bytes + 255) & ~static_cast<size_t>(255);
+    return p;
+  };
+  *X = reinterpret_cast<float4*>(take(n * 16));
+  *A1 = reinterpret_cast<__nv_bfloat16*>(take(n * 64));
+  *A2 = reinterpret_cast<__nv_bfloat16*>(take(n * 64));
+  *A3 = reinterpret_cast<__nv_bfloat16*>(take(n * 64));
+  *r = reinterpret_cast<float*>(take(n * 4));
+  *G1 = reinterpret_cast<__nv_bfloat16*>(take(n * 64));
+  *G2 = reinterpret_cast<__nv_bfloat16*>(take(n * 64));
+}
+
+cudaError_t pack_weights(const float* params, __nv_bfloat16* packed, cudaStream_t s) {
+  cudaError_t e = launch_pack_w32(params + kOffW2, packed, 0, s);
+  if (e == cudaSuccess) e = launch_pack_w32(params + kOffW3, packed + 9 * kC * kC, 0, s);
+  if (e == cudaSuccess) e = launch_pack_w32(params + kOffW2, packed + 2 * 9 * kC * kC, 1, s);
+  if (e == cudaSuccess) e = launch_pack_w32(params + kOffW3, packed + 3 * 9 * kC * kC, 1, s);
+  return e;
+}
+
+cudaError_t forward(const float* params, const __nv_bfloat16* packed, const float* depth, float* out, int batch,
+                    int width, int height, unsigned char* ws, unsigned int* error, cudaStream_t s) {
+  const size_t n = static_cast<size_t>(batch) * width * height;
+  float4* X;
+  __nv_bfloat16 *A1, *A2, *A3, *G1, *G2;
+  float* r;
+  carve(ws, n, &X, &A1, &A2, &A3, &r, &G1, &G2);
+  const int grid = grid_for_elems(static_cast<long long>(n));
+  pack_input_kernel<<<grid, 256, 0, s>>>(depth, X, batch, width, height);
+  conv_in_kernel<<<grid, 256, 0, s>>>(X, params, A1, batch, width, height);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_conv32(A1, packed, params + kOffB2, nullptr, A2, batch, width, height, kForward, 1, error, s);
+  if (e == cudaSuccess) {
+    e = launch_conv32(A2, packed + 9 * kC * kC, params + kOffB3, nullptr, A3, batch, width, height, kForward, 1, error, s);
+  }
+  if (e != cudaSuccess) return e;
+  conv_out_kernel<<<grid, 256, 0, s>>>(A3, params, depth, out, batch, width, height);
+  return cudaGetLastError();
+}
+
+cudaError_t backward(const float* params, const __nv_bfloat16* packed, const float* depth, const float* target,
+                     const float* out, int batch, int width, int height, unsigned char* ws, float* grads, float* loss,
+                     unsigned int* error, cudaStream_t s) {
+  const size_t n = static_cast<size_t>(batch) * width * height;
+  float4* X;
+  __nv_bfloat16 *A1, *A2, *A3, *G1, *G2;
+  float* dr;
+  carve(ws, n, &X, &A1, &A2, &A3, &dr, &G1, &G2);
+  const int grid = grid_for_elems(static_cast<long long>(n));
+  cudaError_t e = cudaMemsetAsync(grads, 0, kParams * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(loss, 0, 2 * sizeof(float), s);
+  if (e != cudaSuccess) return e;
+  const int wg = sm_count();
+  loss_grad_kernel<<<grid, 256, 0, s>>>(out, target, depth, dr, static_cast<long long>(n), loss);
+  // layer 4: weights, then the gradient into A3
+  wgrad_kernel<kC, 1, true, false><<<wg, kC, 0, s>>>(A3, dr, grads + kOffW4, grads + kOffB4, batch, width, height);
+  dgrad_out_kernel<<<grid, 256, 0, s>>>(dr, params, A3, G1, batch, width, height);
+  // layer 3
+  wgrad_kernel<kC, kC, true, true><<<wg, kC * kC, 0, s>>>(A2, G1, grads + kOffW3, grads + kOffB3, batch, width, height);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    e = launch_conv32(G1, packed + 3 * 9 * kC * kC, nullptr, A2, G2, batch, width, height, kGrad, 0, error, s);
+  }
+  if (e != cudaSuccess) return e;
+  // layer 2
+  wgrad_kernel<kC, kC, true, true><<<wg, kC * kC, 0, s>>>(A1, G2, grads + kOffW2, grads + kOffB2, batch, width, height);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    e = launch_conv32(G2, packed + 2 * 9 * kC * kC, nullptr, A1, G1, batch, width, height, kGrad, 0, error, s);
+  }
+  if (e != cudaSuccess) return e;
+  // layer 1
+  wgrad_kernel<kCin, kC, false, true><<<wg, kCin * kC, 0, s>>>(X, G1, grads + kOffW1, grads + kOffB1, batch, width,
+                                                              height);
+  return cudaGetLastError();
+}
+
+cudaError_t adam(float* params, const float* grads, float* m, float* v, float lr, float b1, float b2, float eps,
+                 int step, cudaStream_t s) {
+  const float c1 = 1.0f - powf(b1, static_cast<float>(step)), c2 = 1.0f - powf(b2, static_cast<float>(step));
+  adam_kernel<<<(kParams + 255) / 256, 256, 0, s>>>(params, grads, m, v, kParams, lr, b1, b2, eps, c1, c2);
   return cudaGetLastError();
 }
 

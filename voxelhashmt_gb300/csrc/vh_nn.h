@@ -19,5 +19,20 @@ cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, c
 cudaError_t launch_pack_w32(const float* w, __nv_bfloat16* out, int transpose_flip, cudaStream_t s);
 int conv32_smem_bytes();
 
+// The whole net.  params: FP32 [param_count()]; packed: 4 x 9,216 BF16 (w2, w3 forward, w2, w3 input-gradient);
+// depth / out / target: batch x height x width FP32; ws: workspace_bytes(batch, width, height) of device memory
+// holding the activations the backward pass reads (forward before backward on the same ws).
+int param_count();
+size_t workspace_bytes(int batch, int width, int height);
+cudaError_t pack_weights(const float* params, __nv_bfloat16* packed, cudaStream_t s);
+cudaError_t forward(const float* params, const __nv_bfloat16* packed, const float* depth, float* out, int batch,
+                    int width, int height, unsigned char* ws, unsigned int* error, cudaStream_t s);
+// grads: FP32 [param_count()] (overwritten); loss: [sum of squared errors over masked pixels, their count]
+cudaError_t backward(const float* params, const __nv_bfloat16* packed, const float* depth, const float* target,
+                     const float* out, int batch, int width, int height, unsigned char* ws, float* grads, float* loss,
+                     unsigned int* error, cudaStream_t s);
+cudaError_t adam(float* params, const float* grads, float* m, float* v, float lr, float b1, float b2, float eps,
+                 int step, cudaStream_t s);
+
 }  // namespace nn
 }  // namespace vh

@@ -1,0 +1,186 @@
+"""Learned depth denoiser that can stand in for the bilateral filter (vh_algorithm.depth_filter = 1).
+
+Net: 3x3 convolutions 4 -> 32 -> 32 -> 32 -> 1 with ReLU, residual output (depth' = depth + r / 100 on valid
+pixels).  The input channels per pixel are the depth's local high-pass (centimetres), the validity mask and
+the local depth level.  The weights are BF16 in the two 32 -> 32 layers (tensor cores, FP32 accumulation,
+BF16 activations); the input and output layers and all weight gradients and Adam moments are FP32.
+Every kernel is in the library (vh_nn_*); this module holds the buffers and runs the loop.
+
+Training pairs: raw noisy depth frames and the depth ray-cast (vh_raycast_depth) at the same pose from the
+volume fused from all frames of the scene with the plain FP32 pipeline, cut into random crops.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def param_count() -> int:
+    return int(_capi.lib().vh_nn_param_count())
+
+
+def init_params(seed=0) -> np.ndarray:
+    """He-normal weights, zero biases; the output layer starts small so the net starts near identity."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for cin, cout, scale in ((4, 32, 1.0), (32, 32, 1.0), (32, 32, 1.0), (32, 1, 0.1)):
+        std = scale * np.sqrt(2.0 / (cin * 9))
+        parts.append(rng.normal(0.0, std, size=cout * cin * 9))
+        parts.append(np.zeros(cout))
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.size == param_count()
+    return p
+
+
+class DepthDenoiser:
+    """Parameters, packed tensor-core weights, Adam moments and workspace on one GPU."""
+
+    def __init__(self, params=None, seed=0, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        import torch
+        self.torch = torch
+        p = init_params(seed) if params is None else np.asarray(params, np.float32)
+        self.params = torch.from_numpy(p.copy()).cuda()
+        self.grads = torch.zeros_like(self.params)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.packed = torch.empty(4 * 9 * 32 * 32, dtype=torch.bfloat16, device="cuda")
+        self.loss = torch.zeros(2, dtype=torch.float32, device="cuda")
+        self.error = torch.zeros(1, dtype=torch.int32, device="cuda")
+        self.lr, self.beta1, self.beta2, self.eps = lr, beta1, beta2, eps
+        self.step_count = 0
+        self._ws = None
+        self._ws_shape = None
+        self._repack()
+
+    def _err(self):
+        return C.cast(C.c_void_p(self.error.data_ptr()), C.POINTER(C.c_uint32))
+
+    def _repack(self):
+        _capi.check(_capi.lib().vh_nn_pack(_ptr(self.params), _ptr(self.packed), None))
+
+    def _workspace(self, b, w, h):
+        if self._ws_shape != (b, w, h):
+            n = int(_capi.lib().vh_nn_workspace_bytes(b, w, h))
+            self._ws = self.torch.empty(n, dtype=self.torch.uint8, device="cuda")
+            self._ws_shape = (b, w, h)
+        return self._ws
+
+    def check_error(self):
+        if int(self.error.item()) != 0:
+            raise _capi.VhError(_capi.VH_ERR_TIMEOUT, "tensor cores did not signal completion in time")
+
+    def forward(self, depth):
+        """depth: (B, H, W) float32 CUDA tensor -> denoised (B, H, W)."""
+        depth = depth.contiguous()
+        b, h, w = depth.shape
+        out = self.torch.empty_like(depth)
+        _capi.check(_capi.lib().vh_nn_forward(_ptr(self.params), _ptr(self.packed), _ptr(depth), _ptr(out), b, w, h,
+                                              _ptr(self._workspace(b, w, h)), self._err(), None))
+        return out
+
+    def train_step(self, raw, target):
+        """One Adam step on a batch (B, H, W) of raw depth and targets; returns the batch RMSE (metres) over
+        the pixels valid in input, target and output, before the step."""
+        raw, target = raw.contiguous(), target.contiguous()
+        b, h, w = raw.shape
+        out = self.forward(raw)
+        ws = self._workspace(b, w, h)
+        _capi.check(_capi.lib().vh_nn_backward(_ptr(self.params), _ptr(self.packed), _ptr(raw), _ptr(target), _ptr(out),
+                                               b, w, h, _ptr(ws), _ptr(self.grads), _ptr(self.loss), self._err(), None))
+        self.step_count += 1
+        _capi.check(_capi.lib().vh_nn_adam(_ptr(self.params), _ptr(self.grads), _ptr(self.m), _ptr(self.v), self.lr,
+                                           self.beta1, self.beta2, self.eps, self.step_count, None))
+        self._repack()
+        se, cnt = self.loss.tolist()
+        return float(np.sqrt(se / max(cnt, 1.0)))
+
+    def gradients(self, raw, target):
+        """(gradients (P,) numpy, loss) of one batch without updating: for checks against a reference."""
+        raw, target = raw.contiguous(), target.contiguous()
+        b, h, w = raw.shape
+        out = self.forward(raw)
+        _capi.check(_capi.lib().vh_nn_backward(_ptr(self.params), _ptr(self.packed), _ptr(raw), _ptr(target), _ptr(out),
+                                               b, w, h, _ptr(self._workspace(b, w, h)), _ptr(self.grads),
+                                               _ptr(self.loss), self._err(), None))
+        self.torch.cuda.synchronize()
+        self.check_error()
+        se = float(self.loss[0].item())
+        return self.grads.cpu().numpy(), se / (b * h * w), out
+
+    def params_numpy(self) -> np.ndarray:
+        return self.params.cpu().numpy()
+
+
+def make_training_pairs(seeds, frames_per_scene=120, crops_per_frame=16, crop=128, width=640, height=480,
+                        fuse_frames=None, rng_seed=0):
+    """Random crops (raw, target) from rooms (scenes.room_scene) of the given seeds: raw = the noisy
+    rendered frame; target = the depth ray-cast at the frame's pose from the plain FP32 volume fused from
+    `fuse_frames` frames of the same walk (all of them by default).  Returns two (N, crop, crop) CUDA
+    tensors; crops keep windows where at least half the pixels are valid in both."""
+    import torch
+    from . import backend, scenes
+    rng = np.random.default_rng(rng_seed)
+    raws, tgts = [], []
+    for seed in seeds:
+        n_fuse = fuse_frames or frames_per_scene
+        sc = scenes.room_scene(seed=seed, frames=max(frames_per_scene, n_fuse), width=width, height=height,
+                               fx=525.0 * width / 640, fy=525.0 * width / 640, cx=(width - 1) / 2, cy=(height - 1) / 2)
+        frames = render_frames(sc, torch)
+        vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=600_000)
+        bk = backend.TsdfIntegrationBackend("gpu")
+        for f in range(n_fuse):
+            bk.integrate(vol, backend.DepthFrame(sc.intrinsics, frames[f].view(-1)), sc.poses[f], 1, synchronize=False)
+        vol.synchronize()
+        for f in range(frames_per_scene):
+            tgt = backend.raycast_depth(vol, sc.intrinsics, sc.poses[f], 0.1, sc.max_depth, 0.5, device_out="cuda")
+            raw = frames[f]
+            taken = 0
+            for _ in range(crops_per_frame * 4):  # bounded retries for windows with too little valid depth
+                if taken >= crops_per_frame:
+                    break
+                y0 = int(rng.integers(0, height - crop + 1))
+                x0 = int(rng.integers(0, width - crop + 1))
+                r = raw[y0:y0 + crop, x0:x0 + crop]
+                t = tgt[y0:y0 + crop, x0:x0 + crop]
+                if float(((r > 0) & (t > 0)).float().mean()) >= 0.5:
+                    raws.append(r.clone())
+                    tgts.append(t.clone())
+                    taken += 1
+        vol.close()
+    return torch.stack(raws), torch.stack(tgts)
+
+
+def render_frames(sc, torch):
+    """All frames of a scene rendered on the device (noise as configured in the scene)."""
+    prims = torch.from_numpy(np.ascontiguousarray(sc.prims, np.float32)).cuda()
+    K = sc.intrinsics
+    out = torch.empty((len(sc.poses), K.height, K.width), dtype=torch.float32, device="cuda")
+    Kc = _capi.intrinsics(K)
+    for f in range(len(sc.poses)):
+        P = _capi.pose(sc.poses[f])
+        _capi.check(_capi.lib().vh_render_depth(_ptr(prims), prims.shape[0], C.byref(Kc), C.byref(P), sc.seed, f,
+                                                sc.noise_sigma_z2, sc.dropout, sc.max_depth, _ptr(out[f]), None))
+    torch.cuda.synchronize()
+    return out
+
+
+def train(denoiser: DepthDenoiser, raws, targets, steps, batch=16, seed=0, log_every=0):
+    """Adam over random batches of the pairs; returns the per-step RMSE list."""
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    hist = []
+    for s in range(steps):
+        idx = torch.randint(0, raws.shape[0], (batch,), generator=g).cuda()
+        hist.append(denoiser.train_step(raws[idx], targets[idx]))
+        if log_every and s % log_every == 0:
+            print("step %d rmse %.5f" % (s, hist[-1]), flush=True)
+    torch.cuda.synchronize()
+    denoiser.check_error()
+    return hist
