@@ -28,6 +28,7 @@ sample of the same frames.
 Multi-GPU: independent replicas (one scene per rank, no collective): value = all ranks' pixels / max time.
 """
 import argparse
+import ctypes as C
 import json
 import os
 import statistics
@@ -60,9 +61,14 @@ def parse():
     ap.add_argument("--form", default="chosen", choices=["chosen", "plain"],
                     help="form reported as the headline value (the other is measured beside it)")
     ap.add_argument("--no-chamfer", action="store_true", help="skip the Chamfer distances of the fused meshes")
-    ap.add_argument("--workload", default="room", choices=["room", "batch"],
-                    help="room: the room-scale workload (the headline); batch: N object scans fused as one batch")
+    ap.add_argument("--workload", default="room", choices=["room", "batch", "denoiser"],
+                    help="room: the room-scale workload (the headline); batch: N object scans fused as one batch; "
+                         "denoiser: train the learned filter and compare Chamfer with the bilateral filter")
     ap.add_argument("--scenes", type=int, default=64, help="scenes of the batch workload")
+    ap.add_argument("--train-rooms", type=int, default=4, help="denoiser workload: training rooms")
+    ap.add_argument("--train-frames", type=int, default=250, help="denoiser workload: frames per training room")
+    ap.add_argument("--train-steps", type=int, default=0, help="denoiser workload: Adam steps (0: two epochs)")
+    ap.add_argument("--eval-frames", type=int, default=300, help="denoiser workload: frames of the held-out room")
     return ap.parse_args()
 
 
@@ -575,12 +581,87 @@ def run_batch(args):
     return 0
 
 
+def run_denoiser(args):
+    """Learned depth denoiser (BASELINE config 4): train on raw / ray-cast pairs of new-seed rooms, then fuse a
+    held-out room with the bilateral filter and with the learned filter (plain FP32 form and the opt-in form)
+    and compare the Chamfer distances to the analytic surface and the per-frame filter time."""
+    import torch
+    from voxelhashmt_gb300 import _capi, backend, denoiser, metrics, scenes
+    from voxelhashmt_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    seeds = [1001 + k for k in range(args.train_rooms)]
+    trained = {}
+    for target in ("raycast", "clean"):
+        t0 = time.perf_counter()
+        raws, tgts = denoiser.make_training_pairs(seeds, frames_per_scene=args.train_frames, crops_per_frame=20,
+                                                  target=target)
+        torch.cuda.synchronize()
+        t_data = time.perf_counter() - t0
+        net = denoiser.DepthDenoiser(seed=args.seed)
+        steps = args.train_steps or 2 * raws.shape[0] // 16
+        t0 = time.perf_counter()
+        hist = denoiser.train(net, raws, tgts, steps=steps, batch=16, seed=args.seed)
+        t_train = time.perf_counter() - t0
+        trained[target] = (net.params_numpy(), {
+            "pairs": int(raws.shape[0]), "data_s": round(t_data, 2), "train_s": round(t_train, 2), "steps": steps,
+            "rmse_first_mm": round(1000 * float(np.mean(hist[:10])), 3),
+            "rmse_last_mm": round(1000 * float(np.mean(hist[-50:])), 3)})
+        del raws, tgts
+
+    sc = scenes.room_scene(seed=2001, frames=args.eval_frames)
+    frames = render_all(sc, torch, None, _capi)
+    pts = surface_points(sc, torch, _capi, every=10)
+    K = sc.intrinsics
+    results = {}
+    for name, (algo_kw, fmt), learned in (("plain_bilateral", FORMS["plain"], None),
+                                          ("plain_learned", FORMS["plain"], "raycast"),
+                                          ("chosen_bilateral", FORMS["chosen"], None),
+                                          ("chosen_learned", FORMS["chosen"], "raycast"),
+                                          ("plain_learned_clean_targets", FORMS["plain"], "clean"),
+                                          ("chosen_learned_clean_targets", FORMS["chosen"], "clean")):
+        kw = dict(algo_kw, depth_filter=1 if learned else 0)
+        vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=900_000,
+                                    algorithm=_capi.default_algorithm(**kw), layer_format=fmt)
+        if learned:
+            params = trained[learned][0]
+            _capi.check(_capi.lib().vh_set_depth_denoiser(vol.handle, params.ctypes.data_as(C.POINTER(C.c_float))),
+                        vol.handle)
+        bk = backend.TsdfIntegrationBackend("gpu")
+        vol.profile(True)
+        vol.read_profile()
+        for f in range(len(sc.poses)):
+            bk.integrate(vol, backend.DepthFrame(K, frames[f].view(-1)), sc.poses[f], 1, synchronize=False)
+        vol.synchronize()
+        stage, n = vol.read_profile()
+        q = metrics.chamfer(backend.extract_mesh_cuda(vol), sc, pts)
+        results[name] = {"chamfer_mm": round(q["chamfer_mm"], 4), "accuracy_mm": round(q["accuracy_mm"], 4),
+                         "completeness_mm": round(q["completeness_mm"], 4),
+                         "filter_ms_per_frame": round(stage["filter"] / max(1, n), 4),
+                         "ms_per_frame": round(sum(v for k, v in stage.items() if k != "integrate") / max(1, n), 4)}
+        vol.close()
+    line = {"metric": "chamfer_mm", "value": results["chosen_learned"]["chamfer_mm"], "unit": "mm",
+            "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "room 640x480 (held-out seed 2001, %d frames); net trained on crops 128x128 of "
+                                   "%d new-seed rooms x %d frames, Adam lr 1e-3, batch 16" % (
+                                       len(sc.poses), len(seeds), args.train_frames),
+                       "net": "3x3 conv 4-32-32-32-1, ReLU, residual; BF16 tensor-core hidden layers",
+                       "targets": "raycast: depth ray-cast from the plain FP32 volume fused from all frames of the "
+                                  "training room (the configuration's target); clean: noise-free analytic depth"},
+            "forms": results,
+            "training": {k: v[1] for k, v in trained.items()}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batch":
         return run_batch(args)
+    if args.workload == "denoiser":
+        return run_denoiser(args)
     return run_gb300(args)
 
 

@@ -185,8 +185,9 @@ vh_status vh_pixel_normals(vh_volume* volume, const float* depth_in, float* norm
 /* Depth ray-cast of the fused volume (no reference counterpart: the reference renders only its analytic
  * scenes).  For every pixel of K seen from T_wc, the ray is sampled every step_voxels voxels of path length
  * between camera depths min_depth and max_depth; the surface is the one marching cubes extracts, a voxel's
- * observed layers as planes (cuda_mesh_extractor.cu:237-262): at each sample, the signed plane distance of
- * the camera-facing layer closest to the sample; the first crossing from positive to non-positive (a drop
+ * observed layers as planes (cuda_mesh_extractor.cu:237-262): at each sample, the trilinear blend of the
+ * signed distances, at the sample, of the heaviest camera-facing layer of each of the 8 surrounding voxels
+ * (at least half the weight observed); the first crossing from positive to non-positive (a drop
  * of at most the truncation distance) is the hit, interpolated linearly.  depth_out: W*H floats in device
  * memory, camera depth in metres, 0 where no surface is hit.  Asynchronous on the stream. */
 vh_status vh_raycast_depth(vh_volume* volume, const vh_intrinsics* K, const vh_pose* T_wc, float min_depth,
@@ -280,7 +281,10 @@ vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, 
  * depth, out, target: batch x height x width FP32, device memory.  vh_nn_backward reads the activations
  * vh_nn_forward left in the same workspace and writes the FP32 gradients of the loss
  * sum((out - target)^2) / (batch * height * width) over pixels valid in depth, target and out, and
- * loss[0..1] = (sum of squared errors, pixel count).  error: as vh_nn_conv32. */
+ * loss[0..1] = (sum of squared errors, pixel count); pixels whose depth and target differ by more than the
+ * reference's discontinuity threshold max(0.012, 0.025 * target) are left out (they see different surfaces).
+ * Inside vh_integrate, a correction larger than that threshold falls back to the bilateral filter's value.
+ * error: as vh_nn_conv32. */
 int32_t vh_nn_param_count(void);
 uint64_t vh_nn_workspace_bytes(int32_t batch, int32_t width, int32_t height);
 vh_status vh_nn_pack(const float* params, void* packed, void* stream);

@@ -1244,26 +1244,48 @@ typedef struct {
   float* out;
 } raycast_ctx;
 
-static int ray_plane_distance(const vo_voxel* vox, v3 x, v3 dw, float* sdf) {
+static int ray_plane_distance(const vo_volume* v, int gx, int gy, int gz, v3 x, v3 dw, float* sdf) {
+  const vo_key k = {floor_div(gx, BLOCK), floor_div(gy, BLOCK), floor_div(gz, BLOCK)};
+  const int64_t bi = keymap_find(&v->map, k);
+  if (bi < 0) return 0;
+  const int li = positive_mod(gx, BLOCK) + BLOCK * (positive_mod(gy, BLOCK) + BLOCK * positive_mod(gz, BLOCK));
+  const vo_voxel* vox = &v->voxels[bi * BLOCK_VOLUME + li];
   int any = 0;
-  float best = 0.0f, best_abs = 0.0f;
+  float best = 0.0f, best_w = 0.0f;
   for (int d = 0; d < DIRS; ++d) {
     for (int l = 0; l < LAYERS; ++l) {
       const vo_layer* L = &vox->layers[d][l];
       if (!(L->weight > 0.0f)) continue;
       const v3 n = unpack_normal(GPU, 1, L->packed_normal);
       if (!(vdot(n, dw) < 0.0f)) continue;
-      const float s = n.x * x.x + n.y * x.y + n.z * x.z - L->plane_offset;
-      const float a = fabsf(s);
-      if (!any || a < best_abs) {
+      if (!any || L->weight > best_w) {
         any = 1;
-        best = s;
-        best_abs = a;
+        best = n.x * x.x + n.y * x.y + n.z * x.z - L->plane_offset;
+        best_w = L->weight;
       }
     }
   }
   *sdf = best;
   return any;
+}
+
+static int ray_blended_distance(const vo_volume* v, v3 x, v3 dw, float* sdf) {
+  const float vs = v->vs;
+  const float fx = x.x / vs - 0.5f, fy = x.y / vs - 0.5f, fz = x.z / vs - 0.5f;
+  const int x0 = (int)floorf(fx), y0 = (int)floorf(fy), z0 = (int)floorf(fz);
+  const float tx = fx - (float)x0, ty = fy - (float)y0, tz = fz - (float)z0;
+  float ws = 0.0f, acc = 0.0f;
+  for (int k = 0; k < 8; ++k) {
+    const int ax = k & 1, ay = (k >> 1) & 1, az = k >> 2;
+    const float w = (ax ? tx : 1.0f - tx) * (ay ? ty : 1.0f - ty) * (az ? tz : 1.0f - tz);
+    float s = 0.0f;
+    if (!ray_plane_distance(v, x0 + ax, y0 + ay, z0 + az, x, dw, &s)) continue;
+    acc += w * s;
+    ws += w;
+  }
+  if (!(ws >= 0.5f)) return 0;
+  *sdf = acc / ws;
+  return 1;
 }
 
 static void raycast_row(void* p, int64_t row) {
@@ -1296,9 +1318,8 @@ static void raycast_row(void* p, int64_t row) {
         z = fmaxf(z + dz, zexit + 0.25f * dz);
         continue;
       }
-      const int li = positive_mod(gx, BLOCK) + BLOCK * (positive_mod(gy, BLOCK) + BLOCK * positive_mod(gz, BLOCK));
       float sdf = 0.0f;
-      if (!ray_plane_distance(&v->voxels[bi * BLOCK_VOLUME + li], x, dw, &sdf)) {
+      if (!ray_blended_distance(v, x, dw, &sdf)) {
         prev_ok = 0;
         z += dz;
         continue;

@@ -117,7 +117,8 @@ def _ref_loss(params, depth, target):
     a3 = _bf(torch.relu(z3))
     r = F.conv2d(a3, w4.view(1, 32, 3, 3), b4, padding=1)
     out = torch.where(valid > 0, torch.clamp(d + 0.01 * r, min=0.0), torch.zeros_like(d)).squeeze(1)
-    mask = (depth > 0) & (target > 0) & (out > 0)
+    gate = torch.clamp(0.025 * target, min=0.012)
+    mask = (depth > 0) & (target > 0) & (out > 0) & ((depth - target).abs() <= gate)
     loss = torch.where(mask, (out - target) ** 2, torch.zeros_like(out)).sum() / out.numel()
     return loss, out
 

@@ -27,6 +27,7 @@ struct vh_volume {
   float4* d_normal_map = nullptr;  // per-pixel normals (vh_algorithm.normal_mode 1)
   // learned depth denoiser (vh_algorithm.depth_filter 1)
   float* d_nn_params = nullptr;
+  float* d_depth_bilateral = nullptr;  // the fallback of the learned filter
   __nv_bfloat16* d_nn_packed = nullptr;
   unsigned char* d_nn_ws = nullptr;
   size_t nn_ws_bytes = 0;
@@ -173,9 +174,11 @@ vh_status ensure_depth(vh_volume* v, size_t pixels) {
   dfree(v->d_depth_in);
   dfree(v->d_depth_filtered);
   dfree(v->d_normal_map);
+  dfree(v->d_depth_bilateral);
   v->depth_capacity = 0;
   VH_CUDA(v, dalloc(&v->d_depth_in, pixels));
   VH_CUDA(v, dalloc(&v->d_depth_filtered, pixels));
+  if (v->algo.depth_filter == 1) VH_CUDA(v, dalloc(&v->d_depth_bilateral, pixels));
   if (v->algo.normal_mode == 1) VH_CUDA(v, dalloc(&v->d_normal_map, pixels));
   v->depth_capacity = pixels;
   return VH_OK;
@@ -449,6 +452,7 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_nn_params);
   dfree(v->d_nn_packed);
   dfree(v->d_nn_ws);
+  dfree(v->d_depth_bilateral);
   for (auto& pair : v->tune_events) {
     cudaEventDestroy(pair[0]);
     cudaEventDestroy(pair[1]);
@@ -523,9 +527,10 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
       VH_CUDA(v, cudaMalloc(reinterpret_cast<void**>(&v->d_nn_ws), need));
       v->nn_ws_bytes = need;
     }
-    VH_CUDA(v, vh::launch_begin_frame(v->dev.counters, s));
-    VH_CUDA(v, vh::nn::forward(v->d_nn_params, v->d_nn_packed, src, v->d_depth_filtered, 1, K->width, K->height,
-                               v->d_nn_ws, &v->dev.counters->error, s));
+    // the bilateral filter (which also starts the frame) is the per-pixel fallback of the learned filter
+    VH_CUDA(v, vh::launch_filter(src, v->d_depth_bilateral, p, v->dev.counters, s));
+    VH_CUDA(v, vh::nn::forward(v->d_nn_params, v->d_nn_packed, src, v->d_depth_bilateral, v->d_depth_filtered, 1,
+                               K->width, K->height, v->d_nn_ws, &v->dev.counters->error, s));
   } else {
     VH_CUDA(v, vh::launch_filter(src, v->d_depth_filtered, p, v->dev.counters, s));
   }
@@ -1044,7 +1049,7 @@ vh_status vh_nn_forward(const float* params, const void* packed, const float* de
   if (!params || !packed || !depth || !out || !workspace || !error || batch <= 0 || width <= 0 || height <= 0) {
     return VH_ERR_INVALID_ARGUMENT;
   }
-  return vh::nn::forward(params, static_cast<const __nv_bfloat16*>(packed), depth, out, batch, width, height,
+  return vh::nn::forward(params, static_cast<const __nv_bfloat16*>(packed), depth, nullptr, out, batch, width, height,
                          static_cast<unsigned char*>(workspace), error, as_stream(stream)) == cudaSuccess
              ? VH_OK
              : VH_ERR_CUDA;

@@ -283,6 +283,12 @@ constexpr float kScale = 100.0f, kInvScale = 0.01f;
 constexpr int kOffW1 = 0, kOffB1 = kOffW1 + kC * kCin * 9, kOffW2 = kOffB1 + kC, kOffB2 = kOffW2 + kC * kC * 9;
 constexpr int kOffW3 = kOffB2 + kC, kOffB3 = kOffW3 + kC * kC * 9, kOffW4 = kOffB3 + kC, kOffB4 = kOffW4 + kC * 9;
 constexpr int kParams = kOffB4 + 1;
+// depth-discontinuity threshold max(base, rel * depth) of the reference's GPU path (cuda_tsdf_integrator.cu:27-28):
+// training ignores pixels whose raw depth and target differ by more (they see different surfaces), and at
+// inference a correction larger than it falls back to the bilateral filter's value
+constexpr float kGateBase = 0.012f, kGateRel = 0.025f;
+
+__device__ __forceinline__ float gate(float d) { return fmaxf(kGateBase, kGateRel * d); }
 
 __device__ __forceinline__ bool inside(int x, int y, int w, int h) { return x >= 0 && x < w && y >= 0 && y < h; }
 
@@ -354,7 +360,8 @@ __device__ __forceinline__ void load32(const __nv_bfloat16* p, float* v) {
 // layer 4: 32 -> 1 residual, depth' = d + r / 100 on valid pixels
 __global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __restrict__ A3,
                                                        const float* __restrict__ params,
-                                                       const float* __restrict__ depth, float* __restrict__ out,
+                                                       const float* __restrict__ depth,
+                                                       const float* __restrict__ fallback, float* __restrict__ out,
                                                        int batch, int w, int h) {
   __shared__ float sw[kC * 9 + 1];
   for (int i = threadIdx.x; i < kC * 9 + 1; i += blockDim.x) sw[i] = params[kOffW4 + i];
@@ -378,11 +385,13 @@ __global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __re
 #pragma unroll
       for (int c = 0; c < kC; ++c) r += sw[c * 9 + t] * a[c];
     }
-    out[i] = fmaxf(d + r * kInvScale, 0.0f);
+    const float corr = r * kInvScale;
+    out[i] = (fallback && fabsf(corr) > gate(d)) ? fallback[i] : fmaxf(d + corr, 0.0f);
   }
 }
 
-// loss = sum over pixels valid in input and target of (out - target)^2 / n_pixels; dr = dloss/dr
+// loss = sum over pixels valid in input, target and output whose input and target agree within the
+// discontinuity threshold, of (out - target)^2 / n_pixels; dr = dloss/dr
 __global__ void loss_grad_kernel(const float* __restrict__ out, const float* __restrict__ target,
                                  const float* __restrict__ depth, float* __restrict__ dr, long long n,
                                  float* __restrict__ loss) {
@@ -390,7 +399,7 @@ __global__ void loss_grad_kernel(const float* __restrict__ out, const float* __r
   const float inv_n = 1.0f / static_cast<float>(n);
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const bool m = depth[i] > 0.0f && target[i] > 0.0f && out[i] > 0.0f;
+    const bool m = depth[i] > 0.0f && target[i] > 0.0f && out[i] > 0.0f && fabsf(depth[i] - target[i]) <= gate(target[i]);
     const float diff = m ? out[i] - target[i] : 0.0f;
     dr[i] = 2.0f * diff * kInvScale * inv_n;
     se += diff * diff;
@@ -563,8 +572,9 @@ cudaError_t pack_weights(const float* params, __nv_bfloat16* packed, cudaStream_
   return e;
 }
 
-cudaError_t forward(const float* params, const __nv_bfloat16* packed, const float* depth, float* out, int batch,
-                    int width, int height, unsigned char* ws, unsigned int* error, cudaStream_t s) {
+cudaError_t forward(const float* params, const __nv_bfloat16* packed, const float* depth, const float* fallback,
+                    float* out, int batch, int width, int height, unsigned char* ws, unsigned int* error,
+                    cudaStream_t s) {
   const size_t n = static_cast<size_t>(batch) * width * height;
   float4* X;
   __nv_bfloat16 *A1, *A2, *A3, *G1, *G2;
@@ -579,7 +589,7 @@ cudaError_t forward(const float* params, const __nv_bfloat16* packed, const floa
     e = launch_conv32(A2, packed + 9 * kC * kC, params + kOffB3, nullptr, A3, batch, width, height, kForward, 1, error, s);
   }
   if (e != cudaSuccess) return e;
-  conv_out_kernel<<<grid, 256, 0, s>>>(A3, params, depth, out, batch, width, height);
+  conv_out_kernel<<<grid, 256, 0, s>>>(A3, params, depth, fallback, out, batch, width, height);
   return cudaGetLastError();
 }
 

@@ -25,8 +25,10 @@ int conv32_smem_bytes();
 int param_count();
 size_t workspace_bytes(int batch, int width, int height);
 cudaError_t pack_weights(const float* params, __nv_bfloat16* packed, cudaStream_t s);
-cudaError_t forward(const float* params, const __nv_bfloat16* packed, const float* depth, float* out, int batch,
-                    int width, int height, unsigned char* ws, unsigned int* error, cudaStream_t s);
+// fallback (may be null): per-pixel replacement where the correction exceeds the discontinuity threshold
+cudaError_t forward(const float* params, const __nv_bfloat16* packed, const float* depth, const float* fallback,
+                    float* out, int batch, int width, int height, unsigned char* ws, unsigned int* error,
+                    cudaStream_t s);
 // grads: FP32 [param_count()] (overwritten); loss: [sum of squared errors over masked pixels, their count]
 cudaError_t backward(const float* params, const __nv_bfloat16* packed, const float* depth, const float* target,
                      const float* out, int batch, int width, int height, unsigned char* ws, float* grads, float* loss,

@@ -119,11 +119,12 @@ class DepthDenoiser:
 
 
 def make_training_pairs(seeds, frames_per_scene=120, crops_per_frame=16, crop=128, width=640, height=480,
-                        fuse_frames=None, rng_seed=0):
+                        fuse_frames=None, rng_seed=0, target="raycast"):
     """Random crops (raw, target) from rooms (scenes.room_scene) of the given seeds: raw = the noisy
     rendered frame; target = the depth ray-cast at the frame's pose from the plain FP32 volume fused from
-    `fuse_frames` frames of the same walk (all of them by default).  Returns two (N, crop, crop) CUDA
-    tensors; crops keep windows where at least half the pixels are valid in both."""
+    `fuse_frames` frames of the same walk (all of them by default), or with target="clean" the noise-free
+    analytic depth of the frame.  Returns two (N, crop, crop) CUDA tensors; crops keep windows where at
+    least half the pixels are valid in both."""
     import torch
     from . import backend, scenes
     rng = np.random.default_rng(rng_seed)
@@ -133,13 +134,27 @@ def make_training_pairs(seeds, frames_per_scene=120, crops_per_frame=16, crop=12
         sc = scenes.room_scene(seed=seed, frames=max(frames_per_scene, n_fuse), width=width, height=height,
                                fx=525.0 * width / 640, fy=525.0 * width / 640, cx=(width - 1) / 2, cy=(height - 1) / 2)
         frames = render_frames(sc, torch)
-        vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=600_000)
-        bk = backend.TsdfIntegrationBackend("gpu")
-        for f in range(n_fuse):
-            bk.integrate(vol, backend.DepthFrame(sc.intrinsics, frames[f].view(-1)), sc.poses[f], 1, synchronize=False)
-        vol.synchronize()
+        clean = None
+        vol = None
+        if target == "clean":
+            noise, drop = sc.noise_sigma_z2, sc.dropout
+            sc.noise_sigma_z2, sc.dropout = 0.0, 0.0
+            clean = render_frames(sc, torch)
+            sc.noise_sigma_z2, sc.dropout = noise, drop
+        else:
+            vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets,
+                                        max_blocks=600_000)
+            bk = backend.TsdfIntegrationBackend("gpu")
+            for f in range(n_fuse):
+                bk.integrate(vol, backend.DepthFrame(sc.intrinsics, frames[f].view(-1)), sc.poses[f], 1,
+                             synchronize=False)
+            vol.synchronize()
         for f in range(frames_per_scene):
-            tgt = backend.raycast_depth(vol, sc.intrinsics, sc.poses[f], 0.1, sc.max_depth, 0.5, device_out="cuda")
+            if clean is not None:
+                tgt = clean[f]
+            else:
+                tgt = backend.raycast_depth(vol, sc.intrinsics, sc.poses[f], 0.1, sc.max_depth, 0.5,
+                                            device_out="cuda")
             raw = frames[f]
             taken = 0
             for _ in range(crops_per_frame * 4):  # bounded retries for windows with too little valid depth
@@ -153,7 +168,8 @@ def make_training_pairs(seeds, frames_per_scene=120, crops_per_frame=16, crop=12
                     raws.append(r.clone())
                     tgts.append(t.clone())
                     taken += 1
-        vol.close()
+        if vol is not None:
+            vol.close()
     return torch.stack(raws), torch.stack(tgts)
 
 
