@@ -17,9 +17,10 @@
 // transposed in channels, so the backward pass reuses the kernel.  The 4-channel input layer, the 1-channel
 // output layer, the weight gradients (reductions over pixels) and Adam run on the CUDA cores in FP32.
 //
-// Safety: the shared-memory regions the tensor core reads are padded so that any byte the descriptors can
-// address stays inside this CTA's allocation; the mbarrier wait gives up after a bounded number of polls,
-// sets the error word and still waits (bounded) before freeing tensor memory.
+// Safety: the descriptors address exactly the staged bytes (the A operand reaches kABytes, the B operand
+// kBBytes; the layout is checked bit-for-bit against a float64 convolution), and each region has a margin
+// beyond that; the mbarrier wait gives up after a bounded number of polls, sets the error word and still
+// waits (bounded) before freeing tensor memory.
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -37,10 +38,10 @@ constexpr int kGroups = kC / 8;            // channel groups of 8 (16 bytes of B
 constexpr int kPlane = kRowPix * 16;       // bytes of one channel group of one staged row (the A operand's LBO)
 constexpr int kRowBytes = kGroups * kPlane;
 constexpr int kABytes = 3 * kRowBytes;     // 24,960
-constexpr int kAPad = 65536;               // A region incl. padding (worst-case descriptor reach < 64 KB)
+constexpr int kAPad = kABytes + 2048;      // A region + margin (the descriptors read exactly kABytes)
 constexpr int kBBlock = 2 * kC * 16;       // one (tap, k-step) B operand: 2 groups x 32 rows x 16 B = 1,024
 constexpr int kBBytes = 18 * kBBlock;      // 18,432
-constexpr int kBPad = kBBytes + 8192;
+constexpr int kBPad = kBBytes + 1024;
 constexpr int kThreads = 128;              // 4 warps: one per 32 TMEM lanes
 constexpr int kSmem = kAPad + kBPad + 64;  // + mbarrier and TMEM address
 constexpr uint32_t kMaxPolls = 1u << 24;
@@ -233,11 +234,17 @@ cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, c
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  // two persistent CTAs per SM: each CTA stages the weights and allocates tensor memory once, so fewer CTAs
+  // with more tiles each measured faster than filling the SMs (the tile loop is not pipelined)
+  static int ctas = 0;
+  if (ctas == 0) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ctas = 2 * (sms > 0 ? sms : 152);
+  }
   const long long ntiles = static_cast<long long>(batch) * height * ((width + kTile - 1) / kTile);
-  const int grid = static_cast<int>(ntiles < 2LL * sms ? ntiles : 2LL * sms);
+  const int grid = static_cast<int>(ntiles < ctas ? ntiles : ctas);
   if (grid <= 0) return cudaSuccess;
   conv32_tc_kernel<<<grid, kThreads, kSmem, s>>>(in, wpack, bias, mask, out, batch, width, height, mode, relu, error);
   return cudaGetLastError();
