@@ -324,33 +324,41 @@ __global__ void pack_input_kernel(const float* __restrict__ depth, float4* __res
   }
 }
 
-// layer 1: 4 -> 32, ReLU, one thread per pixel
+// layer 1: 4 -> 32, ReLU, one thread per pixel; weights staged tap-major as float4 over the 4 input channels
+// (sw4[t][co] = w1[co][0..3][t]) so that one 16-byte shared load feeds 4 multiply-adds
 __global__ void __launch_bounds__(256) conv_in_kernel(const float4* __restrict__ X, const float* __restrict__ params,
                                                       __nv_bfloat16* __restrict__ A1, int batch, int w, int h) {
-  __shared__ float sw[kC * kCin * 9 + kC];
-  for (int i = threadIdx.x; i < kC * kCin * 9 + kC; i += blockDim.x) sw[i] = params[kOffW1 + i];
+  __shared__ float4 sw4[9][kC];
+  __shared__ float sb[kC];
+  for (int i = threadIdx.x; i < 9 * kC; i += blockDim.x) {
+    const int t = i / kC, co = i % kC;
+    const float* wc = params + kOffW1 + co * kCin * 9;
+    sw4[t][co] = make_float4(wc[0 * 9 + t], wc[1 * 9 + t], wc[2 * 9 + t], wc[3 * 9 + t]);
+  }
+  for (int i = threadIdx.x; i < kC; i += blockDim.x) sb[i] = params[kOffB1 + i];
   __syncthreads();
   const long long n = static_cast<long long>(batch) * w * h;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x) {
     const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
     const long long img = i / (static_cast<long long>(w) * h);
-    float4 in[9];
+    float acc[kC];
 #pragma unroll
+    for (int co = 0; co < kC; ++co) acc[co] = sb[co];
+#pragma unroll 1
     for (int t = 0; t < 9; ++t) {
       const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
-      in[t] = inside(sx, sy, w, h) ? X[(img * h + sy) * w + sx] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (!inside(sx, sy, w, h)) continue;
+      const float4 in = X[(img * h + sy) * w + sx];
+#pragma unroll
+      for (int co = 0; co < kC; ++co) {
+        const float4 wv = sw4[t][co];
+        acc[co] += wv.x * in.x + wv.y * in.y + wv.z * in.z + wv.w * in.w;
+      }
     }
     __align__(16) __nv_bfloat16 res[kC];
-    for (int co = 0; co < kC; ++co) {
-      float acc = sw[kC * kCin * 9 + co];
-      const float* wc = sw + co * kCin * 9;
 #pragma unroll
-      for (int t = 0; t < 9; ++t) {
-        acc += wc[0 * 9 + t] * in[t].x + wc[1 * 9 + t] * in[t].y + wc[2 * 9 + t] * in[t].z + wc[3 * 9 + t] * in[t].w;
-      }
-      res[co] = __float2bfloat16_rn(fmaxf(acc, 0.0f));
-    }
+    for (int co = 0; co < kC; ++co) res[co] = __float2bfloat16_rn(fmaxf(acc[co], 0.0f));
 #pragma unroll
     for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(A1 + i * kC)[q] = reinterpret_cast<const uint4*>(res)[q];
   }
@@ -364,14 +372,20 @@ __device__ __forceinline__ void load32(const __nv_bfloat16* p, float* v) {
   for (int c = 0; c < kC; ++c) v[c] = __bfloat162float(b[c]);
 }
 
-// layer 4: 32 -> 1 residual, depth' = d + r / 100 on valid pixels
+// layer 4: 32 -> 1 residual, depth' = d + r / 100 on valid pixels; weights staged tap-major (sw[t][c]) and
+// read as float4
 __global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __restrict__ A3,
                                                        const float* __restrict__ params,
                                                        const float* __restrict__ depth,
                                                        const float* __restrict__ fallback, float* __restrict__ out,
                                                        int batch, int w, int h) {
-  __shared__ float sw[kC * 9 + 1];
-  for (int i = threadIdx.x; i < kC * 9 + 1; i += blockDim.x) sw[i] = params[kOffW4 + i];
+  __shared__ float4 sw4[9][kC / 4];
+  __shared__ float sb;
+  for (int i = threadIdx.x; i < 9 * kC; i += blockDim.x) {
+    const int t = i / kC, c = i % kC;
+    reinterpret_cast<float*>(&sw4[t][0])[c] = params[kOffW4 + c * 9 + t];
+  }
+  if (threadIdx.x == 0) sb = params[kOffB4];
   __syncthreads();
   const long long n = static_cast<long long>(batch) * w * h;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
@@ -383,14 +397,22 @@ __global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __re
     }
     const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
     const long long img = i / (static_cast<long long>(w) * h);
-    float r = sw[kC * 9];
+    float r = sb;
+#pragma unroll 1
     for (int t = 0; t < 9; ++t) {
       const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
       if (!inside(sx, sy, w, h)) continue;
-      float a[kC];
-      load32(A3 + ((img * h + sy) * w + sx) * kC, a);
+      const uint4* src = reinterpret_cast<const uint4*>(A3 + ((img * h + sy) * w + sx) * kC);
 #pragma unroll
-      for (int c = 0; c < kC; ++c) r += sw[c * 9 + t] * a[c];
+      for (int q = 0; q < 4; ++q) {  // 8 channels per 16-byte load
+        const uint4 raw = src[q];
+        const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&raw);
+        const float4 wa = sw4[t][2 * q], wb = sw4[t][2 * q + 1];
+        const float2 a0 = __bfloat1622float2(b2[0]), a1 = __bfloat1622float2(b2[1]);
+        const float2 a2 = __bfloat1622float2(b2[2]), a3 = __bfloat1622float2(b2[3]);
+        r += wa.x * a0.x + wa.y * a0.y + wa.z * a1.x + wa.w * a1.y + wb.x * a2.x + wb.y * a2.y + wb.z * a3.x +
+             wb.w * a3.y;
+      }
     }
     const float corr = r * kInvScale;
     out[i] = (fallback && fabsf(corr) > gate(d)) ? fallback[i] : fmaxf(d + corr, 0.0f);
