@@ -124,17 +124,26 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
   // collectSurfaceClusters (:439-507); candidates in shared memory, column `t` of S.cand
   float* cand = const_cast<float*>(&S.cand[0][0]) + t;
   int nc = 0;
+  float nearest = 3.0e38f;  // smallest |candidate - iso|
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
 #pragma unroll
     for (int l = 0; l < kLayers; ++l) {
       if (S.valid[l][si[k]]) {
-        cand[nc * kThreads] = plane_sd(S.plane[l][si[k]], cc);
+        const float c = plane_sd(S.plane[l][si[k]], cc);
+        cand[nc * kThreads] = c;
+        nearest = fminf(nearest, fabsf(c - p.iso));
         ++nc;
       }
     }
   }
   if (nc == 0) return 0;
+  // Every corner value below is a candidate's plane evaluated at a corner, at most sqrt(3)/2 voxel from the
+  // cell centre, so it has the candidate's sign relative to iso when the candidate is farther than that (plus
+  // a rounding margin for the two float evaluations); means of same-sign values keep the sign.  Such a cell
+  // has cube index 0 or 255 for every cluster: no triangles, skipped without changing the output.
+  const float reject = 0.8660254f * vs * 1.00001f + 1e-5f * (1.0f + fabsf(cc.x) + fabsf(cc.y) + fabsf(cc.z));
+  if (nearest > reject) return 0;
   for (int i = 1; i < nc; ++i) {  // insertion sort (:264-274)
     const float x = cand[i * kThreads];
     int j = i - 1;
