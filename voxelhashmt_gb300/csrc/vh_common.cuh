@@ -41,7 +41,8 @@ struct Counters {
   uint32_t new_blocks;         // blocks allocated by the current frame
   uint32_t integrated_voxels;  // voxel layer updates applied by the current frame
   uint32_t active_voxels;      // voxels of the current frame that reached the layer update stage
-  uint32_t pad[7];
+  uint32_t update_queue;       // next chunk of the fused layer update (a device work queue; reset per frame)
+  uint32_t pad[6];
 };
 static_assert(sizeof(Counters) == 64, "Counters is read back as one 64-byte copy");
 

@@ -126,6 +126,7 @@ __device__ __forceinline__ void begin_frame(Counters* counters) {
   counters->new_blocks = 0U;
   counters->integrated_voxels = 0U;
   counters->active_voxels = 0U;
+  counters->update_queue = 0U;
 }
 
 }  // namespace filt

@@ -791,11 +791,11 @@ __device__ __forceinline__ bool map_update_voxel(const float* __restrict__ depth
   return updated;
 }
 
-// One pass over every voxel of the visible blocks with the normal from the map.  Each CTA walks chunks of
-// kThreads voxel slots; the slots that pass voxel_prefix are appended (warp-aggregated) to a shared-memory
-// queue together with their projection, and whenever the queue holds kThreads entries the CTA updates one
-// full batch, one entry per thread.  The expensive part therefore runs on full warps whatever the pass
-// rate, and the survivors of one chunk wait at most one chunk for their batch.
+// One pass over every voxel of the visible blocks with the normal from the map.  The voxel slots are cut in
+// chunks of kT (a CTA's threads); each CTA takes the next chunk from a device work queue (a counter reset when
+// the frame begins), runs voxel_prefix on one slot per thread, appends the survivors (warp-aggregated) to a
+// shared-memory queue with their projection, and then updates the survivors one per thread.  The expensive
+// part runs on compacted threads, and the dynamic order keeps every CTA busy until the last chunk.
 template <int kT>
 struct MapQueue {
   static constexpr int kQueue = 2 * kT;
@@ -827,21 +827,22 @@ template <int kT, int kMinBlocks>
 __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const float* __restrict__ depth,
                                                                      const float4* __restrict__ nmap, const Volume V,
                                                                      const Params p) {
-  constexpr int kThreads = kT;
   static_assert(kBlockVoxels % kT == 0, "CTA size must divide the block's voxel count");
   __shared__ MapQueue<kT> Q;
+  __shared__ uint32_t s_item;
   const uint32_t nvis = V.counters->visible_count;
-  const unsigned long long total = static_cast<unsigned long long>(nvis) * kBlockVoxels;
-  const unsigned long long nchunks = total / kThreads;
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x == 0) Q.count = 0U;
-  __syncthreads();
-  for (unsigned long long chunk = blockIdx.x; chunk < nchunks; chunk += gridDim.x) {
+  const uint32_t nchunks = nvis * static_cast<uint32_t>(kBlockVoxels / kT);
+  const int tid = threadIdx.x, lane = tid & 31;
+  if (tid == 0) Q.count = 0U;
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(&V.counters->update_queue, 1U);
+    __syncthreads();
+    const uint32_t item = s_item;
+    if (item >= nchunks) break;
     // 1. prefix of one slot per thread, survivors appended to the queue
-    const unsigned long long i = chunk * kThreads + threadIdx.x;
-    const uint32_t item = static_cast<uint32_t>(i >> 9);
+    const unsigned long long i = static_cast<unsigned long long>(item) * kT + tid;
     const int li = static_cast<int>(i & 511U);
-    const uint32_t b = V.slot_block[V.visible[item]];
+    const uint32_t b = V.slot_block[V.visible[static_cast<uint32_t>(i >> 9)]];
     bool pass = false;
     f3 pc = mk3(0.0f, 0.0f, 0.0f);
     float u = 0.0f, v = 0.0f, d = 0.0f;
@@ -864,24 +865,14 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
       Q.z[e] = pc.z;
     }
     __syncthreads();
-    // 2. a full batch: the last kThreads entries, one per thread.  Every thread reads the count before any
-    // thread appends again, so the branch below is uniform across the CTA.
+    // 2. the survivors of the chunk, one per thread
     const uint32_t n = Q.count;
-    __syncthreads();
-    if (n >= static_cast<uint32_t>(kThreads)) {
-      bool updated, newly;
-      map_update_entry(depth, nmap, V, p, Q, static_cast<int>(n) - kThreads + threadIdx.x, updated, newly);
-      count_updates(V, updated, newly, lane);
-      __syncthreads();
-      if (threadIdx.x == 0) Q.count = n - kThreads;
-      __syncthreads();
-    }
+    bool updated = false, newly = false;
+    if (static_cast<uint32_t>(tid) < n) map_update_entry(depth, nmap, V, p, Q, tid, updated, newly);
+    count_updates(V, updated, newly, lane);
+    __syncthreads();  // the queue and s_item are rewritten by the next chunk
+    if (tid == 0) Q.count = 0U;
   }
-  // 3. the remainder (< kThreads entries)
-  const uint32_t n = Q.count;
-  bool updated = false, newly = false;
-  if (threadIdx.x < n) map_update_entry(depth, nmap, V, p, Q, threadIdx.x, updated, newly);
-  count_updates(V, updated, newly, lane);
 }
 
 // ---- multi-scene batch: three work-queue kernels over the items of every scene of the step ----
