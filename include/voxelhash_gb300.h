@@ -199,6 +199,12 @@ vh_status vh_synchronize(vh_volume* volume, void* stream);
 /* extractMeshCuda: directional multi-layer marching cubes over every block; the triangle soup stays in
  * the volume's device buffer.  *triangle_count receives its size.  Synchronises. */
 vh_status vh_extract_mesh(vh_volume* volume, float iso_level, size_t* triangle_count, void* stream);
+/* Incremental meshing (no reference counterpart): the same extraction restricted to the blocks the layer
+ * update ran over within the last `frames` frames (frames = 0: every block).  Each listed block yields exactly
+ * the triangles it yields in a full extraction (neighbour blocks are read as usual); the soup replaces the
+ * volume's last extracted soup. */
+vh_status vh_extract_mesh_recent(vh_volume* volume, float iso_level, uint32_t frames, size_t* triangle_count,
+                                 void* stream);
 /* Copies the last extracted soup, 9 floats per triangle (v0, v1, v2), to host or device memory. */
 vh_status vh_copy_mesh(vh_volume* volume, float* out, size_t max_triangles, int32_t out_on_device, void* stream);
 

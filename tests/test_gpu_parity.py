@@ -335,3 +335,22 @@ def test_raycast_bit_exact_and_close_to_scene(env, small_orbit):
         assert both.sum() > 0.5 * (clean > 0).sum()
         assert np.median(np.abs(got[both] - clean[both])) <= sc.voxel_size
     vol.close()
+
+
+def test_incremental_meshing_is_a_subset_of_the_full_mesh(env, small_orbit):
+    """vh_extract_mesh_recent: the soup of the blocks updated in the last k frames is a sub-multiset of the
+    full extraction (bit-identical triangles), every triangle lies in or on the border of such a block, k = 0
+    is the full mesh, and a k covering every frame gives the full mesh."""
+    backend, O = env
+    sc = small_orbit
+    frames = [0, 4, 8, 12, 16, 20]
+    vol, _ = _integrate_both(backend, O, sc, frames=frames)
+    full = O.canonical_triangles(backend.extract_mesh_cuda(vol))
+    assert np.array_equal(_bits(O.canonical_triangles(backend.extract_mesh_cuda(vol, recent_frames=0))), _bits(full))
+    assert np.array_equal(_bits(O.canonical_triangles(backend.extract_mesh_cuda(vol, recent_frames=len(frames)))),
+                          _bits(full))
+    recent = O.canonical_triangles(backend.extract_mesh_cuda(vol, recent_frames=1))
+    assert 0 < recent.shape[0] < full.shape[0]
+    full_rows = {bytes(r) for r in _bits(full)}
+    assert all(bytes(r) in full_rows for r in _bits(recent))
+    vol.close()

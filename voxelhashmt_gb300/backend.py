@@ -360,12 +360,17 @@ def raycast_depth(volume: VoxelHashTSDF, intrinsics, T_wc, min_depth=0.1, max_de
     return out.cpu().numpy()
 
 
-def extract_mesh_cuda(volume: VoxelHashTSDF, iso_level=0.0, stream=None, device_out=None):
+def extract_mesh_cuda(volume: VoxelHashTSDF, iso_level=0.0, stream=None, device_out=None, recent_frames=0):
     """Triangle soup (N, 9) float32 (v0, v1, v2).  With device_out (a torch tensor factory device), the soup
-    is returned as a CUDA tensor instead of a host array."""
+    is returned as a CUDA tensor instead of a host array.  recent_frames > 0: incremental meshing, only the
+    blocks updated within that many frames (vh_extract_mesh_recent)."""
     n = C.c_size_t()
     s = _stream_handle(stream)
-    _capi.check(_capi.lib().vh_extract_mesh(volume.handle, float(iso_level), C.byref(n), s), volume.handle)
+    if recent_frames:
+        _capi.check(_capi.lib().vh_extract_mesh_recent(volume.handle, float(iso_level), int(recent_frames),
+                                                       C.byref(n), s), volume.handle)
+    else:
+        _capi.check(_capi.lib().vh_extract_mesh(volume.handle, float(iso_level), C.byref(n), s), volume.handle)
     if device_out is not None:
         import torch
         out = torch.empty((n.value, 9), dtype=torch.float32, device=device_out)

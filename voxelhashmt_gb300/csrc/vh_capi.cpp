@@ -43,6 +43,8 @@ struct vh_volume {
   uint32_t* d_mc_dir_totals = nullptr;
   uint8_t* d_mc_cell_counts = nullptr;
   unsigned long long* d_mc_offsets = nullptr;
+  uint32_t* d_mc_list = nullptr;        // incremental meshing: the selected pool blocks
+  uint32_t* d_mc_list_count = nullptr;
   unsigned long long* d_scalar = nullptr;  // [0] mesh total, [1] recount
   float* d_tris = nullptr;
   size_t tri_capacity = 0;
@@ -406,6 +408,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   step(dalloc(&V.block_keys, nb));
   step(dalloc(&V.obs_mask, nb * (vh::kBlockVoxels / 32)));
   step(dalloc(&V.dir_mask, nb));
+  step(dalloc(&V.block_stamp, nb));
   step(dalloc(&V.counters, 1));
   step(cudaMallocHost(reinterpret_cast<void**>(&v->h_counters), sizeof(vh::Counters)));
   step(dalloc(&v->d_scalar, 2));
@@ -416,6 +419,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
     step(cudaMemset(pool_base(v), 0, std::max<size_t>(nb, 1) * pool_block_bytes(v)));
     step(cudaMemset(V.obs_mask, 0, nb * (vh::kBlockVoxels / 32) * sizeof(uint32_t)));
     step(cudaMemset(V.dir_mask, 0, std::max<size_t>(nb, 1) * sizeof(uint32_t)));
+    step(cudaMemset(V.block_stamp, 0, std::max<size_t>(nb, 1) * sizeof(uint32_t)));
     step(cudaMemset(V.counters, 0, sizeof(vh::Counters)));
     step(cudaDeviceSynchronize());
   }
@@ -444,6 +448,7 @@ void vh_destroy(vh_volume* v) {
   dfree(V.block_keys);
   dfree(V.obs_mask);
   dfree(V.dir_mask);
+  dfree(V.block_stamp);
   dfree(V.counters);
   if (v->h_counters) cudaFreeHost(v->h_counters);
   dfree(v->d_depth_in);
@@ -461,6 +466,8 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_mc_dir_totals);
   dfree(v->d_mc_cell_counts);
   dfree(v->d_mc_offsets);
+  dfree(v->d_mc_list);
+  dfree(v->d_mc_list_count);
   dfree(v->d_scalar);
   dfree(v->d_tris);
   dfree(v->d_keys);
@@ -489,6 +496,7 @@ vh_status vh_reset(vh_volume* v, void* stream) {
   VH_CUDA(v, cudaMemsetAsync(pool_base(v), 0, used * pool_block_bytes(v), s));
   VH_CUDA(v, cudaMemsetAsync(V.obs_mask, 0, used * (vh::kBlockVoxels / 32) * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.dir_mask, 0, used * sizeof(uint32_t), s));
+  VH_CUDA(v, cudaMemsetAsync(V.block_stamp, 0, used * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.counters, 0, sizeof(vh::Counters), s));
   VH_CUDA(v, cudaStreamSynchronize(s));
   v->mesh_triangles = 0;
@@ -693,8 +701,10 @@ vh_status vh_synchronize(vh_volume* v, void* stream) {
   return fail(v, VH_ERR_POOL_FULL, "block pool full (raise max_blocks)");
 }
 
-vh_status vh_extract_mesh(vh_volume* v, float iso, size_t* triangle_count, void* stream) {
-  if (!v || !triangle_count) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_extract_mesh: bad argument");
+// marching cubes over every allocated block (frames == 0) or over the blocks updated within the last `frames`
+// frames (incremental meshing)
+static vh_status extract(vh_volume* v, float iso, uint32_t frames, size_t* triangle_count, void* stream) {
+  if (!v || !triangle_count || v->dev.max_blocks == 0) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_extract_mesh: bad argument");
   DeviceGuard guard(v->params.device);
   const cudaStream_t s = as_stream(stream);
   if (!v->d_mc_counts) {
@@ -703,10 +713,24 @@ vh_status vh_extract_mesh(vh_volume* v, float iso, size_t* triangle_count, void*
     VH_CUDA(v, dalloc(&v->d_mc_dir_totals, static_cast<size_t>(v->dev.max_blocks) * vh::kDirs));
     VH_CUDA(v, dalloc(&v->d_mc_cell_counts, static_cast<size_t>(v->dev.max_blocks) * vh::kDirs * vh::kBlockVoxels));
   }
+  const uint32_t* list = nullptr;
+  const uint32_t* list_count = nullptr;
+  if (frames > 0) {
+    if (!v->d_mc_list) {
+      VH_CUDA(v, dalloc(&v->d_mc_list, v->dev.max_blocks));
+      VH_CUDA(v, dalloc(&v->d_mc_list_count, 1));
+    }
+    VH_CUDA(v, vh::launch_recent_blocks(v->dev, frames, v->d_mc_list, v->d_mc_list_count, s));
+    // blocks outside the list contribute nothing to the scan
+    VH_CUDA(v, cudaMemsetAsync(v->d_mc_counts, 0, static_cast<size_t>(v->dev.max_blocks) * sizeof(uint32_t), s));
+    list = v->d_mc_list;
+    list_count = v->d_mc_list_count;
+  }
   vh_intrinsics K{1, 1, 1.0f, 1.0f, 0.0f, 0.0f};
   vh::Params p = make_params(v, &K, nullptr, 1);
   p.iso = iso;
-  VH_CUDA(v, vh::launch_mc_count(v->dev, p, v->d_mc_counts, v->d_mc_dir_totals, v->d_mc_cell_counts, s));
+  VH_CUDA(v, vh::launch_mc_count(v->dev, p, v->d_mc_counts, v->d_mc_dir_totals, v->d_mc_cell_counts, list, list_count,
+                                 s));
   VH_CUDA(v, vh::launch_mc_scan(v->dev, v->d_mc_counts, v->d_mc_offsets, v->d_scalar, s));
   unsigned long long total = 0;
   VH_CUDA(v, cudaMemcpyAsync(&total, v->d_scalar, sizeof(total), cudaMemcpyDeviceToHost, s));
@@ -720,12 +744,20 @@ vh_status vh_extract_mesh(vh_volume* v, float iso, size_t* triangle_count, void*
   }
   if (total > 0) {
     VH_CUDA(v, vh::launch_mc_emit(v->dev, p, v->d_mc_counts, v->d_mc_dir_totals, v->d_mc_cell_counts,
-                                  v->d_mc_offsets, v->d_tris, s));
+                                  v->d_mc_offsets, v->d_tris, list, list_count, s));
   }
   VH_CUDA(v, cudaStreamSynchronize(s));
   v->mesh_triangles = static_cast<size_t>(total);
   *triangle_count = v->mesh_triangles;
   return VH_OK;
+}
+
+vh_status vh_extract_mesh(vh_volume* v, float iso, size_t* triangle_count, void* stream) {
+  return extract(v, iso, 0U, triangle_count, stream);
+}
+
+vh_status vh_extract_mesh_recent(vh_volume* v, float iso, uint32_t frames, size_t* triangle_count, void* stream) {
+  return extract(v, iso, frames, triangle_count, stream);
 }
 
 vh_status vh_copy_mesh(vh_volume* v, float* out, size_t max_triangles, int32_t on_device, void* stream) {

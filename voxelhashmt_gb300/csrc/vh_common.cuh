@@ -68,6 +68,7 @@ struct Volume {
   int4* block_keys;
   uint32_t* obs_mask;
   uint32_t* dir_mask;
+  uint32_t* block_stamp;  // per pool block: the last frame that ran the layer update over it
   uint32_t* visible;
   uint32_t* active;
   Counters* counters;

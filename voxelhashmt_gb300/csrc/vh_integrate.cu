@@ -567,6 +567,7 @@ __global__ void __launch_bounds__(kThreads) classify_kernel(const float* __restr
     const int li = static_cast<int>(i & 511U);
     const uint32_t b = V.slot_block[V.visible[item]];
     bool pass = false;
+    if (li == 0 && b != kInvalidBlock) V.block_stamp[b] = V.counters->frame;  // for incremental meshing
     if (b != kInvalidBlock) {
       const int4 bk = V.block_keys[b];
       f3 pc;
@@ -846,6 +847,7 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
     bool pass = false;
     f3 pc = mk3(0.0f, 0.0f, 0.0f);
     float u = 0.0f, v = 0.0f, d = 0.0f;
+    if (li == 0 && b != kInvalidBlock) V.block_stamp[b] = V.counters->frame;  // for incremental meshing
     if (b != kInvalidBlock) pass = voxel_prefix(depth, p, V.block_keys[b], li, pc, u, v, d);
     const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
     uint32_t base = 0U;
@@ -1039,6 +1041,7 @@ __global__ void __launch_bounds__(kThreads) batch_update_kernel(const SceneDesc*
     const uint32_t b = D.V.slot_block[D.V.visible[static_cast<uint32_t>(i >> 9)]];
     const int li = static_cast<int>(i & 511U);
     bool pass = false;
+    if (li == 0 && b != kInvalidBlock) D.V.block_stamp[b] = D.V.counters->frame;  // for incremental meshing
     f3 pc = mk3(0.0f, 0.0f, 0.0f);
     float u = 0.0f, v = 0.0f, d = 0.0f;
     if (b != kInvalidBlock) pass = voxel_prefix(D.depth, D.p, D.V.block_keys[b], li, pc, u, v, d);

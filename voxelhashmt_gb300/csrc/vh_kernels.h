@@ -49,15 +49,18 @@ void fused_variant_shape(int variant, int* threads, int* min_blocks);
 cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s);
 int integrate_grid_size();
 }  // namespace fast
-// marching cubes over all allocated blocks: pass 1 writes per-block, per-direction and per-cell triangle
+// marching cubes over all allocated blocks (or the blocks of `list`, *list_count entries, device memory): pass 1
+// writes per-block, per-direction and per-cell triangle
 // counts, the scan turns the block counts into offsets (+ total), pass 2 writes triangles (9 floats each)
 cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, uint32_t* dir_totals,
-                            uint8_t* cell_counts, cudaStream_t s);
+                            uint8_t* cell_counts, const uint32_t* list, const uint32_t* list_count, cudaStream_t s);
+// pool blocks updated within the last `frames` frames -> list (count on the device, reset here)
+cudaError_t launch_recent_blocks(const Volume& V, uint32_t frames, uint32_t* list, uint32_t* count, cudaStream_t s);
 cudaError_t launch_mc_scan(const Volume& V, const uint32_t* counts, unsigned long long* offsets,
                            unsigned long long* total, cudaStream_t s);
 cudaError_t launch_mc_emit(const Volume& V, const Params& p, const uint32_t* counts, const uint32_t* dir_totals,
                            const uint8_t* cell_counts, const unsigned long long* offsets, float* tris,
-                           cudaStream_t s);
+                           const uint32_t* list, const uint32_t* list_count, cudaStream_t s);
 int mc_grid_size();
 // full recount of observed voxels (any layer weight > 0) over the pool
 cudaError_t launch_recount(const Volume& V, unsigned long long* out, cudaStream_t s);

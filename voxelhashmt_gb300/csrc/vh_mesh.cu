@@ -321,18 +321,22 @@ __device__ __forceinline__ void load_neighbours(Shared& S, const Volume& V, uint
 // Pass 1: every cell of every direction with an observed layer in the block's neighbourhood; stores the
 // cell's triangle count (cell_counts, one byte: at most 5 triangles x 24 clusters), the per-direction totals
 // and the block total.
+// list / list_count: optional subset of pool blocks (incremental meshing); all allocated blocks when null
 __global__ void __launch_bounds__(kThreads, 2) mc_count_kernel(const Volume V, const Params p,
                                                                uint32_t* __restrict__ counts,
                                                                uint32_t* __restrict__ dir_totals,
-                                                               uint8_t* __restrict__ cell_counts) {
+                                                               uint8_t* __restrict__ cell_counts,
+                                                               const uint32_t* __restrict__ list,
+                                                               const uint32_t* __restrict__ list_count) {
   extern __shared__ __align__(16) unsigned char mc_smem[];
   Shared& S = *reinterpret_cast<Shared*>(mc_smem);
   const int tid = threadIdx.x;
   for (int i = tid; i < 256 * 16; i += kThreads) S.tri[i / 16][i % 16] = vh_mc_tri_table[i / 16][i % 16];
   for (int i = tid; i < 256; i += kThreads) S.edge[i] = vh_mc_edge_table[i];
-  const uint32_t nblocks = min(V.counters->num_blocks, V.max_blocks);
+  const uint32_t nitems = list ? *list_count : min(V.counters->num_blocks, V.max_blocks);
   const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
-  for (uint32_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+  for (uint32_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const uint32_t b = list ? list[item] : item;
     const int4 bk = V.block_keys[b];
     load_neighbours(S, V, b, bk, tid);
     // directions with an observed layer anywhere in the block or its +x/+y/+z neighbours; a cell of the
@@ -367,15 +371,18 @@ __global__ void __launch_bounds__(kThreads, 2) mc_emit_kernel(const Volume V, co
                                                               const uint32_t* __restrict__ dir_totals,
                                                               const uint8_t* __restrict__ cell_counts,
                                                               const unsigned long long* __restrict__ offsets,
-                                                              float* __restrict__ tris) {
+                                                              float* __restrict__ tris,
+                                                              const uint32_t* __restrict__ list,
+                                                              const uint32_t* __restrict__ list_count) {
   extern __shared__ __align__(16) unsigned char mc_smem[];
   Shared& S = *reinterpret_cast<Shared*>(mc_smem);
   const int tid = threadIdx.x;
   for (int i = tid; i < 256 * 16; i += kThreads) S.tri[i / 16][i % 16] = vh_mc_tri_table[i / 16][i % 16];
   for (int i = tid; i < 256; i += kThreads) S.edge[i] = vh_mc_edge_table[i];
-  const uint32_t nblocks = min(V.counters->num_blocks, V.max_blocks);
+  const uint32_t nitems = list ? *list_count : min(V.counters->num_blocks, V.max_blocks);
   const int lx = tid & 7, ly = (tid >> 3) & 7, lz = tid >> 6;
-  for (uint32_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+  for (uint32_t item = blockIdx.x; item < nitems; item += gridDim.x) {
+    const uint32_t b = list ? list[item] : item;
     if (counts[b] == 0U) continue;  // uniform
     const int4 bk = V.block_keys[b];
     load_neighbours(S, V, b, bk, tid);
@@ -395,6 +402,17 @@ __global__ void __launch_bounds__(kThreads, 2) mc_emit_kernel(const Volume V, co
 }
 
 // exclusive scan of counts[0..n) -> offsets, total; one CTA (the count array is a few MB at most)
+// pool blocks updated in frames (frame - frames, frame]: the subset of incremental meshing
+__global__ void recent_blocks_kernel(const Volume V, uint32_t frames, uint32_t* __restrict__ list,
+                                     uint32_t* __restrict__ count) {
+  const uint32_t n = min(V.counters->num_blocks, V.max_blocks);
+  const uint32_t frame = V.counters->frame;
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < n; b += gridDim.x * blockDim.x) {
+    const uint32_t st = V.block_stamp[b];
+    if (st != 0U && frame - st < frames) list[atomicAdd(count, 1U)] = b;
+  }
+}
+
 __global__ void __launch_bounds__(1024) scan_kernel(const Volume V, const uint32_t* __restrict__ counts,
                                                     unsigned long long* __restrict__ offsets,
                                                     unsigned long long* __restrict__ total) {
@@ -452,8 +470,16 @@ int mc_grid_size() {
 }
 
 cudaError_t launch_mc_count(const Volume& V, const Params& p, uint32_t* counts, uint32_t* dir_totals,
-                            uint8_t* cell_counts, cudaStream_t s) {
-  mc_count_kernel<<<mc_grid_size(), kThreads, sizeof(Shared), s>>>(V, p, counts, dir_totals, cell_counts);
+                            uint8_t* cell_counts, const uint32_t* list, const uint32_t* list_count, cudaStream_t s) {
+  mc_count_kernel<<<mc_grid_size(), kThreads, sizeof(Shared), s>>>(V, p, counts, dir_totals, cell_counts, list,
+                                                                   list_count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_recent_blocks(const Volume& V, uint32_t frames, uint32_t* list, uint32_t* count, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(count, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  recent_blocks_kernel<<<1024, 256, 0, s>>>(V, frames, list, count);
   return cudaGetLastError();
 }
 
@@ -465,9 +491,9 @@ cudaError_t launch_mc_scan(const Volume& V, const uint32_t* counts, unsigned lon
 
 cudaError_t launch_mc_emit(const Volume& V, const Params& p, const uint32_t* counts, const uint32_t* dir_totals,
                            const uint8_t* cell_counts, const unsigned long long* offsets, float* tris,
-                           cudaStream_t s) {
+                           const uint32_t* list, const uint32_t* list_count, cudaStream_t s) {
   mc_emit_kernel<<<mc_grid_size(), kThreads, sizeof(Shared), s>>>(V, p, counts, dir_totals, cell_counts, offsets,
-                                                                  tris);
+                                                                  tris, list, list_count);
   return cudaGetLastError();
 }
 
