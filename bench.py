@@ -333,6 +333,15 @@ def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
     m1.record(stream)
     torch.cuda.synchronize()
     mc_ms = m0.elapsed_time(m1)
+    # incremental meshing: the blocks updated in the last 100 frames
+    r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n_recent = C.c_size_t()
+    r0.record(stream)
+    capi.check(capi.lib().vh_extract_mesh_recent(vol.handle, 0.0, 100, C.byref(n_recent),
+                                                 C.c_void_p(stream.cuda_stream)), vol.handle)
+    r1.record(stream)
+    torch.cuda.synchronize()
+    recent_ms = r0.elapsed_time(r1)
     tris = backend.extract_mesh_cuda(vol)
     observed = vol.observed_voxel_count()
     tuned = vol.autotune_result()
@@ -347,28 +356,33 @@ def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
             upd.append(st["updated_voxels"])
             act.append(st["active_voxels"])
 
-    # end to end through the public API from pinned host memory
+    # end to end through the public API from pinned host memory: every step copies its frame host->device and
+    # reads its statistics device->host (asynchronously, into a pinned ring; the stream is synchronised once)
     host = torch.empty((len(sc.poses), K.height, K.width), dtype=torch.float32, pin_memory=True)
     host.copy_(frames.cpu())
+    stats_ring = torch.zeros((args.steps + args.warmup, 64), dtype=torch.uint8, pin_memory=True)
     vol.reset(stream)
     for f in range(args.warmup):
         bk.integrate(vol, backend.DepthFrame(K, host[f].numpy()), sc.poses[f], 1, stream=stream, synchronize=False)
-        vol.frame_stats(stream)
+        vol.frame_stats_enqueue(stats_ring[f], stream)
     torch.cuda.synchronize()
     e0 = time.perf_counter()
     for i in range(args.steps):
         f = args.warmup + i
         bk.integrate(vol, backend.DepthFrame(K, host[f].numpy()), sc.poses[f], 1, stream=stream, synchronize=False)
-        vol.frame_stats(stream)
+        vol.frame_stats_enqueue(stats_ring[f], stream)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - e0
+    last_stats = vol.frame_stats_decode(stats_ring[args.warmup + args.steps - 1])
+    assert last_stats["visible_blocks"] > 0, "the end-to-end frames integrated nothing"
     vol.synchronize(stream)
     vol.close()
     return {"value": value, "max_ms": max_ms, "stage_ms": stage_ms, "nprof": nprof, "fstats": fstats,
             "nblocks": nblocks, "mc_ms": mc_ms, "mc_blocks_per_s": nblocks / (mc_ms / 1000.0),
             "triangles": n_tri.value, "tris": tris, "observed": observed, "upd_mean": float(np.mean(upd)),
             "act_mean": float(np.mean(act)), "e2e_value": world * args.steps * px / e2e_s / 1e6,
-            "clocks": clock_info, "autotune": tuned}
+            "clocks": clock_info, "autotune": tuned,
+            "mc_recent": {"frames": 100, "ms": round(recent_ms, 3), "triangles": n_recent.value}}
 
 
 def graph_leg(args, torch, backend, capi, sc, frames, flush):
@@ -470,6 +484,7 @@ def run_gb300(args):
                 "visible_blocks_last_frame": r["fstats"]["visible_blocks"],
                 "updated_voxels_per_frame": round(r["upd_mean"]), "active_voxels_per_frame": round(r["act_mean"]),
                 "update_launch_shape": r["autotune"] if r["autotune"]["variant"] >= 0 else None,
+                "mc_incremental_last_100_frames": r["mc_recent"],
                 "chamfer": quality.get(name)}
 
     if rank == 0:

@@ -213,6 +213,12 @@ vh_status vh_observed_voxel_count(vh_volume* volume, uint64_t* count);
 /* Recounts observed voxels from the pool (the incremental counter's cross-check). */
 vh_status vh_recount_observed_voxels(vh_volume* volume, uint64_t* count, void* stream);
 vh_status vh_frame_stats_get(vh_volume* volume, vh_frame_stats* stats, void* stream);
+/* Asynchronous statistics: enqueues on the stream a copy of the volume's 64-byte device counter block into
+ * counters64 (host memory; pinned for the copy to be asynchronous), so a caller can read each frame's result
+ * without stalling the stream; once the stream has passed that point, vh_frame_stats_decode turns the block
+ * into the statistics struct, with the values vh_frame_stats_get returns at that point. */
+vh_status vh_frame_stats_enqueue(vh_volume* volume, void* counters64, void* stream);
+vh_status vh_frame_stats_decode(const vh_volume* volume, const void* counters64, vh_frame_stats* stats);
 
 /* Blocks [first, first + count) in allocation order: keys (3 int32 each) and voxels in the reference's
  * Voxel layout (include/tsdfmc/voxel_hash_tsdf.h:18-31: 512 voxels x 6 directions x 3 layers x 16 bytes

@@ -108,6 +108,8 @@ _SIGNATURES = {
     "vh_synchronize": (C.c_int, [_vp, _vp]),
     "vh_extract_mesh": (C.c_int, [_vp, C.c_float, _szp, _vp]),
     "vh_extract_mesh_recent": (C.c_int, [_vp, C.c_float, C.c_uint32, _szp, _vp]),
+    "vh_frame_stats_enqueue": (C.c_int, [_vp, _vp, _vp]),
+    "vh_frame_stats_decode": (C.c_int, [_vp, _vp, C.POINTER(VhFrameStats)]),
     "vh_copy_mesh": (C.c_int, [_vp, _vp, C.c_size_t, C.c_int32, _vp]),
     "vh_block_count": (C.c_int, [_vp, _u64p]),
     "vh_observed_voxel_count": (C.c_int, [_vp, _u64p]),

@@ -151,6 +151,19 @@ class VoxelHashTSDF:
                     self.handle)
         return {"variant": v.value, "threads_per_cta": t.value, "min_ctas_per_sm": b.value, "ms": ms.value}
 
+    def frame_stats_enqueue(self, counters64, stream=None):
+        """Enqueue the asynchronous read of this frame's counters into counters64 (a pinned 64-byte host
+        buffer: a torch uint8 tensor or a numpy array); decode with frame_stats_decode once the stream passed."""
+        ptr = counters64.data_ptr() if hasattr(counters64, "data_ptr") else counters64.ctypes.data
+        _capi.check(_capi.lib().vh_frame_stats_enqueue(self.handle, C.c_void_p(ptr), _stream_handle(stream)),
+                    self.handle)
+
+    def frame_stats_decode(self, counters64):
+        ptr = counters64.data_ptr() if hasattr(counters64, "data_ptr") else counters64.ctypes.data
+        s = _capi.VhFrameStats()
+        _capi.check(_capi.lib().vh_frame_stats_decode(self.handle, C.c_void_p(ptr), C.byref(s)), self.handle)
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
     def profile(self, enable=True):
         """Stage timing of vh_integrate with CUDA events (see read_profile)."""
         _capi.check(_capi.lib().vh_profile_enable(self.handle, 1 if enable else 0), self.handle)

@@ -816,6 +816,27 @@ vh_status vh_frame_stats_get(vh_volume* v, vh_frame_stats* stats, void* stream) 
   return VH_OK;
 }
 
+vh_status vh_frame_stats_enqueue(vh_volume* v, void* counters64, void* stream) {
+  if (!v || !counters64) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_frame_stats_enqueue: bad argument");
+  DeviceGuard guard(v->params.device);
+  VH_CUDA(v, cudaMemcpyAsync(counters64, v->dev.counters, sizeof(vh::Counters), cudaMemcpyDeviceToHost,
+                             as_stream(stream)));
+  return VH_OK;
+}
+
+vh_status vh_frame_stats_decode(const vh_volume* v, const void* counters64, vh_frame_stats* stats) {
+  if (!v || !counters64 || !stats) return VH_ERR_INVALID_ARGUMENT;
+  vh::Counters c;
+  std::memcpy(&c, counters64, sizeof(c));
+  stats->visible_blocks = c.visible_count;
+  stats->new_blocks = c.new_blocks;
+  stats->active_voxels = c.active_voxels;
+  stats->updated_voxels = c.integrated_voxels;
+  stats->total_blocks = std::min<uint64_t>(c.num_blocks, v->dev.max_blocks);
+  stats->observed_voxels = c.observed_voxels;
+  return VH_OK;
+}
+
 vh_status vh_export_blocks(vh_volume* v, uint64_t first, uint64_t count, int32_t* keys, void* voxels,
                            int32_t on_device, void* stream) {
   if (!v) return VH_ERR_INVALID_ARGUMENT;
