@@ -629,7 +629,7 @@ def run_batch(args):
 
 
 def run_denoiser(args):
-    """Learned depth denoiser (BASELINE config 4): train on raw / ray-cast pairs of new-seed rooms, then fuse a
+    """Learned depth denoiser workload: train on raw / ray-cast pairs of new-seed rooms, then fuse a
     held-out room with the bilateral filter and with the learned filter (plain FP32 form and the opt-in form)
     and compare the Chamfer distances to the analytic surface and the per-frame filter time."""
     import torch

@@ -33,7 +33,7 @@ def product_lib():
 
 @pytest.fixture(scope="session")
 def small_orbit():
-    """Config-1 geometry at 64x48 (focal length scaled with the resolution), 24 orbit poses, with the
+    """The orbit scene (plane, sphere, box) at 64x48 (focal length scaled with the resolution), 24 orbit poses, with the
     reference volume's default voxel size and truncation (voxel_hash_tsdf.h:191-192: 2 cm, 6 cm) so the
     oracle finishes in about a second."""
     from voxelhashmt_gb300 import scenes

@@ -48,7 +48,8 @@ def _fuse(backend, sc, frames, depths, stride=1, max_blocks=60000, **algo):
 
 @pytest.fixture(scope="module")
 def orbit_half():
-    """Config-1 geometry at 160x120 (focal length halved), voxel 1 cm, truncation 4 cm, 16 orbit frames."""
+    """The orbit scene (plane, sphere, box) at 160x120 (focal length halved), voxel 1 cm, truncation 4 cm,
+    16 orbit frames."""
     from voxelhashmt_gb300 import scenes
     sc = scenes.orbit_scene(seed=3, frames=16, width=160, height=120, fx=138.5, fy=138.5, cx=80.0, cy=60.0)
     sc.voxel_size, sc.truncation = 0.01, 0.04

@@ -1,7 +1,7 @@
 """ctypes binding of the C ABI in include/voxelhash_gb300.h (libvoxelhash_gb300.so, built in-tree).
 
 The library is the product: there is no fallback.  ``lib()`` raises if the shared library has not been
-built (``python -m voxelhashmt_gb300.build`` or ``__graft_entry__.build()``), and every call that
+built (``python -m voxelhashmt_gb300.build``), and every call that
 returns a non-zero vh_status raises ``VhError`` carrying the status and the volume's last error message.
 """
 from __future__ import annotations
@@ -162,7 +162,7 @@ def lib():
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise RuntimeError("libvoxelhash_gb300.so is not built (%s); run __graft_entry__.build()" % LIB_PATH)
+            raise RuntimeError("libvoxelhash_gb300.so is not built (%s); run python -m voxelhashmt_gb300.build" % LIB_PATH)
         L = C.CDLL(LIB_PATH)
         for name, (res, args) in _SIGNATURES.items():
             f = getattr(L, name)

@@ -640,7 +640,7 @@ __global__ void __launch_bounds__(kUpdateThreads) update_kernel(const float* __r
 // tap), so estimateSurfaceNormalCamera evaluated at every pixel centre is a 5x5 stencil over the depth image:
 // computed once per pixel here from a shared-memory tile, then bilinearly interpolated at each voxel's
 // projection.  This replaces the reference's 50 subpixel samples per voxel by 4 map taps; the normal differs
-// from the reference's at subpixel positions, which is why the mode is opt-in (results are judged by the
+// from the reference's at subpixel positions, which is why the mode is opt-in (results are evaluated by the
 // Chamfer distance of the fused surface, not bit parity).
 constexpr int kMapTX = 32, kMapTY = 8, kMapHalo = 2;
 constexpr int kMapW = kMapTX + 2 * kMapHalo, kMapH = kMapTY + 2 * kMapHalo;
