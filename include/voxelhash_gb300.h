@@ -97,8 +97,9 @@ typedef struct vh_algorithm {
   /* 0 (default): the reference's allocation rule, 3 points x 27-block neighbourhood per pixel;
    * 1: truncation band, the blocks crossed by each pixel's [depth - trunc, depth + trunc] ray segment. */
   int32_t allocation_mode;
-  /* 0 (default): plain FP32, bit-reproducible; 1: the update pass with fused multiply-adds and hardware
-   * approximations of exp, division and square root (results differ in the last bits). */
+  /* 0 (default): plain FP32, bit-reproducible; 1: the depth filter and the update pass with fused
+   * multiply-adds and hardware approximations of exp, division and square root (results differ in the last
+   * bits). */
   int32_t fast_math;
   /* 0 (default): the reference's bilateral surface normal evaluated at each voxel's projection (50 subpixel
    * depth samples); 1: the same normal evaluated once per pixel, bilinearly interpolated per voxel. */

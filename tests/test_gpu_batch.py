@@ -99,15 +99,21 @@ def test_batch_fast_math_graph_and_stream_agree(backend, oracle_lib):
     g = _run_batch(backend, scs, 1, True, steps)
     s = _run_batch(backend, scs, 1, False, steps)
     e = _run_batch(backend, scs, 0, True, steps)
+    alone = _run_alone(backend, scs, 1)
     for k, (a, b, c) in enumerate(zip(g, s, e)):
         ka, va = O.sort_blocks(*a.export_blocks())
         kb, vb = O.sort_blocks(*b.export_blocks())
         assert np.array_equal(ka, kb) and np.array_equal(va, vb), k
+        # every queued survivor is updated and counted: the same observed voxels as the scene fused alone in
+        # the fast-math form (up to rounding at the band and image edges), and the counter equals a recount
+        n_alone = alone[k].observed_voxel_count()
+        assert a.observed_voxel_count() == a.recount_observed_voxels(), k
+        assert abs(a.observed_voxel_count() - n_alone) <= 1e-3 * n_alone + 10, (k, a.observed_voxel_count(), n_alone)
         sc = scs[k][0]
         frames = list(range(12 - k))
         pts = metrics.observed_surface_points(sc, frames, stride=2)
         qa = metrics.chamfer(backend.extract_mesh_cuda(a), sc, pts)
         qc = metrics.chamfer(backend.extract_mesh_cuda(c), sc, pts)
         assert abs(qa["chamfer_mm"] - qc["chamfer_mm"]) <= 0.03 * qc["chamfer_mm"] + 0.05, (k, qa, qc)
-    for v in g + s + e:
+    for v in g + s + e + alone:
         v.close()

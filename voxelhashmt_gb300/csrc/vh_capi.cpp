@@ -503,6 +503,12 @@ vh_status vh_reset(vh_volume* v, void* stream) {
   return VH_OK;
 }
 
+// the bilateral filter of a frame that also starts it: exact, or the fast-math compile's (vh_algorithm.fast_math 1)
+static cudaError_t frame_filter(vh_volume* v, const float* in, float* out, const vh::Params& p, cudaStream_t s) {
+  return v->algo.fast_math ? vh::fast::launch_frame_filter(in, out, p, v->dev.counters, s)
+                           : vh::launch_filter(in, out, p, v->dev.counters, s);
+}
+
 vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, const vh_intrinsics* K,
                        const vh_pose* T_wc, int32_t stride, void* stream) {
   if (!v || !depth || !valid_intrinsics(K) || !T_wc) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_integrate: bad argument");
@@ -536,11 +542,11 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
       v->nn_ws_bytes = need;
     }
     // the bilateral filter (which also starts the frame) is the per-pixel fallback of the learned filter
-    VH_CUDA(v, vh::launch_filter(src, v->d_depth_bilateral, p, v->dev.counters, s));
+    VH_CUDA(v, frame_filter(v, src, v->d_depth_bilateral, p, s));
     VH_CUDA(v, vh::nn::forward(v->d_nn_params, v->d_nn_packed, src, v->d_depth_bilateral, v->d_depth_filtered, 1,
                                K->width, K->height, v->d_nn_ws, &v->dev.counters->error, s));
   } else {
-    VH_CUDA(v, vh::launch_filter(src, v->d_depth_filtered, p, v->dev.counters, s));
+    VH_CUDA(v, frame_filter(v, src, v->d_depth_filtered, p, s));
   }
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));

@@ -4,6 +4,8 @@
 // One CTA of kTX x kTY threads stages a 32x8 output tile of depth plus a 3-pixel halo in shared memory,
 // computes the normals of the tile plus a 2-pixel halo into shared memory, and runs the 5x5 joint bilateral
 // from shared memory: HBM traffic is one read and one write of the depth image.
+// Compiled with VH_FAST_MATH (the opt-in fast-math form), a tap's range and angular Gaussians are one hardware
+// exponential of the summed exponents instead of two exact ones.
 #pragma once
 
 #include "vh_common.cuh"
@@ -67,12 +69,54 @@ struct Smem {
   float spatial[(2 * kR + 1) * (2 * kR + 1)];
 };
 
+// The taps of radius R around staged pixel (tx, ty), in the reference's order (rows dv outer, columns du
+// inner).  No image-bounds test per tap: the staged tile holds 0 outside the image, which the sd <= 0 test
+// rejects exactly as the reference's bounds test does.
+template <int R>
+__device__ __forceinline__ void bilateral_taps(const Smem& S, int tx, int ty, float center, bool has_cn, f3 cn,
+                                               float thr, const Params& p, float& wds, float& ws) {
+#pragma unroll
+  for (int dv = -R; dv <= R; ++dv) {
+#pragma unroll
+    for (int du = -R; du <= R; ++du) {
+      const float sd = S.depth[ty + kR + 1 + dv][tx + kR + 1 + du];
+      if (sd <= 0.0f || fabsf(sd - center) > thr) continue;
+      const float delta = sd - center;
+      const float range = delta * delta;
+#ifdef VH_FAST_MATH
+      // one hardware exponential of the summed exponents: exp(-a) exp(-b) = exp(-(a + b))
+      float e = range * p.filter_k_range;
+      if (has_cn) {
+        const float4 sn = S.normal[ty + kR + dv][tx + kR + du];
+        if (sn.w == 0.0f) continue;
+        const float cosine = clampf(dot3(cn, mk3(sn.x, sn.y, sn.z)), -1.0f, 1.0f);
+        if (cosine < p.filter_min_cos) continue;
+        const float ad = 1.0f - cosine;
+        e += ad * ad * p.filter_k_angular;
+      }
+      const float w = S.spatial[(dv + kR) * (2 * kR + 1) + (du + kR)] * __expf(-e);
+#else
+      float w = S.spatial[(dv + kR) * (2 * kR + 1) + (du + kR)] * gaussian(range, p.filter_k_range);
+      if (has_cn) {
+        const float4 sn = S.normal[ty + kR + dv][tx + kR + du];
+        if (sn.w == 0.0f) continue;
+        const float cosine = clampf(dot3(cn, mk3(sn.x, sn.y, sn.z)), -1.0f, 1.0f);
+        if (cosine < p.filter_min_cos) continue;
+        const float ad = 1.0f - cosine;
+        w *= gaussian(ad * ad, p.filter_k_angular);
+      }
+#endif
+      wds += w * sd;
+      ws += w;
+    }
+  }
+}
+
 // bilateralFilterDepthKernel (cuda_tsdf_integrator.cu:650-725) for the output tile at (u0, v0); every thread of
 // the CTA calls it (it synchronises); thread (tx, ty) = tid % kTX, tid / kTX writes pixel (u0 + tx, v0 + ty).
 __device__ __forceinline__ void filter_tile(const float* __restrict__ in, float* __restrict__ out, const Params& p,
                                             int u0, int v0, int tid, Smem& S) {
   const int tx = tid % kTX, ty = tid / kTX;
-  const int R = p.filter_radius;
   if (tid < (2 * kR + 1) * (2 * kR + 1)) {
     const int du = tid % (2 * kR + 1) - kR, dv = tid / (2 * kR + 1) - kR;
     // exp of the spatial term depends only on (du, dv): evaluated once per tile, same value as per tap
@@ -93,28 +137,12 @@ __device__ __forceinline__ void filter_tile(const float* __restrict__ in, float*
   const f3 cn = has_cn ? mk3(cn4.x, cn4.y, cn4.z) : mk3(0.0f, 0.0f, 0.0f);
   const float thr = disc_threshold(p, center);
   float wds = 0.0f, ws = 0.0f;
-  for (int dv = -R; dv <= R; ++dv) {
-    const int sv = v + dv;
-    if (sv < 0 || sv >= p.height) continue;
-    for (int du = -R; du <= R; ++du) {
-      const int su = u + du;
-      if (su < 0 || su >= p.width) continue;
-      const float sd = S.depth[ty + kR + 1 + dv][tx + kR + 1 + du];
-      if (sd <= 0.0f || fabsf(sd - center) > thr) continue;
-      const float delta = sd - center;
-      const float range = delta * delta;
-      float w = S.spatial[(dv + kR) * (2 * kR + 1) + (du + kR)] * gaussian(range, p.filter_k_range);
-      if (has_cn) {
-        const float4 sn = S.normal[ty + kR + dv][tx + kR + du];
-        if (sn.w == 0.0f) continue;
-        const float cosine = clampf(dot3(cn, mk3(sn.x, sn.y, sn.z)), -1.0f, 1.0f);
-        if (cosine < p.filter_min_cos) continue;
-        const float ad = 1.0f - cosine;
-        w *= gaussian(ad * ad, p.filter_k_angular);
-      }
-      wds += w * sd;
-      ws += w;
-    }
+  if (p.filter_radius == 2) {
+    bilateral_taps<2>(S, tx, ty, center, has_cn, cn, thr, p, wds, ws);
+  } else if (p.filter_radius == 1) {
+    bilateral_taps<1>(S, tx, ty, center, has_cn, cn, thr, p, wds, ws);
+  } else {
+    bilateral_taps<0>(S, tx, ty, center, has_cn, cn, thr, p, wds, ws);
   }
   out[ci] = ws > 1e-6f ? (wds / ws) : center;
 }

@@ -795,8 +795,9 @@ __device__ __forceinline__ bool map_update_voxel(const float* __restrict__ depth
 // One pass over every voxel of the visible blocks with the normal from the map.  The voxel slots are cut in
 // chunks of kT (a CTA's threads); each CTA takes the next chunk from a device work queue (a counter reset when
 // the frame begins), runs voxel_prefix on one slot per thread, appends the survivors (warp-aggregated) to a
-// shared-memory queue with their projection, and then updates the survivors one per thread.  The expensive
-// part runs on compacted threads, and the dynamic order keeps every CTA busy until the last chunk.
+// shared-memory queue with their projection, and updates them one per thread in batches of kT (survivors
+// carry over between chunks).  The expensive part runs on compacted threads, and the dynamic order keeps every
+// CTA busy until the last chunk.
 template <int kT>
 struct MapQueue {
   static constexpr int kQueue = 2 * kT;
@@ -814,16 +815,27 @@ __device__ __forceinline__ void map_update_entry(const float* __restrict__ depth
                              Q.u[e], Q.v[e], Q.d[e], newly);
 }
 
-__device__ __forceinline__ void count_updates(const Volume& V, bool updated, bool newly, int lane) {
+// per-CTA sums of the frame statistics, flushed to the volume's counters once per CTA (and scene): the
+// counters share one L2 line, so per-warp atomics on them (hundreds of thousands a frame) would serialise there
+struct CtaStats {
+  uint32_t active, integrated;
+  unsigned long long observed;
+};
+
+__device__ __forceinline__ void tally_updates(CtaStats& st, bool updated, bool newly, int lane) {
   const uint32_t upd = __ballot_sync(0xffffffffU, updated);
   const uint32_t nw_ = __ballot_sync(0xffffffffU, newly);
   if (lane == 0) {
-    if (upd) atomicAdd(&V.counters->integrated_voxels, static_cast<uint32_t>(__popc(upd)));
-    if (nw_) atomicAdd(&V.counters->observed_voxels, static_cast<unsigned long long>(__popc(nw_)));
+    if (upd) atomicAdd(&st.integrated, static_cast<uint32_t>(__popc(upd)));
+    if (nw_) atomicAdd(&st.observed, static_cast<unsigned long long>(__popc(nw_)));
   }
 }
 
-// kT threads per CTA (a divisor of 512), at least kMinBlocks resident CTAs per SM (which caps the registers)
+// kT threads per CTA (a divisor of 512), at least kMinBlocks resident CTAs per SM (which caps the registers).
+// Survivors carry over between chunks: a chunk's survivors are appended to the queue, and whenever it holds at
+// least kT entries the CTA updates the last kT of them, one per thread, so every thread of the update phase has
+// a voxel; the rest are updated when the work queue is empty.  Each voxel is updated by exactly one thread and
+// the updates of different voxels touch different bins, so the order does not change the result.
 template <int kT, int kMinBlocks>
 __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const float* __restrict__ depth,
                                                                      const float4* __restrict__ nmap, const Volume V,
@@ -831,49 +843,72 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
   static_assert(kBlockVoxels % kT == 0, "CTA size must divide the block's voxel count");
   __shared__ MapQueue<kT> Q;
   __shared__ uint32_t s_item;
+  __shared__ CtaStats s_stats;
   const uint32_t nvis = V.counters->visible_count;
   const uint32_t nchunks = nvis * static_cast<uint32_t>(kBlockVoxels / kT);
   const int tid = threadIdx.x, lane = tid & 31;
-  if (tid == 0) Q.count = 0U;
+  if (tid == 0) {
+    Q.count = 0U;
+    s_stats.active = 0U;
+    s_stats.integrated = 0U;
+    s_stats.observed = 0ULL;
+  }
+  // The loop exits through the break at its end, after the drained pass: the equivalent form with a
+  // loop-carried flag as the loop condition lost one warp's survivors per chunk in the fast-math compile.
   for (;;) {
     if (tid == 0) s_item = atomicAdd(&V.counters->update_queue, 1U);
     __syncthreads();
     const uint32_t item = s_item;
-    if (item >= nchunks) break;
-    // 1. prefix of one slot per thread, survivors appended to the queue
-    const unsigned long long i = static_cast<unsigned long long>(item) * kT + tid;
-    const int li = static_cast<int>(i & 511U);
-    const uint32_t b = V.slot_block[V.visible[static_cast<uint32_t>(i >> 9)]];
-    bool pass = false;
-    f3 pc = mk3(0.0f, 0.0f, 0.0f);
-    float u = 0.0f, v = 0.0f, d = 0.0f;
-    if (li == 0 && b != kInvalidBlock) V.block_stamp[b] = V.counters->frame;  // for incremental meshing
-    if (b != kInvalidBlock) pass = voxel_prefix(depth, p, V.block_keys[b], li, pc, u, v, d);
-    const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
-    uint32_t base = 0U;
-    if (lane == 0 && ballot) {
-      base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
-      atomicAdd(&V.counters->active_voxels, static_cast<uint32_t>(__popc(ballot)));
-    }
-    base = __shfl_sync(0xffffffffU, base, 0);
-    if (pass) {
-      const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
-      Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
-      Q.u[e] = u;
-      Q.v[e] = v;
-      Q.d[e] = d;
-      Q.x[e] = pc.x;
-      Q.y[e] = pc.y;
-      Q.z[e] = pc.z;
+    const bool drained = item >= nchunks;
+    if (!drained) {
+      // 1. prefix of one slot per thread, survivors appended to the queue (fewer than kT entries carried over)
+      const unsigned long long i = static_cast<unsigned long long>(item) * kT + tid;
+      const int li = static_cast<int>(i & 511U);
+      const uint32_t b = V.slot_block[V.visible[static_cast<uint32_t>(i >> 9)]];
+      bool pass = false;
+      f3 pc = mk3(0.0f, 0.0f, 0.0f);
+      float u = 0.0f, v = 0.0f, d = 0.0f;
+      if (li == 0 && b != kInvalidBlock) V.block_stamp[b] = V.counters->frame;  // for incremental meshing
+      if (b != kInvalidBlock) pass = voxel_prefix(depth, p, V.block_keys[b], li, pc, u, v, d);
+      const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
+      uint32_t base = 0U;
+      if (lane == 0 && ballot) {
+        base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
+        atomicAdd(&s_stats.active, static_cast<uint32_t>(__popc(ballot)));
+      }
+      base = __shfl_sync(0xffffffffU, base, 0);
+      if (pass) {
+        const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
+        Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
+        Q.u[e] = u;
+        Q.v[e] = v;
+        Q.d[e] = d;
+        Q.x[e] = pc.x;
+        Q.y[e] = pc.y;
+        Q.z[e] = pc.z;
+      }
     }
     __syncthreads();
-    // 2. the survivors of the chunk, one per thread
+    // 2. entries [first, n), one per thread: a full batch (the last kT entries; [0, n - kT) stay for later
+    // chunks), nothing while fewer than kT are queued, and the carried-over rest once the work queue is empty.
+    // One call site, so every voxel runs the same instructions (with contraction on, two inlined copies of
+    // the update could round differently).
     const uint32_t n = Q.count;
+    const uint32_t first = drained ? 0U : (n >= static_cast<uint32_t>(kT) ? n - static_cast<uint32_t>(kT) : n);
     bool updated = false, newly = false;
-    if (static_cast<uint32_t>(tid) < n) map_update_entry(depth, nmap, V, p, Q, tid, updated, newly);
-    count_updates(V, updated, newly, lane);
-    __syncthreads();  // the queue and s_item are rewritten by the next chunk
-    if (tid == 0) Q.count = 0U;
+    if (first + static_cast<uint32_t>(tid) < n) {
+      map_update_entry(depth, nmap, V, p, Q, static_cast<int>(first) + tid, updated, newly);
+    }
+    tally_updates(s_stats, updated, newly, lane);
+    __syncthreads();  // the batch's entries and s_item are rewritten by the next chunk
+    if (tid == 0) Q.count = first;
+    if (drained) break;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (s_stats.active) atomicAdd(&V.counters->active_voxels, s_stats.active);
+    if (s_stats.integrated) atomicAdd(&V.counters->integrated_voxels, s_stats.integrated);
+    if (s_stats.observed) atomicAdd(&V.counters->observed_voxels, s_stats.observed);
   }
 }
 
@@ -998,6 +1033,8 @@ __global__ void __launch_bounds__(alloc::kThreads) batch_stage2_kernel(const Sce
   }
 }
 
+// Survivors carry over between the chunks of a scene as in fused_update_kernel; when the CTA's next chunk
+// belongs to another scene, it first updates the scene's remaining survivors and flushes its statistics.
 __global__ void __launch_bounds__(kThreads) batch_update_kernel(const SceneDesc* __restrict__ descs,
                                                                 const BatchHeader* __restrict__ hdr,
                                                                 uint32_t* __restrict__ queue) {
@@ -1006,6 +1043,7 @@ __global__ void __launch_bounds__(kThreads) batch_update_kernel(const SceneDesc*
   __shared__ uint32_t s_first[kMaxBatchScenes + 1];
   __shared__ uint32_t s_item;
   __shared__ int s_scene;
+  __shared__ CtaStats s_stats;
   const int tid = threadIdx.x, lane = tid & 31;
   const int nsc = static_cast<int>(hdr->nscenes);
   constexpr uint32_t kChunksPerBlock = kBlockVoxels / kThreads;
@@ -1017,60 +1055,104 @@ __global__ void __launch_bounds__(kThreads) batch_update_kernel(const SceneDesc*
     }
     s_first[nsc] = run;
     Q.count = 0U;
+    s_stats.active = 0U;
+    s_stats.integrated = 0U;
+    s_stats.observed = 0ULL;
   }
   __syncthreads();
   const uint32_t total = s_first[nsc];
-  int cur = -1;
+  int cur = -1;  // scene whose descriptor is in D and whose survivors are in the queue
+  uint32_t item = 0U;
+  int sc = -1;
+  bool fetched = false;
   for (;;) {
-    if (tid == 0) {
-      const uint32_t it = atomicAdd(&queue[2], 1U);
-      s_item = it;
-      s_scene = it < total ? find_scene(nsc, it, [&](int k) { return s_first[k]; }) : -1;
-    }
-    __syncthreads();
-    const uint32_t item = s_item;
-    const int sc = s_scene;
-    if (item >= total) break;
-    if (sc != cur) {
-      copy_desc(D, descs + sc, tid, kThreads);
-      cur = sc;
+    if (!fetched) {
+      if (tid == 0) {
+        const uint32_t it = atomicAdd(&queue[2], 1U);
+        s_item = it;
+        s_scene = it < total ? find_scene(nsc, it, [&](int k) { return s_first[k]; }) : -1;
+      }
       __syncthreads();
+      item = s_item;
+      sc = s_scene;
+      fetched = true;
     }
-    // 1. prefix of one slot per thread, survivors appended to the queue
-    const unsigned long long i = static_cast<unsigned long long>(item - s_first[sc]) * kThreads + tid;
-    const uint32_t b = D.V.slot_block[D.V.visible[static_cast<uint32_t>(i >> 9)]];
-    const int li = static_cast<int>(i & 511U);
-    bool pass = false;
-    if (li == 0 && b != kInvalidBlock) D.V.block_stamp[b] = D.V.counters->frame;  // for incremental meshing
-    f3 pc = mk3(0.0f, 0.0f, 0.0f);
-    float u = 0.0f, v = 0.0f, d = 0.0f;
-    if (b != kInvalidBlock) pass = voxel_prefix(D.depth, D.p, D.V.block_keys[b], li, pc, u, v, d);
-    const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
-    uint32_t base = 0U;
-    if (lane == 0 && ballot) {
-      base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
-      atomicAdd(&D.V.counters->active_voxels, static_cast<uint32_t>(__popc(ballot)));
-    }
-    base = __shfl_sync(0xffffffffU, base, 0);
-    if (pass) {
-      const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
-      Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
-      Q.u[e] = u;
-      Q.v[e] = v;
-      Q.d[e] = d;
-      Q.x[e] = pc.x;
-      Q.y[e] = pc.y;
-      Q.z[e] = pc.z;
+    // the current scene ends when the work queue is empty or the fetched chunk belongs to another scene: its
+    // carried-over survivors are updated and its statistics flushed before the next scene starts
+    const bool scene_end = cur >= 0 && (item >= total || sc != cur);
+    if (!scene_end) {
+      if (item >= total) break;
+      if (sc != cur) {
+        copy_desc(D, descs + sc, tid, kThreads);
+        cur = sc;
+        __syncthreads();
+      }
+      // 1. prefix of one slot per thread, survivors appended to the queue
+      const unsigned long long i = static_cast<unsigned long long>(item - s_first[sc]) * kThreads + tid;
+      const uint32_t b = D.V.slot_block[D.V.visible[static_cast<uint32_t>(i >> 9)]];
+      const int li = static_cast<int>(i & 511U);
+      bool pass = false;
+      if (li == 0 && b != kInvalidBlock) D.V.block_stamp[b] = D.V.counters->frame;  // for incremental meshing
+      f3 pc = mk3(0.0f, 0.0f, 0.0f);
+      float u = 0.0f, v = 0.0f, d = 0.0f;
+      if (b != kInvalidBlock) pass = voxel_prefix(D.depth, D.p, D.V.block_keys[b], li, pc, u, v, d);
+      const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
+      uint32_t base = 0U;
+      if (lane == 0 && ballot) {
+        base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
+        atomicAdd(&s_stats.active, static_cast<uint32_t>(__popc(ballot)));
+      }
+      base = __shfl_sync(0xffffffffU, base, 0);
+      if (pass) {
+        const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
+        Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
+        Q.u[e] = u;
+        Q.v[e] = v;
+        Q.d[e] = d;
+        Q.x[e] = pc.x;
+        Q.y[e] = pc.y;
+        Q.z[e] = pc.z;
+      }
+      fetched = false;
     }
     __syncthreads();
-    // 2. the survivors of the chunk, one per thread
+    // 2. entries [first, n) of the current scene, one per thread, from one call site (as in
+    // fused_update_kernel): a full batch, nothing, or at the scene's end the carried-over rest
     const uint32_t n = Q.count;
+    const uint32_t first =
+        scene_end ? 0U : (n >= static_cast<uint32_t>(kThreads) ? n - static_cast<uint32_t>(kThreads) : n);
     bool updated = false, newly = false;
-    if (static_cast<uint32_t>(tid) < n) map_update_entry(D.depth, D.nmap, D.V, D.p, Q, tid, updated, newly);
-    count_updates(D.V, updated, newly, lane);
+    if (first + static_cast<uint32_t>(tid) < n) {
+      map_update_entry(D.depth, D.nmap, D.V, D.p, Q, static_cast<int>(first) + tid, updated, newly);
+    }
+    tally_updates(s_stats, updated, newly, lane);
     __syncthreads();
-    if (tid == 0) Q.count = 0U;
+    if (tid == 0) {
+      Q.count = first;
+      if (scene_end) {
+        if (s_stats.active) atomicAdd(&D.V.counters->active_voxels, s_stats.active);
+        if (s_stats.integrated) atomicAdd(&D.V.counters->integrated_voxels, s_stats.integrated);
+        if (s_stats.observed) atomicAdd(&D.V.counters->observed_voxels, s_stats.observed);
+        s_stats.active = 0U;
+        s_stats.integrated = 0U;
+        s_stats.observed = 0ULL;
+      }
+    }
+    if (scene_end) {
+      __syncthreads();  // D, the statistics and the queue are rewritten by the next scene
+      cur = -1;
+    }
   }
+}
+
+// the depth filter of one frame in this compile (the fast-math form's filter in the fast compile)
+__global__ void __launch_bounds__(filt::kTX * filt::kTY) frame_filter_kernel(const float* __restrict__ in,
+                                                                             float* __restrict__ out, const Params p,
+                                                                             Counters* counters) {
+  __shared__ filt::Smem S;
+  const int tid = threadIdx.x;
+  if (counters && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) filt::begin_frame(counters);
+  filt::filter_tile(in, out, p, blockIdx.x * filt::kTX, blockIdx.y * filt::kTY, tid, S);
 }
 
 }  // namespace
@@ -1087,6 +1169,13 @@ int integrate_grid_size() {
   static int grid = 0;
   if (grid == 0) grid = grid_for(reinterpret_cast<const void*>(update_kernel), kUpdateThreads);
   return grid;
+}
+
+cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s) {
+  if (p.filter_radius < 0 || p.filter_radius > filt::kR) return cudaErrorInvalidValue;
+  const dim3 grid((p.width + filt::kTX - 1) / filt::kTX, (p.height + filt::kTY - 1) / filt::kTY);
+  frame_filter_kernel<<<grid, filt::kTX * filt::kTY, 0, s>>>(in, out, p, begin_frame);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s) {

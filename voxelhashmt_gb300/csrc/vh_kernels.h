@@ -20,6 +20,8 @@ cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, c
 // FP32 form; fast: the same source compiled with fused multiply-adds and hardware approximations.  With
 // Params::normal_mode 1, nmap (width x height float4) receives the per-pixel normal map.
 namespace exact {
+// the depth filter of one frame, begin_frame as in vh::launch_filter (the fast compile is the fast-math form's)
+cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s);
 // one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
 // scenes (queue: 3 counters, cleared here)
 cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);
@@ -35,6 +37,8 @@ cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nm
 int integrate_grid_size();
 }  // namespace exact
 namespace fast {
+// the depth filter of one frame, begin_frame as in vh::launch_filter (the fast compile is the fast-math form's)
+cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s);
 // one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
 // scenes (queue: 3 counters, cleared here)
 cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);

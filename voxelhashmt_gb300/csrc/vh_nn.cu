@@ -4,11 +4,14 @@
 // The two 32 -> 32 layers carry ~95 % of the arithmetic and run on the 5th-generation tensor cores
 // (tcgen05.mma, kind::f16 with BF16 operands, FP32 accumulator in tensor memory) as an implicit GEMM: one CTA
 // computes 128 consecutive output pixels of one image row x 32 output channels, M = 128, N = 32,
-// K = 9 taps x 32 input channels, issued as 18 MMAs of m128n32k16 into one TMEM accumulator (32 columns).
-// The three input rows the tile needs (130 pixels each, 1-pixel halo) are staged in shared memory in the
-// canonical no-swizzle K-major layout: [row][channel group of 8][pixel][8 channels], 16 bytes per pixel per
-// group, so the A operand of tap (dy, dx) is the same layout starting dx pixels further -- a descriptor
-// start address 16 bytes * dx higher; no im2col copy.  Weights are staged once per CTA as
+// K = 9 taps x 32 input channels, issued as 18 MMAs of m128n32k16 into a TMEM accumulator (32 columns; two
+// accumulators and two staged tiles, so the loads, MMAs and epilogue of consecutive tiles overlap).
+// The three input rows the tile needs (130 pixels each, 1-pixel halo) are loaded by TMA (12 tensor-map boxes
+// of {8 channels, 130 pixels}, zero fill outside the image) into shared memory in the canonical no-swizzle
+// K-major layout: [row][channel group of 8][pixel][8 channels], 16 bytes per pixel per group (each group's
+// plane padded to 2,176 bytes for the TMA's 128-byte destination alignment), so the A operand of tap (dy, dx)
+// is the same layout starting dx pixels further -- a descriptor start address 16 bytes * dx higher; no im2col
+// copy.  Weights are staged once per CTA as
 // [tap][k-step][channel group][output channel][8 channels].  The epilogue reads the accumulator with
 // tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = pixels 32w..32w+31), adds the bias and applies ReLU, or,
 // for the input gradient, multiplies by the ReLU mask of the layer's input, and stores BF16.
@@ -21,9 +24,11 @@
 // kBBytes; the layout is checked bit-for-bit against a float64 convolution), and each region has a margin
 // beyond that; the mbarrier wait gives up after a bounded number of polls, sets the error word and still
 // waits (bounded) before freeing tensor memory.
+#include <cuda.h>  // CUtensorMap and the tensor-map encoder's types (resolved at run time, no link dependency)
 #include <cuda_bf16.h>
 
 #include <cstdint>
+#include <cstdlib>
 
 #include "vh_nn.h"
 
@@ -35,15 +40,20 @@ constexpr int kTile = 128;                 // output pixels per CTA tile (MMA M)
 constexpr int kC = 32;                     // channels of the hidden layers (MMA N, and K per tap)
 constexpr int kRowPix = kTile + 2;         // staged pixels per input row
 constexpr int kGroups = kC / 8;            // channel groups of 8 (16 bytes of BF16)
-constexpr int kPlane = kRowPix * 16;       // bytes of one channel group of one staged row (the A operand's LBO)
+constexpr int kPlaneData = kRowPix * 16;   // bytes of one channel group of one staged row: one TMA box
+constexpr int kPlane = 2176;               // the plane padded to a multiple of 128 (TMA destination alignment);
+                                           // the A operand's LBO
 constexpr int kRowBytes = kGroups * kPlane;
-constexpr int kABytes = 3 * kRowBytes;     // 24,960
-constexpr int kAPad = kABytes + 2048;      // A region + margin (the descriptors read exactly kABytes)
+constexpr int kABytes = 3 * kRowBytes;     // 26,112 (24,960 of them written by the 12 TMA boxes of a tile)
+constexpr int kAPad = kABytes + 256;       // A region + margin (the descriptors read below kABytes)
+constexpr uint32_t kTileTxBytes = 3 * kGroups * kPlaneData;
 constexpr int kBBlock = 2 * kC * 16;       // one (tap, k-step) B operand: 2 groups x 32 rows x 16 B = 1,024
 constexpr int kBBytes = 18 * kBBlock;      // 18,432
 constexpr int kBPad = kBBytes + 1024;
 constexpr int kThreads = 128;              // 4 warps: one per 32 TMEM lanes
-constexpr int kSmem = kAPad + kBPad + 64;  // + mbarrier and TMEM address
+constexpr int kSmem = 128 + 2 * kAPad + kBPad + 64;  // alignment slack, two A stages, B, 4 mbarriers, TMEM address
+static_assert(kPlaneData <= kPlane && kPlane % 128 == 0 && kAPad % 128 == 0, "TMA destinations 128-byte aligned");
+constexpr int kCtasPerSm = 3;  // measured best of 1, 2, 3 (B = 16, 640 x 480: 583, 327, 278 us)
 constexpr uint32_t kMaxPolls = 1u << 24;
 constexpr unsigned int kErrorBit = 8u;  // the volume error word's timeout bit
 
@@ -104,89 +114,159 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// TMA-loads the three input rows of a tile (image img, row y, pixels x0-1 .. x0+128) into the stage at a_base as
+// [row][g][pixel][8 channels]: 12 boxes {8 channels, 130 pixels} of the NHWC tensor map; rows and pixels
+// outside the image read as zeros (the map's out-of-bounds fill).  Completion: kTileTxBytes on bar.
+// The innermost coordinate is the channel 8 g, i.e. 16 g bytes: always 16-byte aligned.
+__device__ __forceinline__ void load_tile(const CUtensorMap* map, uint32_t a_base, uint32_t bar, int img, int y,
+                                          int x0) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(kTileTxBytes) : "memory");
+  const uint64_t m = reinterpret_cast<uint64_t>(map);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int g = 0; g < kGroups; ++g) {
+      asm volatile(
+          "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+          "[%6];\n" ::"r"(a_base + r * kRowBytes + g * kPlane),
+          "l"(m), "r"(8 * g), "r"(x0 - 1), "r"(y - 1 + r), "r"(img), "r"(bar)
+          : "memory");
+    }
+  }
+}
+
+// the 18 MMAs of one tile: A from the staged rows at a_base, accumulator at tmem; completion arrives on bar
+__device__ __forceinline__ void issue_tile(uint32_t a_base, uint32_t b_base, uint32_t tmem, uint32_t bar) {
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  int k = 0;
+  for (int dy = 0; dy < 3; ++dy) {
+    for (int dx = 0; dx < 3; ++dx) {
+      for (int ks = 0; ks < 2; ++ks, ++k) {
+        const uint64_t a = smem_desc(a_base + dy * kRowBytes + (2 * ks) * kPlane + dx * 16, kPlane, 128);
+        const uint64_t b = smem_desc(b_base + k * kBBlock, kC * 16, 128);
+        mma(tmem, a, b, k > 0 ? 1u : 0u);
+      }
+    }
+  }
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+
 // One 32 -> 32 3x3 convolution over a batch of images (NHWC BF16, zero padding), tcgen05 implicit GEMM.
 // mode kForward: out = relu?(conv(in) + bias); mode kGrad: out = conv(in) * (mask > 0) (mask = the layer
 // input's activations; the input gradient of the previous layer's ReLU).
-__global__ void __launch_bounds__(kThreads) conv32_tc_kernel(const __nv_bfloat16* __restrict__ in,
+// Pipeline over the CTA's tiles k = 0, 1, ... (tile blockIdx.x + k gridDim.x), two stages and two
+// accumulators: thread 0 keeps the TMA loads of tiles k+1 and k+2 in flight and issues the MMAs of tile k+1
+// while the four warps run the epilogue of tile k; no thread stages data.  Barriers: full[q] (TMA bytes of
+// the tile in stage q landed), done[q] (the MMAs reading stage q and writing accumulator q completed).
+__global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_constant__ CUtensorMap in_map,
                                                              const __nv_bfloat16* __restrict__ wpack,
                                                              const float* __restrict__ bias,
                                                              const __nv_bfloat16* __restrict__ mask,
                                                              __nv_bfloat16* __restrict__ out, int batch, int width,
                                                              int height, int mode, int relu,
                                                              unsigned int* __restrict__ error) {
-  extern __shared__ __align__(1024) unsigned char smem[];
-  unsigned char* sA = smem;
-  unsigned char* sB = smem + kAPad;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kAPad + kBPad);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + kAPad + kBPad + 16);
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA destinations: 128 B
+  unsigned char* sA[2] = {smem, smem + kAPad};
+  unsigned char* sB = smem + 2 * kAPad;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sB + kBPad);  // full[0], full[1], done[0], done[1]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sB + kBPad + 32);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   // weights: [tap][ks][g][co][8] BF16, 18,432 bytes, already packed in this order in global memory
   for (int i = tid; i < kBBytes / 16; i += kThreads) {
     reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(wpack)[i];
   }
-  for (int i = tid; i < (kAPad - kABytes) / 16; i += kThreads) reinterpret_cast<uint4*>(sA + kABytes)[i] = make_uint4(0, 0, 0, 0);
+  for (int q = 0; q < 2; ++q) {
+    for (int i = tid; i < (kAPad - kABytes) / 16; i += kThreads) {
+      reinterpret_cast<uint4*>(sA[q] + kABytes)[i] = make_uint4(0, 0, 0, 0);
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the weights, for the MMAs' async reads
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;\n" ::"r"(smem_u32(tmem_slot)));
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(smem_u32(tmem_slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(bar)));
+    for (int i = 0; i < 4; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar[i])));
     asm volatile("fence.mbarrier_init.release.cluster;\n");
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&in_map)) : "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n");
-  const uint32_t tmem = *tmem_slot;
-  const uint32_t a_base = smem_u32(sA), b_base = smem_u32(sB), bar_addr = smem_u32(bar);
+  const uint32_t tmem = *tmem_slot;  // accumulator q at columns 32 q
+  const uint32_t a_base[2] = {smem_u32(sA[0]), smem_u32(sA[1])};
+  const uint32_t b_base = smem_u32(sB);
+  const uint32_t full[2] = {smem_u32(&bar[0]), smem_u32(&bar[1])};
+  const uint32_t done[2] = {smem_u32(&bar[2]), smem_u32(&bar[3])};
 
   const int tiles_x = (width + kTile - 1) / kTile;
   const long long ntiles = static_cast<long long>(batch) * height * tiles_x;
-  uint32_t phase = 0;
-  bool ok = true;
-  for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-    const int tx = static_cast<int>(t % tiles_x);
+  const long long stride = gridDim.x;
+  auto coords = [&](long long t, int& img, int& y, int& x0) {
+    x0 = static_cast<int>(t % tiles_x) * kTile;
     const long long rest = t / tiles_x;
-    const int y = static_cast<int>(rest % height);
-    const int img = static_cast<int>(rest / height);
-    const int x0 = tx * kTile;
-    // stage rows y-1, y, y+1, pixels x0-1 .. x0+128, as [row][g][pixel][8 channels]
-    for (int i = tid; i < 3 * kRowPix * kGroups; i += kThreads) {
-      const int g = i % kGroups;
-      const int px = (i / kGroups) % kRowPix;
-      const int r = i / (kGroups * kRowPix);
-      const int sx = x0 - 1 + px, sy = y - 1 + r;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (sx >= 0 && sx < width && sy >= 0 && sy < height) {
-        v = reinterpret_cast<const uint4*>(in + ((static_cast<size_t>(img) * height + sy) * width + sx) * kC)[g];
+    y = static_cast<int>(rest % height);
+    img = static_cast<int>(rest / height);
+  };
+  // phases of the barriers; loading / pending: a TMA load / an MMA group in flight (thread 0's view)
+  uint32_t fphase[2] = {0u, 0u}, dphase[2] = {0u, 0u};
+  bool loading[2] = {false, false}, pending[2] = {false, false};
+  bool mine = true;
+  if (tid == 0) {  // prologue: loads of tiles 0 and 1, MMAs of tile 0
+    for (int q = 0; q < 2; ++q) {
+      const long long t = blockIdx.x + q * stride;
+      if (t < ntiles) {
+        int img, y, x0;
+        coords(t, img, y, x0);
+        load_tile(&in_map, a_base[q], full[q], img, y, x0);
+        loading[q] = true;
       }
-      *reinterpret_cast<uint4*>(sA + r * kRowBytes + g * kPlane + px * 16) = v;
     }
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;\n");
-      int k = 0;
-      for (int dy = 0; dy < 3; ++dy) {
-        for (int dx = 0; dx < 3; ++dx) {
-          for (int ks = 0; ks < 2; ++ks, ++k) {
-            const uint64_t a = smem_desc(a_base + dy * kRowBytes + (2 * ks) * kPlane + dx * 16, kPlane, 128);
-            const uint64_t b = smem_desc(b_base + k * kBBlock, kC * 16, 128);
-            mma(tmem, a, b, k > 0 ? 1u : 0u);
-          }
-        }
+    if (loading[0]) {
+      if (mbar_wait(full[0], fphase[0])) {
+        fphase[0] ^= 1u;
+        loading[0] = false;
+        issue_tile(a_base[0], b_base, tmem, done[0]);
+        pending[0] = true;
+      } else {
+        mine = false;
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_addr)
-                   : "memory");
     }
-    // every thread polls the barrier; the CTA continues only if all saw the phase complete (uniform branch)
-    ok = __syncthreads_and(mbar_wait(bar_addr, phase) ? 1 : 0) != 0;
-    phase ^= 1u;
-    asm volatile("tcgen05.fence::after_thread_sync;\n");
+  }
+  bool ok = __syncthreads_and(mine ? 1 : 0) != 0;
+  for (long long k = 0, t = blockIdx.x; ok && t < ntiles; ++k, t += stride) {
+    // stage / accumulator q of this tile and nq of the next; selects, not indexing, keep the pairs in registers
+    const bool odd = (k & 1) != 0;
+    const uint32_t q = odd ? 1u : 0u, nq = q ^ 1u;
+    mine = true;
+    if (tid == 0 && t + stride < ntiles) {  // MMAs of the next tile, whose rows are landing in stage nq
+      if (mbar_wait(odd ? full[0] : full[1], odd ? fphase[0] : fphase[1])) {
+        if (odd) { fphase[0] ^= 1u; loading[0] = false; } else { fphase[1] ^= 1u; loading[1] = false; }
+        issue_tile(odd ? a_base[0] : a_base[1], b_base, tmem + 32u * nq, odd ? done[0] : done[1]);
+        if (odd) pending[0] = true; else pending[1] = true;
+      } else {
+        mine = false;
+      }
+    }
+    // every thread polls; the CTA continues only if all saw tile t complete (uniform branch)
+    mine = mbar_wait(odd ? done[1] : done[0], odd ? dphase[1] : dphase[0]) && mine;
+    ok = __syncthreads_and(mine ? 1 : 0) != 0;
     if (!ok) break;
-    // epilogue: warp w, lane l = output pixel 32w + l of the tile
+    if (odd) { dphase[1] ^= 1u; pending[1] = false; } else { dphase[0] ^= 1u; pending[0] = false; }
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    if (tid == 0 && t + 2 * stride < ntiles) {  // stage q is free again: load tile k+2 into it
+      int img, y, x0;
+      coords(t + 2 * stride, img, y, x0);
+      load_tile(&in_map, odd ? a_base[1] : a_base[0], odd ? full[1] : full[0], img, y, x0);
+      if (odd) loading[1] = true; else loading[0] = true;
+    }
+    // epilogue of tile t: warp w, lane l = output pixel 32w + l
+    int img, y, x0;
+    coords(t, img, y, x0);
     float acc[32];
-    tmem_ld32(tmem + (static_cast<uint32_t>(warp * 32) << 16), acc);
+    tmem_ld32(tmem + 32u * q + (static_cast<uint32_t>(warp * 32) << 16), acc);
     const int x = x0 + warp * 32 + lane;
     if (x < width) {
       const size_t o = ((static_cast<size_t>(img) * height + y) * width + x) * kC;
@@ -201,24 +281,58 @@ __global__ void __launch_bounds__(kThreads) conv32_tc_kernel(const __nv_bfloat16
       } else {
         __align__(16) __nv_bfloat16 m[32];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(m)[q] = reinterpret_cast<const uint4*>(mask + o)[q];
+        for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(m)[u] = reinterpret_cast<const uint4*>(mask + o)[u];
 #pragma unroll
         for (int c = 0; c < 32; ++c) res[c] = __float2bfloat16_rn(__bfloat162float(m[c]) > 0.0f ? acc[c] : 0.0f);
       }
 #pragma unroll
-      for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(out + o)[q] = reinterpret_cast<const uint4*>(res)[q];
+      for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(out + o)[u] = reinterpret_cast<const uint4*>(res)[u];
     }
-    // the accumulator and the staged tile are reused by the next tile
+    // accumulator q is written again by the MMAs of tile k+2, issued after this barrier
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
   }
-  if (!ok) {
-    if (tid == 0) atomicOr(error, kErrorBit);
-    mbar_wait(bar_addr, phase ^ 1u);  // the MMAs in flight, bounded
+  if (!ok && tid == 0) {
+    atomicOr(error, kErrorBit);
+    // the TMA loads and MMA groups still in flight, bounded
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (pending[q]) mbar_wait(done[q], dphase[q]);
+      if (loading[q]) mbar_wait(full[q], fphase[q]);
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;\n" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem));
+}
+
+// cuTensorMapEncodeTiled, resolved through the runtime's driver entry point (no link dependency on libcuda)
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+cudaError_t encode_input_map(const __nv_bfloat16* in, int batch, int width, int height, CUtensorMap* map) {
+  static EncodeTiledFn encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult qr = cudaDriverEntryPointSymbolNotFound;
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &qr);
+    if (e != cudaSuccess) return e;
+    if (qr != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    encode = reinterpret_cast<EncodeTiledFn>(fn);
+  }
+  if (reinterpret_cast<uintptr_t>(in) % 16 != 0) return cudaErrorInvalidValue;
+  // NHWC BF16: dims innermost first {channel, x, y, image}; byte strides of x, y, image
+  const cuuint64_t dims[4] = {static_cast<cuuint64_t>(kC), static_cast<cuuint64_t>(width),
+                              static_cast<cuuint64_t>(height), static_cast<cuuint64_t>(batch)};
+  const cuuint64_t strides[3] = {static_cast<cuuint64_t>(kC) * 2, static_cast<cuuint64_t>(width) * kC * 2,
+                                 static_cast<cuuint64_t>(height) * width * kC * 2};
+  const cuuint32_t box[4] = {8, static_cast<cuuint32_t>(kRowPix), 1, 1};
+  const cuuint32_t elem[4] = {1, 1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(in), dims, strides,
+                            box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -234,19 +348,27 @@ cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, c
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  // two persistent CTAs per SM: each CTA stages the weights and allocates tensor memory once, so fewer CTAs
-  // with more tiles each measured faster than filling the SMs (the tile loop is not pipelined)
+  // persistent CTAs, kCtasPerSm per SM (VH_CONV32_CTAS_PER_SM overrides it for launch-shape sweeps): each
+  // CTA stages the weights and allocates tensor memory once and pipelines its tiles
   static int ctas = 0;
   if (ctas == 0) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    ctas = 2 * (sms > 0 ? sms : 152);
+    int per_sm = kCtasPerSm;
+    if (const char* env = std::getenv("VH_CONV32_CTAS_PER_SM")) {
+      const int v = std::atoi(env);
+      if (v >= 1 && v <= 3) per_sm = v;  // three stages of kSmem fit in one SM's shared memory
+    }
+    ctas = per_sm * (sms > 0 ? sms : 152);
   }
   const long long ntiles = static_cast<long long>(batch) * height * ((width + kTile - 1) / kTile);
   const int grid = static_cast<int>(ntiles < ctas ? ntiles : ctas);
   if (grid <= 0) return cudaSuccess;
-  conv32_tc_kernel<<<grid, kThreads, kSmem, s>>>(in, wpack, bias, mask, out, batch, width, height, mode, relu, error);
+  CUtensorMap map;
+  const cudaError_t e = encode_input_map(in, batch, width, height, &map);
+  if (e != cudaSuccess) return e;
+  conv32_tc_kernel<<<grid, kThreads, kSmem, s>>>(map, wpack, bias, mask, out, batch, width, height, mode, relu, error);
   return cudaGetLastError();
 }
 
