@@ -28,7 +28,6 @@ constexpr int kTX = 32;
 constexpr int kTY = 8;
 constexpr int kThreads = kTX * kTY;
 constexpr int kCenterSlots = 1024;  // >= 3 * kThreads centres
-constexpr int kNbrSlots = 4096;
 constexpr int kMaxSmemProbes = 64;
 
 __device__ __forceinline__ uint32_t smem_hash(unsigned long long k, int bits) {
@@ -93,7 +92,8 @@ __device__ __forceinline__ int smem_insert(unsigned long long* set, int bits, un
 
 // Blocks crossed by the segment a -> b (3-D DDA over the block grid, Amanatides & Woo 1987), each inserted into
 // the tile set; returns false when a block leaves the packed key range.
-__device__ inline bool insert_band_blocks(const Volume& V, unsigned long long* s_nset, f3 a, f3 b, float bws, uint32_t frame) {
+__device__ inline bool insert_band_blocks(const Volume& V, unsigned long long* s_nset, int set_bits, f3 a, f3 b, float bws,
+                                          uint32_t frame) {
   int c[3] = {static_cast<int>(floorf(a.x / bws)), static_cast<int>(floorf(a.y / bws)), static_cast<int>(floorf(a.z / bws))};
   const int e[3] = {static_cast<int>(floorf(b.x / bws)), static_cast<int>(floorf(b.y / bws)),
                     static_cast<int>(floorf(b.z / bws))};
@@ -110,62 +110,79 @@ __device__ inline bool insert_band_blocks(const Volume& V, unsigned long long* s
   for (int it = 0; it < 64; ++it) {
     unsigned long long key;
     if (!pack_block_key(c[0], c[1], c[2], key)) return false;
-    if (smem_insert(s_nset, 12, key) < 0) insert_global(V, key, frame);
+    if (smem_insert(s_nset, set_bits, key) < 0) insert_global(V, key, frame);
     if (c[0] == e[0] && c[1] == e[1] && c[2] == e[2]) break;
     const int k = (tmax[0] < tmax[1]) ? (tmax[0] < tmax[2] ? 0 : 2) : (tmax[1] < tmax[2] ? 1 : 2);
-    if (tmax[k] > 1.0f) break;  // rounding ended the walk one cell short of the end block
-    c[k] += st[k];
-    tmax[k] += tdel[k];
+    // the step on axis k, written per axis so that the arrays stay in registers (no indexing by a run-time k)
+    const float tk = k == 0 ? tmax[0] : (k == 1 ? tmax[1] : tmax[2]);
+    if (tk > 1.0f) break;  // rounding ended the walk one cell short of the end block
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      if (j == k) {
+        c[j] += st[j];
+        tmax[j] += tdel[j];
+      }
+    }
   }
   unsigned long long key;  // the end block always belongs to the band (the set drops the duplicate)
   if (!pack_block_key(e[0], e[1], e[2], key)) return false;
-  if (smem_insert(s_nset, 12, key) < 0) insert_global(V, key, frame);
+  if (smem_insert(s_nset, set_bits, key) < 0) insert_global(V, key, frame);
   return true;
 }
 
-struct Smem {
+// Shared-memory sets of one tile.  kBand: the truncation-band rule only (Params::alloc_mode 1), which needs
+// just the tile's key set, and a small one: a tile's band crosses tens of blocks, and a key that finds the set
+// full goes straight to the device table.
+template <bool kBand>
+struct TileSets;
+template <>
+struct TileSets<false> {
+  static constexpr int kSetBits = 12;
   unsigned long long cset[kCenterSlots];
   unsigned long long clist[3 * kThreads];
-  unsigned long long nset[kNbrSlots];
+  unsigned long long nset[1 << kSetBits];
   uint32_t ccount;
 };
+template <>
+struct TileSets<true> {
+  static constexpr int kSetBits = 10;
+  unsigned long long nset[1 << kSetBits];
+};
+using Smem = TileSets<false>;
 
-// buildActiveBlockHashKernel (cuda_block_allocator.cu:231-272) for the 32x8 tile of samples at (sx0, sy0);
-// every thread of the CTA calls it (it synchronises).
-__device__ __forceinline__ void alloc_tile(const float* __restrict__ depth, const Volume& V, const Params& p, int sx0,
-                                           int sy0, int tid, Smem& S) {
-  unsigned long long* s_cset = S.cset;
-  unsigned long long* s_clist = S.clist;
+// buildActiveBlockHashKernel (cuda_block_allocator.cu:231-272) for one tile of kThreads samples; every thread
+// of the CTA calls it (it synchronises).  Thread tid holds one sample: has = it exists and lies in the image,
+// (u, v) its pixel, d its depth.  kBand = false runs the rule p.alloc_mode selects; kBand = true requires
+// p.alloc_mode == 1.
+template <bool kBand>
+__device__ __forceinline__ void alloc_samples(const Volume& V, const Params& p, bool has, int u, int v, float d, int tid,
+                                              TileSets<kBand>& S) {
+  constexpr int kSetBits = TileSets<kBand>::kSetBits;
   unsigned long long* s_nset = S.nset;
-  uint32_t& s_ccount = S.ccount;
-  const int tx = tid % kTX, ty = tid / kTX;
   const uint32_t frame = V.counters->frame;
-  for (int i = tid; i < kCenterSlots; i += kThreads) s_cset[i] = kEmptyKey;
-  for (int i = tid; i < kNbrSlots; i += kThreads) s_nset[i] = kEmptyKey;
-  if (tid == 0) s_ccount = 0U;
+  for (int i = tid; i < (1 << kSetBits); i += kThreads) s_nset[i] = kEmptyKey;
+  if constexpr (!kBand) {
+    for (int i = tid; i < kCenterSlots; i += kThreads) S.cset[i] = kEmptyKey;
+    if (tid == 0) S.ccount = 0U;
+  }
   __syncthreads();
 
   // 1. centre blocks of this sample (buildActiveBlockHashKernel, cuda_block_allocator.cu:231-272)
-  const int sx = sx0 + tx;
-  const int sy = sy0 + ty;
-  if (sx < p.sample_width && sy < p.sample_height) {
-    const int u = sx * p.stride, v = sy * p.stride;
-    if (u < p.width && v < p.height) {
-      const float d = __ldg(&depth[static_cast<size_t>(v) * p.width + u]);
-      if (d > 0.0f) {
-        const f3 pc = mk3((static_cast<float>(u) - p.cx) * d / p.fx, (static_cast<float>(v) - p.cy) * d / p.fy, d);
-        const f3 pw = xform_point(p.T_wc, pc);
-        const f3 ray = normalize3(mk3(pw.x - p.T_wc.t[0], pw.y - p.T_wc.t[1], pw.z - p.T_wc.t[2]));
-        const f3 pts[3] = {
-            pw,
-            mk3(pw.x - ray.x * p.truncation, pw.y - ray.y * p.truncation, pw.z - ray.z * p.truncation),
-            mk3(pw.x + ray.x * p.truncation, pw.y + ray.y * p.truncation, pw.z + ray.z * p.truncation),
-        };
-        if (p.alloc_mode == 1) {
-          if (!insert_band_blocks(V, s_nset, pts[1], pts[2], p.block_world_size, frame)) {
-            atomicOr(&V.counters->error, kErrKeyRange);
-          }
-        } else
+  if (has && d > 0.0f) {
+    const f3 pc = mk3((static_cast<float>(u) - p.cx) * d / p.fx, (static_cast<float>(v) - p.cy) * d / p.fy, d);
+    const f3 pw = xform_point(p.T_wc, pc);
+    const f3 ray = normalize3(mk3(pw.x - p.T_wc.t[0], pw.y - p.T_wc.t[1], pw.z - p.T_wc.t[2]));
+    const f3 pts[3] = {
+        pw,
+        mk3(pw.x - ray.x * p.truncation, pw.y - ray.y * p.truncation, pw.z - ray.z * p.truncation),
+        mk3(pw.x + ray.x * p.truncation, pw.y + ray.y * p.truncation, pw.z + ray.z * p.truncation),
+    };
+    if (kBand || p.alloc_mode == 1) {
+      if (!insert_band_blocks(V, s_nset, kSetBits, pts[1], pts[2], p.block_world_size, frame)) {
+        atomicOr(&V.counters->error, kErrKeyRange);
+      }
+    } else {
+      if constexpr (!kBand) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           const int bx = static_cast<int>(floorf(pts[k].x / p.block_world_size));
@@ -179,10 +196,10 @@ __device__ __forceinline__ void alloc_tile(const float* __restrict__ depth, cons
           }
           unsigned long long key;
           pack_block_key(bx, by, bz, key);
-          const int r = smem_insert(s_cset, 10, key);
+          const int r = smem_insert(S.cset, 10, key);
           if (r == 1) {
-            const uint32_t pos = atomicAdd(&s_ccount, 1U);
-            s_clist[pos] = key;
+            const uint32_t pos = atomicAdd(&S.ccount, 1U);
+            S.clist[pos] = key;
           } else if (r < 0) {  // centre set saturated: expand this centre straight into the table
             for (int o = 0; o < 27; ++o) {
               unsigned long long nk;
@@ -196,23 +213,35 @@ __device__ __forceinline__ void alloc_tile(const float* __restrict__ depth, cons
   }
   __syncthreads();
 
-  // 2. 27-neighbourhoods of the unique centres (insertNeighborhood, :198-220)
-  const int ncent = static_cast<int>(s_ccount);
-  for (int w = tid; w < ncent * 27; w += kThreads) {
-    const int c = w / 27, o = w - c * 27;
-    int x, y, z;
-    unpack_block_key(s_clist[c], x, y, z);
-    unsigned long long key;
-    pack_block_key(x + (o % 3) - 1, y + ((o / 3) % 3) - 1, z + (o / 9) - 1, key);
-    if (smem_insert(s_nset, 12, key) < 0) insert_global(V, key, frame);  // tile set saturated
+  if constexpr (!kBand) {
+    // 2. 27-neighbourhoods of the unique centres (insertNeighborhood, :198-220)
+    const int ncent = static_cast<int>(S.ccount);
+    for (int w = tid; w < ncent * 27; w += kThreads) {
+      const int c = w / 27, o = w - c * 27;
+      int x, y, z;
+      unpack_block_key(S.clist[c], x, y, z);
+      unsigned long long key;
+      pack_block_key(x + (o % 3) - 1, y + ((o / 3) % 3) - 1, z + (o / 9) - 1, key);
+      if (smem_insert(s_nset, kSetBits, key) < 0) insert_global(V, key, frame);  // tile set saturated
+    }
+    __syncthreads();
   }
-  __syncthreads();
 
   // 3. one persistent-hash insert per unique key of the tile
-  for (int s = tid; s < kNbrSlots; s += kThreads) {
+  for (int s = tid; s < (1 << kSetBits); s += kThreads) {
     const unsigned long long key = s_nset[s];
     if (key != kEmptyKey) insert_global(V, key, frame);
   }
+}
+
+// the tile of samples at (sx0, sy0) (sample (sx, sy) = pixel (sx * stride, sy * stride)), depth from global memory
+__device__ __forceinline__ void alloc_tile(const float* __restrict__ depth, const Volume& V, const Params& p, int sx0,
+                                           int sy0, int tid, Smem& S) {
+  const int sx = sx0 + tid % kTX, sy = sy0 + tid / kTX;
+  const int u = sx * p.stride, v = sy * p.stride;
+  const bool has = sx < p.sample_width && sy < p.sample_height && u < p.width && v < p.height;
+  const float d = has ? __ldg(&depth[static_cast<size_t>(v) * p.width + u]) : 0.0f;
+  alloc_samples<false>(V, p, has, u, v, d, tid, S);
 }
 
 }  // namespace alloc

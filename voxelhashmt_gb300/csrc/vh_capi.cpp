@@ -397,6 +397,7 @@ vh_status vh_create(const vh_params* params, const vh_algorithm* algo, vh_volume
   step(dalloc(&V.slot_block, buckets));
   step(dalloc(&V.slot_stamp, buckets));
   step(dalloc(&V.visible, buckets));
+  step(dalloc(&V.visible_keys, buckets));
   step(dalloc(&V.active, nb * vh::kBlockVoxels));
   V.voxel_size = params->voxel_size;
   V.inv_voxel_size = 1.0f / params->voxel_size;
@@ -442,6 +443,7 @@ void vh_destroy(vh_volume* v) {
   dfree(V.slot_block);
   dfree(V.slot_stamp);
   dfree(V.visible);
+  dfree(V.visible_keys);
   dfree(V.active);
   dfree(V.layers);
   dfree(V.layers16);
@@ -545,11 +547,14 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
     VH_CUDA(v, frame_filter(v, src, v->d_depth_bilateral, p, s));
     VH_CUDA(v, vh::nn::forward(v->d_nn_params, v->d_nn_packed, src, v->d_depth_bilateral, v->d_depth_filtered, 1,
                                K->width, K->height, v->d_nn_ws, &v->dev.counters->error, s));
+    if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
+    VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
   } else {
-    VH_CUDA(v, frame_filter(v, src, v->d_depth_filtered, p, s));
+    // the bilateral filter and the allocation in one kernel: the profile's allocation stage is then empty
+    VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_filter_alloc(src, v->d_depth_filtered, v->dev, p, s)
+                                  : vh::exact::launch_filter_alloc(src, v->d_depth_filtered, v->dev, p, s));
+    if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   }
-  if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
-  VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[2], s));
   VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_integrate_prepare(v->d_depth_filtered, v->dev, p, v->d_normal_map, s)
                                 : vh::exact::launch_integrate_prepare(v->d_depth_filtered, v->dev, p, v->d_normal_map, s));

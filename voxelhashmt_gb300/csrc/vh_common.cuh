@@ -57,6 +57,8 @@ static_assert(sizeof(Counters) == 64, "Counters is read back as one 64-byte copy
 //   obs_mask    u32[max_blocks][16]     one bit per voxel: any layer observed
 //   dir_mask    u32[max_blocks]         bit d set once any voxel of the block has an observed layer in bin d
 //   visible     u32[capacity]           slots touched by the current frame (unordered)
+//   visible_keys int4[capacity]         per visible entry {x, y, z, pool index}: written after the allocation
+//                                       by the normal-map pass, read once per chunk by the fused update
 //   active      u32[max_blocks * 512]   (block << 9 | voxel) of the current frame's voxels that pass the
 //                                       projection / depth / truncation tests (unordered)
 struct Volume {
@@ -70,6 +72,7 @@ struct Volume {
   uint32_t* dir_mask;
   uint32_t* block_stamp;  // per pool block: the last frame that ran the layer update over it
   uint32_t* visible;
+  int4* visible_keys;
   uint32_t* active;
   Counters* counters;
   uint32_t capacity;

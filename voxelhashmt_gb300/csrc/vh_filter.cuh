@@ -113,9 +113,10 @@ __device__ __forceinline__ void bilateral_taps(const Smem& S, int tx, int ty, fl
 }
 
 // bilateralFilterDepthKernel (cuda_tsdf_integrator.cu:650-725) for the output tile at (u0, v0); every thread of
-// the CTA calls it (it synchronises); thread (tx, ty) = tid % kTX, tid / kTX writes pixel (u0 + tx, v0 + ty).
-__device__ __forceinline__ void filter_tile(const float* __restrict__ in, float* __restrict__ out, const Params& p,
-                                            int u0, int v0, int tid, Smem& S) {
+// the CTA calls it (it synchronises); thread (tx, ty) = tid % kTX, tid / kTX writes pixel (u0 + tx, v0 + ty)
+// and returns the value it wrote (0 for a pixel outside the image).
+__device__ __forceinline__ float filter_tile(const float* __restrict__ in, float* __restrict__ out, const Params& p,
+                                             int u0, int v0, int tid, Smem& S) {
   const int tx = tid % kTX, ty = tid / kTX;
   if (tid < (2 * kR + 1) * (2 * kR + 1)) {
     const int du = tid % (2 * kR + 1) - kR, dv = tid / (2 * kR + 1) - kR;
@@ -125,12 +126,12 @@ __device__ __forceinline__ void filter_tile(const float* __restrict__ in, float*
   stage_tile(in, S.depth, S.normal, u0, v0, p, tid);
 
   const int u = u0 + tx, v = v0 + ty;
-  if (u >= p.width || v >= p.height) return;
+  if (u >= p.width || v >= p.height) return 0.0f;
   const size_t ci = static_cast<size_t>(v) * p.width + u;
   const float center = S.depth[ty + kR + 1][tx + kR + 1];
   if (center <= 0.0f) {
     out[ci] = 0.0f;
-    return;
+    return 0.0f;
   }
   const float4 cn4 = S.normal[ty + kR][tx + kR];
   const bool has_cn = cn4.w != 0.0f;
@@ -144,7 +145,9 @@ __device__ __forceinline__ void filter_tile(const float* __restrict__ in, float*
   } else {
     bilateral_taps<0>(S, tx, ty, center, has_cn, cn, thr, p, wds, ws);
   }
-  out[ci] = ws > 1e-6f ? (wds / ws) : center;
+  const float result = ws > 1e-6f ? (wds / ws) : center;
+  out[ci] = result;
+  return result;
 }
 
 // the per-frame counter reset of a new frame (the frame stamp marks visible slots)

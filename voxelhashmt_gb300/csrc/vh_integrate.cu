@@ -731,6 +731,27 @@ __global__ void __launch_bounds__(kMapTX * kMapTY) pixel_normal_kernel(const flo
   map_tile(depth, p, nmap, blockIdx.x * kMapTX, blockIdx.y * kMapTY, threadIdx.y * kMapTX + threadIdx.x, S);
 }
 
+// The normal map of a frame (pixel_normal_kernel) plus, grid-stride over the frame's visible list (final: the
+// allocation ran before), each entry's {block key, pool index} into V.visible_keys, so that the fused update
+// reads one int4 per chunk instead of the dependent chain visible -> slot_block -> block_keys.
+__global__ void __launch_bounds__(kMapTX * kMapTY) map_prepare_kernel(const float* __restrict__ depth, const Volume V,
+                                                                      const Params p, float4* __restrict__ nmap) {
+  __shared__ MapSmem S;
+  const int tid = threadIdx.y * kMapTX + threadIdx.x;
+  const uint32_t nvis = V.counters->visible_count;
+  const uint32_t nthreads = gridDim.x * gridDim.y * kMapTX * kMapTY;
+  for (uint32_t i = (blockIdx.y * gridDim.x + blockIdx.x) * (kMapTX * kMapTY) + tid; i < nvis; i += nthreads) {
+    const uint32_t b = V.slot_block[V.visible[i]];
+    int4 k = make_int4(0, 0, 0, static_cast<int>(kInvalidBlock));
+    if (b != kInvalidBlock) {
+      const int4 bk = V.block_keys[b];
+      k = make_int4(bk.x, bk.y, bk.z, static_cast<int>(b));
+    }
+    V.visible_keys[i] = k;
+  }
+  map_tile(depth, p, nmap, blockIdx.x * kMapTX, blockIdx.y * kMapTY, tid, S);
+}
+
 // Normal at a voxel's projection (u, v): bilinear blend of the valid map taps around it, renormalised.
 __device__ __forceinline__ bool map_normal(const float4* __restrict__ nmap, const Params& p, float u, float v, f3& n) {
   const int x0 = static_cast<int>(floorf(u)), y0 = static_cast<int>(floorf(v));
@@ -852,24 +873,30 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
     s_stats.active = 0U;
     s_stats.integrated = 0U;
     s_stats.observed = 0ULL;
+    s_item = atomicAdd(&V.counters->update_queue, 1U);
   }
+  const uint32_t frame = V.counters->frame;
   // The loop exits through the break at its end, after the drained pass: the equivalent form with a
   // loop-carried flag as the loop condition lost one warp's survivors per chunk in the fast-math compile.
   for (;;) {
-    if (tid == 0) s_item = atomicAdd(&V.counters->update_queue, 1U);
-    __syncthreads();
+    __syncthreads();  // s_item and Q.count of this pass published
     const uint32_t item = s_item;
     const bool drained = item >= nchunks;
+    // the following chunk is taken from the work queue now; its index is published at the end of the pass,
+    // so the atomic's latency overlaps this chunk's work
+    uint32_t next = 0U;
+    if (tid == 0 && !drained) next = atomicAdd(&V.counters->update_queue, 1U);
     if (!drained) {
       // 1. prefix of one slot per thread, survivors appended to the queue (fewer than kT entries carried over)
       const unsigned long long i = static_cast<unsigned long long>(item) * kT + tid;
       const int li = static_cast<int>(i & 511U);
-      const uint32_t b = V.slot_block[V.visible[static_cast<uint32_t>(i >> 9)]];
+      const int4 vk = V.visible_keys[static_cast<uint32_t>(i >> 9)];
+      const uint32_t b = static_cast<uint32_t>(vk.w);
       bool pass = false;
       f3 pc = mk3(0.0f, 0.0f, 0.0f);
       float u = 0.0f, v = 0.0f, d = 0.0f;
-      if (li == 0 && b != kInvalidBlock) V.block_stamp[b] = V.counters->frame;  // for incremental meshing
-      if (b != kInvalidBlock) pass = voxel_prefix(depth, p, V.block_keys[b], li, pc, u, v, d);
+      if (li == 0 && b != kInvalidBlock) V.block_stamp[b] = frame;  // for incremental meshing
+      if (b != kInvalidBlock) pass = voxel_prefix(depth, p, vk, li, pc, u, v, d);
       const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
       uint32_t base = 0U;
       if (lane == 0 && ballot) {
@@ -901,7 +928,10 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
     }
     tally_updates(s_stats, updated, newly, lane);
     __syncthreads();  // the batch's entries and s_item are rewritten by the next chunk
-    if (tid == 0) Q.count = first;
+    if (tid == 0) {
+      Q.count = first;
+      s_item = next;
+    }
     if (drained) break;
   }
   __syncthreads();
@@ -1155,6 +1185,29 @@ __global__ void __launch_bounds__(filt::kTX * filt::kTY) frame_filter_kernel(con
   filt::filter_tile(in, out, p, blockIdx.x * filt::kTX, blockIdx.y * filt::kTY, tid, S);
 }
 
+// Filter and allocation of one frame in one pass (the frame was started by a preceding launch): each CTA filters
+// its 32x8 tile, then allocates the blocks of the tile's samples from the filtered depths it just computed.
+// The allocation's dependent hash probes overlap the filter arithmetic of the other CTAs on the SM, and the
+// filtered depth is not re-read.  kBand: the truncation-band rule (smaller tile sets, higher occupancy).
+template <bool kBand>
+__global__ void __launch_bounds__(filt::kTX * filt::kTY) filter_alloc_kernel(const float* __restrict__ in,
+                                                                             float* __restrict__ out, const Volume V,
+                                                                             const Params p) {
+  static_assert(filt::kTX == alloc::kTX && filt::kTY == alloc::kTY, "one tile for both passes");
+  __shared__ union Shared {
+    filt::Smem f;
+    alloc::TileSets<kBand> a;
+  } S;
+  const int tid = threadIdx.x;
+  const int u0 = blockIdx.x * filt::kTX, v0 = blockIdx.y * filt::kTY;
+  const float d = filt::filter_tile(in, out, p, u0, v0, tid, S.f);
+  __syncthreads();  // the filter's staged tiles become the allocation's sets
+  const int u = u0 + tid % filt::kTX, v = v0 + tid / filt::kTX;
+  const bool has = u < p.width && v < p.height && u % p.stride == 0 && v % p.stride == 0 &&
+                   u / p.stride < p.sample_width && v / p.stride < p.sample_height;
+  alloc::alloc_samples<kBand>(V, p, has, u, v, d, tid, S.a);
+}
+
 }  // namespace
 
 static int grid_for(const void* kernel, int threads) {
@@ -1178,6 +1231,19 @@ cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Co
   return cudaGetLastError();
 }
 
+cudaError_t launch_filter_alloc(const float* in, float* out, const Volume& V, const Params& p, cudaStream_t s) {
+  if (p.filter_radius < 0 || p.filter_radius > filt::kR || p.stride < 1) return cudaErrorInvalidValue;
+  const cudaError_t e = launch_begin_frame(V.counters, s);
+  if (e != cudaSuccess) return e;
+  const dim3 grid((p.width + filt::kTX - 1) / filt::kTX, (p.height + filt::kTY - 1) / filt::kTY);
+  if (p.alloc_mode == 1) {
+    filter_alloc_kernel<true><<<grid, filt::kTX * filt::kTY, 0, s>>>(in, out, V, p);
+  } else {
+    filter_alloc_kernel<false><<<grid, filt::kTX * filt::kTY, 0, s>>>(in, out, V, p);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nmap, cudaStream_t s) {
   const dim3 mb(kMapTX, kMapTY), mg((p.width + kMapTX - 1) / kMapTX, (p.height + kMapTY - 1) / kMapTY);
   pixel_normal_kernel<<<mg, mb, 0, s>>>(depth, p, nmap);
@@ -1189,7 +1255,9 @@ cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const 
                                      cudaStream_t s) {
   if (p.normal_mode == 1) {
     if (nmap == nullptr) return cudaErrorInvalidValue;
-    return launch_pixel_normals(depth, p, nmap, s);
+    const dim3 mb(kMapTX, kMapTY), mg((p.width + kMapTX - 1) / kMapTX, (p.height + kMapTY - 1) / kMapTY);
+    map_prepare_kernel<<<mg, mb, 0, s>>>(depth, V, p, nmap);
+    return cudaGetLastError();
   }
   static int classify_grid = 0;
   if (classify_grid == 0) classify_grid = grid_for(reinterpret_cast<const void*>(classify_kernel), kThreads);

@@ -22,6 +22,8 @@ cudaError_t launch_alloc(const float* depth, const Volume& V, const Params& p, c
 namespace exact {
 // the depth filter of one frame, begin_frame as in vh::launch_filter (the fast compile is the fast-math form's)
 cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s);
+// starts a frame, then filters it and allocates its blocks in one kernel (out: the filtered depth)
+cudaError_t launch_filter_alloc(const float* in, float* out, const Volume& V, const Params& p, cudaStream_t s);
 // one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
 // scenes (queue: 3 counters, cleared here)
 cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);
@@ -39,6 +41,8 @@ int integrate_grid_size();
 namespace fast {
 // the depth filter of one frame, begin_frame as in vh::launch_filter (the fast compile is the fast-math form's)
 cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s);
+// starts a frame, then filters it and allocates its blocks in one kernel (out: the filtered depth)
+cudaError_t launch_filter_alloc(const float* in, float* out, const Volume& V, const Params& p, cudaStream_t s);
 // one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
 // scenes (queue: 3 counters, cleared here)
 cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);
