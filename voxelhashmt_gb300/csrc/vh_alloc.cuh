@@ -34,9 +34,9 @@ __device__ __forceinline__ uint32_t smem_hash(unsigned long long k, int bits) {
   return static_cast<uint32_t>((k * 0x9E3779B97F4A7C15ULL) >> (64 - bits));
 }
 
-// slot was found or inserted this frame: put it on the visible list once
+// slot was found or inserted this frame: put it on the visible list once (the exchange both tests and sets the
+// slot's frame stamp: one round trip to L2)
 __device__ __forceinline__ void mark_visible(const Volume& V, uint32_t slot, uint32_t frame) {
-  if (*reinterpret_cast<volatile uint32_t*>(&V.slot_stamp[slot]) == frame) return;
   if (atomicExch(&V.slot_stamp[slot], frame) == frame) return;
   const uint32_t pos = atomicAdd(&V.counters->visible_count, 1U);
   V.visible[pos] = slot;
@@ -147,6 +147,8 @@ template <>
 struct TileSets<true> {
   static constexpr int kSetBits = 10;
   unsigned long long nset[1 << kSetBits];
+  unsigned long long klist[1 << kSetBits];  // the set's keys, compacted
+  uint32_t nkeys;
 };
 using Smem = TileSets<false>;
 
@@ -164,6 +166,8 @@ __device__ __forceinline__ void alloc_samples(const Volume& V, const Params& p, 
   if constexpr (!kBand) {
     for (int i = tid; i < kCenterSlots; i += kThreads) S.cset[i] = kEmptyKey;
     if (tid == 0) S.ccount = 0U;
+  } else {
+    if (tid == 0) S.nkeys = 0U;
   }
   __syncthreads();
 
@@ -227,10 +231,22 @@ __device__ __forceinline__ void alloc_samples(const Volume& V, const Params& p, 
     __syncthreads();
   }
 
-  // 3. one persistent-hash insert per unique key of the tile
-  for (int s = tid; s < (1 << kSetBits); s += kThreads) {
-    const unsigned long long key = s_nset[s];
-    if (key != kEmptyKey) insert_global(V, key, frame);
+  // 3. one persistent-hash insert per unique key of the tile.  The band's set is sparse (tens of keys in 1,024
+  // slots): its keys are compacted first, so that every insert (a chain of dependent L2/DRAM round trips) runs
+  // on its own thread at once instead of one after another in the threads that own several set slots.
+  if constexpr (kBand) {
+    for (int s = tid; s < (1 << kSetBits); s += kThreads) {
+      const unsigned long long key = s_nset[s];
+      if (key != kEmptyKey) S.klist[atomicAdd(&S.nkeys, 1U)] = key;
+    }
+    __syncthreads();
+    const int n = static_cast<int>(S.nkeys);
+    for (int i = tid; i < n; i += kThreads) insert_global(V, S.klist[i], frame);
+  } else {
+    for (int s = tid; s < (1 << kSetBits); s += kThreads) {
+      const unsigned long long key = s_nset[s];
+      if (key != kEmptyKey) insert_global(V, key, frame);
+    }
   }
 }
 

@@ -447,9 +447,12 @@ __device__ __forceinline__ bool integrate_bin16(const Params& p, const Volume& V
       if (empty < 0) empty = l;
       continue;
     }
+    // a layer farther than merge_tol from the sample can never be the merged one (the best match is taken
+    // only within merge_tol), so its normal is not decoded: the decision is the same as testing it
+    const float delta = fabsf(ls[l] - sc);
+    if (!(delta <= p.merge_tol)) continue;
     ln[l] = bin_normal(nk[l]);
     if (dot3(ln[l], n) < p.layer_normal_cos) continue;
-    const float delta = fabsf(ls[l] - sc);
     if (delta < best_delta) {
       best_delta = delta;
       best = l;
