@@ -929,6 +929,7 @@ struct vh_batch {
   std::vector<vh_volume*> vols;
   int device = 0;
   int fast = 0;
+  bool band = false;  // every volume allocates by the truncation-band rule (smaller tile sets)
   bool use_graph = false;
   size_t bytes = 0;                 // header + descriptors
   unsigned char* d_buf = nullptr;   // [BatchHeader][SceneDesc x n]
@@ -950,7 +951,8 @@ static cudaError_t batch_launch(vh_batch* b, int slot, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const auto* hdr = reinterpret_cast<const vh::BatchHeader*>(b->d_buf);
   const auto* desc = reinterpret_cast<const vh::SceneDesc*>(b->d_buf + sizeof(vh::BatchHeader));
-  return b->fast ? vh::fast::launch_batch(desc, hdr, b->d_queue, s) : vh::exact::launch_batch(desc, hdr, b->d_queue, s);
+  return b->fast ? vh::fast::launch_batch(desc, hdr, b->d_queue, b->band, s)
+                 : vh::exact::launch_batch(desc, hdr, b->d_queue, b->band, s);
 }
 
 void vh_batch_destroy(vh_batch* b) {
@@ -983,6 +985,8 @@ vh_status vh_batch_create(vh_volume* const* volumes, int32_t count, int32_t use_
   b->vols.assign(volumes, volumes + count);
   b->device = volumes[0]->params.device;
   b->fast = volumes[0]->algo.fast_math;
+  b->band = true;
+  for (int i = 0; i < count; ++i) b->band = b->band && volumes[i]->algo.allocation_mode == 1;
   b->use_graph = use_graph != 0;
   b->bytes = sizeof(vh::BatchHeader) + static_cast<size_t>(count) * sizeof(vh::SceneDesc);
   DeviceGuard guard(b->device);
@@ -1014,7 +1018,7 @@ vh_status vh_batch_integrate(vh_batch* b, const float* const* depth_device, cons
   auto* hdr = reinterpret_cast<vh::BatchHeader*>(b->h_stage[slot]);
   auto* desc = reinterpret_cast<vh::SceneDesc*>(b->h_stage[slot] + sizeof(vh::BatchHeader));
   const int n = static_cast<int>(b->vols.size());
-  uint32_t filter_total = 0, alloc_total = 0, map_total = 0;
+  uint32_t filter_total = 0, map_total = 0;
   for (int i = 0; i < n; ++i) {
     vh_volume* v = b->vols[i];
     vh::SceneDesc& d = desc[i];
@@ -1031,23 +1035,18 @@ vh_status vh_batch_integrate(vh_batch* b, const float* const* depth_device, cons
       d.depth = v->d_depth_filtered;
       d.nmap = v->d_normal_map;
       d.filter_items = tiles(K[i].width, K[i].height, 32, 8);
-      d.alloc_items = tiles(d.p.sample_width, d.p.sample_height, 32, 8);
       d.map_items = tiles(K[i].width, K[i].height, 32, 8);
       d.active = 1U;
     }
     d.filter_first = filter_total;
-    d.alloc_first = alloc_total;
+    d.map_first = map_total;
     filter_total += d.filter_items;
-    alloc_total += d.alloc_items;
-  }
-  for (int i = 0; i < n; ++i) {
-    desc[i].map_first = alloc_total + map_total;
-    map_total += desc[i].map_items;
+    map_total += d.map_items;
   }
   hdr->nscenes = static_cast<uint32_t>(n);
   hdr->filter_total = filter_total;
-  hdr->alloc_total = alloc_total;
-  hdr->stage2_total = alloc_total + map_total;
+  hdr->stage2_total = map_total;
+  hdr->pad = 0U;
   cudaError_t e = cudaSuccess;
   if (b->use_graph) {
     if (!b->exec[slot]) {

@@ -120,18 +120,17 @@ struct SceneDesc {
   const float* depth_in;  // raw depth, device
   float* depth;           // filtered depth, device
   float4* nmap;           // per-pixel normal map, device
-  uint32_t filter_first, filter_items;  // [first, first + items) in the filter kernel's item space
-  uint32_t alloc_first, alloc_items;    // in the allocation + normal-map kernel's item space
-  uint32_t map_first, map_items;        // (allocation items of all scenes come first)
+  uint32_t filter_first, filter_items;  // [first, first + items) in the filter + allocation kernel's item space
+  uint32_t map_first, map_items;        // in the normal-map kernel's item space
   uint32_t active, pad;
 };
 
 // Step header of a batch (device memory): scene count and item totals.
 struct BatchHeader {
   uint32_t nscenes;
-  uint32_t filter_total;
-  uint32_t stage2_total;  // allocation + normal-map items
-  uint32_t alloc_total;   // allocation items (they precede the normal-map items)
+  uint32_t filter_total;  // filter + allocation items
+  uint32_t stage2_total;  // normal-map items
+  uint32_t pad;
 };
 
 constexpr int kMaxBatchScenes = 256;

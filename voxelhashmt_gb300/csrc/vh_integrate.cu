@@ -947,10 +947,11 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
 
 // ---- multi-scene batch: three work-queue kernels over the items of every scene of the step ----
 //
-// 1. batch_filter_kernel: the filter tiles of all scenes (the first tile of a scene also starts its frame);
-// 2. batch_stage2_kernel: the allocation tiles, then the normal-map tiles, of all scenes;
+// 0. batch_begin_kernel: clears the work queues and starts every active scene's frame;
+// 1. batch_filter_alloc_kernel: the filter + allocation tiles of all scenes;
+// 2. batch_map_kernel: the normal-map tiles of all scenes, and each scene's visible-list keys;
 // 3. batch_update_kernel: chunks of kThreads voxel slots of every scene's visible blocks (the per-scene
-//    visible counts are final after kernel 2; every CTA derives the chunk prefix from them).
+//    visible counts are final after kernel 1; every CTA derives the chunk prefix from them).
 // Each CTA takes the next item from a global counter (a device work queue), so scenes of very different
 // sizes share the GPU without idle tails; the scene of an item is found by binary search over the
 // per-scene first items, and its descriptor is copied to shared memory when it changes.
@@ -977,11 +978,28 @@ __device__ __forceinline__ void copy_desc(SceneDesc& dst, const SceneDesc* __res
   for (int i = tid; i < static_cast<int>(sizeof(SceneDesc) / 4); i += nthreads) d[i] = s[i];
 }
 
-__global__ void __launch_bounds__(filt::kTX * filt::kTY) batch_filter_kernel(const SceneDesc* __restrict__ descs,
-                                                                             const BatchHeader* __restrict__ hdr,
-                                                                             uint32_t* __restrict__ queue) {
+// 0. the step's start: work-queue counters cleared, every active scene's frame started (before any
+// allocation of the step touches a scene's counters)
+__global__ void batch_begin_kernel(const SceneDesc* __restrict__ descs, const BatchHeader* __restrict__ hdr,
+                                   uint32_t* __restrict__ queue) {
+  if (threadIdx.x < 3) queue[threadIdx.x] = 0U;
+  const int nsc = static_cast<int>(hdr->nscenes);
+  for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
+    if (descs[k].active) filt::begin_frame(descs[k].V.counters);
+  }
+}
+
+// 1. filter + allocation tiles of all scenes (filter_alloc_kernel per tile)
+template <bool kBand>
+__global__ void __launch_bounds__(filt::kTX * filt::kTY) batch_filter_alloc_kernel(const SceneDesc* __restrict__ descs,
+                                                                                   const BatchHeader* __restrict__ hdr,
+                                                                                   uint32_t* __restrict__ queue) {
   constexpr int kT = filt::kTX * filt::kTY;
-  __shared__ filt::Smem S;
+  static_assert(filt::kTX == alloc::kTX && filt::kTY == alloc::kTY, "one tile for both passes");
+  __shared__ union Shared {
+    filt::Smem f;
+    alloc::TileSets<kBand> a;
+  } S;
   __shared__ SceneDesc D;
   __shared__ uint32_t s_item;
   __shared__ int s_scene;
@@ -1006,62 +1024,61 @@ __global__ void __launch_bounds__(filt::kTX * filt::kTY) batch_filter_kernel(con
     }
     const uint32_t local = item - D.filter_first;
     const uint32_t tiles_x = (static_cast<uint32_t>(D.p.width) + filt::kTX - 1) / filt::kTX;
-    if (local == 0U && tid == 0) filt::begin_frame(D.V.counters);
-    filt::filter_tile(D.depth_in, D.depth, D.p, static_cast<int>(local % tiles_x) * filt::kTX,
-                      static_cast<int>(local / tiles_x) * filt::kTY, tid, S);
+    const int u0 = static_cast<int>(local % tiles_x) * filt::kTX, v0 = static_cast<int>(local / tiles_x) * filt::kTY;
+    const float d = filt::filter_tile(D.depth_in, D.depth, D.p, u0, v0, tid, S.f);
+    __syncthreads();  // the filter's staged tiles become the allocation's sets
+    const int u = u0 + tid % filt::kTX, v = v0 + tid / filt::kTX;
+    const int st = D.p.stride;
+    const bool has = u < D.p.width && v < D.p.height && u % st == 0 && v % st == 0 && u / st < D.p.sample_width &&
+                     v / st < D.p.sample_height;
+    alloc::alloc_samples<kBand>(D.V, D.p, has, u, v, d, tid, S.a);
     __syncthreads();
   }
 }
 
-union Stage2Smem {
-  alloc::Smem a;
-  MapSmem m;
-};
-
-__global__ void __launch_bounds__(alloc::kThreads) batch_stage2_kernel(const SceneDesc* __restrict__ descs,
-                                                                       const BatchHeader* __restrict__ hdr,
-                                                                       uint32_t* __restrict__ queue) {
-  static_assert(alloc::kThreads == kMapTX * kMapTY, "one CTA shape for both stages");
-  __shared__ Stage2Smem U;
+// 2. normal-map tiles of all scenes; the tiles of a scene also write its visible list's {key, pool index}
+// entries (the list is final after kernel 1), tile L of M taking entries L * 256 + tid + j * M * 256
+__global__ void __launch_bounds__(kMapTX * kMapTY) batch_map_kernel(const SceneDesc* __restrict__ descs,
+                                                                    const BatchHeader* __restrict__ hdr,
+                                                                    uint32_t* __restrict__ queue) {
+  constexpr int kT = kMapTX * kMapTY;
+  __shared__ MapSmem M;
   __shared__ SceneDesc D;
   __shared__ uint32_t s_item;
   __shared__ int s_scene;
   const int tid = threadIdx.x;
   const int nsc = static_cast<int>(hdr->nscenes);
-  const uint32_t total = hdr->stage2_total, alloc_total = hdr->alloc_total;
+  const uint32_t total = hdr->stage2_total;
   int cur = -1;
   for (;;) {
     if (tid == 0) {
       const uint32_t it = atomicAdd(&queue[1], 1U);
       s_item = it;
-      int scn = -1;
-      if (it < alloc_total) {
-        scn = find_scene(nsc, it, [&](int k) { return descs[k].alloc_first; });
-      } else if (it < total) {
-        scn = find_scene(nsc, it, [&](int k) { return descs[k].map_first; });
-      }
-      s_scene = scn;
+      s_scene = it < total ? find_scene(nsc, it, [&](int k) { return descs[k].map_first; }) : -1;
     }
     __syncthreads();
     const uint32_t item = s_item;
     const int sc = s_scene;
     if (item >= total) break;
     if (sc != cur) {
-      copy_desc(D, descs + sc, tid, alloc::kThreads);
+      copy_desc(D, descs + sc, tid, kT);
       cur = sc;
       __syncthreads();
     }
-    if (item < alloc_total) {
-      const uint32_t local = item - D.alloc_first;
-      const uint32_t tiles_x = (static_cast<uint32_t>(D.p.sample_width) + alloc::kTX - 1) / alloc::kTX;
-      alloc::alloc_tile(D.depth, D.V, D.p, static_cast<int>(local % tiles_x) * alloc::kTX,
-                        static_cast<int>(local / tiles_x) * alloc::kTY, tid, U.a);
-    } else {
-      const uint32_t local = item - D.map_first;
-      const uint32_t tiles_x = (static_cast<uint32_t>(D.p.width) + kMapTX - 1) / kMapTX;
-      map_tile(D.depth, D.p, D.nmap, static_cast<int>(local % tiles_x) * kMapTX,
-               static_cast<int>(local / tiles_x) * kMapTY, tid, U.m);
+    const uint32_t local = item - D.map_first;
+    const uint32_t nvis = D.V.counters->visible_count;
+    for (uint32_t i = local * kT + tid; i < nvis; i += D.map_items * kT) {
+      const uint32_t b = D.V.slot_block[D.V.visible[i]];
+      int4 k = make_int4(0, 0, 0, static_cast<int>(kInvalidBlock));
+      if (b != kInvalidBlock) {
+        const int4 bk = D.V.block_keys[b];
+        k = make_int4(bk.x, bk.y, bk.z, static_cast<int>(b));
+      }
+      D.V.visible_keys[i] = k;
     }
+    const uint32_t tiles_x = (static_cast<uint32_t>(D.p.width) + kMapTX - 1) / kMapTX;
+    map_tile(D.depth, D.p, D.nmap, static_cast<int>(local % tiles_x) * kMapTX, static_cast<int>(local / tiles_x) * kMapTY,
+             tid, M);
     __syncthreads();
   }
 }
@@ -1120,15 +1137,16 @@ __global__ void __launch_bounds__(kThreads) batch_update_kernel(const SceneDesc*
         cur = sc;
         __syncthreads();
       }
-      // 1. prefix of one slot per thread, survivors appended to the queue
+        // 1. prefix of one slot per thread, survivors appended to the queue
       const unsigned long long i = static_cast<unsigned long long>(item - s_first[sc]) * kThreads + tid;
-      const uint32_t b = D.V.slot_block[D.V.visible[static_cast<uint32_t>(i >> 9)]];
+      const int4 vk = D.V.visible_keys[static_cast<uint32_t>(i >> 9)];
+      const uint32_t b = static_cast<uint32_t>(vk.w);
       const int li = static_cast<int>(i & 511U);
       bool pass = false;
       if (li == 0 && b != kInvalidBlock) D.V.block_stamp[b] = D.V.counters->frame;  // for incremental meshing
       f3 pc = mk3(0.0f, 0.0f, 0.0f);
       float u = 0.0f, v = 0.0f, d = 0.0f;
-      if (b != kInvalidBlock) pass = voxel_prefix(D.depth, D.p, D.V.block_keys[b], li, pc, u, v, d);
+      if (b != kInvalidBlock) pass = voxel_prefix(D.depth, D.p, vk, li, pc, u, v, d);
       const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
       uint32_t base = 0U;
       if (lane == 0 && ballot) {
@@ -1318,18 +1336,22 @@ cudaError_t launch_integrate_update(const float* depth, const Volume& V, const P
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s) {
-  static int grids[3] = {0, 0, 0};
+cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, bool band, cudaStream_t s) {
+  static int grids[4] = {0, 0, 0, 0};
   if (grids[0] == 0) {
-    grids[0] = grid_for(reinterpret_cast<const void*>(batch_filter_kernel), filt::kTX * filt::kTY);
-    grids[1] = grid_for(reinterpret_cast<const void*>(batch_stage2_kernel), alloc::kThreads);
-    grids[2] = grid_for(reinterpret_cast<const void*>(batch_update_kernel), kThreads);
+    grids[0] = grid_for(reinterpret_cast<const void*>(batch_filter_alloc_kernel<false>), filt::kTX * filt::kTY);
+    grids[1] = grid_for(reinterpret_cast<const void*>(batch_filter_alloc_kernel<true>), filt::kTX * filt::kTY);
+    grids[2] = grid_for(reinterpret_cast<const void*>(batch_map_kernel), kMapTX * kMapTY);
+    grids[3] = grid_for(reinterpret_cast<const void*>(batch_update_kernel), kThreads);
   }
-  cudaError_t e = cudaMemsetAsync(queue, 0, 3 * sizeof(uint32_t), s);
-  if (e != cudaSuccess) return e;
-  batch_filter_kernel<<<grids[0], filt::kTX * filt::kTY, 0, s>>>(descs, hdr, queue);
-  batch_stage2_kernel<<<grids[1], alloc::kThreads, 0, s>>>(descs, hdr, queue);
-  batch_update_kernel<<<grids[2], kThreads, 0, s>>>(descs, hdr, queue);
+  batch_begin_kernel<<<1, 256, 0, s>>>(descs, hdr, queue);
+  if (band) {
+    batch_filter_alloc_kernel<true><<<grids[1], filt::kTX * filt::kTY, 0, s>>>(descs, hdr, queue);
+  } else {
+    batch_filter_alloc_kernel<false><<<grids[0], filt::kTX * filt::kTY, 0, s>>>(descs, hdr, queue);
+  }
+  batch_map_kernel<<<grids[2], kMapTX * kMapTY, 0, s>>>(descs, hdr, queue);
+  batch_update_kernel<<<grids[3], kThreads, 0, s>>>(descs, hdr, queue);
   return cudaGetLastError();
 }
 

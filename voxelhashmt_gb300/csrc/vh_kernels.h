@@ -24,9 +24,9 @@ namespace exact {
 cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s);
 // starts a frame, then filters it and allocates its blocks in one kernel (out: the filtered depth)
 cudaError_t launch_filter_alloc(const float* in, float* out, const Volume& V, const Params& p, cudaStream_t s);
-// one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
-// scenes (queue: 3 counters, cleared here)
-cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);
+// one step of a multi-scene batch: filter + allocation, normal map, update, each a work-queue kernel over all
+// scenes (queue: 3 counters, cleared here); band: every scene uses the truncation-band allocation rule
+cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, bool band, cudaStream_t s);
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
@@ -43,9 +43,9 @@ namespace fast {
 cudaError_t launch_frame_filter(const float* in, float* out, const Params& p, Counters* begin_frame, cudaStream_t s);
 // starts a frame, then filters it and allocates its blocks in one kernel (out: the filtered depth)
 cudaError_t launch_filter_alloc(const float* in, float* out, const Volume& V, const Params& p, cudaStream_t s);
-// one step of a multi-scene batch: filter, allocation + normal map, update, each a work-queue kernel over all
-// scenes (queue: 3 counters, cleared here)
-cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, cudaStream_t s);
+// one step of a multi-scene batch: filter + allocation, normal map, update, each a work-queue kernel over all
+// scenes (queue: 3 counters, cleared here); band: every scene uses the truncation-band allocation rule
+cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, bool band, cudaStream_t s);
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
