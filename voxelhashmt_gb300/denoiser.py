@@ -200,3 +200,37 @@ def train(denoiser: DepthDenoiser, raws, targets, steps, batch=16, seed=0, log_e
     torch.cuda.synchronize()
     denoiser.check_error()
     return hist
+
+
+def _time_forward(frames=20, batch=1, seed=3):
+    """Forward passes of a seeded net over rendered 640x480 room frames: (ms per pass, batch)."""
+    import torch
+    from . import build, scenes
+    build.build()
+    torch.cuda.set_device(0)
+    sc = scenes.room_scene(seed=5, frames=4)
+    depth = render_frames(sc, torch)
+    net = DepthDenoiser(seed=seed)
+    x = depth[:1].repeat(batch, 1, 1) if batch > 1 else depth[:1]
+    for _ in range(3):
+        net.forward(x)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(frames):
+        net.forward(x if batch > 1 else depth[i % 4:i % 4 + 1])
+    e1.record()
+    torch.cuda.synchronize()
+    net.check_error()
+    return e0.elapsed_time(e1) / frames
+
+
+if __name__ == "__main__":
+    # python -m voxelhashmt_gb300.denoiser [--frames N] [--batch B]: time the net's forward pass
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--frames", type=int, default=20)
+    ap.add_argument("--batch", type=int, default=1)
+    a = ap.parse_args()
+    ms = _time_forward(a.frames, a.batch)
+    print("denoiser forward: %.4f ms per pass of %d 640x480 frame(s)" % (ms, a.batch))
