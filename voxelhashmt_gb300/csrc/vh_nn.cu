@@ -5,7 +5,8 @@
 // (tcgen05.mma, kind::f16 with BF16 operands, FP32 accumulator in tensor memory) as an implicit GEMM: one CTA
 // computes 128 consecutive output pixels of one image row x 32 output channels, M = 128, N = 32,
 // K = 9 taps x 32 input channels, issued as 18 MMAs of m128n32k16 into a TMEM accumulator (32 columns; two
-// accumulators and two staged tiles, so the loads, MMAs and epilogue of consecutive tiles overlap).
+// accumulators and a ring of staged tiles, filled, consumed and drained by separate warps, so the loads, MMAs
+// and epilogue of consecutive tiles overlap).
 // The three input rows the tile needs (130 pixels each, 1-pixel halo) are loaded by TMA (12 tensor-map boxes
 // of {8 channels, 130 pixels}, zero fill outside the image) into shared memory in the canonical no-swizzle
 // K-major layout: [row][channel group of 8][pixel][8 channels], 16 bytes per pixel per group (each group's
@@ -50,10 +51,17 @@ constexpr uint32_t kTileTxBytes = 3 * kGroups * kPlaneData;
 constexpr int kBBlock = 2 * kC * 16;       // one (tap, k-step) B operand: 2 groups x 32 rows x 16 B = 1,024
 constexpr int kBBytes = 18 * kBBlock;      // 18,432
 constexpr int kBPad = kBBytes + 1024;
-constexpr int kThreads = 128;              // 4 warps: one per 32 TMEM lanes
-constexpr int kSmem = 128 + 2 * kAPad + kBPad + 64;  // alignment slack, two A stages, B, 4 mbarriers, TMEM address
+// warps 0-3: epilogue (warp w owns TMEM lanes 32w..32w+31); warp 4: TMA producer; warp 5: TMEM owner, MMA issuer
+constexpr int kEpilogueWarps = 4;
+constexpr int kThreads = 32 * (kEpilogueWarps + 2);
+constexpr int kAccs = 2;  // accumulators in tensor memory (32 columns each)
 static_assert(kPlaneData <= kPlane && kPlane % 128 == 0 && kAPad % 128 == 0, "TMA destinations 128-byte aligned");
-constexpr int kCtasPerSm = 3;  // measured best of 1, 2, 3 (B = 16, 640 x 480: 583, 327, 278 us)
+// dynamic shared memory of a kStages-deep ring: alignment slack, the A stages, B, the mbarriers
+// (full / empty per stage, acc_full / acc_empty per accumulator) and the TMEM address
+template <int kStages>
+constexpr int smem_bytes() {
+  return 128 + kStages * kAPad + kBPad + 8 * (2 * kStages + 2 * kAccs) + 16;
+}
 constexpr uint32_t kMaxPolls = 1u << 24;
 constexpr unsigned int kErrorBit = 8u;  // the volume error word's timeout bit
 
@@ -135,9 +143,8 @@ __device__ __forceinline__ void load_tile(const CUtensorMap* map, uint32_t a_bas
   }
 }
 
-// the 18 MMAs of one tile: A from the staged rows at a_base, accumulator at tmem; completion arrives on bar
-__device__ __forceinline__ void issue_tile(uint32_t a_base, uint32_t b_base, uint32_t tmem, uint32_t bar) {
-  asm volatile("tcgen05.fence::after_thread_sync;\n");
+// the 18 MMAs of one tile: A from the staged rows at a_base, accumulator at tmem (accumulate from the first)
+__device__ __forceinline__ void issue_tile(uint32_t a_base, uint32_t b_base, uint32_t tmem) {
   int k = 0;
   for (int dy = 0; dy < 3; ++dy) {
     for (int dx = 0; dx < 3; ++dx) {
@@ -148,162 +155,199 @@ __device__ __forceinline__ void issue_tile(uint32_t a_base, uint32_t b_base, uin
       }
     }
   }
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
 }
 
 // One 32 -> 32 3x3 convolution over a batch of images (NHWC BF16, zero padding), tcgen05 implicit GEMM.
 // mode kForward: out = relu?(conv(in) + bias); mode kGrad: out = conv(in) * (mask > 0) (mask = the layer
 // input's activations; the input gradient of the previous layer's ReLU).
-// Pipeline over the CTA's tiles k = 0, 1, ... (tile blockIdx.x + k gridDim.x), two stages and two
-// accumulators: thread 0 keeps the TMA loads of tiles k+1 and k+2 in flight and issues the MMAs of tile k+1
-// while the four warps run the epilogue of tile k; no thread stages data.  Barriers: full[q] (TMA bytes of
-// the tile in stage q landed), done[q] (the MMAs reading stage q and writing accumulator q completed).
+//
+// Warp-specialised pipeline over the CTA's tiles k = 0, 1, ... (tile blockIdx.x + k gridDim.x), handing off
+// through mbarriers only:
+//   producer (warp 4, one lane): waits empty[s] (the MMAs of tile k - kStages released stage s), then TMA-loads
+//     tile k's three input rows into stage s = k mod kStages, completing full[s] by transaction bytes;
+//   MMA issuer (warp 5, one lane): waits full[s] and acc_empty[a] (the epilogue of tile k - kAccs has read
+//     accumulator a = k mod kAccs), issues the 18 MMAs, and commits them to empty[s] and acc_full[a];
+//   epilogue (warps 0-3): waits acc_full[a], reads its 32 TMEM lanes, releases the accumulator (acc_empty[a],
+//     one arrival per warp) and then applies bias / ReLU or the gradient mask and stores BF16.
+// Phase j of a barrier completes at its j-th use, so the waits for tile k use parity (k / kStages) & 1 or
+// (k / kAccs) & 1, and the releases of an earlier tile the parity before.  Every wait gives up after a bounded
+// number of polls: that role stops, the error word gets the timeout bit, and the roles waiting on it give up
+// in turn; before tensor memory is freed, the loads and MMA groups still in flight are waited for (bounded).
+template <int kStages>
 __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_constant__ CUtensorMap in_map,
-                                                             const __nv_bfloat16* __restrict__ wpack,
-                                                             const float* __restrict__ bias,
-                                                             const __nv_bfloat16* __restrict__ mask,
-                                                             __nv_bfloat16* __restrict__ out, int batch, int width,
-                                                             int height, int mode, int relu,
-                                                             unsigned int* __restrict__ error) {
+                                                                const __nv_bfloat16* __restrict__ wpack,
+                                                                const float* __restrict__ bias,
+                                                                const __nv_bfloat16* __restrict__ mask,
+                                                                __nv_bfloat16* __restrict__ out, int batch, int width,
+                                                                int height, int mode, int relu,
+                                                                unsigned int* __restrict__ error) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA destinations: 128 B
-  unsigned char* sA[2] = {smem, smem + kAPad};
-  unsigned char* sB = smem + 2 * kAPad;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(sB + kBPad);  // full[0], full[1], done[0], done[1]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sB + kBPad + 32);
+  unsigned char* sB = smem + kStages * kAPad;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kBPad);  // full[S], empty[S], acc_full[A], acc_empty[A]
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 2 * kAccs);
+  uint32_t* consumed = tmem_slot + 1;  // tiles whose loads the MMA issuer has waited for (teardown)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   // weights: [tap][ks][g][co][8] BF16, 18,432 bytes, already packed in this order in global memory
   for (int i = tid; i < kBBytes / 16; i += kThreads) {
     reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(wpack)[i];
   }
-  for (int q = 0; q < 2; ++q) {
+  for (int q = 0; q < kStages; ++q) {
     for (int i = tid; i < (kAPad - kABytes) / 16; i += kThreads) {
-      reinterpret_cast<uint4*>(sA[q] + kABytes)[i] = make_uint4(0, 0, 0, 0);
+      reinterpret_cast<uint4*>(smem + q * kAPad + kABytes)[i] = make_uint4(0, 0, 0, 0);
     }
   }
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the weights, for the MMAs' async reads
-  if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 64;\n" ::"r"(smem_u32(tmem_slot)));
+  if (warp == kEpilogueWarps + 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(32 * kAccs));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
   if (tid == 0) {
-    for (int i = 0; i < 4; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bar[i])));
+    for (int i = 0; i < 2 * kStages + kAccs; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bars[i])));
+    }
+    for (int i = 0; i < kAccs; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&bars[2 * kStages + kAccs + i])),
+                   "r"(kEpilogueWarps));
+    }
+    *consumed = 0u;
     asm volatile("fence.mbarrier_init.release.cluster;\n");
-    asm volatile("prefetch.tensormap [%0];\n" ::"l"(reinterpret_cast<uint64_t>(&in_map)) : "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n");
-  const uint32_t tmem = *tmem_slot;  // accumulator q at columns 32 q
-  const uint32_t a_base[2] = {smem_u32(sA[0]), smem_u32(sA[1])};
-  const uint32_t b_base = smem_u32(sB);
-  const uint32_t full[2] = {smem_u32(&bar[0]), smem_u32(&bar[1])};
-  const uint32_t done[2] = {smem_u32(&bar[2]), smem_u32(&bar[3])};
+  const uint32_t tmem = *tmem_slot;  // accumulator a at columns 32 a
+  const uint32_t a_base0 = smem_u32(smem), b_base = smem_u32(sB);
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[kStages]);
+  const uint32_t accf0 = smem_u32(&bars[2 * kStages]), acce0 = smem_u32(&bars[2 * kStages + kAccs]);
 
-  const int tiles_x = (width + kTile - 1) / kTile;
-  const long long ntiles = static_cast<long long>(batch) * height * tiles_x;
-  const long long stride = gridDim.x;
-  auto coords = [&](long long t, int& img, int& y, int& x0) {
-    x0 = static_cast<int>(t % tiles_x) * kTile;
-    const long long rest = t / tiles_x;
-    y = static_cast<int>(rest % height);
-    img = static_cast<int>(rest / height);
+  // tile t = blockIdx.x + k gridDim.x of the CTA; the launcher guarantees that the tile count fits in 31 bits,
+  // so the coordinates take two 32-bit divisions (64-bit ones cost hundreds of instructions per tile)
+  const uint32_t tiles_x = static_cast<uint32_t>((width + kTile - 1) / kTile);
+  const uint32_t ntiles = static_cast<uint32_t>(batch) * static_cast<uint32_t>(height) * tiles_x;
+  const uint32_t stride = gridDim.x;
+  const int my_tiles = blockIdx.x < ntiles ? static_cast<int>((ntiles - 1u - blockIdx.x) / stride + 1u) : 0;
+  auto coords = [&](int k, int& img, int& y, int& x0) {
+    const uint32_t t = blockIdx.x + static_cast<uint32_t>(k) * stride;
+    const uint32_t row = t / tiles_x;
+    x0 = static_cast<int>(t - row * tiles_x) * kTile;
+    const uint32_t im = row / static_cast<uint32_t>(height);
+    y = static_cast<int>(row - im * static_cast<uint32_t>(height));
+    img = static_cast<int>(im);
   };
-  // phases of the barriers; loading / pending: a TMA load / an MMA group in flight (thread 0's view)
-  uint32_t fphase[2] = {0u, 0u}, dphase[2] = {0u, 0u};
-  bool loading[2] = {false, false}, pending[2] = {false, false};
-  bool mine = true;
-  if (tid == 0) {  // prologue: loads of tiles 0 and 1, MMAs of tile 0
-    for (int q = 0; q < 2; ++q) {
-      const long long t = blockIdx.x + q * stride;
-      if (t < ntiles) {
-        int img, y, x0;
-        coords(t, img, y, x0);
-        load_tile(&in_map, a_base[q], full[q], img, y, x0);
-        loading[q] = true;
-      }
-    }
-    if (loading[0]) {
-      if (mbar_wait(full[0], fphase[0])) {
-        fphase[0] ^= 1u;
-        loading[0] = false;
-        issue_tile(a_base[0], b_base, tmem, done[0]);
-        pending[0] = true;
-      } else {
-        mine = false;
-      }
-    }
-  }
-  bool ok = __syncthreads_and(mine ? 1 : 0) != 0;
-  for (long long k = 0, t = blockIdx.x; ok && t < ntiles; ++k, t += stride) {
-    // stage / accumulator q of this tile and nq of the next; selects, not indexing, keep the pairs in registers
-    const bool odd = (k & 1) != 0;
-    const uint32_t q = odd ? 1u : 0u, nq = q ^ 1u;
-    mine = true;
-    if (tid == 0 && t + stride < ntiles) {  // MMAs of the next tile, whose rows are landing in stage nq
-      if (mbar_wait(odd ? full[0] : full[1], odd ? fphase[0] : fphase[1])) {
-        if (odd) { fphase[0] ^= 1u; loading[0] = false; } else { fphase[1] ^= 1u; loading[1] = false; }
-        issue_tile(odd ? a_base[0] : a_base[1], b_base, tmem + 32u * nq, odd ? done[0] : done[1]);
-        if (odd) pending[0] = true; else pending[1] = true;
-      } else {
-        mine = false;
-      }
-    }
-    // every thread polls; the CTA continues only if all saw tile t complete (uniform branch)
-    mine = mbar_wait(odd ? done[1] : done[0], odd ? dphase[1] : dphase[0]) && mine;
-    ok = __syncthreads_and(mine ? 1 : 0) != 0;
-    if (!ok) break;
-    if (odd) { dphase[1] ^= 1u; pending[1] = false; } else { dphase[0] ^= 1u; pending[0] = false; }
-    asm volatile("tcgen05.fence::after_thread_sync;\n");
-    if (tid == 0 && t + 2 * stride < ntiles) {  // stage q is free again: load tile k+2 into it
-      int img, y, x0;
-      coords(t + 2 * stride, img, y, x0);
-      load_tile(&in_map, odd ? a_base[1] : a_base[0], odd ? full[1] : full[0], img, y, x0);
-      if (odd) loading[1] = true; else loading[0] = true;
-    }
-    // epilogue of tile t: warp w, lane l = output pixel 32w + l
-    int img, y, x0;
-    coords(t, img, y, x0);
-    float acc[32];
-    tmem_ld32(tmem + 32u * q + (static_cast<uint32_t>(warp * 32) << 16), acc);
-    const int x = x0 + warp * 32 + lane;
-    if (x < width) {
-      const size_t o = ((static_cast<size_t>(img) * height + y) * width + x) * kC;
-      __align__(16) __nv_bfloat16 res[32];
-      if (mode == kForward) {
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          float v = acc[c] + (bias ? bias[c] : 0.0f);
-          if (relu) v = fmaxf(v, 0.0f);
-          res[c] = __float2bfloat16_rn(v);
+  bool ok = true;
+  int issued = 0;  // producer: tiles loaded; MMA issuer: tiles whose MMAs were issued
+
+  if (warp == kEpilogueWarps) {
+    if (lane == 0) {  // producer
+      for (int k = 0; k < my_tiles; ++k) {
+        const int st = k % kStages;
+        if (k >= kStages && !mbar_wait(empty0 + 8 * st, static_cast<uint32_t>((k / kStages - 1) & 1))) {
+          ok = false;
+          break;
         }
-      } else {
-        __align__(16) __nv_bfloat16 m[32];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(m)[u] = reinterpret_cast<const uint4*>(mask + o)[u];
-#pragma unroll
-        for (int c = 0; c < 32; ++c) res[c] = __float2bfloat16_rn(__bfloat162float(m[c]) > 0.0f ? acc[c] : 0.0f);
+        int img, y, x0;
+        coords(k, img, y, x0);
+        load_tile(&in_map, a_base0 + st * kAPad, full0 + 8 * st, img, y, x0);
+        issued = k + 1;
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(out + o)[u] = reinterpret_cast<const uint4*>(res)[u];
     }
-    // accumulator q is written again by the MMAs of tile k+2, issued after this barrier
-    asm volatile("tcgen05.fence::before_thread_sync;\n");
-    __syncthreads();
+  } else if (warp == kEpilogueWarps + 1) {
+    if (lane == 0) {  // MMA issuer
+      for (int k = 0; k < my_tiles; ++k) {
+        const int st = k % kStages, a = k % kAccs;
+        if (!mbar_wait(full0 + 8 * st, static_cast<uint32_t>((k / kStages) & 1))) {
+          ok = false;
+          break;
+        }
+        *reinterpret_cast<volatile uint32_t*>(consumed) = static_cast<uint32_t>(k + 1);
+        if (k >= kAccs && !mbar_wait(acce0 + 8 * a, static_cast<uint32_t>((k / kAccs - 1) & 1))) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        issue_tile(a_base0 + st * kAPad, b_base, tmem + 32u * a);
+        commit(empty0 + 8 * st);
+        commit(accf0 + 8 * a);
+        issued = k + 1;
+      }
+    }
+  } else {  // epilogue: warp w, lane l = output pixel 32w + l of the tile
+    float bv[32];  // the layer's bias, in registers for the whole launch
+#pragma unroll
+    for (int c = 0; c < 32; ++c) bv[c] = (mode == kForward && bias) ? __ldg(&bias[c]) : 0.0f;
+    for (int k = 0; k < my_tiles; ++k) {
+      const int a = k % kAccs;
+      const bool got = mbar_wait(accf0 + 8 * a, static_cast<uint32_t>((k / kAccs) & 1));
+      if (!__all_sync(0xffffffffu, got)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n");
+      float acc[32];
+      tmem_ld32(tmem + 32u * a + (static_cast<uint32_t>(warp * 32) << 16), acc);
+      asm volatile("tcgen05.fence::before_thread_sync;\n");
+      __syncwarp();
+      if (lane == 0) arrive(acce0 + 8 * a);  // the accumulator may be overwritten by tile k + kAccs
+      int img, y, x0;
+      coords(k, img, y, x0);
+      const int x = x0 + warp * 32 + lane;
+      if (x < width) {
+        const size_t o = ((static_cast<size_t>(img) * height + y) * width + x) * kC;
+        __align__(16) __nv_bfloat162 res[16];
+        if (mode == kForward) {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            float v0 = acc[2 * c] + bv[2 * c], v1 = acc[2 * c + 1] + bv[2 * c + 1];
+            if (relu) {
+              v0 = fmaxf(v0, 0.0f);
+              v1 = fmaxf(v1, 0.0f);
+            }
+            res[c] = __floats2bfloat162_rn(v0, v1);
+          }
+        } else {
+          __align__(16) __nv_bfloat162 m[16];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(m)[u] = reinterpret_cast<const uint4*>(mask + o)[u];
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const float2 mf = __bfloat1622float2(m[c]);
+            res[c] = __floats2bfloat162_rn(mf.x > 0.0f ? acc[2 * c] : 0.0f, mf.y > 0.0f ? acc[2 * c + 1] : 0.0f);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(out + o)[u] = reinterpret_cast<const uint4*>(res)[u];
+      }
+    }
   }
-  if (!ok && tid == 0) {
-    atomicOr(error, kErrorBit);
-    // the TMA loads and MMA groups still in flight, bounded
-#pragma unroll
-    for (int q = 0; q < 2; ++q) {
-      if (pending[q]) mbar_wait(done[q], dphase[q]);
-      if (loading[q]) mbar_wait(full[q], fphase[q]);
+  if (!ok && lane == 0) atomicOr(error, kErrorBit);
+  __syncthreads();
+  // in-flight work after a timeout (the waits return at once when nothing is pending): the producer waits for
+  // the loads nobody consumed, the MMA issuer for its last MMA group
+  if (warp == kEpilogueWarps && lane == 0) {
+    for (int k = static_cast<int>(*consumed); k < issued; ++k) {
+      mbar_wait(full0 + 8 * (k % kStages), static_cast<uint32_t>((k / kStages) & 1));
     }
+  }
+  if (warp == kEpilogueWarps + 1 && lane == 0 && issued > 0) {
+    mbar_wait(accf0 + 8 * ((issued - 1) % kAccs), static_cast<uint32_t>(((issued - 1) / kAccs) & 1));
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 64;\n" ::"r"(tmem));
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  if (warp == kEpilogueWarps + 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(32 * kAccs));
+  }
 }
 
 // cuTensorMapEncodeTiled, resolved through the runtime's driver entry point (no link dependency on libcuda)
@@ -335,41 +379,61 @@ cudaError_t encode_input_map(const __nv_bfloat16* in, int batch, int width, int 
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
+// Launch shapes of conv32_tc_kernel: ring depth and resident CTAs per SM (both CTAs' rings fit in one SM's
+// shared memory when two are resident)
+struct Conv32Variant {
+  const void* fn;
+  int stages, smem, ctas_per_sm;
+};
+const Conv32Variant kConv32Variants[] = {
+    {reinterpret_cast<const void*>(conv32_tc_kernel<3>), 3, smem_bytes<3>(), 2},
+    {reinterpret_cast<const void*>(conv32_tc_kernel<4>), 4, smem_bytes<4>(), 1},
+    {reinterpret_cast<const void*>(conv32_tc_kernel<6>), 6, smem_bytes<6>(), 1},
+};
+// measured (640x480, batch 1 / batch 16): 3 stages x 2 CTAs 24.8 / 294 us, 4 x 1 22.8 / 277 us, 6 x 1 24.9 / 293 us;
+// VH_CONV32_VARIANT selects another for launch-shape sweeps
+constexpr int kConv32Default = 1;
+
+const Conv32Variant& conv32_variant() {
+  static int v = -1;
+  if (v < 0) {
+    v = kConv32Default;
+    if (const char* env = std::getenv("VH_CONV32_VARIANT")) {
+      const int x = std::atoi(env);
+      if (x >= 0 && x < static_cast<int>(sizeof(kConv32Variants) / sizeof(kConv32Variants[0]))) v = x;
+    }
+  }
+  return kConv32Variants[v];
+}
+
 }  // namespace
 
-int conv32_smem_bytes() { return kSmem; }
+int conv32_smem_bytes() { return conv32_variant().smem; }
 
 cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, const float* bias,
                           const __nv_bfloat16* mask, __nv_bfloat16* out, int batch, int width, int height, int mode,
                           int relu, unsigned int* error, cudaStream_t s) {
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(conv32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
-  // persistent CTAs, kCtasPerSm per SM (VH_CONV32_CTAS_PER_SM overrides it for launch-shape sweeps): each
-  // CTA stages the weights and allocates tensor memory once and pipelines its tiles
+  const Conv32Variant& cv = conv32_variant();
+  // persistent CTAs, cv.ctas_per_sm per SM: each CTA stages the weights and allocates tensor memory once
   static int ctas = 0;
   if (ctas == 0) {
+    cudaError_t e = cudaFuncSetAttribute(cv.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, cv.smem);
+    if (e != cudaSuccess) return e;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int per_sm = kCtasPerSm;
-    if (const char* env = std::getenv("VH_CONV32_CTAS_PER_SM")) {
-      const int v = std::atoi(env);
-      if (v >= 1 && v <= 3) per_sm = v;  // three stages of kSmem fit in one SM's shared memory
-    }
-    ctas = per_sm * (sms > 0 ? sms : 152);
+    ctas = cv.ctas_per_sm * (sms > 0 ? sms : 152);
   }
   const long long ntiles = static_cast<long long>(batch) * height * ((width + kTile - 1) / kTile);
+  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;  // the kernel's tile arithmetic is 32-bit
   const int grid = static_cast<int>(ntiles < ctas ? ntiles : ctas);
   if (grid <= 0) return cudaSuccess;
   CUtensorMap map;
   const cudaError_t e = encode_input_map(in, batch, width, height, &map);
   if (e != cudaSuccess) return e;
-  conv32_tc_kernel<<<grid, kThreads, kSmem, s>>>(map, wpack, bias, mask, out, batch, width, height, mode, relu, error);
-  return cudaGetLastError();
+  void* args[] = {&map,    const_cast<__nv_bfloat16**>(&wpack), const_cast<float**>(&bias),
+                  const_cast<__nv_bfloat16**>(&mask), &out, &batch, &width, &height, &mode, &relu, &error};
+  return cudaLaunchKernel(cv.fn, dim3(grid), dim3(kThreads), args, static_cast<size_t>(cv.smem), s);
 }
 
 // Packs 32 x 32 x 3 x 3 FP32 weights w[co][ci][ky][kx] (transpose_flip: the input-gradient form, w'[ci][co][2-ky][2-kx])
