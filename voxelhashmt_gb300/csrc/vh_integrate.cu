@@ -506,9 +506,11 @@ __device__ __forceinline__ bool integrate_bin16(const Params& p, const Volume& V
     ls[a] = sw ? ls[b] : ls[a];
     ls[b] = sw ? t : ls[b];
   };
-  step(0, 1);
-  step(1, 2);
-  step(0, 1);
+  if (w16[1] != 0U || w16[2] != 0U) {  // with at most layer 0 observed the network swaps nothing
+    step(0, 1);
+    step(1, 2);
+    step(0, 1);
+  }
   A = make_uint4(w16[0] | (s16[0] << 16), p16[0] | (w16[1] << 16), s16[1] | (p16[1] << 16), w16[2] | (s16[2] << 16));
   B = make_uint4(p16[2], w16[0] ? nk[0] : 0U, w16[1] ? nk[1] : 0U, w16[2] ? nk[2] : 0U);
   return true;

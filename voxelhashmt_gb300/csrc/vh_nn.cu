@@ -559,7 +559,10 @@ __device__ __forceinline__ void load32(const __nv_bfloat16* p, float* v) {
 }
 
 // layer 4: 32 -> 1 residual, depth' = d + r / 100 on valid pixels; weights staged tap-major (sw[t][c]) and
-// read as float4
+// read as float4.  Four lanes per pixel, lane q = lane % 4 summing channels 8q..8q+7 over the taps: a warp
+// covers 8 consecutive pixels, so its 16-byte loads of their 64-byte channel vectors are contiguous, and the
+// 9 taps' loads are issued together.  The pixel's four lanes then add their sums; the loop runs over
+// warp-sized groups of 8 pixels so that every lane takes part in the shuffles.
 __global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __restrict__ A3,
                                                        const float* __restrict__ params,
                                                        const float* __restrict__ depth,
@@ -574,25 +577,30 @@ __global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __re
   if (threadIdx.x == 0) sb = params[kOffB4];
   __syncthreads();
   const long long n = static_cast<long long>(batch) * w * h;
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const float d = depth[i];
-    if (!(d > 0.0f)) {
-      out[i] = 0.0f;
-      continue;
-    }
-    const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
-    const long long img = i / (static_cast<long long>(w) * h);
-    float r = sb;
-#pragma unroll 1
-    for (int t = 0; t < 9; ++t) {
-      const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
-      if (!inside(sx, sy, w, h)) continue;
-      const uint4* src = reinterpret_cast<const uint4*>(A3 + ((img * h + sy) * w + sx) * kC);
+  const int lane = threadIdx.x & 31, q = lane & 3;
+  const long long warps = static_cast<long long>(gridDim.x) * (blockDim.x >> 5);
+  for (long long base = (blockIdx.x * static_cast<long long>(blockDim.x >> 5) + (threadIdx.x >> 5)) * 8; base < n;
+       base += warps * 8) {
+    const long long i = base + (lane >> 2);
+    const float d = i < n ? depth[i] : 0.0f;
+    float r = 0.0f;
+    if (d > 0.0f) {
+      const uint32_t i32 = static_cast<uint32_t>(i), row = i32 / static_cast<uint32_t>(w);  // 32-bit, as in conv_in
+      const int x = static_cast<int>(i32 - row * static_cast<uint32_t>(w));
+      const uint32_t im = row / static_cast<uint32_t>(h);
+      const int y = static_cast<int>(row - im * static_cast<uint32_t>(h));
+      const long long img = im;
+      // the 9 taps' loads are issued together (zero outside the image, which adds nothing), then used
+      uint4 raw9[9];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {  // 8 channels per 16-byte load
-        const uint4 raw = src[q];
-        const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&raw);
+      for (int t = 0; t < 9; ++t) {
+        const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
+        raw9[t] = inside(sx, sy, w, h) ? *reinterpret_cast<const uint4*>(A3 + ((img * h + sy) * w + sx) * kC + 8 * q)
+                                       : make_uint4(0, 0, 0, 0);
+      }
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&raw9[t]);
         const float4 wa = sw4[t][2 * q], wb = sw4[t][2 * q + 1];
         const float2 a0 = __bfloat1622float2(b2[0]), a1 = __bfloat1622float2(b2[1]);
         const float2 a2 = __bfloat1622float2(b2[2]), a3 = __bfloat1622float2(b2[3]);
@@ -600,8 +608,16 @@ __global__ void __launch_bounds__(256) conv_out_kernel(const __nv_bfloat16* __re
              wb.w * a3.y;
       }
     }
-    const float corr = r * kInvScale;
-    out[i] = (fallback && fabsf(corr) > gate(d)) ? fallback[i] : fmaxf(d + corr, 0.0f);
+    r += __shfl_xor_sync(0xffffffffU, r, 1);
+    r += __shfl_xor_sync(0xffffffffU, r, 2);
+    if (q == 0 && i < n) {
+      if (!(d > 0.0f)) {
+        out[i] = 0.0f;
+      } else {
+        const float corr = (sb + r) * kInvScale;
+        out[i] = (fallback && fabsf(corr) > gate(d)) ? fallback[i] : fmaxf(d + corr, 0.0f);
+      }
+    }
   }
 }
 
@@ -791,6 +807,7 @@ cudaError_t forward(const float* params, const __nv_bfloat16* packed, const floa
                     float* out, int batch, int width, int height, unsigned char* ws, unsigned int* error,
                     cudaStream_t s) {
   const size_t n = static_cast<size_t>(batch) * width * height;
+  if (n > 0x7fffffffULL) return cudaErrorInvalidValue;  // the layers' pixel arithmetic is 32-bit
   float4* X;
   __nv_bfloat16 *A1, *A2, *A3, *G1, *G2;
   float* r;
