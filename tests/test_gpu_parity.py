@@ -140,9 +140,12 @@ def test_integrate_bit_exact(env, small_orbit):
     vol.close()
 
 
-def test_integrate_stride_and_device_input(env, small_orbit):
+@pytest.mark.parametrize("stride", [2, 3])
+def test_integrate_stride_and_device_input(env, small_orbit, stride):
+    """Strided sampling through the fused filter + allocation kernel (samples are the pixels whose coordinates
+    are multiples of the stride, inside each 32x8 filter tile), bit-identical to the oracle."""
     backend, O = env
-    vol, ora = _integrate_both(backend, O, small_orbit, frames=[2, 9], stride=2, device_input=True)
+    vol, ora = _integrate_both(backend, O, small_orbit, frames=[2, 9], stride=stride, device_input=True)
     gk, gv = O.sort_blocks(*vol.export_blocks())
     ok_, ov = O.sort_blocks(*ora.blocks())
     assert np.array_equal(gk, ok_)
