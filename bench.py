@@ -495,7 +495,12 @@ def run_gb300(args):
             "config": dict(workload_config(sc, args.steps, args.warmup), form=FORM_NOTE[args.form]),
             "mc_blocks_per_s": round(head["mc_blocks_per_s"], 1),
             "e2e": {"value": round(head["e2e_value"], 3), "unit": "Mpix/s", "h2d_bytes_per_step": px * 4,
-                    "d2h_bytes_per_step": 64},
+                    "d2h_bytes_per_step": 64,
+                    "note": "wall clock over back-to-back frames through TsdfIntegrationBackend.integrate from "
+                            "pinned host depth (the copy of frame k+1 overlaps frame k's kernels) with the 64-byte "
+                            "statistics read per frame; no L2 flush between frames: each frame's layer update "
+                            "alone moves about 230 MB of DRAM (ncu), more than the 129 MB L2, so consecutive "
+                            "frames reuse only part of it"},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": head["clocks"],
             "gpu_launches": args.steps * 4,
             args.form: summary(head, args.form), other: summary(res[other], other),

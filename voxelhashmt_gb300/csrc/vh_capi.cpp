@@ -23,6 +23,16 @@ struct vh_volume {
   vh::Volume dev{};
   vh::Counters* h_counters = nullptr;  // pinned mirror for read-back
   float* d_depth_in = nullptr;
+  // vh_integrate's host depth is staged through two device buffers filled on an internal copy stream: the copy
+  // of the next frame overlaps this frame's kernels.  stage_copied[k]: buffer k holds its frame; stage_free[k]:
+  // the kernels that read buffer k are done (recorded once stage_used[k]).
+  float* d_depth_stage[2] = {nullptr, nullptr};
+  size_t stage_capacity = 0;  // pixels
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t stage_copied[2] = {nullptr, nullptr};
+  cudaEvent_t stage_free[2] = {nullptr, nullptr};
+  bool stage_used[2] = {false, false};
+  int stage_next = 0;
   float* d_depth_filtered = nullptr;
   float4* d_normal_map = nullptr;  // per-pixel normals (vh_algorithm.normal_mode 1)
   // learned depth denoiser (vh_algorithm.depth_filter 1)
@@ -203,6 +213,51 @@ vh_status stage_depth(vh_volume* v, const float* depth, int on_device, const vh_
     VH_CUDA(v, cudaMemcpyAsync(v->d_depth_in, depth, pixels * sizeof(float), cudaMemcpyHostToDevice, s));
     *src = v->d_depth_in;
   }
+  return VH_OK;
+}
+
+// vh_integrate's staging of host depth (see vh_volume::d_depth_stage): the copy runs on the copy stream into
+// the buffer whose last readers have finished, and stream s waits for it.  *slot: the buffer, whose readers
+// record stage_free[*slot] on s when they have been enqueued (stage_release).
+vh_status stage_depth_overlapped(vh_volume* v, const float* depth, const vh_intrinsics* K, cudaStream_t s,
+                                 const float** src, int* slot) {
+  const size_t pixels = static_cast<size_t>(K->width) * static_cast<size_t>(K->height);
+  const vh_status st = ensure_depth(v, pixels);
+  if (st != VH_OK) return st;
+  if (!v->copy_stream) {
+    VH_CUDA(v, cudaStreamCreateWithFlags(&v->copy_stream, cudaStreamNonBlocking));
+    for (int k = 0; k < 2; ++k) {
+      VH_CUDA(v, cudaEventCreateWithFlags(&v->stage_copied[k], cudaEventDisableTiming));
+      VH_CUDA(v, cudaEventCreateWithFlags(&v->stage_free[k], cudaEventDisableTiming));
+    }
+  }
+  if (pixels > v->stage_capacity) {
+    for (int k = 0; k < 2; ++k) {
+      if (v->stage_used[k]) VH_CUDA(v, cudaEventSynchronize(v->stage_free[k]));
+      dfree(v->d_depth_stage[k]);
+    }
+    VH_CUDA(v, cudaStreamSynchronize(v->copy_stream));
+    v->stage_capacity = 0;
+    for (int k = 0; k < 2; ++k) VH_CUDA(v, dalloc(&v->d_depth_stage[k], pixels));
+    v->stage_capacity = pixels;
+  }
+  const int k = v->stage_next;
+  v->stage_next ^= 1;
+  if (v->stage_used[k]) VH_CUDA(v, cudaStreamWaitEvent(v->copy_stream, v->stage_free[k], 0));
+  VH_CUDA(v, cudaMemcpyAsync(v->d_depth_stage[k], depth, pixels * sizeof(float), cudaMemcpyHostToDevice,
+                             v->copy_stream));
+  VH_CUDA(v, cudaEventRecord(v->stage_copied[k], v->copy_stream));
+  VH_CUDA(v, cudaStreamWaitEvent(s, v->stage_copied[k], 0));
+  *src = v->d_depth_stage[k];
+  *slot = k;
+  return VH_OK;
+}
+
+// the kernels reading staging buffer slot (all enqueued on s) are done when s reaches this point
+vh_status stage_release(vh_volume* v, int slot, cudaStream_t s) {
+  if (slot < 0) return VH_OK;
+  VH_CUDA(v, cudaEventRecord(v->stage_free[slot], s));
+  v->stage_used[slot] = true;
   return VH_OK;
 }
 
@@ -454,6 +509,15 @@ void vh_destroy(vh_volume* v) {
   dfree(V.counters);
   if (v->h_counters) cudaFreeHost(v->h_counters);
   dfree(v->d_depth_in);
+  if (v->copy_stream) {
+    cudaStreamSynchronize(v->copy_stream);
+    cudaStreamDestroy(v->copy_stream);
+  }
+  for (int k = 0; k < 2; ++k) {
+    dfree(v->d_depth_stage[k]);
+    if (v->stage_copied[k]) cudaEventDestroy(v->stage_copied[k]);
+    if (v->stage_free[k]) cudaEventDestroy(v->stage_free[k]);
+  }
   dfree(v->d_depth_filtered);
   dfree(v->d_normal_map);
   dfree(v->d_nn_params);
@@ -518,7 +582,9 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
   DeviceGuard guard(v->params.device);
   const cudaStream_t s = as_stream(stream);
   const float* src = nullptr;
-  vh_status st = stage_depth(v, depth, on_device, K, s, &src);
+  int slot = -1;  // staging buffer of host depth
+  vh_status st = on_device ? stage_depth(v, depth, on_device, K, s, &src)
+                           : stage_depth_overlapped(v, depth, K, s, &src, &slot);
   if (st != VH_OK) return st;
   const vh::Params p = make_params(v, K, T_wc, stride);
   std::vector<cudaEvent_t> ev;
@@ -547,12 +613,16 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
     VH_CUDA(v, frame_filter(v, src, v->d_depth_bilateral, p, s));
     VH_CUDA(v, vh::nn::forward(v->d_nn_params, v->d_nn_packed, src, v->d_depth_bilateral, v->d_depth_filtered, 1,
                                K->width, K->height, v->d_nn_ws, &v->dev.counters->error, s));
+    st = stage_release(v, slot, s);  // the raw depth's last readers
+    if (st != VH_OK) return st;
     if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
     VH_CUDA(v, vh::launch_alloc(v->d_depth_filtered, v->dev, p, s));
   } else {
     // the bilateral filter and the allocation in one kernel: the profile's allocation stage is then empty
     VH_CUDA(v, v->algo.fast_math ? vh::fast::launch_filter_alloc(src, v->d_depth_filtered, v->dev, p, s)
                                   : vh::exact::launch_filter_alloc(src, v->d_depth_filtered, v->dev, p, s));
+    st = stage_release(v, slot, s);  // the raw depth's last reader
+    if (st != VH_OK) return st;
     if (v->profile) VH_CUDA(v, cudaEventRecord(ev[1], s));
   }
   if (v->profile) VH_CUDA(v, cudaEventRecord(ev[2], s));
