@@ -153,6 +153,39 @@ def test_integrate_stride_and_device_input(env, small_orbit, stride):
     vol.close()
 
 
+def test_pinned_host_frames_back_to_back_match_device_input(env, small_orbit):
+    """Host depth is staged through two device buffers on an internal copy stream (the copy of the next frame
+    overlaps this frame's kernels).  Frames enqueued back to back from pinned host memory, without a
+    synchronisation in between, fuse into the same volume, bit for bit, as the same frames from device memory;
+    seven frames through the two buffers make every buffer wait for its previous readers."""
+    backend, _ = env
+    from voxelhashmt_gb300 import scenes
+    sc = small_orbit
+    frames = [0, 3, 6, 9, 12, 15, 18]
+    depths = [scenes.render_depth(sc, f) for f in frames]
+    pinned = torch.empty((len(frames),) + depths[0].shape, dtype=torch.float32, pin_memory=True)
+    for k, d in enumerate(depths):
+        pinned[k].copy_(torch.from_numpy(d))
+    bk = backend.TsdfIntegrationBackend("gpu")
+    host_vol, dev_vol = _volume(backend, sc), _volume(backend, sc)
+    for k, f in enumerate(frames):
+        bk.integrate(host_vol, backend.DepthFrame(sc.intrinsics, pinned[k].numpy()), sc.poses[f], 1,
+                     synchronize=False)
+    host_vol.synchronize()
+    for k, f in enumerate(frames):
+        bk.integrate(dev_vol, backend.DepthFrame(sc.intrinsics, _dev(depths[k])), sc.poses[f], 1)
+    hk, hv = _sorted_blocks(env, host_vol)
+    dk, dv = _sorted_blocks(env, dev_vol)
+    assert hk.shape[0] > 0
+    assert np.array_equal(hk, dk) and np.array_equal(hv, dv)
+    host_vol.close()
+    dev_vol.close()
+
+
+def _sorted_blocks(env, vol):
+    return env[1].sort_blocks(*vol.export_blocks())
+
+
 def test_mesh_bit_exact_and_deterministic(env, small_orbit):
     backend, O = env
     vol, ora = _integrate_both(backend, O, small_orbit, frames=[0, 4, 8, 12, 16, 20])
