@@ -17,6 +17,13 @@
 // float coordinates, so the 21 distinct samples are computed once and reused; the result is bit-identical.
 // Otherwise (u or v within 2 of a power of two, or below 1) the literal 50-sample sequence runs.
 //
+// The per-pixel normal-map form (Params::normal_mode 1) runs map_prepare_kernel (the normal map once per
+// pixel, plus the visible list's {block key, pool index} entries) and fused_update_kernel (prefix, a
+// shared-memory queue of the survivors and their update with the bilinearly interpolated map normal, from a
+// device work queue of voxel-slot chunks).  filter_alloc_kernel filters a frame's depth and allocates its
+// blocks tile by tile in one pass, and the batch_* kernels run the same device code as work-queue kernels
+// over many volumes.
+//
 // The file is compiled twice: as vh::exact (the bit-reproducible FP32 form: -fmad=false, IEEE division and
 // square root, vh_expf) and, with VH_FAST_MATH, as vh::fast (fused multiply-adds, approximate division, square
 // root and exponential; selected per volume by vh_algorithm.fast_math).
@@ -1273,7 +1280,8 @@ cudaError_t launch_pixel_normals(const float* depth, const Params& p, float4* nm
   return cudaGetLastError();
 }
 
-// first kernel of the update: the active-voxel list (classify_kernel) or the per-pixel normal map
+// first kernel of the update: the active-voxel list (classify_kernel) or the per-pixel normal map with the
+// visible-list keys (map_prepare_kernel)
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
                                      cudaStream_t s) {
   if (p.normal_mode == 1) {
