@@ -2,29 +2,28 @@
 // -> 32 -> 32 -> 1, ReLU between layers, residual output), BF16 weights and activations, FP32 accumulation.
 //
 // The two 32 -> 32 layers carry ~95 % of the arithmetic and run on the 5th-generation tensor cores
-// (tcgen05.mma, kind::f16 with BF16 operands, FP32 accumulator in tensor memory) as an implicit GEMM: one CTA
-// computes 128 consecutive output pixels of one image row x 32 output channels, M = 128, N = 32,
-// K = 9 taps x 32 input channels, issued as 18 MMAs of m128n32k16 into a TMEM accumulator (32 columns; two
-// accumulators and a ring of staged tiles, filled, consumed and drained by separate warps, so the loads, MMAs
-// and epilogue of consecutive tiles overlap).
-// The three input rows the tile needs (130 pixels each, 1-pixel halo) are loaded by TMA (12 tensor-map boxes
-// of {8 channels, 130 pixels}, zero fill outside the image) into shared memory in the canonical no-swizzle
-// K-major layout: [row][channel group of 8][pixel][8 channels], 16 bytes per pixel per group (each group's
-// plane padded to 2,176 bytes for the TMA's 128-byte destination alignment), so the A operand of tap (dy, dx)
-// is the same layout starting dx pixels further -- a descriptor start address 16 bytes * dx higher; no im2col
-// copy.  Weights are staged once per CTA as
-// [tap][k-step][channel group][output channel][8 channels].  The epilogue reads the accumulator with
-// tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = pixels 32w..32w+31), adds the bias and applies ReLU, or,
-// for the input gradient, multiplies by the ReLU mask of the layer's input, and stores BF16.
+// (tcgen05.mma, kind::f16 with BF16 operands, FP32 accumulator in tensor memory) as an implicit GEMM: each
+// output row of a 128-pixel strip is M = 128 pixels x N = 32 output channels, K = 9 taps x 32 input channels,
+// issued as 18 MMAs of m128n32k16 into a TMEM accumulator (32 columns; two accumulators).
+// Input rows (130 pixels each, 1-pixel halo) are loaded by TMA (4 tensor-map boxes of {8 channels, 130
+// pixels} per row, zero fill outside the image) into a ring of row slots in the canonical no-swizzle K-major
+// layout: [channel group of 8][pixel][8 channels], 16 bytes per pixel per group (each group's plane padded to
+// 2,176 bytes for the TMA's 128-byte destination alignment).  The A operand of tap (dy, dx) is the slot of
+// input row y - 1 + dy starting dx pixels further -- a descriptor start address 16 bytes * dx higher; no
+// im2col copy.  A CTA streams blocks of output rows of one strip, loading each input row once.  Weights are
+// staged once per CTA as [tap][k-step][channel group][output channel][8 channels].  The epilogue reads the
+// accumulator with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = pixels 32w..32w+31), adds the bias and
+// applies ReLU, or, for the input gradient, multiplies by the ReLU mask of the layer's input, and stores BF16.
 //
 // The input gradient of a 32 -> 32 layer is the same convolution with the weights flipped in space and
 // transposed in channels, so the backward pass reuses the kernel.  The 4-channel input layer, the 1-channel
 // output layer, the weight gradients (reductions over pixels) and Adam run on the CUDA cores in FP32.
 //
-// Safety: the descriptors address exactly the staged bytes (the A operand reaches kABytes, the B operand
-// kBBytes; the layout is checked bit-for-bit against a float64 convolution), and each region has a margin
-// beyond that; the mbarrier wait gives up after a bounded number of polls, sets the error word and still
-// waits (bounded) before freeing tensor memory.
+// Safety: the descriptors address only staged bytes: an A operand reads at most 8,608 bytes into its 8,704-byte
+// slot (pixels dx .. dx + 127 of each plane), the B operand exactly kBBytes, followed by a margin; the layout is
+// checked bit-for-bit against a float64 convolution.  Every mbarrier wait gives up after a bounded number of
+// polls, sets the error word and the kernel still waits (bounded) for its loads and MMAs before freeing tensor
+// memory.
 #include <cuda.h>  // CUtensorMap and the tensor-map encoder's types (resolved at run time, no link dependency)
 #include <cuda_bf16.h>
 
@@ -44,10 +43,7 @@ constexpr int kGroups = kC / 8;            // channel groups of 8 (16 bytes of B
 constexpr int kPlaneData = kRowPix * 16;   // bytes of one channel group of one staged row: one TMA box
 constexpr int kPlane = 2176;               // the plane padded to a multiple of 128 (TMA destination alignment);
                                            // the A operand's LBO
-constexpr int kRowBytes = kGroups * kPlane;
-constexpr int kABytes = 3 * kRowBytes;     // 26,112 (24,960 of them written by the 12 TMA boxes of a tile)
-constexpr int kAPad = kABytes + 256;       // A region + margin (the descriptors read below kABytes)
-constexpr uint32_t kTileTxBytes = 3 * kGroups * kPlaneData;
+constexpr int kRowBytes = kGroups * kPlane;  // one ring slot: 8,704 bytes (8,320 written by a row's 4 boxes)
 constexpr int kBBlock = 2 * kC * 16;       // one (tap, k-step) B operand: 2 groups x 32 rows x 16 B = 1,024
 constexpr int kBBytes = 18 * kBBlock;      // 18,432
 constexpr int kBPad = kBBytes + 1024;
@@ -55,13 +51,7 @@ constexpr int kBPad = kBBytes + 1024;
 constexpr int kEpilogueWarps = 4;
 constexpr int kThreads = 32 * (kEpilogueWarps + 2);
 constexpr int kAccs = 2;  // accumulators in tensor memory (32 columns each)
-static_assert(kPlaneData <= kPlane && kPlane % 128 == 0 && kAPad % 128 == 0, "TMA destinations 128-byte aligned");
-// dynamic shared memory of a kStages-deep ring: alignment slack, the A stages, B, the mbarriers
-// (full / empty per stage, acc_full / acc_empty per accumulator) and the TMEM address
-template <int kStages>
-constexpr int smem_bytes() {
-  return 128 + kStages * kAPad + kBPad + 8 * (2 * kStages + 2 * kAccs) + 16;
-}
+static_assert(kPlaneData <= kPlane && kPlane % 128 == 0, "TMA destinations 128-byte aligned");
 constexpr uint32_t kMaxPolls = 1u << 24;
 constexpr unsigned int kErrorBit = 8u;  // the volume error word's timeout bit
 
@@ -122,41 +112,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// TMA-loads the three input rows of a tile (image img, row y, pixels x0-1 .. x0+128) into the stage at a_base as
-// [row][g][pixel][8 channels]: 12 boxes {8 channels, 130 pixels} of the NHWC tensor map; rows and pixels
-// outside the image read as zeros (the map's out-of-bounds fill).  Completion: kTileTxBytes on bar.
-// The innermost coordinate is the channel 8 g, i.e. 16 g bytes: always 16-byte aligned.
-__device__ __forceinline__ void load_tile(const CUtensorMap* map, uint32_t a_base, uint32_t bar, int img, int y,
-                                          int x0) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(kTileTxBytes) : "memory");
-  const uint64_t m = reinterpret_cast<uint64_t>(map);
-#pragma unroll
-  for (int r = 0; r < 3; ++r) {
-#pragma unroll
-    for (int g = 0; g < kGroups; ++g) {
-      asm volatile(
-          "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-          "[%6];\n" ::"r"(a_base + r * kRowBytes + g * kPlane),
-          "l"(m), "r"(8 * g), "r"(x0 - 1), "r"(y - 1 + r), "r"(img), "r"(bar)
-          : "memory");
-    }
-  }
-}
-
-// the 18 MMAs of one tile: A from the staged rows at a_base, accumulator at tmem (accumulate from the first)
-__device__ __forceinline__ void issue_tile(uint32_t a_base, uint32_t b_base, uint32_t tmem) {
-  int k = 0;
-  for (int dy = 0; dy < 3; ++dy) {
-    for (int dx = 0; dx < 3; ++dx) {
-      for (int ks = 0; ks < 2; ++ks, ++k) {
-        const uint64_t a = smem_desc(a_base + dy * kRowBytes + (2 * ks) * kPlane + dx * 16, kPlane, 128);
-        const uint64_t b = smem_desc(b_base + k * kBBlock, kC * 16, 128);
-        mma(tmem, a, b, k > 0 ? 1u : 0u);
-      }
-    }
-  }
-}
-
 __device__ __forceinline__ void commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
 }
@@ -165,46 +120,86 @@ __device__ __forceinline__ void arrive(uint32_t bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
 }
 
+// A CTA owns blocks of kRows output rows of one 128-pixel strip and streams the block's kRows + 2 input rows
+// once each through a ring of kSlots row slots, so an output row costs one new input row (4 TMA boxes) instead
+// of three; the three taps' rows are three resident slots.
+
+constexpr uint32_t kRowTxBytes = kGroups * kPlaneData;
+static_assert(kRowBytes % 128 == 0, "ring slots keep the TMA destinations 128-byte aligned");
+
+// loads input row y of image img (pixels x0-1 .. x0+128, 4 channel-group boxes, zero fill outside the image)
+__device__ __forceinline__ void load_row(const CUtensorMap* map, uint32_t slot_base, uint32_t bar, int img, int y,
+                                         int x0) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(kRowTxBytes) : "memory");
+  const uint64_t m = reinterpret_cast<uint64_t>(map);
+#pragma unroll
+  for (int g = 0; g < kGroups; ++g) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];\n" ::"r"(slot_base + g * kPlane),
+        "l"(m), "r"(8 * g), "r"(x0 - 1), "r"(y), "r"(img), "r"(bar)
+        : "memory");
+  }
+}
+
+// the 18 MMAs of one output row: tap row dy reads the slot r0 / r1 / r2 (input rows y - 1, y, y + 1)
+__device__ __forceinline__ void issue_row(uint32_t r0, uint32_t r1, uint32_t r2, uint32_t b_base, uint32_t tmem) {
+  int k = 0;
+  for (int dy = 0; dy < 3; ++dy) {
+    const uint32_t rb = dy == 0 ? r0 : (dy == 1 ? r1 : r2);
+    for (int dx = 0; dx < 3; ++dx) {
+      for (int ks = 0; ks < 2; ++ks, ++k) {
+        const uint64_t a = smem_desc(rb + (2 * ks) * kPlane + dx * 16, kPlane, 128);
+        const uint64_t b = smem_desc(b_base + k * kBBlock, kC * 16, 128);
+        mma(tmem, a, b, k > 0 ? 1u : 0u);
+      }
+    }
+  }
+}
+
+template <int kSlots>
+constexpr int ring_smem_bytes() {
+  return 128 + kSlots * kRowBytes + kBPad + 8 * (2 * kSlots + 2 * kAccs) + 16;
+}
+
 // One 32 -> 32 3x3 convolution over a batch of images (NHWC BF16, zero padding), tcgen05 implicit GEMM.
 // mode kForward: out = relu?(conv(in) + bias); mode kGrad: out = conv(in) * (mask > 0) (mask = the layer
 // input's activations; the input gradient of the previous layer's ReLU).
 //
-// Warp-specialised pipeline over the CTA's tiles k = 0, 1, ... (tile blockIdx.x + k gridDim.x), handing off
-// through mbarriers only:
-//   producer (warp 4, one lane): waits empty[s] (the MMAs of tile k - kStages released stage s), then TMA-loads
-//     tile k's three input rows into stage s = k mod kStages, completing full[s] by transaction bytes;
-//   MMA issuer (warp 5, one lane): waits full[s] and acc_empty[a] (the epilogue of tile k - kAccs has read
-//     accumulator a = k mod kAccs), issues the 18 MMAs, and commits them to empty[s] and acc_full[a];
+// Warp-specialised, handing off through mbarriers only:
+//   producer (warp 4, one lane): waits empty[s] (the MMAs that read the slot's previous row completed), then
+//     TMA-loads input row q into slot s = q mod kSlots, completing full[s] by transaction bytes;
+//   MMA issuer (warp 5, one lane): for each output row waits full[s] of the rows it adds and acc_empty[a] (the
+//     epilogue has read accumulator a = row mod kAccs), issues the 18 MMAs and commits them to the top row's
+//     empty[s] (that row is not read again) and to acc_full[a]; a block's last two rows are released after
+//     its last output row;
 //   epilogue (warps 0-3): waits acc_full[a], reads its 32 TMEM lanes, releases the accumulator (acc_empty[a],
-//     one arrival per warp) and then applies bias / ReLU or the gradient mask and stores BF16.
-// Phase j of a barrier completes at its j-th use, so the waits for tile k use parity (k / kStages) & 1 or
-// (k / kAccs) & 1, and the releases of an earlier tile the parity before.  Every wait gives up after a bounded
-// number of polls: that role stops, the error word gets the timeout bit, and the roles waiting on it give up
-// in turn; before tensor memory is freed, the loads and MMA groups still in flight are waited for (bounded).
-template <int kStages>
+//     one arrival per warp) and applies bias / ReLU or the gradient mask and stores BF16.
+// Phase j of a barrier completes at its j-th use, so the waits use parity (q / kSlots) & 1 or (row / kAccs) & 1
+// and the releases of an earlier use the parity before.  A ring of at least 3 slots cannot deadlock: the row
+// an output row still needs to load was released by an earlier output row.  Every wait gives up after a
+// bounded number of polls: that role stops, the error word gets the timeout bit, and the roles waiting on it
+// give up in turn; before tensor memory is freed, the loads and MMA groups still in flight are waited for
+// (bounded).
+template <int kSlots, int kRows>
 __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_constant__ CUtensorMap in_map,
-                                                                const __nv_bfloat16* __restrict__ wpack,
-                                                                const float* __restrict__ bias,
-                                                                const __nv_bfloat16* __restrict__ mask,
-                                                                __nv_bfloat16* __restrict__ out, int batch, int width,
-                                                                int height, int mode, int relu,
-                                                                unsigned int* __restrict__ error) {
+                                                                  const __nv_bfloat16* __restrict__ wpack,
+                                                                  const float* __restrict__ bias,
+                                                                  const __nv_bfloat16* __restrict__ mask,
+                                                                  __nv_bfloat16* __restrict__ out, int batch,
+                                                                  int width, int height, int mode, int relu,
+                                                                  unsigned int* __restrict__ error) {
+  static_assert(kSlots >= 3, "an output row needs three resident input rows");
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA destinations: 128 B
-  unsigned char* sB = smem + kStages * kAPad;
+  unsigned char* sB = smem + kSlots * kRowBytes;
   uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kBPad);  // full[S], empty[S], acc_full[A], acc_empty[A]
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kStages + 2 * kAccs);
-  uint32_t* consumed = tmem_slot + 1;  // tiles whose loads the MMA issuer has waited for (teardown)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSlots + 2 * kAccs);
+  uint32_t* consumed = tmem_slot + 1;  // rows whose loads the MMA issuer has waited for (teardown)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-  // weights: [tap][ks][g][co][8] BF16, 18,432 bytes, already packed in this order in global memory
   for (int i = tid; i < kBBytes / 16; i += kThreads) {
     reinterpret_cast<uint4*>(sB)[i] = reinterpret_cast<const uint4*>(wpack)[i];
-  }
-  for (int q = 0; q < kStages; ++q) {
-    for (int i = tid; i < (kAPad - kABytes) / 16; i += kThreads) {
-      reinterpret_cast<uint4*>(smem + q * kAPad + kABytes)[i] = make_uint4(0, 0, 0, 0);
-    }
   }
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the weights, for the MMAs' async reads
   if (warp == kEpilogueWarps + 1) {
@@ -213,11 +208,11 @@ __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_con
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
   }
   if (tid == 0) {
-    for (int i = 0; i < 2 * kStages + kAccs; ++i) {
+    for (int i = 0; i < 2 * kSlots + kAccs; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bars[i])));
     }
     for (int i = 0; i < kAccs; ++i) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&bars[2 * kStages + kAccs + i])),
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&bars[2 * kSlots + kAccs + i])),
                    "r"(kEpilogueWarps));
     }
     *consumed = 0u;
@@ -226,121 +221,138 @@ __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_con
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n");
-  const uint32_t tmem = *tmem_slot;  // accumulator a at columns 32 a
-  const uint32_t a_base0 = smem_u32(smem), b_base = smem_u32(sB);
-  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[kStages]);
-  const uint32_t accf0 = smem_u32(&bars[2 * kStages]), acce0 = smem_u32(&bars[2 * kStages + kAccs]);
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t ring0 = smem_u32(smem), b_base = smem_u32(sB);
+  const uint32_t full0 = smem_u32(&bars[0]), empty0 = smem_u32(&bars[kSlots]);
+  const uint32_t accf0 = smem_u32(&bars[2 * kSlots]), acce0 = smem_u32(&bars[2 * kSlots + kAccs]);
+  auto slot_addr = [&](uint32_t q) { return ring0 + (q % kSlots) * static_cast<uint32_t>(kRowBytes); };
 
-  // tile t = blockIdx.x + k gridDim.x of the CTA; the launcher guarantees that the tile count fits in 31 bits,
-  // so the coordinates take two 32-bit divisions (64-bit ones cost hundreds of instructions per tile)
+  // work item t = blockIdx.x + k gridDim.x: strip xt, row block rb, image img (32-bit: checked by the launcher)
   const uint32_t tiles_x = static_cast<uint32_t>((width + kTile - 1) / kTile);
-  const uint32_t ntiles = static_cast<uint32_t>(batch) * static_cast<uint32_t>(height) * tiles_x;
+  const uint32_t blocks_y = static_cast<uint32_t>((height + kRows - 1) / kRows);
+  const uint32_t nitems = static_cast<uint32_t>(batch) * blocks_y * tiles_x;
   const uint32_t stride = gridDim.x;
-  const int my_tiles = blockIdx.x < ntiles ? static_cast<int>((ntiles - 1u - blockIdx.x) / stride + 1u) : 0;
-  auto coords = [&](int k, int& img, int& y, int& x0) {
+  const int my_items = blockIdx.x < nitems ? static_cast<int>((nitems - 1u - blockIdx.x) / stride + 1u) : 0;
+  auto item = [&](int k, int& img, int& y0, int& x0, int& rows) {
     const uint32_t t = blockIdx.x + static_cast<uint32_t>(k) * stride;
-    const uint32_t row = t / tiles_x;
-    x0 = static_cast<int>(t - row * tiles_x) * kTile;
-    const uint32_t im = row / static_cast<uint32_t>(height);
-    y = static_cast<int>(row - im * static_cast<uint32_t>(height));
+    const uint32_t rest = t / tiles_x;
+    x0 = static_cast<int>(t - rest * tiles_x) * kTile;
+    const uint32_t im = rest / blocks_y;
+    y0 = static_cast<int>(rest - im * blocks_y) * kRows;
     img = static_cast<int>(im);
+    rows = min(kRows, height - y0);
   };
   bool ok = true;
-  int issued = 0;  // producer: tiles loaded; MMA issuer: tiles whose MMAs were issued
+  uint32_t loaded = 0;  // producer: rows loaded
+  uint32_t issued = 0;  // MMA issuer: output rows issued
 
   if (warp == kEpilogueWarps) {
     if (lane == 0) {  // producer
-      for (int k = 0; k < my_tiles; ++k) {
-        const int st = k % kStages;
-        if (k >= kStages && !mbar_wait(empty0 + 8 * st, static_cast<uint32_t>((k / kStages - 1) & 1))) {
-          ok = false;
-          break;
+      for (int k = 0; k < my_items && ok; ++k) {
+        int img, y0, x0, rows;
+        item(k, img, y0, x0, rows);
+        for (int i = 0; i < rows + 2; ++i) {
+          const uint32_t q = loaded;
+          if (q >= kSlots && !mbar_wait(empty0 + 8 * (q % kSlots), (q / kSlots - 1) & 1u)) {
+            ok = false;
+            break;
+          }
+          load_row(&in_map, slot_addr(q), full0 + 8 * (q % kSlots), img, y0 - 1 + i, x0);
+          loaded = q + 1;
         }
-        int img, y, x0;
-        coords(k, img, y, x0);
-        load_tile(&in_map, a_base0 + st * kAPad, full0 + 8 * st, img, y, x0);
-        issued = k + 1;
       }
     }
   } else if (warp == kEpilogueWarps + 1) {
     if (lane == 0) {  // MMA issuer
-      for (int k = 0; k < my_tiles; ++k) {
-        const int st = k % kStages, a = k % kAccs;
-        if (!mbar_wait(full0 + 8 * st, static_cast<uint32_t>((k / kStages) & 1))) {
-          ok = false;
-          break;
+      uint32_t q = 0;  // first row of the current block
+      for (int k = 0; k < my_items && ok; ++k) {
+        int img, y0, x0, rows;
+        item(k, img, y0, x0, rows);
+        for (int r = 0; r < rows && ok; ++r) {
+          for (uint32_t w = (r == 0 ? q : q + r + 2); w <= q + r + 2; ++w) {
+            if (!mbar_wait(full0 + 8 * (w % kSlots), (w / kSlots) & 1u)) {
+              ok = false;
+              break;
+            }
+            *reinterpret_cast<volatile uint32_t*>(consumed) = w + 1;
+          }
+          if (!ok) break;
+          const uint32_t a = issued % kAccs;
+          if (issued >= kAccs && !mbar_wait(acce0 + 8 * a, (issued / kAccs - 1) & 1u)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n");
+          issue_row(slot_addr(q + r), slot_addr(q + r + 1), slot_addr(q + r + 2), b_base, tmem + 32u * a);
+          commit(empty0 + 8 * ((q + r) % kSlots));
+          commit(accf0 + 8 * a);
+          issued += 1;
         }
-        *reinterpret_cast<volatile uint32_t*>(consumed) = static_cast<uint32_t>(k + 1);
-        if (k >= kAccs && !mbar_wait(acce0 + 8 * a, static_cast<uint32_t>((k / kAccs - 1) & 1))) {
+        if (!ok) break;
+        commit(empty0 + 8 * ((q + rows) % kSlots));
+        commit(empty0 + 8 * ((q + rows + 1) % kSlots));
+        q += rows + 2;
+      }
+    }
+  } else {  // epilogue: warp w, lane l = output pixel 32w + l of the row
+    float bv[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) bv[c] = (mode == kForward && bias) ? __ldg(&bias[c]) : 0.0f;
+    uint32_t j = 0;
+    for (int k = 0; k < my_items && ok; ++k) {
+      int img, y0, x0, rows;
+      item(k, img, y0, x0, rows);
+      for (int r = 0; r < rows; ++r, ++j) {
+        const uint32_t a = j % kAccs;
+        const bool got = mbar_wait(accf0 + 8 * a, (j / kAccs) & 1u);
+        if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;\n");
-        issue_tile(a_base0 + st * kAPad, b_base, tmem + 32u * a);
-        commit(empty0 + 8 * st);
-        commit(accf0 + 8 * a);
-        issued = k + 1;
-      }
-    }
-  } else {  // epilogue: warp w, lane l = output pixel 32w + l of the tile
-    float bv[32];  // the layer's bias, in registers for the whole launch
+        float acc[32];
+        tmem_ld32(tmem + 32u * a + (static_cast<uint32_t>(warp * 32) << 16), acc);
+        asm volatile("tcgen05.fence::before_thread_sync;\n");
+        __syncwarp();
+        if (lane == 0) arrive(acce0 + 8 * a);
+        const int x = x0 + warp * 32 + lane;
+        if (x < width) {
+          const size_t o = ((static_cast<size_t>(img) * height + (y0 + r)) * width + x) * kC;
+          __align__(16) __nv_bfloat162 res[16];
+          if (mode == kForward) {
 #pragma unroll
-    for (int c = 0; c < 32; ++c) bv[c] = (mode == kForward && bias) ? __ldg(&bias[c]) : 0.0f;
-    for (int k = 0; k < my_tiles; ++k) {
-      const int a = k % kAccs;
-      const bool got = mbar_wait(accf0 + 8 * a, static_cast<uint32_t>((k / kAccs) & 1));
-      if (!__all_sync(0xffffffffu, got)) {
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;\n");
-      float acc[32];
-      tmem_ld32(tmem + 32u * a + (static_cast<uint32_t>(warp * 32) << 16), acc);
-      asm volatile("tcgen05.fence::before_thread_sync;\n");
-      __syncwarp();
-      if (lane == 0) arrive(acce0 + 8 * a);  // the accumulator may be overwritten by tile k + kAccs
-      int img, y, x0;
-      coords(k, img, y, x0);
-      const int x = x0 + warp * 32 + lane;
-      if (x < width) {
-        const size_t o = ((static_cast<size_t>(img) * height + y) * width + x) * kC;
-        __align__(16) __nv_bfloat162 res[16];
-        if (mode == kForward) {
-#pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            float v0 = acc[2 * c] + bv[2 * c], v1 = acc[2 * c + 1] + bv[2 * c + 1];
-            if (relu) {
-              v0 = fmaxf(v0, 0.0f);
-              v1 = fmaxf(v1, 0.0f);
+            for (int c = 0; c < 16; ++c) {
+              float v0 = acc[2 * c] + bv[2 * c], v1 = acc[2 * c + 1] + bv[2 * c + 1];
+              if (relu) {
+                v0 = fmaxf(v0, 0.0f);
+                v1 = fmaxf(v1, 0.0f);
+              }
+              res[c] = __floats2bfloat162_rn(v0, v1);
             }
-            res[c] = __floats2bfloat162_rn(v0, v1);
-          }
-        } else {
-          __align__(16) __nv_bfloat162 m[16];
+          } else {
+            __align__(16) __nv_bfloat162 m[16];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(m)[u] = reinterpret_cast<const uint4*>(mask + o)[u];
+            for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(m)[u] = reinterpret_cast<const uint4*>(mask + o)[u];
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const float2 mf = __bfloat1622float2(m[c]);
-            res[c] = __floats2bfloat162_rn(mf.x > 0.0f ? acc[2 * c] : 0.0f, mf.y > 0.0f ? acc[2 * c + 1] : 0.0f);
+            for (int c = 0; c < 16; ++c) {
+              const float2 mf = __bfloat1622float2(m[c]);
+              res[c] = __floats2bfloat162_rn(mf.x > 0.0f ? acc[2 * c] : 0.0f, mf.y > 0.0f ? acc[2 * c + 1] : 0.0f);
+            }
           }
+#pragma unroll
+          for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(out + o)[u] = reinterpret_cast<const uint4*>(res)[u];
         }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(out + o)[u] = reinterpret_cast<const uint4*>(res)[u];
       }
     }
   }
   if (!ok && lane == 0) atomicOr(error, kErrorBit);
   __syncthreads();
-  // in-flight work after a timeout (the waits return at once when nothing is pending): the producer waits for
-  // the loads nobody consumed, the MMA issuer for its last MMA group
+  // in-flight work after a timeout (the waits return at once when nothing is pending)
   if (warp == kEpilogueWarps && lane == 0) {
-    for (int k = static_cast<int>(*consumed); k < issued; ++k) {
-      mbar_wait(full0 + 8 * (k % kStages), static_cast<uint32_t>((k / kStages) & 1));
-    }
+    for (uint32_t w = *consumed; w < loaded; ++w) mbar_wait(full0 + 8 * (w % kSlots), (w / kSlots) & 1u);
   }
   if (warp == kEpilogueWarps + 1 && lane == 0 && issued > 0) {
-    mbar_wait(accf0 + 8 * ((issued - 1) % kAccs), static_cast<uint32_t>(((issued - 1) / kAccs) & 1));
+    mbar_wait(accf0 + 8 * ((issued - 1) % kAccs), ((issued - 1) / kAccs) & 1u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n");
   __syncthreads();
@@ -379,20 +391,20 @@ cudaError_t encode_input_map(const __nv_bfloat16* in, int batch, int width, int 
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
 
-// Launch shapes of conv32_tc_kernel: ring depth and resident CTAs per SM (both CTAs' rings fit in one SM's
-// shared memory when two are resident)
+// Launch shapes of conv32_tc_kernel: ring slots, resident CTAs per SM, output rows per block.  Measured on
+// 640x480 layers (CUDA events, batch 1 / batch 16): 6 slots x 2 CTAs x 8 rows 18.7 / 169 us; 8 x 2 x 8
+// 18.7 / 178; 8 x 2 x 16 24.1 / 171; 6 x 3 x 8 18.7 / 219; 4 x 4 x 8 24.8 / 206; the earlier one-row-tile
+// kernel (3 input rows loaded per output row) 22.8 / 277 us.
 struct Conv32Variant {
   const void* fn;
-  int stages, smem, ctas_per_sm;
+  int slots, smem, ctas_per_sm, rows;
 };
 const Conv32Variant kConv32Variants[] = {
-    {reinterpret_cast<const void*>(conv32_tc_kernel<3>), 3, smem_bytes<3>(), 2},
-    {reinterpret_cast<const void*>(conv32_tc_kernel<4>), 4, smem_bytes<4>(), 1},
-    {reinterpret_cast<const void*>(conv32_tc_kernel<6>), 6, smem_bytes<6>(), 1},
+    {reinterpret_cast<const void*>(conv32_tc_kernel<6, 8>), 6, ring_smem_bytes<6>(), 2, 8},
+    {reinterpret_cast<const void*>(conv32_tc_kernel<8, 8>), 8, ring_smem_bytes<8>(), 2, 8},
+    {reinterpret_cast<const void*>(conv32_tc_kernel<8, 16>), 8, ring_smem_bytes<8>(), 2, 16},
 };
-// measured (640x480, batch 1 / batch 16): 3 stages x 2 CTAs 24.8 / 294 us, 4 x 1 22.8 / 277 us, 6 x 1 24.9 / 293 us;
-// VH_CONV32_VARIANT selects another for launch-shape sweeps
-constexpr int kConv32Default = 1;
+constexpr int kConv32Default = 0;  // VH_CONV32_VARIANT selects another for launch-shape sweeps
 
 const Conv32Variant& conv32_variant() {
   static int v = -1;
@@ -425,8 +437,10 @@ cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, c
     ctas = cv.ctas_per_sm * (sms > 0 ? sms : 152);
   }
   const long long ntiles = static_cast<long long>(batch) * height * ((width + kTile - 1) / kTile);
-  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;  // the kernel's tile arithmetic is 32-bit
-  const int grid = static_cast<int>(ntiles < ctas ? ntiles : ctas);
+  if (ntiles > 0x7fffffffLL) return cudaErrorInvalidValue;  // the kernels' tile arithmetic is 32-bit
+  const long long nitems =
+      static_cast<long long>(batch) * ((height + cv.rows - 1) / cv.rows) * ((width + kTile - 1) / kTile);
+  const int grid = static_cast<int>(nitems < ctas ? nitems : ctas);
   if (grid <= 0) return cudaSuccess;
   CUtensorMap map;
   const cudaError_t e = encode_input_map(in, batch, width, height, &map);
