@@ -1094,7 +1094,7 @@ __global__ void __launch_bounds__(kMapTX * kMapTY) batch_map_kernel(const SceneD
 
 // Survivors carry over between the chunks of a scene as in fused_update_kernel; when the CTA's next chunk
 // belongs to another scene, it first updates the scene's remaining survivors and flushes its statistics.
-// Six resident CTAs per SM (42 registers, a small spill) measured faster than the four that 64 registers allow
+// Six resident CTAs per SM (40 registers, a small spill) measured faster than the four that 64 registers allow
 // (64-scene batch 3,485 vs 3,221 Mpix/s), as the single-volume autotuner also finds for its kernel.
 __global__ void __launch_bounds__(kThreads, 6) batch_update_kernel(const SceneDesc* __restrict__ descs,
                                                                 const BatchHeader* __restrict__ hdr,
