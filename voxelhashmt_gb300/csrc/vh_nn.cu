@@ -157,10 +157,19 @@ __device__ __forceinline__ void issue_row(uint32_t r0, uint32_t r1, uint32_t r2,
   }
 }
 
+// the epilogue's per-warp transpose buffer: 32 pixels x 64 bytes
+constexpr int kEpiStage = 32 * kC * 2;
+
 template <int kSlots>
 constexpr int ring_smem_bytes() {
-  return 128 + kSlots * kRowBytes + kBPad + 8 * (2 * kSlots + 2 * kAccs) + 16;
+  return 128 + kSlots * kRowBytes + kBPad + kEpilogueWarps * kEpiStage + 8 * (2 * kSlots + 2 * kAccs) + 16;
 }
+
+// The epilogue moves a warp's 32 pixels x 64 bytes between registers (lane l: pixel l) and global memory
+// through its shared-memory buffer, so that every global access instruction covers 512 contiguous bytes
+// (lane l: 16-byte chunk u * 32 + l of the warp's 2 KB), not 32 half sectors.  Chunk q of pixel p sits at
+// position 4p + (q ^ ((p >> 1) & 3)): the XOR spreads the lanes of each access phase over distinct banks.
+__device__ __forceinline__ int epi_pos(int p, int q) { return 4 * p + (q ^ ((p >> 1) & 3)); }
 
 // One 32 -> 32 3x3 convolution over a batch of images (NHWC BF16, zero padding), tcgen05 implicit GEMM.
 // mode kForward: out = relu?(conv(in) + bias); mode kGrad: out = conv(in) * (mask > 0) (mask = the layer
@@ -193,7 +202,9 @@ __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_con
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // TMA destinations: 128 B
   unsigned char* sB = smem + kSlots * kRowBytes;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kBPad);  // full[S], empty[S], acc_full[A], acc_empty[A]
+  uint4* sEpi = reinterpret_cast<uint4*>(sB + kBPad);  // kEpilogueWarps x kEpiStage
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sB + kBPad + kEpilogueWarps * kEpiStage);  // full[S], empty[S],
+                                                                                         // acc_full[A], acc_empty[A]
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kSlots + 2 * kAccs);
   uint32_t* consumed = tmem_slot + 1;  // rows whose loads the MMA issuer has waited for (teardown)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -315,33 +326,53 @@ __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_con
         asm volatile("tcgen05.fence::before_thread_sync;\n");
         __syncwarp();
         if (lane == 0) arrive(acce0 + 8 * a);
-        const int x = x0 + warp * 32 + lane;
-        if (x < width) {
-          const size_t o = ((static_cast<size_t>(img) * height + (y0 + r)) * width + x) * kC;
-          __align__(16) __nv_bfloat162 res[16];
-          if (mode == kForward) {
+        // the warp's 32 pixels start at pixel xw of row y0 + r; chunk u * 32 + lane belongs to pixel
+        // xw + 8u + lane / 4, which must lie inside the image
+        uint4* buf = sEpi + warp * (kEpiStage / 16);
+        const int xw = x0 + warp * 32;
+        const size_t row0 = ((static_cast<size_t>(img) * height + (y0 + r)) * width + xw) * kC;
+        __align__(16) __nv_bfloat162 res[16];
+        if (mode == kForward) {
 #pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              float v0 = acc[2 * c] + bv[2 * c], v1 = acc[2 * c + 1] + bv[2 * c + 1];
-              if (relu) {
-                v0 = fmaxf(v0, 0.0f);
-                v1 = fmaxf(v1, 0.0f);
-              }
-              res[c] = __floats2bfloat162_rn(v0, v1);
+          for (int c = 0; c < 16; ++c) {
+            float v0 = acc[2 * c] + bv[2 * c], v1 = acc[2 * c + 1] + bv[2 * c + 1];
+            if (relu) {
+              v0 = fmaxf(v0, 0.0f);
+              v1 = fmaxf(v1, 0.0f);
             }
-          } else {
-            __align__(16) __nv_bfloat162 m[16];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(m)[u] = reinterpret_cast<const uint4*>(mask + o)[u];
-#pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              const float2 mf = __bfloat1622float2(m[c]);
-              res[c] = __floats2bfloat162_rn(mf.x > 0.0f ? acc[2 * c] : 0.0f, mf.y > 0.0f ? acc[2 * c + 1] : 0.0f);
-            }
+            res[c] = __floats2bfloat162_rn(v0, v1);
           }
+        } else {
+          // the gradient mask, read coalesced and transposed to lane = pixel through the buffer
 #pragma unroll
-          for (int u = 0; u < 4; ++u) reinterpret_cast<uint4*>(out + o)[u] = reinterpret_cast<const uint4*>(res)[u];
+          for (int u = 0; u < 4; ++u) {
+            const int p = 8 * u + (lane >> 2), q = lane & 3;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (xw + p < width) v = *reinterpret_cast<const uint4*>(mask + row0 + static_cast<size_t>(p) * kC + 8 * q);
+            buf[epi_pos(p, q)] = v;
+          }
+          __syncwarp();
+          __align__(16) __nv_bfloat162 m[16];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(m)[q] = buf[epi_pos(lane, q)];
+          __syncwarp();
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const float2 mf = __bfloat1622float2(m[c]);
+            res[c] = __floats2bfloat162_rn(mf.x > 0.0f ? acc[2 * c] : 0.0f, mf.y > 0.0f ? acc[2 * c + 1] : 0.0f);
+          }
         }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) buf[epi_pos(lane, q)] = reinterpret_cast<const uint4*>(res)[q];
+        __syncwarp();
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int p = 8 * u + (lane >> 2), q = lane & 3;
+          if (xw + p < width) {
+            *reinterpret_cast<uint4*>(out + row0 + static_cast<size_t>(p) * kC + 8 * q) = buf[epi_pos(p, q)];
+          }
+        }
+        __syncwarp();  // the buffer is rewritten for the next row
       }
     }
   }
