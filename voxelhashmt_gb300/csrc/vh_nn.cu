@@ -556,11 +556,15 @@ __global__ void pack_input_kernel(const float* __restrict__ depth, float4* __res
 }
 
 // layer 1: 4 -> 32, ReLU, one thread per pixel; weights staged tap-major as float4 over the 4 input channels
-// (sw4[t][co] = w1[co][0..3][t]) so that one 16-byte shared load feeds 4 multiply-adds
+// (sw4[t][co] = w1[co][0..3][t]) so that one 16-byte shared load feeds 4 multiply-adds.  The 9 taps' loads
+// are issued together, and each warp writes its 32 pixels x 64 bytes through its shared-memory buffer
+// (epi_pos), 512 contiguous bytes per store instruction; the loop runs over whole warps so that every lane
+// takes part in the buffer's warp-synchronous steps.
 __global__ void __launch_bounds__(256) conv_in_kernel(const float4* __restrict__ X, const float* __restrict__ params,
                                                       __nv_bfloat16* __restrict__ A1, int batch, int w, int h) {
   __shared__ float4 sw4[9][kC];
   __shared__ float sb[kC];
+  __shared__ uint4 sbuf[8][128];  // one 2 KB transpose buffer per warp of the 256 threads
   for (int i = threadIdx.x; i < 9 * kC; i += blockDim.x) {
     const int t = i / kC, co = i % kC;
     const float* wc = params + kOffW1 + co * kCin * 9;
@@ -569,29 +573,52 @@ __global__ void __launch_bounds__(256) conv_in_kernel(const float4* __restrict__
   for (int i = threadIdx.x; i < kC; i += blockDim.x) sb[i] = params[kOffB1 + i];
   __syncthreads();
   const long long n = static_cast<long long>(batch) * w * h;
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const int x = static_cast<int>(i % w), y = static_cast<int>((i / w) % h);
-    const long long img = i / (static_cast<long long>(w) * h);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint4* buf = sbuf[warp];
+  const long long warps = static_cast<long long>(gridDim.x) * (blockDim.x >> 5);
+  for (long long base = (blockIdx.x * static_cast<long long>(blockDim.x >> 5) + warp) * 32; base < n;
+       base += warps * 32) {
+    const long long i = base + lane;
+    float4 in[9];
+    if (i < n) {
+      // 32-bit coordinates (the launcher keeps the pixel count below 2^31)
+      const uint32_t i32 = static_cast<uint32_t>(i), row = i32 / static_cast<uint32_t>(w);
+      const int x = static_cast<int>(i32 - row * static_cast<uint32_t>(w));
+      const uint32_t im = row / static_cast<uint32_t>(h);
+      const int y = static_cast<int>(row - im * static_cast<uint32_t>(h));
+      const long long img = im;
+#pragma unroll
+      for (int t = 0; t < 9; ++t) {
+        const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
+        in[t] = inside(sx, sy, w, h) ? X[(img * h + sy) * w + sx] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      }
+    } else {
+#pragma unroll
+      for (int t = 0; t < 9; ++t) in[t] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
     float acc[kC];
 #pragma unroll
     for (int co = 0; co < kC; ++co) acc[co] = sb[co];
-#pragma unroll 1
+#pragma unroll
     for (int t = 0; t < 9; ++t) {
-      const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
-      if (!inside(sx, sy, w, h)) continue;
-      const float4 in = X[(img * h + sy) * w + sx];
 #pragma unroll
       for (int co = 0; co < kC; ++co) {
         const float4 wv = sw4[t][co];
-        acc[co] += wv.x * in.x + wv.y * in.y + wv.z * in.z + wv.w * in.w;
+        acc[co] += wv.x * in[t].x + wv.y * in[t].y + wv.z * in[t].z + wv.w * in[t].w;
       }
     }
-    __align__(16) __nv_bfloat16 res[kC];
+    __align__(16) __nv_bfloat162 res[kC / 2];
 #pragma unroll
-    for (int co = 0; co < kC; ++co) res[co] = __float2bfloat16_rn(fmaxf(acc[co], 0.0f));
+    for (int c = 0; c < kC / 2; ++c) res[c] = __floats2bfloat162_rn(fmaxf(acc[2 * c], 0.0f), fmaxf(acc[2 * c + 1], 0.0f));
 #pragma unroll
-    for (int q = 0; q < 4; ++q) reinterpret_cast<uint4*>(A1 + i * kC)[q] = reinterpret_cast<const uint4*>(res)[q];
+    for (int q = 0; q < 4; ++q) buf[epi_pos(lane, q)] = reinterpret_cast<const uint4*>(res)[q];
+    __syncwarp();
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int p = 8 * u + (lane >> 2), q = lane & 3;
+      if (base + p < n) *reinterpret_cast<uint4*>(A1 + (base + p) * kC + 8 * q) = buf[epi_pos(p, q)];
+    }
+    __syncwarp();  // the buffer is rewritten by the next group
   }
 }
 
