@@ -216,7 +216,7 @@ def run_reference(args):
     from voxelhashmt_gb300 import scenes
     sc = make_scene(args.seed, args.warmup + args.steps)
     threads = os.cpu_count() or 1
-    warm = min(args.warmup, 2)
+    warm = min(max(args.warmup, 3), 5)  # at least 3 warm-up frames; at most 5 (about 0.8 s each on the CPU)
     budget = 60.0
     max_frames = min(args.steps, 16)  # frames are ray-cast on the CPU too: keep the run to a few minutes
     K = sc.intrinsics
