@@ -1094,12 +1094,14 @@ __global__ void __launch_bounds__(kMapTX * kMapTY) batch_map_kernel(const SceneD
 
 // Survivors carry over between the chunks of a scene as in fused_update_kernel; when the CTA's next chunk
 // belongs to another scene, it first updates the scene's remaining survivors and flushes its statistics.
-// Six resident CTAs per SM (40 registers, a small spill) measured faster than the four that 64 registers allow
-// (64-scene batch 3,485 vs 3,221 Mpix/s), as the single-volume autotuner also finds for its kernel.
-__global__ void __launch_bounds__(kThreads, 6) batch_update_kernel(const SceneDesc* __restrict__ descs,
+// kUT threads per CTA (the chunk of voxel slots), at least kUMinB resident CTAs per SM.  128 x 12 (40
+// registers, a small spill) measured fastest, as the single-volume autotuner also finds for its kernel:
+// 64-scene batch 3,614 Mpix/s, against 3,485 for 256 x 6 and 3,221 for 256 x 4 (64 registers).
+template <int kUT, int kUMinB>
+__global__ void __launch_bounds__(kUT, kUMinB) batch_update_kernel(const SceneDesc* __restrict__ descs,
                                                                 const BatchHeader* __restrict__ hdr,
                                                                 uint32_t* __restrict__ queue) {
-  __shared__ MapQueue<kThreads> Q;
+  __shared__ MapQueue<kUT> Q;
   __shared__ SceneDesc D;
   __shared__ uint32_t s_first[kMaxBatchScenes + 1];
   __shared__ uint32_t s_item;
@@ -1107,7 +1109,7 @@ __global__ void __launch_bounds__(kThreads, 6) batch_update_kernel(const SceneDe
   __shared__ CtaStats s_stats;
   const int tid = threadIdx.x, lane = tid & 31;
   const int nsc = static_cast<int>(hdr->nscenes);
-  constexpr uint32_t kChunksPerBlock = kBlockVoxels / kThreads;
+  constexpr uint32_t kChunksPerBlock = kBlockVoxels / kUT;
   if (tid == 0) {
     uint32_t run = 0U;
     for (int k = 0; k < nsc; ++k) {
@@ -1144,12 +1146,12 @@ __global__ void __launch_bounds__(kThreads, 6) batch_update_kernel(const SceneDe
     if (!scene_end) {
       if (item >= total) break;
       if (sc != cur) {
-        copy_desc(D, descs + sc, tid, kThreads);
+        copy_desc(D, descs + sc, tid, kUT);
         cur = sc;
         __syncthreads();
       }
         // 1. prefix of one slot per thread, survivors appended to the queue
-      const unsigned long long i = static_cast<unsigned long long>(item - s_first[sc]) * kThreads + tid;
+      const unsigned long long i = static_cast<unsigned long long>(item - s_first[sc]) * kUT + tid;
       const int4 vk = D.V.visible_keys[static_cast<uint32_t>(i >> 9)];
       const uint32_t b = static_cast<uint32_t>(vk.w);
       const int li = static_cast<int>(i & 511U);
@@ -1182,7 +1184,7 @@ __global__ void __launch_bounds__(kThreads, 6) batch_update_kernel(const SceneDe
     // fused_update_kernel): a full batch, nothing, or at the scene's end the carried-over rest
     const uint32_t n = Q.count;
     const uint32_t first =
-        scene_end ? 0U : (n >= static_cast<uint32_t>(kThreads) ? n - static_cast<uint32_t>(kThreads) : n);
+        scene_end ? 0U : (n >= static_cast<uint32_t>(kUT) ? n - static_cast<uint32_t>(kUT) : n);
     bool updated = false, newly = false;
     if (first + static_cast<uint32_t>(tid) < n) {
       map_update_entry(D.depth, D.nmap, D.V, D.p, Q, static_cast<int>(first) + tid, updated, newly);
@@ -1348,13 +1350,16 @@ cudaError_t launch_integrate_update(const float* depth, const Volume& V, const P
   return cudaGetLastError();
 }
 
+// launch shape of batch_update_kernel: threads per CTA (the chunk of voxel slots) and resident CTAs per SM
+constexpr int kBatchUT = 128, kBatchUMinB = 12;
+
 cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, bool band, cudaStream_t s) {
   static int grids[4] = {0, 0, 0, 0};
   if (grids[0] == 0) {
     grids[0] = grid_for(reinterpret_cast<const void*>(batch_filter_alloc_kernel<false>), filt::kTX * filt::kTY);
     grids[1] = grid_for(reinterpret_cast<const void*>(batch_filter_alloc_kernel<true>), filt::kTX * filt::kTY);
     grids[2] = grid_for(reinterpret_cast<const void*>(batch_map_kernel), kMapTX * kMapTY);
-    grids[3] = grid_for(reinterpret_cast<const void*>(batch_update_kernel), kThreads);
+    grids[3] = grid_for(reinterpret_cast<const void*>(batch_update_kernel<kBatchUT, kBatchUMinB>), kBatchUT);
   }
   batch_begin_kernel<<<1, 256, 0, s>>>(descs, hdr, queue);
   if (band) {
@@ -1363,7 +1368,7 @@ cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_
     batch_filter_alloc_kernel<false><<<grids[0], filt::kTX * filt::kTY, 0, s>>>(descs, hdr, queue);
   }
   batch_map_kernel<<<grids[2], kMapTX * kMapTY, 0, s>>>(descs, hdr, queue);
-  batch_update_kernel<<<grids[3], kThreads, 0, s>>>(descs, hdr, queue);
+  batch_update_kernel<kBatchUT, kBatchUMinB><<<grids[3], kBatchUT, 0, s>>>(descs, hdr, queue);
   return cudaGetLastError();
 }
 
