@@ -47,7 +47,7 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # summarised in profiles/ (plain: update_kernel_room640.md, one launch over 6.55 M active voxels; opt-in form:
 # fused_update_room640.md, one launch over 3.16 M active voxels); scaled by the active voxels of a launch.
 UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL = {"plain": (539.49e6 + 267.04e6) / 6.548e6,
-                                         "chosen": (189.938e6 + 56.967e6) / 3.163e6}
+                                         "chosen": (189.351e6 + 57.310e6) / 3.163e6}
 
 
 def parse():
