@@ -214,11 +214,11 @@ def run_reference(args):
     ob.build_oracle()
     from oracle import oracle as O
     from voxelhashmt_gb300 import scenes
-    sc = make_scene(args.seed, args.warmup + args.steps)
     threads = os.cpu_count() or 1
     warm = min(max(args.warmup, 3), 5)  # at least 3 warm-up frames; at most 5 (about 0.8 s each on the CPU)
     budget = 60.0
     max_frames = min(args.steps, 16)  # frames are ray-cast on the CPU too: keep the run to a few minutes
+    sc = make_scene(args.seed, max(args.warmup + args.steps, warm + max_frames))
     K = sc.intrinsics
     cfg = O.config(O.FLAVOR_REF_CPU, O.EXP_LIBM, threads=threads)
     vol = O.Volume(cfg, sc.voxel_size, sc.truncation)
