@@ -182,6 +182,34 @@ def test_pinned_host_frames_back_to_back_match_device_input(env, small_orbit):
     dev_vol.close()
 
 
+def test_pinned_host_frames_of_changing_resolution(env, small_orbit):
+    """A larger host frame reallocates the two staging buffers while earlier frames may still be in flight
+    (the copy stream and the readers are waited for first): 64x48 and 128x96 frames of one orbit, enqueued
+    back to back from pinned memory, fuse bit-identically to the same frames from device memory."""
+    backend, _ = env
+    from voxelhashmt_gb300 import scenes
+    small = small_orbit
+    big = scenes.orbit_scene(seed=7, frames=24, width=128, height=96, fx=277.0 * 0.4, fy=277.0 * 0.4, cx=64.0,
+                             cy=48.0)
+    big.voxel_size, big.truncation = small.voxel_size, small.truncation
+    plan = [(small, 0), (small, 3), (big, 6), (big, 9), (small, 12), (big, 15)]
+    depths = [scenes.render_depth(sc, f) for sc, f in plan]
+    pinned = [torch.from_numpy(d).pin_memory() for d in depths]
+    bk = backend.TsdfIntegrationBackend("gpu")
+    host_vol, dev_vol = _volume(backend, small), _volume(backend, small)
+    for (sc, f), h in zip(plan, pinned):
+        bk.integrate(host_vol, backend.DepthFrame(sc.intrinsics, h.numpy()), sc.poses[f], 1, synchronize=False)
+    host_vol.synchronize()
+    for (sc, f), d in zip(plan, depths):
+        bk.integrate(dev_vol, backend.DepthFrame(sc.intrinsics, _dev(d)), sc.poses[f], 1)
+    hk, hv = _sorted_blocks(env, host_vol)
+    dk, dv = _sorted_blocks(env, dev_vol)
+    assert hk.shape[0] > 0
+    assert np.array_equal(hk, dk) and np.array_equal(hv, dv)
+    host_vol.close()
+    dev_vol.close()
+
+
 def _sorted_blocks(env, vol):
     return env[1].sort_blocks(*vol.export_blocks())
 
