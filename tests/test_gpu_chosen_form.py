@@ -213,6 +213,39 @@ def test_fused_update_visits_every_active_voxel(backend, orbit_half, fast_math):
             assert abs(t["active_voxels"] - tr["active_voxels"]) <= 1e-5 * tr["active_voxels"], (variant, t, tr)
 
 
+def test_opt_in_form_empty_frame_and_full_pool(backend, small_orbit):
+    """The opt-in form (band allocation, normal map, fast math, FP16 bins) on the edge cases the plain form is
+    tested on.  An all-zero frame allocates and updates nothing: the fused update then has no chunk.  A pool
+    too small for the frame reports VH_ERR_POOL_FULL and keeps the blocks that fit; the visible entries left
+    without a pool block are skipped by the normal-map pass and the fused update, and the counters stay
+    consistent with a recount."""
+    from voxelhashmt_gb300 import _capi, scenes
+    sc = small_orbit
+    algo = _capi.default_algorithm(allocation_mode=1, normal_mode=1, fast_math=1)
+    d = scenes.render_depth(sc, 0)
+    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=1 << 16, max_blocks=8192, layer_format=1,
+                                algorithm=algo)
+    z = np.zeros((sc.intrinsics.height, sc.intrinsics.width), np.float32)
+    backend.integrate_depth_frame_cuda(vol, backend.DepthFrame(sc.intrinsics, z), sc.poses[0])
+    st = vol.frame_stats()
+    assert st["visible_blocks"] == 0 and st["active_voxels"] == 0 and st["updated_voxels"] == 0
+    assert vol.block_count() == 0 and vol.observed_voxel_count() == 0
+    assert backend.extract_mesh_cuda(vol).shape == (0, 9)
+    backend.integrate_depth_frame_cuda(vol, backend.DepthFrame(sc.intrinsics, d), sc.poses[0])
+    assert vol.block_count() > 0 and vol.observed_voxel_count() > 0
+    assert vol.observed_voxel_count() == vol.recount_observed_voxels()
+    vol.close()
+    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=1 << 16, max_blocks=16, layer_format=1,
+                                algorithm=algo)
+    with pytest.raises(_capi.VhError) as e:
+        backend.integrate_depth_frame_cuda(vol, backend.DepthFrame(sc.intrinsics, d), sc.poses[0])
+    assert e.value.status == _capi.VH_ERR_POOL_FULL
+    assert vol.block_count() == 16
+    n = vol.observed_voxel_count()
+    assert 0 < n <= 16 * 512 and n == vol.recount_observed_voxels()
+    vol.close()
+
+
 @pytest.mark.parametrize("fast_math", [0, 1])
 def test_pixel_normal_map_matches_reference_normal(backend, oracle_lib, fast_math):
     """The map at pixel centres against the oracle's estimateSurfaceNormalCamera at integer coordinates:
