@@ -117,3 +117,42 @@ def test_batch_fast_math_graph_and_stream_agree(backend, oracle_lib):
         assert abs(qa["chamfer_mm"] - qc["chamfer_mm"]) <= 0.03 * qc["chamfer_mm"] + 0.05, (k, qa, qc)
     for v in g + s + e + alone:
         v.close()
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_scene_with_full_pool_does_not_affect_the_others(backend, oracle_lib, use_graph):
+    """One scene of a batch runs out of pool blocks: its error surfaces on its own volume (vh_synchronize
+    reports VH_ERR_POOL_FULL, the blocks that fit are kept and consistently counted), its visible entries
+    without a pool block are skipped by the normal-map and update kernels, and the other scene fuses exactly
+    as it does alone (exact compile)."""
+    O = oracle_lib
+    from voxelhashmt_gb300 import _capi
+    scs = _scenes()[:2]
+    (sc0, fmt0, dep0), (sc1, fmt1, dep1) = scs
+    small = backend.VoxelHashTSDF(sc0.voxel_size, sc0.truncation, hash_buckets=1 << 16, max_blocks=16,
+                                  layer_format=fmt0,
+                                  algorithm=_capi.default_algorithm(allocation_mode=1, normal_mode=1, fast_math=0))
+    other = _volume(backend, sc1, fmt1, 0)
+    batch = backend.VolumeBatch([small, other], use_graph=use_graph)
+    for f in range(6):
+        batch.integrate([torch.from_numpy(dep0[f]).cuda().view(-1), torch.from_numpy(dep1[f]).cuda().view(-1)],
+                        [sc0.intrinsics, sc1.intrinsics], [sc0.poses[f], sc1.poses[f]])
+    torch.cuda.synchronize()
+    with pytest.raises(_capi.VhError) as e:
+        small.synchronize()
+    assert e.value.status == _capi.VH_ERR_POOL_FULL
+    assert small.block_count() == 16
+    n = small.observed_voxel_count()
+    assert 0 < n <= 16 * 512 and n == small.recount_observed_voxels()
+    other.synchronize()
+    alone = _volume(backend, sc1, fmt1, 0)
+    bk = backend.TsdfIntegrationBackend("gpu")
+    for f in range(6):
+        bk.integrate(alone, backend.DepthFrame(sc1.intrinsics, torch.from_numpy(dep1[f]).cuda().view(-1)), sc1.poses[f])
+    ka, va = O.sort_blocks(*other.export_blocks())
+    kb, vb = O.sort_blocks(*alone.export_blocks())
+    assert ka.shape[0] > 0 and np.array_equal(ka, kb) and np.array_equal(va, vb)
+    batch.close()
+    for v in (small, other, alone):
+        v.close()
+
