@@ -83,6 +83,9 @@ def lib():
         L.vo_collect_blocks.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose),
                                         C.c_float, C.c_float, C.c_int32, _ip, C.c_int64]
         L.vo_collect_blocks.restype = C.c_int64
+        L.vo_collect_band_blocks.argtypes = [_fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose), C.c_float, C.c_float,
+                                             C.c_int32, _ip, C.c_int64]
+        L.vo_collect_band_blocks.restype = C.c_int64
         L.vo_volume_new.argtypes = [C.POINTER(VoConfig), C.c_float, C.c_float]
         L.vo_volume_new.restype = C.c_void_p
         L.vo_volume_free.argtypes = [C.c_void_p]
@@ -180,6 +183,18 @@ def collect_blocks(cfg, depth, K, P, voxel_size, truncation, stride=1):
     keys = np.zeros((cap, 3), np.int32)
     n = lib().vo_collect_blocks(C.byref(cfg), dp, C.byref(intrinsics(K)), C.byref(pose(P)), voxel_size,
                                 truncation, stride, keys.ctypes.data_as(_ip), cap)
+    if n < 0:
+        return None
+    return keys[:n].copy()
+
+
+def collect_band_blocks(depth, K, P, voxel_size, truncation, stride=1):
+    """Keys of the truncation-band rule (the library's opt-in allocation mode), sorted; None on key overflow."""
+    d, dp = _f32(depth)
+    cap = max(1024, int(d.size) * 64 // max(1, stride * stride) + 1024)
+    keys = np.zeros((cap, 3), np.int32)
+    n = lib().vo_collect_band_blocks(dp, C.byref(intrinsics(K)), C.byref(pose(P)), voxel_size, truncation, stride,
+                                     keys.ctypes.data_as(_ip), cap)
     if n < 0:
         return None
     return keys[:n].copy()

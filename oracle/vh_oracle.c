@@ -820,6 +820,84 @@ int64_t vo_collect_blocks(const vo_config* c, const float* depth, const vo_intri
   return n;
 }
 
+/* The truncation-band allocation rule (the library's opt-in allocation mode 1; the reference has no such
+ * rule): every block crossed by the segment [p - trunc*ray, p + trunc*ray] of each valid pixel, found by a
+ * voxel walk (Amanatides & Woo, "A Fast Voxel Traversal Algorithm for Ray Tracing", 1987) over cells of
+ * 8 vs with the start and end cells taken by floorf(x / (8 vs)).  The walk takes at most 64 steps, ends on
+ * the end cell or when the next crossing lies past the segment (t > 1), and the end cell is always added.
+ * Every visited key must pack into 21 bits per axis.  The point, ray and segment ends are computed as the
+ * GPU flavour of the reference rule computes them (cuda_block_allocator.cu:231-258). */
+static int insert_band(v3 a, v3 b, float bws, keymap* set) {
+  int c[3] = {(int)floorf(a.x / bws), (int)floorf(a.y / bws), (int)floorf(a.z / bws)};
+  const int e[3] = {(int)floorf(b.x / bws), (int)floorf(b.y / bws), (int)floorf(b.z / bws)};
+  const float o[3] = {a.x, a.y, a.z};
+  const float d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
+  int st[3];
+  float tmax[3], tdel[3];
+  for (int k = 0; k < 3; ++k) {
+    st[k] = d[k] > 0.0f ? 1 : (d[k] < 0.0f ? -1 : 0);
+    if (st[k] != 0) {
+      const float edge = (float)(c[k] + (st[k] > 0 ? 1 : 0)) * bws;
+      tmax[k] = (edge - o[k]) / d[k];
+      tdel[k] = bws / fabsf(d[k]);
+    } else {
+      tmax[k] = 3.0e38f;
+      tdel[k] = 3.0e38f;
+    }
+  }
+  uint64_t packed;
+  for (int step = 0; step < 64; ++step) {
+    if (!vo_pack_block_key(c[0], c[1], c[2], &packed)) return 0;
+    keymap_insert(set, (vo_key){c[0], c[1], c[2]}, 0);
+    if (c[0] == e[0] && c[1] == e[1] && c[2] == e[2]) break;
+    /* the axis of the nearest crossing; ties go to the later axis */
+    int k = 2;
+    if (tmax[0] < tmax[1]) {
+      if (tmax[0] < tmax[2]) k = 0;
+    } else if (tmax[1] < tmax[2]) {
+      k = 1;
+    }
+    if (tmax[k] > 1.0f) break;
+    c[k] += st[k];
+    tmax[k] += tdel[k];
+  }
+  if (!vo_pack_block_key(e[0], e[1], e[2], &packed)) return 0;
+  keymap_insert(set, (vo_key){e[0], e[1], e[2]}, 0);
+  return 1;
+}
+
+int64_t vo_collect_band_blocks(const float* depth, const vo_intrinsics* K, const vo_pose* T, float vs, float trunc,
+                               int32_t stride, vo_key* out, int64_t max_out) {
+  const int s = stride > 1 ? stride : 1;
+  const v3 cam = mk(T->t[0], T->t[1], T->t[2]);
+  const float bws = vs * 8.0f;
+  keymap set;
+  keymap_init(&set, 1024);
+  for (int v = 0; v < K->height; v += s) {
+    for (int u = 0; u < K->width; u += s) {
+      const float d = depth[(size_t)v * K->width + u];
+      if (!(d > 0.0f)) continue;
+      const v3 pw = pose_point(T, back_project(u, v, d, K));
+      const v3 ray = vnormalize(GPU, vsub(pw, cam));
+      if (!insert_band(vsub(pw, vmul(ray, trunc)), vadd(pw, vmul(ray, trunc)), bws, &set)) {
+        keymap_free(&set);
+        return -1;
+      }
+    }
+  }
+  if (set.count > max_out) {
+    const int64_t n = set.count;
+    keymap_free(&set);
+    return n > 0 ? -2 : 0;
+  }
+  int64_t n = 0;
+  for (int64_t i = 0; i < set.cap; ++i)
+    if (set.vals[i] >= 0) out[n++] = set.keys[i];
+  qsort(out, (size_t)n, sizeof(vo_key), key_cmp);
+  keymap_free(&set);
+  return n;
+}
+
 /* ------------------------------------------------------------------ volume */
 struct vo_volume {
   vo_config cfg;

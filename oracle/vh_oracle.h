@@ -115,6 +115,11 @@ void vo_depth_normals(const vo_config* cfg, const float* depth, const vo_intrins
 int64_t vo_collect_blocks(const vo_config* cfg, const float* depth, const vo_intrinsics* K, const vo_pose* T_wc,
                           float voxel_size, float truncation, int32_t stride, vo_key* out, int64_t max_out);
 
+/* The truncation-band rule (the library's opt-in allocation mode): the blocks crossed by each valid pixel's
+ * [p - trunc*ray, p + trunc*ray] segment.  Same return convention as vo_collect_blocks. */
+int64_t vo_collect_band_blocks(const float* depth, const vo_intrinsics* K, const vo_pose* T_wc, float voxel_size,
+                               float truncation, int32_t stride, vo_key* out, int64_t max_out);
+
 typedef struct vo_volume vo_volume;
 vo_volume* vo_volume_new(const vo_config* cfg, float voxel_size, float truncation);
 void vo_volume_free(vo_volume* vol);

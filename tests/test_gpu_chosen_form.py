@@ -101,6 +101,9 @@ def test_band_keys_subset_of_reference_rule(backend, oracle_lib, small_orbit, st
         filtered = O.filter_depth(cfg, d, sc.intrinsics)  # allocation reads the filtered depth
         need = {tuple(k) for k in _block_of_points(sc, filtered, f, stride)}
         assert need <= got_set, "a block holding a sample point is missing from the band"
+        # the exact compile walks the segments exactly as the oracle's statement of the band rule does
+        want = O.collect_band_blocks(filtered, sc.intrinsics, sc.poses[f], sc.voxel_size, sc.truncation, stride)
+        assert np.array_equal(got, want)
 
 
 def _chamfer(backend, vol, sc, clean, frames):

@@ -178,3 +178,49 @@ def test_oracle_parallel_equals_serial(O):
         v.close()
     assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
     assert np.array_equal(_bits(res[0][2]), _bits(res[1][2]))
+
+
+def test_band_rule_known_answers(O):
+    """The truncation-band rule on single rays whose crossings are known by hand."""
+    from voxelhashmt_gb300 import scenes
+    K = scenes.Intrinsics(1, 1, 1.0, 1.0, 0.0, 0.0)
+    eye = scenes.Pose(np.eye(3, dtype=np.float32), np.zeros(3, np.float32))
+    # along +z from the origin: segment z in [0.3, 0.5], cells of 0.08 -> z cells 3, 4, 5, 6
+    keys = O.collect_band_blocks(np.full((1, 1), 0.4, np.float32), K, eye, 0.01, 0.1)
+    assert keys.tolist() == [[0, 0, 3], [0, 0, 4], [0, 0, 5], [0, 0, 6]]
+    # no valid depth, no keys
+    assert O.collect_band_blocks(np.zeros((1, 1), np.float32), K, eye, 0.01, 0.1).shape == (0, 3)
+    # a camera far outside the 21-bit key range: overflow is reported, as for the reference rule
+    far = scenes.Pose(np.eye(3, dtype=np.float32), np.array([1.0e6, 0.0, 0.0], np.float32))
+    assert O.collect_band_blocks(np.full((1, 1), 0.4, np.float32), K, far, 0.01, 0.1) is None
+
+
+def test_band_rule_is_a_walk_of_the_segment(O):
+    """On a rendered frame: the band holds the cells that dense samples of each segment fall in (those clear of a
+    cell face), and the band lies inside the reference rule's 3 x 27 neighbourhood (a segment of half-length
+    trunc < 8 vs stays within one cell of p)."""
+    from voxelhashmt_gb300 import scenes
+    sc = scenes.orbit_scene(seed=5, frames=4, width=40, height=30, fx=36.0, fy=36.0, cx=19.5, cy=14.5)
+    K = sc.intrinsics
+    cfg = O.config(O.FLAVOR_REF_GPU, O.EXP_OWN)
+    bws = 8 * sc.voxel_size
+    for f in (0, 2):
+        d = scenes.render_depth(sc, f)
+        band = O.collect_band_blocks(d, K, sc.poses[f], sc.voxel_size, sc.truncation)
+        ref = O.collect_blocks(cfg, d, K, sc.poses[f], sc.voxel_size, sc.truncation)
+        band_set = {tuple(k) for k in band}
+        assert len(band_set) == band.shape[0] and band_set <= {tuple(k) for k in ref}
+        assert len(band_set) < ref.shape[0]
+        v, u = np.nonzero(d > 0)
+        z = d[v, u].astype(np.float64)
+        pc = np.stack([(u - K.cx) * z / K.fx, (v - K.cy) * z / K.fy, z], 1)
+        R = np.asarray(sc.poses[f].R, np.float64)
+        t = np.asarray(sc.poses[f].t, np.float64)
+        pw = pc @ R.T + t
+        ray = (pw - t) / np.linalg.norm(pw - t, axis=1, keepdims=True)
+        for s in np.linspace(-1.0, 1.0, 65):
+            g = (pw + ray * (s * sc.truncation)) / bws
+            frac = g - np.floor(g)
+            safe = np.all((frac > 1e-3) & (frac < 1 - 1e-3), axis=1)
+            need = {tuple(k) for k in np.floor(g[safe]).astype(np.int64).tolist()}
+            assert need <= band_set, "a cell on a pixel's segment is missing from the band"
