@@ -281,12 +281,19 @@ vh_status vh_batch_integrate(vh_batch* batch, const float* const* depth_device, 
  * vh_nn_pack_conv32_weights: FP32 weights w[co][ci][3][3] (32 x 32) -> the packed BF16 tensor-core operand
  * (18,432 bytes); transpose_flip packs w[ci][co][2-ky][2-kx], the weights of the input gradient.
  * vh_nn_conv32: 3x3 convolution with zero padding on the tensor cores (tcgen05, FP32 accumulation); mode 0:
- * out = conv(in) + bias, then ReLU if relu; mode 1: out = conv(in) where mask > 0, else 0.  *error becomes
- * nonzero if the tensor cores did not signal completion within a bounded wait. */
+ * out = conv(in) + bias, then ReLU if relu; mode 1: out = conv(in) where mask > 0, else 0.  *error gets
+ * the timeout bit (8) if a wait on the loads or the tensor cores gave up (about a second). */
 vh_status vh_nn_pack_conv32_weights(const float* w, void* packed, int32_t transpose_flip, void* stream);
 vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, const void* mask, void* out,
                        int32_t batch, int32_t width, int32_t height, int32_t mode, int32_t relu, uint32_t* error,
                        void* stream);
+/* vh_nn_conv32 whose input loads start only once *gate (device memory) is nonzero.  A gate that stays zero
+ * makes every wait of the kernel give up after about a second: *error gets the timeout bit (8, which the
+ * volume calls report as VH_ERR_TIMEOUT), `out` is left unwritten and the CUDA context stays usable.  This is
+ * how the bounded-wait path is tested without a GPU fault; with an open gate the result equals vh_nn_conv32's. */
+vh_status vh_nn_conv32_gated(const void* in, const void* packed_w, const float* bias, const void* mask, void* out,
+                             int32_t batch, int32_t width, int32_t height, int32_t mode, int32_t relu,
+                             const uint32_t* gate, uint32_t* error, void* stream);
 
 /* The whole denoiser (3x3 convolutions 4 -> 32 -> 32 -> 32 -> 1, ReLU, residual output; the two 32 -> 32 layers
  * on the tensor cores).  params: FP32 [vh_nn_param_count()] = w1[32][4][3][3] b1[32] w2[32][32][3][3] b2[32]

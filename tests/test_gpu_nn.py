@@ -185,3 +185,39 @@ def test_denoiser_training_and_gain(capi):
           % (1000 * rmse(ev_raw), 1000 * rmse(bil), 1000 * rmse(out)))
     assert rmse(out) < rmse(bil) and rmse(out) < rmse(ev_raw)
     vol.close()
+
+
+def test_conv32_bounded_wait_gives_up_and_context_stays_usable(capi):
+    """Failure detection without a GPU fault: a load gate that nothing opens leaves every wait of the tensor-core
+    convolution unanswered.  Each gives up after about a second, the error word gets the timeout bit, the output
+    is left unwritten, and the next launches on the same context run and match."""
+    import time
+    B, H, W = 1, 12, 200
+    g = torch.Generator().manual_seed(11)
+    x = torch.randn(B, H, W, 32, generator=g).to(torch.bfloat16).cuda().contiguous()
+    w = (torch.randn(32, 32, 3, 3, generator=g) * 0.1).float().cuda().contiguous()
+    b = (torch.randn(32, generator=g) * 0.1).float().cuda().contiguous()
+    packed = torch.empty(9 * 32 * 32, dtype=torch.bfloat16, device="cuda")
+    capi.check(capi.lib().vh_nn_pack_conv32_weights(_ptr(w), _ptr(packed), 0, None))
+    want = _run(capi, x, w, b, None, 0, 1)
+
+    def gated(open_gate):
+        gate = torch.full((1,), 1 if open_gate else 0, dtype=torch.int32, device="cuda")
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        out = torch.full_like(x, float("nan"))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        capi.check(capi.lib().vh_nn_conv32_gated(_ptr(x), _ptr(packed), _ptr(b), None, _ptr(out), B, W, H, 0, 1,
+                                                 _ptr(gate), C.cast(C.c_void_p(err.data_ptr()), C.POINTER(C.c_uint32)),
+                                                 None))
+        torch.cuda.synchronize()
+        return out, int(err.item()), time.perf_counter() - t0
+
+    out, err, secs = gated(False)
+    assert err & 8, "the timeout bit was not set"
+    assert 0.5 < secs < 30.0, secs
+    assert torch.isnan(out.float()).all(), "a timed-out launch wrote output"
+    out, err, _ = gated(True)
+    assert err == 0 and torch.equal(out, want)
+    again = _run(capi, x, w, b, None, 0, 1)  # the ungated kernel after the timeout
+    assert torch.equal(again, want)

@@ -1164,6 +1164,20 @@ vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, 
   return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
 }
 
+vh_status vh_nn_conv32_gated(const void* in, const void* packed_w, const float* bias, const void* mask, void* out,
+                             int32_t batch, int32_t width, int32_t height, int32_t mode, int32_t relu,
+                             const uint32_t* gate, uint32_t* error, void* stream) {
+  if (!in || !packed_w || !out || !gate || !error || batch <= 0 || width <= 0 || height <= 0 ||
+      (mode != 0 && mode != 1) || (mode == 1 && !mask)) {
+    return VH_ERR_INVALID_ARGUMENT;
+  }
+  const cudaError_t e = vh::nn::launch_conv32(static_cast<const __nv_bfloat16*>(in),
+                                              static_cast<const __nv_bfloat16*>(packed_w), bias,
+                                              static_cast<const __nv_bfloat16*>(mask), static_cast<__nv_bfloat16*>(out),
+                                              batch, width, height, mode, relu, error, as_stream(stream), gate);
+  return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
+}
+
 int32_t vh_nn_param_count(void) { return vh::nn::param_count(); }
 
 uint64_t vh_nn_workspace_bytes(int32_t batch, int32_t width, int32_t height) {

@@ -21,9 +21,8 @@
 //
 // Safety: the descriptors address only staged bytes: an A operand reads at most 8,608 bytes into its 8,704-byte
 // slot (pixels dx .. dx + 127 of each plane), the B operand exactly kBBytes, followed by a margin; the layout is
-// checked bit-for-bit against a float64 convolution.  Every mbarrier wait gives up after a bounded number of
-// polls, sets the error word and the kernel still waits (bounded) for its loads and MMAs before freeing tensor
-// memory.
+// checked bit-for-bit against a float64 convolution.  Every mbarrier wait gives up after about a second, sets
+// the error word and the kernel still waits (bounded) for its loads and MMAs before freeing tensor memory.
 #include <cuda.h>  // CUtensorMap and the tensor-map encoder's types (resolved at run time, no link dependency)
 #include <cuda_bf16.h>
 
@@ -52,7 +51,10 @@ constexpr int kEpilogueWarps = 4;
 constexpr int kThreads = 32 * (kEpilogueWarps + 2);
 constexpr int kAccs = 2;  // accumulators in tensor memory (32 columns each)
 static_assert(kPlaneData <= kPlane && kPlane % 128 == 0, "TMA destinations 128-byte aligned");
-constexpr uint32_t kMaxPolls = 1u << 24;
+// A wait gives up once kWaitNs of global time have passed since its first poll (kMaxPolls bounds the polls as
+// well, should the timer not advance).  Legitimate waits in this kernel last microseconds.
+constexpr uint64_t kWaitNs = 1000000000ull;
+constexpr uint32_t kMaxPolls = 1u << 28;
 constexpr unsigned int kErrorBit = 8u;  // the volume error word's timeout bit
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -83,7 +85,14 @@ __device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint3
       "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
 }
 
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+  uint64_t start = 0;
   for (uint32_t i = 0; i < kMaxPolls; ++i) {
     uint32_t done;
     asm volatile(
@@ -93,6 +102,25 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
         : "=r"(done)
         : "r"(bar), "r"(phase));
     if (done) return true;
+    if ((i & 255u) == 0u) {
+      const uint64_t now = global_ns();
+      if (i == 0u) {
+        start = now;
+      } else if (now - start > kWaitNs) {
+        return false;
+      }
+    }
+  }
+  return false;
+}
+
+// The load gate of vh_nn_conv32_gated: true once *gate is nonzero, false if it stays zero for kWaitNs.
+__device__ __forceinline__ bool gate_wait(const unsigned int* gate) {
+  const uint64_t start = global_ns();
+  for (uint32_t i = 0; i < kMaxPolls; ++i) {
+    if (*reinterpret_cast<const volatile unsigned int*>(gate) != 0u) return true;
+    if (global_ns() - start > kWaitNs) return false;
+    __nanosleep(1000);
   }
   return false;
 }
@@ -186,8 +214,8 @@ __device__ __forceinline__ int epi_pos(int p, int q) { return 4 * p + (q ^ ((p >
 //     one arrival per warp) and applies bias / ReLU or the gradient mask and stores BF16.
 // Phase j of a barrier completes at its j-th use, so the waits use parity (q / kSlots) & 1 or (row / kAccs) & 1
 // and the releases of an earlier use the parity before.  A ring of at least 3 slots cannot deadlock: the row
-// an output row still needs to load was released by an earlier output row.  Every wait gives up after a
-// bounded number of polls: that role stops, the error word gets the timeout bit, and the roles waiting on it
+// an output row still needs to load was released by an earlier output row.  Every wait gives up after about
+// a second: that role stops, the error word gets the timeout bit, and the roles waiting on it
 // give up in turn; before tensor memory is freed, the loads and MMA groups still in flight are waited for
 // (bounded).
 template <int kSlots, int kRows>
@@ -197,6 +225,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_con
                                                                   const __nv_bfloat16* __restrict__ mask,
                                                                   __nv_bfloat16* __restrict__ out, int batch,
                                                                   int width, int height, int mode, int relu,
+                                                                  const unsigned int* __restrict__ gate,
                                                                   unsigned int* __restrict__ error) {
   static_assert(kSlots >= 3, "an output row needs three resident input rows");
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -259,6 +288,7 @@ __global__ void __launch_bounds__(kThreads, 1) conv32_tc_kernel(const __grid_con
 
   if (warp == kEpilogueWarps) {
     if (lane == 0) {  // producer
+      if (gate != nullptr && my_items > 0 && !gate_wait(gate)) ok = false;  // nothing loaded, nothing in flight
       for (int k = 0; k < my_items && ok; ++k) {
         int img, y0, x0, rows;
         item(k, img, y0, x0, rows);
@@ -455,7 +485,7 @@ int conv32_smem_bytes() { return conv32_variant().smem; }
 
 cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, const float* bias,
                           const __nv_bfloat16* mask, __nv_bfloat16* out, int batch, int width, int height, int mode,
-                          int relu, unsigned int* error, cudaStream_t s) {
+                          int relu, unsigned int* error, cudaStream_t s, const unsigned int* gate) {
   const Conv32Variant& cv = conv32_variant();
   // persistent CTAs, cv.ctas_per_sm per SM: each CTA stages the weights and allocates tensor memory once
   static int ctas = 0;
@@ -477,7 +507,8 @@ cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, c
   const cudaError_t e = encode_input_map(in, batch, width, height, &map);
   if (e != cudaSuccess) return e;
   void* args[] = {&map,    const_cast<__nv_bfloat16**>(&wpack), const_cast<float**>(&bias),
-                  const_cast<__nv_bfloat16**>(&mask), &out, &batch, &width, &height, &mode, &relu, &error};
+                  const_cast<__nv_bfloat16**>(&mask), &out, &batch, &width, &height, &mode, &relu,
+                  const_cast<unsigned int**>(&gate), &error};
   return cudaLaunchKernel(cv.fn, dim3(grid), dim3(kThreads), args, static_cast<size_t>(cv.smem), s);
 }
 
