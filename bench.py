@@ -343,6 +343,16 @@ def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
     torch.cuda.synchronize()
     recent_ms = r0.elapsed_time(r1)
     tris = backend.extract_mesh_cuda(vol)
+    # the indexed mesh of that full soup, welded on the device (the first call sizes the buffers)
+    nv_w, nf_w = C.c_size_t(), C.c_size_t()
+    sh = C.c_void_p(stream.cuda_stream)
+    capi.check(capi.lib().vh_weld_mesh(vol.handle, C.byref(nv_w), C.byref(nf_w), sh), vol.handle)
+    w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    w0.record(stream)
+    capi.check(capi.lib().vh_weld_mesh(vol.handle, C.byref(nv_w), C.byref(nf_w), sh), vol.handle)
+    w1.record(stream)
+    torch.cuda.synchronize()
+    weld = {"ms": round(w0.elapsed_time(w1), 3), "vertices": nv_w.value, "faces": nf_w.value}
     observed = vol.observed_voxel_count()
     tuned = vol.autotune_result()
 
@@ -382,7 +392,7 @@ def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
             "triangles": n_tri.value, "tris": tris, "observed": observed, "upd_mean": float(np.mean(upd)),
             "act_mean": float(np.mean(act)), "e2e_value": world * args.steps * px / e2e_s / 1e6,
             "clocks": clock_info, "autotune": tuned,
-            "mc_recent": {"frames": 100, "ms": round(recent_ms, 3), "triangles": n_recent.value}}
+            "mc_recent": {"frames": 100, "ms": round(recent_ms, 3), "triangles": n_recent.value}, "weld": weld}
 
 
 def graph_leg(args, torch, backend, capi, sc, frames, flush):
@@ -485,6 +495,7 @@ def run_gb300(args):
                 "updated_voxels_per_frame": round(r["upd_mean"]), "active_voxels_per_frame": round(r["act_mean"]),
                 "update_launch_shape": r["autotune"] if r["autotune"]["variant"] >= 0 else None,
                 "mc_incremental_last_100_frames": r["mc_recent"],
+                "mesh_weld": r["weld"],
                 "chamfer": quality.get(name)}
 
     if rank == 0:

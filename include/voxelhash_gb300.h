@@ -208,6 +208,17 @@ vh_status vh_extract_mesh_recent(vh_volume* volume, float iso_level, uint32_t fr
                                  void* stream);
 /* Copies the last extracted soup, 9 floats per triangle (v0, v1, v2), to host or device memory. */
 vh_status vh_copy_mesh(vh_volume* volume, float* out, size_t max_triangles, int32_t out_on_device, void* stream);
+/* Indexed mesh of the last extracted soup, built on the device (the indexed output of the reference demo's
+ * PLY writer, src/main.cpp:337-398, has no counterpart: it writes the soup).  Soup vertices are merged when
+ * their float32 coordinates are bit-identical (marching cubes computes an edge's vertex once per cell, so
+ * these are exactly the shared vertices).  Vertices are numbered in the order of their first use in the soup;
+ * faces keep the soup's order; faces with a repeated vertex or |cross(v1 - v0, v2 - v0)| <= 1e-8 (float32,
+ * the PLY writer's test) are dropped.  Deterministic.  Synchronises.  VH_ERR_CAPACITY above about 3.1e8
+ * triangles (32-bit indices). */
+vh_status vh_weld_mesh(vh_volume* volume, size_t* vertex_count, size_t* face_count, void* stream);
+/* Copies the last welded mesh: vertices 3 floats each, faces 3 int32 vertex numbers each. */
+vh_status vh_copy_welded_mesh(vh_volume* volume, float* vertices, size_t max_vertices, int32_t* faces,
+                              size_t max_faces, int32_t out_on_device, void* stream);
 
 vh_status vh_block_count(vh_volume* volume, uint64_t* count);
 vh_status vh_observed_voxel_count(vh_volume* volume, uint64_t* count);

@@ -229,6 +229,9 @@ def test_mesh_bit_exact_and_deterministic(env, small_orbit):
     from voxelhashmt_gb300 import mesh_io
     verts, faces = mesh_io.weld(got)
     assert 0 < verts.shape[0] < 3 * got.shape[0] and 0 < faces.shape[0] <= got.shape[0]
+    # the device weld builds the same indexed mesh
+    dv, df = backend.extract_mesh_indexed(vol)
+    assert np.array_equal(_bits(dv), _bits(verts)) and np.array_equal(df, faces)
     vol.close()
 
 
@@ -351,6 +354,10 @@ def test_room_frame_full_resolution_properties(env):
     assert vol.observed_voxel_count() == vol.recount_observed_voxels()
     tris = backend.extract_mesh_cuda(vol)
     assert tris.shape[0] > 1000 and np.all(np.isfinite(tris))
+    from voxelhashmt_gb300 import mesh_io
+    verts, faces = mesh_io.weld(tris)
+    dv, df = backend.extract_mesh_indexed(vol)
+    assert np.array_equal(_bits(dv), _bits(verts)) and np.array_equal(df, faces)
     vol.close()
 
 

@@ -64,3 +64,19 @@ def test_soup_writer_matches_reference_writer_bytes(reference_demo):
     mesh_io.write_ply_soup(mine, tris, comment="generated by tsdf_voxel_hash_demo")
     assert open(out, "rb").read() == open(mine, "rb").read()
     os.remove(mine)
+
+
+def test_weld_known_answer():
+    """Vertices numbered by first use, faces in soup order; a collapsed face and a zero-area face dropped; -0.0
+    and 0.0 are different bit patterns and stay different vertices."""
+    from voxelhashmt_gb300 import mesh_io
+    A, B, C, D = [0.0, 0.0, 1.0], [1.0, 0.0, 1.0], [0.0, 1.0, 1.0], [1.0, 1.0, 1.0]
+    E, F, G = [2.0, 0.0, 0.0], [3.0, 0.0, 0.0], [4.0, 0.0, 0.0]  # collinear
+    Z, Zm = [0.0, 0.0, 0.0], [-0.0, 0.0, 0.0]
+    soup = np.array([A + B + C, C + B + D, A + A + B, E + F + G, D + C + E, Z + A + B, Zm + C + D], np.float32)
+    verts, faces = mesh_io.weld(soup)
+    want_v = np.array([A, B, C, D, E, F, G, Z, Zm], np.float32)
+    assert np.array_equal(verts.view(np.uint32), want_v.view(np.uint32))
+    assert faces.tolist() == [[0, 1, 2], [2, 1, 3], [3, 2, 4], [7, 0, 1], [8, 2, 3]]
+    v0, f0 = mesh_io.weld(np.zeros((0, 9), np.float32))
+    assert v0.shape == (0, 3) and f0.shape == (0, 3)

@@ -111,6 +111,8 @@ _SIGNATURES = {
     "vh_frame_stats_enqueue": (C.c_int, [_vp, _vp, _vp]),
     "vh_frame_stats_decode": (C.c_int, [_vp, _vp, C.POINTER(VhFrameStats)]),
     "vh_copy_mesh": (C.c_int, [_vp, _vp, C.c_size_t, C.c_int32, _vp]),
+    "vh_weld_mesh": (C.c_int, [_vp, _szp, _szp, _vp]),
+    "vh_copy_welded_mesh": (C.c_int, [_vp, _vp, C.c_size_t, _vp, C.c_size_t, C.c_int32, _vp]),
     "vh_block_count": (C.c_int, [_vp, _u64p]),
     "vh_observed_voxel_count": (C.c_int, [_vp, _u64p]),
     "vh_recount_observed_voxels": (C.c_int, [_vp, _u64p, _vp]),

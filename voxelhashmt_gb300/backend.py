@@ -398,6 +398,25 @@ def extract_mesh_cuda(volume: VoxelHashTSDF, iso_level=0.0, stream=None, device_
     return out
 
 
+def extract_mesh_indexed(volume: VoxelHashTSDF, iso_level=0.0, stream=None, recent_frames=0):
+    """Indexed mesh (vertices (V, 3) float32, faces (F, 3) int32) welded on the device (vh_weld_mesh): soup
+    vertices merged when bit-identical, numbered by first use; collapsed and zero-area faces dropped."""
+    n = C.c_size_t()
+    s = _stream_handle(stream)
+    if recent_frames:
+        _capi.check(_capi.lib().vh_extract_mesh_recent(volume.handle, float(iso_level), int(recent_frames),
+                                                       C.byref(n), s), volume.handle)
+    else:
+        _capi.check(_capi.lib().vh_extract_mesh(volume.handle, float(iso_level), C.byref(n), s), volume.handle)
+    nv, nf = C.c_size_t(), C.c_size_t()
+    _capi.check(_capi.lib().vh_weld_mesh(volume.handle, C.byref(nv), C.byref(nf), s), volume.handle)
+    verts = np.zeros((nv.value, 3), np.float32)
+    faces = np.zeros((nf.value, 3), np.int32)
+    _capi.check(_capi.lib().vh_copy_welded_mesh(volume.handle, C.c_void_p(verts.ctypes.data), nv.value,
+                                                C.c_void_p(faces.ctypes.data), nf.value, 0, s), volume.handle)
+    return verts, faces
+
+
 def gpu_volume_cache_block_count(volume: VoxelHashTSDF):
     return volume.block_count()
 

@@ -59,6 +59,11 @@ struct vh_volume {
   float* d_tris = nullptr;
   size_t tri_capacity = 0;
   size_t mesh_triangles = 0;
+  // indexed mesh of the last extraction (vh_weld_mesh)
+  vh::WeldBuffers weld{};
+  size_t weld_capacity = 0;  // triangles
+  size_t weld_vertices = 0;
+  size_t weld_faces = 0;
   int* d_keys = nullptr;
   float4* d_export = nullptr;
   int* d_export_keys = nullptr;
@@ -326,6 +331,44 @@ vh_status autotune_step(vh_volume* v, int* variant, cudaEvent_t ev[2]) {
   return VH_OK;
 }
 
+void free_weld(vh_volume* v) {
+  vh::WeldBuffers& W = v->weld;
+  dfree(W.slot_first);
+  dfree(W.vslot);
+  dfree(W.vid);
+  dfree(W.flags);
+  dfree(W.number);
+  dfree(W.sums);
+  dfree(W.verts);
+  dfree(W.faces);
+  dfree(W.counts);
+  W.slot_mask = 0U;
+  v->weld_capacity = 0;
+}
+
+// weld buffers for a soup of `triangles` triangles (3 * triangles < 2^30)
+vh_status ensure_weld(vh_volume* v, size_t triangles) {
+  if (triangles <= v->weld_capacity && v->weld.counts) return VH_OK;
+  free_weld(v);
+  const size_t cap = std::max<size_t>(triangles + triangles / 8, 1024);
+  const size_t nv = 3 * cap;
+  size_t slots = 1024;
+  while (slots < 2 * nv) slots <<= 1;  // load factor <= 1/2
+  vh::WeldBuffers& W = v->weld;
+  VH_CUDA(v, dalloc(&W.slot_first, slots));
+  VH_CUDA(v, dalloc(&W.vslot, nv));
+  VH_CUDA(v, dalloc(&W.vid, nv));
+  VH_CUDA(v, dalloc(&W.flags, nv));
+  VH_CUDA(v, dalloc(&W.number, nv));
+  VH_CUDA(v, dalloc(&W.sums, vh::weld_scan_tiles(static_cast<uint32_t>(nv))));
+  VH_CUDA(v, dalloc(&W.verts, 3 * nv));
+  VH_CUDA(v, dalloc(&W.faces, nv));
+  VH_CUDA(v, dalloc(&W.counts, 3));
+  W.slot_mask = static_cast<uint32_t>(slots - 1);
+  v->weld_capacity = cap;
+  return VH_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -536,6 +579,7 @@ void vh_destroy(vh_volume* v) {
   dfree(v->d_mc_list_count);
   dfree(v->d_scalar);
   dfree(v->d_tris);
+  free_weld(v);
   dfree(v->d_keys);
   dfree(v->d_export);
   dfree(v->d_export_keys);
@@ -849,6 +893,50 @@ vh_status vh_copy_mesh(vh_volume* v, float* out, size_t max_triangles, int32_t o
   const cudaStream_t s = as_stream(stream);
   VH_CUDA(v, cudaMemcpyAsync(out, v->d_tris, v->mesh_triangles * 9 * sizeof(float),
                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  return VH_OK;
+}
+
+vh_status vh_weld_mesh(vh_volume* v, size_t* vertex_count, size_t* face_count, void* stream) {
+  if (!v || !vertex_count || !face_count) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_weld_mesh: bad argument");
+  const size_t nt = v->mesh_triangles;
+  // 32-bit vertex indices and a table of at most 2^31 slots: fewer than 2^30 soup vertices
+  if (3 * nt >= (static_cast<size_t>(1) << 30) / 9 * 8) {
+    return fail(v, VH_ERR_CAPACITY, "vh_weld_mesh: soup too large for 32-bit vertex indices");
+  }
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  const vh_status st = ensure_weld(v, nt);
+  if (st != VH_OK) return st;
+  VH_CUDA(v, vh::launch_weld(v->d_tris, static_cast<uint32_t>(nt), v->weld, s));
+  uint32_t counts[3] = {0U, 0U, 0U};
+  VH_CUDA(v, cudaMemcpyAsync(counts, v->weld.counts, sizeof(counts), cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  if (counts[2] != 0U) return fail(v, VH_ERR_HASH_FULL, "vh_weld_mesh: vertex table full");
+  v->weld_vertices = counts[0];
+  v->weld_faces = counts[1];
+  *vertex_count = v->weld_vertices;
+  *face_count = v->weld_faces;
+  return VH_OK;
+}
+
+vh_status vh_copy_welded_mesh(vh_volume* v, float* vertices, size_t max_vertices, int32_t* faces, size_t max_faces,
+                              int32_t on_device, void* stream) {
+  if (!v || (!vertices && v->weld_vertices) || (!faces && v->weld_faces)) {
+    return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_copy_welded_mesh: bad argument");
+  }
+  if (max_vertices < v->weld_vertices || max_faces < v->weld_faces) {
+    return fail(v, VH_ERR_BUFFER_TOO_SMALL, "vh_copy_welded_mesh: buffer too small");
+  }
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (v->weld_vertices) {
+    VH_CUDA(v, cudaMemcpyAsync(vertices, v->weld.verts, v->weld_vertices * 3 * sizeof(float), kind, s));
+  }
+  if (v->weld_faces) {
+    VH_CUDA(v, cudaMemcpyAsync(faces, v->weld.faces, v->weld_faces * 3 * sizeof(int32_t), kind, s));
+  }
   VH_CUDA(v, cudaStreamSynchronize(s));
   return VH_OK;
 }

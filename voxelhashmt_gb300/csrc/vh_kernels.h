@@ -85,6 +85,25 @@ cudaError_t launch_import(const Volume& V, const int* keys, const float4* voxels
 // depth ray-cast of the fused volume from pose p.T_wc: out[W*H] camera depth of the first plane crossing, 0 = none
 cudaError_t launch_raycast(const Volume& V, const Params& p, float min_depth, float max_depth, float step, float* out,
                            cudaStream_t s);
+// indexed mesh of a triangle soup (vertices merged when bit-identical, numbered by first use; faces in soup
+// order, collapsed and zero-area ones dropped).  Buffers for a soup of up to `capacity` triangles: slot_first
+// (slot_mask + 1 >= 6 * capacity slots, a power of two), vslot / vid / flags / number (3 * capacity words),
+// sums (weld_scan_tiles(3 * capacity) words), verts (9 * capacity floats), faces (3 * capacity ints), counts
+// (3 words: vertices, faces, table-full flag).  3 * ntri must be below 2^30.
+struct WeldBuffers {
+  uint32_t* slot_first;
+  uint32_t slot_mask;
+  uint32_t* vslot;
+  uint32_t* vid;
+  uint32_t* flags;
+  uint32_t* number;
+  uint32_t* sums;
+  float* verts;
+  int32_t* faces;
+  uint32_t* counts;
+};
+uint32_t weld_scan_tiles(uint32_t n);
+cudaError_t launch_weld(const float* tris, uint32_t ntri, const WeldBuffers& W, cudaStream_t s);
 // synthetic depth for the analytic benchmark scenes (prims: n x 10 floats, device memory)
 cudaError_t launch_render(const float* prims, int n_prims, const Params& p, uint32_t seed, uint32_t frame,
                           float sigma_z2, float dropout, float max_depth, float* out, cudaStream_t s);

@@ -6,7 +6,9 @@
   in the reference's order, so the bytes match apart from the comment line.
 * ``weld`` turns the soup from extract_mesh into an indexed mesh.  Vertices are merged only when their three
   float32 coordinates are bit-identical.  Neighbouring marching-cubes cells recompute a shared edge's vertex
-  from their own cluster centres, so only bit-identical copies are the same point.
+  from their own cluster centres, so only bit-identical copies are the same point.  Vertices are numbered by
+  first use and faces keep the soup's order, so the device weld (vh_weld_mesh, backend.extract_mesh_indexed)
+  returns the same arrays.
 * ``write_ply_indexed`` writes the welded mesh with area-weighted vertex normals.
 """
 from __future__ import annotations
@@ -65,15 +67,19 @@ def write_ply_soup(path, tris, comment="generated by voxelhashmt_gb300"):
 
 
 def weld(tris):
-    """(vertices (V, 3) float32, faces (F, 3) int32) from a soup; vertices merged when bit-identical; faces that
-    collapse (a repeated index) or have zero area are dropped."""
+    """(vertices (V, 3) float32, faces (F, 3) int32) from a soup; vertices merged when bit-identical and numbered
+    in the order of their first use in the soup; faces keep the soup's order, and faces that collapse (a
+    repeated index) or have zero area are dropped.  The device weld (vh_weld_mesh) gives the same arrays."""
     t = np.ascontiguousarray(np.asarray(tris, np.float32).reshape(-1, 3))
     if t.shape[0] == 0:
         return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
     keys = t.view(np.uint32)
-    uniq, inverse = np.unique(keys, axis=0, return_inverse=True)
-    verts = uniq.view(np.float32).reshape(-1, 3)
-    faces = inverse.reshape(-1, 3).astype(np.int32)
+    _, first, inverse = np.unique(keys, axis=0, return_index=True, return_inverse=True)
+    order = np.argsort(first, kind="stable")  # unique keys by first use
+    rank = np.empty(order.shape[0], np.int64)
+    rank[order] = np.arange(order.shape[0])
+    verts = t[first[order]]
+    faces = rank[inverse.reshape(-1)].reshape(-1, 3).astype(np.int32)
     ok = (faces[:, 0] != faces[:, 1]) & (faces[:, 1] != faces[:, 2]) & (faces[:, 0] != faces[:, 2])
     faces = faces[ok]
     area = _norm(_cross(verts[faces[:, 1]] - verts[faces[:, 0]], verts[faces[:, 2]] - verts[faces[:, 0]]))
