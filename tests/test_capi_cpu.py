@@ -32,13 +32,20 @@ def test_default_constants_are_the_reference_gpu_constants(product_lib):
 def test_status_strings_and_argument_checks(product_lib):
     capi = product_lib
     L = capi.lib()
-    for s in range(0, 10):
-        assert L.vh_status_string(s)
+    for s in range(0, 13):
+        assert L.vh_status_string(s) != b"unknown status"
     h = C.c_void_p()
     bad = capi.default_params(hash_buckets=1000)  # not a power of two
     assert L.vh_create(C.byref(bad), None, C.byref(h)) == capi.VH_ERR_INVALID_ARGUMENT
     bad = capi.default_params(max_blocks=(1 << 23) + 1)
     assert L.vh_create(C.byref(bad), None, C.byref(h)) == capi.VH_ERR_INVALID_ARGUMENT
+    # the checks come before any device call
+    n1, n2 = C.c_size_t(), C.c_size_t()
+    assert L.vh_weld_mesh(None, C.byref(n1), C.byref(n2), None) == capi.VH_ERR_INVALID_ARGUMENT
+    assert L.vh_copy_welded_mesh(None, None, 0, None, 0, 0, None) == capi.VH_ERR_INVALID_ARGUMENT
+    err = (C.c_uint32 * 1)()
+    assert L.vh_nn_conv32_gated(None, None, None, None, None, 1, 8, 8, 0, 0, None, err, None) == \
+        capi.VH_ERR_INVALID_ARGUMENT
 
 
 def test_no_device_is_reported_not_faked(product_lib):
