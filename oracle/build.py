@@ -1,6 +1,7 @@
 """Build recipes for the parity oracle (test infrastructure only).
 
-* ``build_oracle()`` compiles oracle/vh_oracle.c into oracle/liboracle.so with gcc.
+* ``build_oracle()`` compiles oracle/vh_oracle.c into oracle/liboracle.so with gcc, and again with
+  -DVO_FP64 (double arithmetic: the FP64 transcription) into oracle/liboracle64.so.
   ``-ffp-contract=off`` is mandatory: the restatement must round every a*b+c twice,
   exactly as the reference source is written (gcc on aarch64 contracts by default).
 * ``build_ref()`` compiles the reference itself, from the read-only reference tree, into
@@ -25,6 +26,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 REFERENCE = os.environ.get("VH_REFERENCE_ROOT", "/root/reference")
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
+ORACLE64_SO = os.path.join(HERE, "liboracle64.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libref.so")
 
@@ -40,16 +42,22 @@ def _run(cmd, stdin_text=None):
 
 
 def build_oracle(force=False):
+    """oracle/liboracle.so (float arithmetic: the restatement) and oracle/liboracle64.so (the same source with
+    -DVO_FP64: the FP64 transcription), compiled in parallel."""
     src = [os.path.join(HERE, "vh_oracle.c")]
     deps = src + [os.path.join(HERE, "vh_oracle.h"),
                   os.path.join(REPO, "voxelhashmt_gb300", "csrc", "vh_mc_tables.h")]
-    if not force and os.path.exists(ORACLE_SO) and \
-            os.path.getmtime(ORACLE_SO) >= max(os.path.getmtime(d) for d in deps):
-        return ORACLE_SO
-    cmd = ["gcc", "-std=c11", *FP_FLAGS, "-shared", "-I", os.path.join(REPO, "voxelhashmt_gb300", "csrc"),
-           *src, "-o", ORACLE_SO + ".tmp", "-lpthread", "-lm"]
-    _run(cmd)
-    os.replace(ORACLE_SO + ".tmp", ORACLE_SO)
+    newest = max(os.path.getmtime(d) for d in deps)
+    jobs = []
+    for so, defs in ((ORACLE_SO, []), (ORACLE64_SO, ["-DVO_FP64"])):
+        if force or not os.path.exists(so) or os.path.getmtime(so) < newest:
+            jobs.append((so, ["gcc", "-std=c11", *FP_FLAGS, *defs, "-shared", "-I",
+                              os.path.join(REPO, "voxelhashmt_gb300", "csrc"), *src, "-o", so + ".tmp", "-lpthread",
+                              "-lm"]))
+    with ThreadPoolExecutor(max_workers=2) as ex:
+        list(ex.map(lambda j: _run(j[1]), jobs))
+    for so, _ in jobs:
+        os.replace(so + ".tmp", so)
     return ORACLE_SO
 
 

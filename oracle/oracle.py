@@ -50,6 +50,7 @@ class VoPose(C.Structure):
 
 
 _lib = None
+_lib64 = None
 _ref = None
 
 _fp = C.POINTER(C.c_float)
@@ -61,61 +62,70 @@ def _f32(a):
     return a, a.ctypes.data_as(_fp)
 
 
-def lib():
-    global _lib
+def lib(fp64=False):
+    """The restatement (float arithmetic, bit-identical to the reference) or, with fp64, the FP64 transcription:
+    the same source built with double arithmetic (oracle/liboracle64.so)."""
+    global _lib, _lib64
+    if fp64:
+        if _lib64 is None:
+            _lib64 = _load(os.path.join(HERE, "liboracle64.so"))
+        return _lib64
     if _lib is None:
-        path = os.path.join(HERE, "liboracle.so")
-        if not os.path.exists(path):
-            from oracle import build as _b
-            _b.build_oracle()
-        L = C.CDLL(path)
-        L.vo_config_default.argtypes = [C.POINTER(VoConfig), C.c_int32]
-        L.vo_expf_own.argtypes = [C.c_float]
-        L.vo_expf_own.restype = C.c_float
-        L.vo_filter_depth.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp]
-        L.vo_depth_normals.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp,
-                                       C.POINTER(C.c_uint8)]
-        L.vo_raycast_depth.argtypes = [C.c_void_p, C.POINTER(VoIntrinsics), C.POINTER(VoPose), C.c_float, C.c_float,
-                                       C.c_float, _fp]
-        L.vo_surface_normal.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.c_float, C.c_float,
-                                        _fp]
-        L.vo_surface_normal.restype = C.c_int32
-        L.vo_collect_blocks.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose),
-                                        C.c_float, C.c_float, C.c_int32, _ip, C.c_int64]
-        L.vo_collect_blocks.restype = C.c_int64
-        L.vo_collect_band_blocks.argtypes = [_fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose), C.c_float, C.c_float,
-                                             C.c_int32, _ip, C.c_int64]
-        L.vo_collect_band_blocks.restype = C.c_int64
-        L.vo_volume_new.argtypes = [C.POINTER(VoConfig), C.c_float, C.c_float]
-        L.vo_volume_new.restype = C.c_void_p
-        L.vo_volume_free.argtypes = [C.c_void_p]
-        L.vo_volume_integrate_frame.argtypes = [C.c_void_p, _fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose),
-                                                C.c_int32]
-        L.vo_volume_integrate_frame.restype = C.c_int64
-        L.vo_volume_integrate_blocks.argtypes = [C.c_void_p, _ip, C.c_int64, _fp, C.POINTER(VoIntrinsics),
-                                                 C.POINTER(VoPose)]
-        L.vo_volume_block_count.argtypes = [C.c_void_p]
-        L.vo_volume_block_count.restype = C.c_int64
-        L.vo_volume_observed_voxels.argtypes = [C.c_void_p]
-        L.vo_volume_observed_voxels.restype = C.c_int64
-        L.vo_volume_get_block.argtypes = [C.c_void_p, C.c_int64, _ip, C.c_void_p]
-        L.vo_volume_find_block.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
-        L.vo_volume_find_block.restype = C.c_int64
-        L.vo_volume_set_block.argtypes = [C.c_void_p, C.c_int32 * 3, C.c_void_p]
-        L.vo_volume_extract_mesh.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_void_p)]
-        L.vo_volume_extract_mesh.restype = C.c_int64
-        L.vo_free.argtypes = [C.c_void_p]
-        L.vo_pack_normal.argtypes = [C.c_int32, _fp]
-        L.vo_pack_normal.restype = C.c_uint32
-        L.vo_unpack_normal.argtypes = [C.c_int32, C.c_int32, C.c_uint32, _fp]
-        L.vo_hash_block_key.argtypes = [C.c_int32, C.c_int32, C.c_int32]
-        L.vo_hash_block_key.restype = C.c_uint32
-        L.vo_pack_block_key.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]
-        L.vo_pack_block_key.restype = C.c_int32
-        L.vo_observation_weight.argtypes = [C.POINTER(VoConfig), C.c_float, C.c_float, C.c_float, C.c_float]
-        L.vo_observation_weight.restype = C.c_float
-        _lib = L
+        _lib = _load(os.path.join(HERE, "liboracle.so"))
     return _lib
+
+
+def _load(path):
+    if not os.path.exists(path):
+        from oracle import build as _b
+        _b.build_oracle()
+    L = C.CDLL(path)
+    L.vo_config_default.argtypes = [C.POINTER(VoConfig), C.c_int32]
+    L.vo_expf_own.argtypes = [C.c_float]
+    L.vo_expf_own.restype = C.c_float
+    L.vo_filter_depth.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp]
+    L.vo_depth_normals.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp,
+                                   C.POINTER(C.c_uint8)]
+    L.vo_raycast_depth.argtypes = [C.c_void_p, C.POINTER(VoIntrinsics), C.POINTER(VoPose), C.c_float, C.c_float,
+                                   C.c_float, _fp]
+    L.vo_surface_normal.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.c_float, C.c_float,
+                                    _fp]
+    L.vo_surface_normal.restype = C.c_int32
+    L.vo_collect_blocks.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose),
+                                    C.c_float, C.c_float, C.c_int32, _ip, C.c_int64]
+    L.vo_collect_blocks.restype = C.c_int64
+    L.vo_collect_band_blocks.argtypes = [_fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose), C.c_float, C.c_float,
+                                         C.c_int32, _ip, C.c_int64]
+    L.vo_collect_band_blocks.restype = C.c_int64
+    L.vo_volume_new.argtypes = [C.POINTER(VoConfig), C.c_float, C.c_float]
+    L.vo_volume_new.restype = C.c_void_p
+    L.vo_volume_free.argtypes = [C.c_void_p]
+    L.vo_volume_integrate_frame.argtypes = [C.c_void_p, _fp, C.POINTER(VoIntrinsics), C.POINTER(VoPose),
+                                            C.c_int32]
+    L.vo_volume_integrate_frame.restype = C.c_int64
+    L.vo_volume_integrate_blocks.argtypes = [C.c_void_p, _ip, C.c_int64, _fp, C.POINTER(VoIntrinsics),
+                                             C.POINTER(VoPose)]
+    L.vo_volume_block_count.argtypes = [C.c_void_p]
+    L.vo_volume_block_count.restype = C.c_int64
+    L.vo_volume_observed_voxels.argtypes = [C.c_void_p]
+    L.vo_volume_observed_voxels.restype = C.c_int64
+    L.vo_volume_get_block.argtypes = [C.c_void_p, C.c_int64, _ip, C.c_void_p]
+    L.vo_volume_find_block.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
+    L.vo_volume_find_block.restype = C.c_int64
+    L.vo_volume_set_block.argtypes = [C.c_void_p, C.c_int32 * 3, C.c_void_p]
+    L.vo_volume_extract_mesh.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_void_p)]
+    L.vo_volume_extract_mesh.restype = C.c_int64
+    L.vo_free.argtypes = [C.c_void_p]
+    L.vo_pack_normal.argtypes = [C.c_int32, _fp]
+    L.vo_pack_normal.restype = C.c_uint32
+    L.vo_unpack_normal.argtypes = [C.c_int32, C.c_int32, C.c_uint32, _fp]
+    L.vo_hash_block_key.argtypes = [C.c_int32, C.c_int32, C.c_int32]
+    L.vo_hash_block_key.restype = C.c_uint32
+    L.vo_pack_block_key.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]
+    L.vo_pack_block_key.restype = C.c_int32
+    L.vo_observation_weight.argtypes = [C.POINTER(VoConfig), C.c_float, C.c_float, C.c_float, C.c_float]
+    L.vo_observation_weight.restype = C.c_float
+    return L
 
 
 def config(flavor=FLAVOR_REF_GPU, exp_impl=EXP_OWN, threads=1, **overrides) -> VoConfig:
@@ -146,19 +156,19 @@ def expf_own(x: float) -> float:
     return lib().vo_expf_own(x)
 
 
-def filter_depth(cfg, depth, K):
+def filter_depth(cfg, depth, K, fp64=False):
     d, dp = _f32(depth)
     out = np.zeros_like(d)
-    lib().vo_filter_depth(C.byref(cfg), dp, C.byref(intrinsics(K)), out.ctypes.data_as(_fp))
+    lib(fp64).vo_filter_depth(C.byref(cfg), dp, C.byref(intrinsics(K)), out.ctypes.data_as(_fp))
     return out
 
 
-def depth_normals(cfg, depth, K):
+def depth_normals(cfg, depth, K, fp64=False):
     d, dp = _f32(depth)
     n = np.zeros(d.shape + (3,), np.float32)
     v = np.zeros(d.shape, np.uint8)
-    lib().vo_depth_normals(C.byref(cfg), dp, C.byref(intrinsics(K)), n.ctypes.data_as(_fp),
-                           v.ctypes.data_as(C.POINTER(C.c_uint8)))
+    lib(fp64).vo_depth_normals(C.byref(cfg), dp, C.byref(intrinsics(K)), n.ctypes.data_as(_fp),
+                               v.ctypes.data_as(C.POINTER(C.c_uint8)))
     return n, v
 
 
@@ -177,11 +187,11 @@ def pixel_normals(cfg, depth, K):
     return n, ok
 
 
-def collect_blocks(cfg, depth, K, P, voxel_size, truncation, stride=1):
+def collect_blocks(cfg, depth, K, P, voxel_size, truncation, stride=1, fp64=False):
     d, dp = _f32(depth)
     cap = max(1024, int(d.size) * 81 // max(1, stride * stride) + 1024)
     keys = np.zeros((cap, 3), np.int32)
-    n = lib().vo_collect_blocks(C.byref(cfg), dp, C.byref(intrinsics(K)), C.byref(pose(P)), voxel_size,
+    n = lib(fp64).vo_collect_blocks(C.byref(cfg), dp, C.byref(intrinsics(K)), C.byref(pose(P)), voxel_size,
                                 truncation, stride, keys.ctypes.data_as(_ip), cap)
     if n < 0:
         return None
@@ -203,13 +213,15 @@ def collect_band_blocks(depth, K, P, voxel_size, truncation, stride=1):
 class Volume:
     """The oracle's voxel-hash volume (reference layout: 12-byte key + 512 x 288-byte voxels)."""
 
-    def __init__(self, cfg, voxel_size, truncation):
+    def __init__(self, cfg, voxel_size, truncation, fp64=False):
+        """fp64: the FP64 transcription's volume (double arithmetic, float voxel records)."""
         self.cfg = cfg
-        self.h = lib().vo_volume_new(C.byref(cfg), voxel_size, truncation)
+        self.L = lib(fp64)
+        self.h = self.L.vo_volume_new(C.byref(cfg), voxel_size, truncation)
 
     def close(self):
         if self.h:
-            lib().vo_volume_free(self.h)
+            self.L.vo_volume_free(self.h)
             self.h = None
 
     def __del__(self):
@@ -217,26 +229,26 @@ class Volume:
 
     def integrate(self, depth, K, P, stride=1):
         d, dp = _f32(depth)
-        return lib().vo_volume_integrate_frame(self.h, dp, C.byref(intrinsics(K)), C.byref(pose(P)), stride)
+        return self.L.vo_volume_integrate_frame(self.h, dp, C.byref(intrinsics(K)), C.byref(pose(P)), stride)
 
     def integrate_blocks(self, keys, depth, K, P):
         k = np.ascontiguousarray(keys, np.int32).reshape(-1, 3)
         d, dp = _f32(depth)
-        lib().vo_volume_integrate_blocks(self.h, k.ctypes.data_as(_ip), k.shape[0], dp, C.byref(intrinsics(K)),
+        self.L.vo_volume_integrate_blocks(self.h, k.ctypes.data_as(_ip), k.shape[0], dp, C.byref(intrinsics(K)),
                                          C.byref(pose(P)))
 
     def raycast_depth(self, K, P, min_depth=0.1, max_depth=8.0, step_voxels=0.5):
         """Depth (H, W) float32 of the product's ray-cast definition on this volume; 0 = no hit."""
         out = np.zeros((K.height, K.width), np.float32)
-        lib().vo_raycast_depth(self.h, C.byref(intrinsics(K)), C.byref(pose(P)), float(min_depth), float(max_depth),
+        self.L.vo_raycast_depth(self.h, C.byref(intrinsics(K)), C.byref(pose(P)), float(min_depth), float(max_depth),
                                float(step_voxels), out.ctypes.data_as(_fp))
         return out
 
     def block_count(self):
-        return lib().vo_volume_block_count(self.h)
+        return self.L.vo_volume_block_count(self.h)
 
     def observed_voxels(self):
-        return lib().vo_volume_observed_voxels(self.h)
+        return self.L.vo_volume_observed_voxels(self.h)
 
     def blocks(self):
         """(keys (N,3) int32, voxels (N,512,6,3) structured VOXEL_DTYPE) in insertion order."""
@@ -244,21 +256,21 @@ class Volume:
         keys = np.zeros((n, 3), np.int32)
         vox = np.zeros((n, BLOCK_VOXELS, 6, 3), VOXEL_DTYPE)
         for i in range(n):
-            lib().vo_volume_get_block(self.h, i, keys[i].ctypes.data_as(_ip), vox[i].ctypes.data)
+            self.L.vo_volume_get_block(self.h, i, keys[i].ctypes.data_as(_ip), vox[i].ctypes.data)
         return keys, vox
 
     def set_block(self, key, voxels):
         v = np.ascontiguousarray(voxels, VOXEL_DTYPE)
-        lib().vo_volume_set_block(self.h, (C.c_int32 * 3)(*map(int, key)), v.ctypes.data)
+        self.L.vo_volume_set_block(self.h, (C.c_int32 * 3)(*map(int, key)), v.ctypes.data)
 
     def extract_mesh(self, iso=0.0):
         ptr = C.c_void_p()
-        n = lib().vo_volume_extract_mesh(self.h, iso, C.byref(ptr))
+        n = self.L.vo_volume_extract_mesh(self.h, iso, C.byref(ptr))
         if n == 0:
-            lib().vo_free(ptr)
+            self.L.vo_free(ptr)
             return np.zeros((0, 9), np.float32)
         arr = np.ctypeslib.as_array(C.cast(ptr, _fp), shape=(n * 9,)).reshape(n, 9).copy()
-        lib().vo_free(ptr)
+        self.L.vo_free(ptr)
         return arr
 
 

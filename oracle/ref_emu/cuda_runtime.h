@@ -1,5 +1,5 @@
 /*
- * cuda_runtime.h -- host-only CUDA emulation prelude used by oracle/build_ref.py to compile the
+ * cuda_runtime.h -- host-only CUDA emulation prelude used by oracle/build.py (build_ref) to compile the
  * reference's CUDA sources (src/cuda_*.cu) as ordinary C++ for the CPU.
  *
  * TEST INFRASTRUCTURE ONLY: it lets the reference's own kernels run sequentially on the host so

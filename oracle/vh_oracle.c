@@ -4,7 +4,15 @@
  * TEST INFRASTRUCTURE ONLY (parity oracle and CPU timing baseline); the CUDA
  * product never links it.  Every function cites the reference lines it follows.
  * Paths are relative to the reference project root.  Build with
- * -ffp-contract=off and without fast-math (see oracle/Makefile).
+ * -ffp-contract=off and without fast-math (oracle/build.py).
+ *
+ * Arithmetic type.  Built as is, `real` is float: every operation is rounded as the reference's float code
+ * rounds it, and the results are bit-identical to the reference (the pinned restatement).  Built with
+ * -DVO_FP64, `real` is double and the math functions are the double ones: the same equations in FP64
+ * arithmetic (the FP64 transcription).  Its inputs and stored data stay the reference's float data: depth,
+ * intrinsics, pose and its float inverse, the float constants, the filtered depth image and the voxel
+ * records, which are rounded to float when stored, as the reference stores them.  The exponential is libm's
+ * double exp in that build.
  */
 #define _GNU_SOURCE
 #include "vh_oracle.h"
@@ -14,6 +22,24 @@
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+
+#ifdef VO_FP64
+typedef double real;
+#define VO_FLOOR floor
+#define VO_FABS fabs
+#define VO_SQRT sqrt
+#define VO_LROUND lround
+#define VO_FMIN fmin
+#define VO_FMAX fmax
+#else
+typedef float real;
+#define VO_FLOOR floorf
+#define VO_FABS fabsf
+#define VO_SQRT sqrtf
+#define VO_LROUND lroundf
+#define VO_FMIN fminf
+#define VO_FMAX fmaxf
+#endif
 
 #define GPU VO_FLAVOR_REF_GPU
 #define CPU VO_FLAVOR_REF_CPU
@@ -25,10 +51,10 @@
 /* ------------------------------------------------------------------ vectors */
 /* math_types.h:44-101, cuda_tsdf_integrator.cu:181-217 */
 typedef struct {
-  float x, y, z;
+  real x, y, z;
 } v3;
 
-static inline v3 mk(float x, float y, float z) {
+static inline v3 mk(real x, real y, real z) {
   v3 r;
   r.x = x;
   r.y = y;
@@ -37,21 +63,21 @@ static inline v3 mk(float x, float y, float z) {
 }
 static inline v3 vsub(v3 a, v3 b) { return mk(a.x - b.x, a.y - b.y, a.z - b.z); }
 static inline v3 vadd(v3 a, v3 b) { return mk(a.x + b.x, a.y + b.y, a.z + b.z); }
-static inline v3 vmul(v3 v, float s) { return mk(v.x * s, v.y * s, v.z * s); }
-static inline v3 vdivs(v3 v, float s) { return mk(v.x / s, v.y / s, v.z / s); }
-static inline float vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 vmul(v3 v, real s) { return mk(v.x * s, v.y * s, v.z * s); }
+static inline v3 vdivs(v3 v, real s) { return mk(v.x / s, v.y / s, v.z / s); }
+static inline real vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 static inline v3 vcross(v3 a, v3 b) {
   return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
-static inline float vnorm(v3 v) { return sqrtf(vdot(v, v)); }
+static inline real vnorm(v3 v) { return VO_SQRT(vdot(v, v)); }
 
 /* GPU: cuda_tsdf_integrator.cu:201-209 and cuda_block_allocator.cu:127-135 (<=1e-6, multiply by 1/len);
  * CPU: math_types.h:95-101 (<=1e-8, divide by len). */
 static inline v3 vnormalize(int fl, v3 v) {
-  const float len = vnorm(v);
+  const real len = vnorm(v);
   if (fl == GPU) {
     if (len <= 1e-6f) return mk(0.0f, 0.0f, 0.0f);
-    const float inv = 1.0f / len;
+    const real inv = 1.0f / len;
     return mk(v.x * inv, v.y * inv, v.z * inv);
   }
   if (len <= 1e-8f) return mk(0.0f, 0.0f, 0.0f);
@@ -59,9 +85,9 @@ static inline v3 vnormalize(int fl, v3 v) {
 }
 
 /* CPU std::max/std::min (a<b?b:a) vs GPU fmaxf/fminf: equal for the finite non-NaN values used here. */
-static inline float fmax_f(float a, float b) { return (a < b) ? b : a; }
-static inline float fmin_f(float a, float b) { return (b < a) ? b : a; }
-static inline float clamp_f(float v, float lo, float hi) { return fmax_f(lo, fmin_f(hi, v)); }
+static inline real fmax_f(real a, real b) { return (a < b) ? b : a; }
+static inline real fmin_f(real a, real b) { return (b < a) ? b : a; }
+static inline real clamp_f(real v, real lo, real hi) { return fmax_f(lo, fmin_f(hi, v)); }
 
 /* math_types.h:180-198 / cuda_tsdf_integrator.cu:452-466 */
 static inline v3 pose_point(const vo_pose* P, v3 p) {
@@ -76,28 +102,28 @@ static inline v3 pose_vector(const vo_pose* P, v3 p) {
 /* Pose::inverse, math_types.h:192-197: R' = R^T, t' = R' * (t * -1) */
 static void pose_inverse(const vo_pose* P, vo_pose* out) {
   const float* R = P->R;
-  const float Rt[9] = {R[0], R[3], R[6], R[1], R[4], R[7], R[2], R[5], R[8]};
-  const float nt[3] = {P->t[0] * -1.0f, P->t[1] * -1.0f, P->t[2] * -1.0f};
-  memcpy(out->R, Rt, sizeof(Rt));
+  const real Rt[9] = {R[0], R[3], R[6], R[1], R[4], R[7], R[2], R[5], R[8]};
+  const real nt[3] = {P->t[0] * -1.0f, P->t[1] * -1.0f, P->t[2] * -1.0f};
+  for (int i = 0; i < 9; ++i) out->R[i] = (float)Rt[i];
   out->t[0] = Rt[0] * nt[0] + Rt[1] * nt[1] + Rt[2] * nt[2];
   out->t[1] = Rt[3] * nt[0] + Rt[4] * nt[1] + Rt[5] * nt[2];
   out->t[2] = Rt[6] * nt[0] + Rt[7] * nt[1] + Rt[8] * nt[2];
 }
 
 /* math_types.h:228-232, cuda_block_allocator.cu:145-151 */
-static inline v3 back_project(int u, int v, float d, const vo_intrinsics* K) {
-  return mk(((float)u - K->cx) * d / K->fx, ((float)v - K->cy) * d / K->fy, d);
+static inline v3 back_project(int u, int v, real d, const vo_intrinsics* K) {
+  return mk(((real)u - K->cx) * d / K->fx, ((real)v - K->cy) * d / K->fy, d);
 }
 /* voxel_hash_tsdf.h:586-593, cuda_tsdf_integrator.cu:570-579 */
-static inline v3 back_project_cont(float u, float v, float d, const vo_intrinsics* K) {
+static inline v3 back_project_cont(real u, real v, real d, const vo_intrinsics* K) {
   return mk((u - K->cx) * d / K->fx, (v - K->cy) * d / K->fy, d);
 }
 /* math_types.h:234-244, cuda_tsdf_integrator.cu:468-477 */
-static inline int project_point(v3 pc, const vo_intrinsics* K, float* u, float* v) {
+static inline int project_point(v3 pc, const vo_intrinsics* K, real* u, real* v) {
   if (pc.z <= 1e-6f) return 0;
   *u = K->fx * pc.x / pc.z + K->cx;
   *v = K->fy * pc.y / pc.z + K->cy;
-  return *u >= 0.0f && *u <= (float)(K->width - 1) && *v >= 0.0f && *v <= (float)(K->height - 1);
+  return *u >= 0.0f && *u <= (real)(K->width - 1) && *v >= 0.0f && *v <= (real)(K->height - 1);
 }
 
 /* ---------------------------------------------------------------------- exp */
@@ -136,14 +162,19 @@ float vo_expf_own(float x) {
   return (p * s.f) * 0x1p-64f;
 }
 
-static inline float vo_exp(const vo_config* c, float x) {
+static inline real vo_exp(const vo_config* c, real x) {
+#ifdef VO_FP64
+  (void)c;
+  return exp(x);
+#else
   return c->exp_impl == VO_EXP_OWN ? vo_expf_own(x) : expf(x);
+#endif
 }
 /* voxel_hash_tsdf.h:552-554, cuda_tsdf_integrator.cu:173-175 */
-static inline float gaussian(const vo_config* c, float sq, float inv_two_sigma_sq) {
+static inline real gaussian(const vo_config* c, real sq, real inv_two_sigma_sq) {
   return vo_exp(c, -sq * inv_two_sigma_sq);
 }
-static inline float inv_two_sigma_sq(float s) { return 1.0f / (2.0f * s * s); }
+static inline real inv_two_sigma_sq(real s) { return 1.0f / (2.0f * s * s); }
 
 /* ------------------------------------------------------------------- config */
 void vo_config_default(vo_config* c, int32_t flavor) {
@@ -217,7 +248,7 @@ static void parallel_for(int threads, int64_t n, pf_fn fn, void* ctx) {
 
 /* ----------------------------------------------------------- depth helpers */
 /* cuda_tsdf_integrator.cu:177-179, voxel_hash_tsdf.h:226-228, reconstruction_backend.cpp:38-40 */
-static inline float disc_threshold(const vo_config* c, float ref) {
+static inline real disc_threshold(const vo_config* c, real ref) {
   return fmax_f(c->disc_base, c->disc_rel * fmax_f(ref, 0.0f));
 }
 
@@ -232,23 +263,23 @@ static inline v3 orient_toward_camera(int fl, v3 n, v3 pc) {
 static int pixel_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, int u, int v, v3* normal) {
   const int W = K->width, H = K->height;
   if (u <= 0 || v <= 0 || u + 1 >= W || v + 1 >= H) return 0;
-  const float dc = depth[(size_t)v * W + u];
-  const float dl = depth[(size_t)v * W + u - 1];
-  const float dr = depth[(size_t)v * W + u + 1];
-  const float du = depth[(size_t)(v - 1) * W + u];
-  const float dd = depth[(size_t)(v + 1) * W + u];
+  const real dc = depth[(size_t)v * W + u];
+  const real dl = depth[(size_t)v * W + u - 1];
+  const real dr = depth[(size_t)v * W + u + 1];
+  const real du = depth[(size_t)(v - 1) * W + u];
+  const real dd = depth[(size_t)(v + 1) * W + u];
   if (!(dc > 0.0f) || !(dl > 0.0f) || !(dr > 0.0f) || !(du > 0.0f) || !(dd > 0.0f)) return 0;
-  const float thr = disc_threshold(c, dc);
-  if (fabsf(dl - dc) > thr || fabsf(dr - dc) > thr || fabsf(du - dc) > thr || fabsf(dd - dc) > thr) return 0;
-  const v3 pl = back_project_cont((float)(u - 1), (float)v, dl, K);
-  const v3 pr = back_project_cont((float)(u + 1), (float)v, dr, K);
-  const v3 pu = back_project_cont((float)u, (float)(v - 1), du, K);
-  const v3 pd = back_project_cont((float)u, (float)(v + 1), dd, K);
+  const real thr = disc_threshold(c, dc);
+  if (VO_FABS(dl - dc) > thr || VO_FABS(dr - dc) > thr || VO_FABS(du - dc) > thr || VO_FABS(dd - dc) > thr) return 0;
+  const v3 pl = back_project_cont((real)(u - 1), (real)v, dl, K);
+  const v3 pr = back_project_cont((real)(u + 1), (real)v, dr, K);
+  const v3 pu = back_project_cont((real)u, (real)(v - 1), du, K);
+  const v3 pd = back_project_cont((real)u, (real)(v + 1), dd, K);
   const v3 dx = vsub(pr, pl);
   const v3 dy = vsub(pd, pu);
   v3 n = vnormalize(c->flavor, vcross(dy, dx));
   if (vnorm(n) <= 1e-6f) return 0;
-  const v3 cp = back_project_cont((float)u, (float)v, dc, K);
+  const v3 cp = back_project_cont((real)u, (real)v, dc, K);
   n = orient_toward_camera(c->flavor, n, cp);
   *normal = n;
   return vnorm(n) > 1e-6f;
@@ -288,20 +319,20 @@ static void bilateral_row(void* p, int64_t vv) {
   filter_ctx* f = (filter_ctx*)p;
   const vo_config* c = f->c;
   const int W = f->K->width, H = f->K->height, v = (int)vv, R = c->filter_radius;
-  const float ks = inv_two_sigma_sq(c->filter_sigma_spatial);
-  const float kr = inv_two_sigma_sq(c->filter_sigma_range);
-  const float ka = inv_two_sigma_sq(c->filter_sigma_angular);
+  const real ks = inv_two_sigma_sq(c->filter_sigma_spatial);
+  const real kr = inv_two_sigma_sq(c->filter_sigma_range);
+  const real ka = inv_two_sigma_sq(c->filter_sigma_angular);
   for (int u = 0; u < W; ++u) {
     const size_t ci = (size_t)v * W + u;
-    const float center = f->depth[ci];
+    const real center = f->depth[ci];
     if (center <= 0.0f) {
       f->out[ci] = 0.0f;
       continue;
     }
     const int has_cn = f->valid[ci] != 0;
     const v3 cn = has_cn ? mk(f->normals[3 * ci], f->normals[3 * ci + 1], f->normals[3 * ci + 2]) : mk(0.0f, 0.0f, 0.0f);
-    const float thr = disc_threshold(c, center);
-    float wds = 0.0f, ws = 0.0f;
+    const real thr = disc_threshold(c, center);
+    real wds = 0.0f, ws = 0.0f;
     for (int dv = -R; dv <= R; ++dv) {
       const int sv = v + dv;
       if (sv < 0 || sv >= H) continue;
@@ -309,18 +340,18 @@ static void bilateral_row(void* p, int64_t vv) {
         const int su = u + du;
         if (su < 0 || su >= W) continue;
         const size_t si = (size_t)sv * W + su;
-        const float sd = f->depth[si];
-        if (sd <= 0.0f || fabsf(sd - center) > thr) continue;
-        const float spatial = (float)(du * du + dv * dv);
-        const float delta = sd - center;
-        const float range = delta * delta;
-        float w = gaussian(c, spatial, ks) * gaussian(c, range, kr);
+        const real sd = f->depth[si];
+        if (sd <= 0.0f || VO_FABS(sd - center) > thr) continue;
+        const real spatial = (real)(du * du + dv * dv);
+        const real delta = sd - center;
+        const real range = delta * delta;
+        real w = gaussian(c, spatial, ks) * gaussian(c, range, kr);
         if (has_cn) {
           if (f->valid[si] == 0) continue;
           const v3 sn = mk(f->normals[3 * si], f->normals[3 * si + 1], f->normals[3 * si + 2]);
-          const float cosine = clamp_f(vdot(cn, sn), -1.0f, 1.0f);
+          const real cosine = clamp_f(vdot(cn, sn), -1.0f, 1.0f);
           if (cosine < c->filter_min_cos) continue;
-          const float ad = 1.0f - cosine;
+          const real ad = 1.0f - cosine;
           w *= gaussian(c, ad * ad, ka);
         }
         wds += w * sd;
@@ -351,14 +382,14 @@ void vo_filter_depth(const vo_config* c, const float* depth, const vo_intrinsics
 
 /* ---------------------------------------------------------------- sampling */
 /* cuda_tsdf_integrator.cu:479-489 (floorf(x+0.5)), voxel_hash_tsdf.h:673-682 (lround) */
-static inline int sample_nearest(int fl, const float* depth, const vo_intrinsics* K, float u, float v, float* d) {
+static inline int sample_nearest(int fl, const float* depth, const vo_intrinsics* K, real u, real v, real* d) {
   int ui, vi;
   if (fl == GPU) {
-    ui = (int)floorf(u + 0.5f);
-    vi = (int)floorf(v + 0.5f);
+    ui = (int)VO_FLOOR(u + 0.5f);
+    vi = (int)VO_FLOOR(v + 0.5f);
   } else {
-    ui = (int)lroundf(u);
-    vi = (int)lroundf(v);
+    ui = (int)VO_LROUND(u);
+    vi = (int)VO_LROUND(v);
   }
   if (ui < 0 || ui >= K->width || vi < 0 || vi >= K->height) return 0;
   *d = depth[(size_t)vi * K->width + ui];
@@ -366,38 +397,38 @@ static inline int sample_nearest(int fl, const float* depth, const vo_intrinsics
 }
 
 /* cuda_tsdf_integrator.cu:504-568, voxel_hash_tsdf.h:684-748 */
-static int sample_bilinear(const vo_config* c, const float* depth, const vo_intrinsics* K, float u, float v,
-                           float* out) {
+static int sample_bilinear(const vo_config* c, const float* depth, const vo_intrinsics* K, real u, real v,
+                           real* out) {
   const int W = K->width, H = K->height;
   if (W <= 0 || H <= 0) return 0;
-  if (u < 0.0f || v < 0.0f || u > (float)(W - 1) || v > (float)(H - 1)) return 0;
-  const int x0 = (int)floorf(u);
-  const int y0 = (int)floorf(v);
+  if (u < 0.0f || v < 0.0f || u > (real)(W - 1) || v > (real)(H - 1)) return 0;
+  const int x0 = (int)VO_FLOOR(u);
+  const int y0 = (int)VO_FLOOR(v);
   const int x1 = x0 + 1 < W - 1 ? x0 + 1 : W - 1;
   const int y1 = y0 + 1 < H - 1 ? y0 + 1 : H - 1;
-  const float tx = u - (float)x0;
-  const float ty = v - (float)y0;
-  const float d00 = depth[(size_t)y0 * W + x0];
-  const float d10 = depth[(size_t)y0 * W + x1];
-  const float d01 = depth[(size_t)y1 * W + x0];
-  const float d11 = depth[(size_t)y1 * W + x1];
+  const real tx = u - (real)x0;
+  const real ty = v - (real)y0;
+  const real d00 = depth[(size_t)y0 * W + x0];
+  const real d10 = depth[(size_t)y0 * W + x1];
+  const real d01 = depth[(size_t)y1 * W + x0];
+  const real d11 = depth[(size_t)y1 * W + x1];
   if (d00 > 0.0f && d10 > 0.0f && d01 > 0.0f && d11 > 0.0f) {
-    float ref = 0.0f;
+    real ref = 0.0f;
     if (!sample_nearest(c->flavor, depth, K, u, v, &ref)) ref = d00;
-    const float thr = disc_threshold(c, ref);
-    const float mn = fmin_f(fmin_f(d00, d10), fmin_f(d01, d11));
-    const float mx = fmax_f(fmax_f(d00, d10), fmax_f(d01, d11));
-    const float top = d00 + (d10 - d00) * tx;
-    const float bottom = d01 + (d11 - d01) * tx;
+    const real thr = disc_threshold(c, ref);
+    const real mn = fmin_f(fmin_f(d00, d10), fmin_f(d01, d11));
+    const real mx = fmax_f(fmax_f(d00, d10), fmax_f(d01, d11));
+    const real top = d00 + (d10 - d00) * tx;
+    const real bottom = d01 + (d11 - d01) * tx;
     if (mx - mn <= thr) {
       *out = top + (bottom - top) * ty;
       return 1;
     }
-    const float bw[4] = {(1.0f - tx) * (1.0f - ty), tx * (1.0f - ty), (1.0f - tx) * ty, tx * ty};
-    const float nd[4] = {d00, d10, d01, d11};
-    float wds = 0.0f, ws = 0.0f;
+    const real bw[4] = {(1.0f - tx) * (1.0f - ty), tx * (1.0f - ty), (1.0f - tx) * ty, tx * ty};
+    const real nd[4] = {d00, d10, d01, d11};
+    real wds = 0.0f, ws = 0.0f;
     for (int i = 0; i < 4; ++i) {
-      if (fabsf(nd[i] - ref) > thr) continue;
+      if (VO_FABS(nd[i] - ref) > thr) continue;
       wds += bw[i] * nd[i];
       ws += bw[i];
     }
@@ -410,8 +441,8 @@ static int sample_bilinear(const vo_config* c, const float* depth, const vo_intr
 }
 
 /* cuda_tsdf_integrator.cu:727-752, voxel_hash_tsdf.h:750-771 */
-static int base_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, float u, float v, v3* n) {
-  float dl = 0.0f, dr = 0.0f, du = 0.0f, dd = 0.0f;
+static int base_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, real u, real v, v3* n) {
+  real dl = 0.0f, dr = 0.0f, du = 0.0f, dd = 0.0f;
   if (!sample_bilinear(c, depth, K, u - 1.0f, v, &dl) || !sample_bilinear(c, depth, K, u + 1.0f, v, &dr) ||
       !sample_bilinear(c, depth, K, u, v - 1.0f, &du) || !sample_bilinear(c, depth, K, u, v + 1.0f, &dd)) {
     return 0;
@@ -427,38 +458,38 @@ static int base_normal(const vo_config* c, const float* depth, const vo_intrinsi
 }
 
 /* cuda_tsdf_integrator.cu:754-832, voxel_hash_tsdf.h:773-840 */
-static int surface_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, float u, float v,
+static int surface_normal(const vo_config* c, const float* depth, const vo_intrinsics* K, real u, real v,
                           v3* normal) {
   const int fl = c->flavor;
   v3 cn = mk(0.0f, 0.0f, 0.0f);
   if (!base_normal(c, depth, K, u, v, &cn)) return 0;
-  float cd = 0.0f;
+  real cd = 0.0f;
   if (!sample_bilinear(c, depth, K, u, v, &cd)) return 0;
   const v3 cp = back_project_cont(u, v, cd, K);
   cn = orient_toward_camera(fl, cn, cp);
-  const float ks = inv_two_sigma_sq(c->normal_sigma_spatial);
-  const float kr = inv_two_sigma_sq(c->normal_sigma_range);
-  const float ka = inv_two_sigma_sq(c->normal_sigma_angular);
+  const real ks = inv_two_sigma_sq(c->normal_sigma_spatial);
+  const real kr = inv_two_sigma_sq(c->normal_sigma_range);
+  const real ka = inv_two_sigma_sq(c->normal_sigma_angular);
   v3 wsum = mk(0.0f, 0.0f, 0.0f);
-  float ws = 0.0f;
+  real ws = 0.0f;
   const int R = c->normal_radius;
   for (int dv = -R; dv <= R; ++dv) {
     for (int du = -R; du <= R; ++du) {
-      const float su = u + (float)du;
-      const float sv = v + (float)dv;
+      const real su = u + (real)du;
+      const real sv = v + (real)dv;
       v3 sn = mk(0.0f, 0.0f, 0.0f);
       if (!base_normal(c, depth, K, su, sv, &sn)) continue;
-      float sd = 0.0f;
+      real sd = 0.0f;
       if (!sample_bilinear(c, depth, K, su, sv, &sd)) continue;
       const v3 sp = back_project_cont(su, sv, sd, K);
       sn = orient_toward_camera(fl, sn, sp);
-      const float spatial = (float)(du * du + dv * dv);
-      const float delta = sd - cd;
-      const float range = delta * delta;
-      const float cosine = clamp_f(vdot(cn, sn), -1.0f, 1.0f);
-      const float ad = 1.0f - cosine;
-      const float as = ad * ad;
-      const float w = gaussian(c, spatial, ks) * gaussian(c, range, kr) * gaussian(c, as, ka);
+      const real spatial = (real)(du * du + dv * dv);
+      const real delta = sd - cd;
+      const real range = delta * delta;
+      const real cosine = clamp_f(vdot(cn, sn), -1.0f, 1.0f);
+      const real ad = 1.0f - cosine;
+      const real as = ad * ad;
+      const real w = gaussian(c, spatial, ks) * gaussian(c, range, kr) * gaussian(c, as, ka);
       wsum.x += sn.x * w;
       wsum.y += sn.y * w;
       wsum.z += sn.z * w;
@@ -469,7 +500,7 @@ static int surface_normal(const vo_config* c, const float* depth, const vo_intri
     *normal = cn;
     return 1;
   }
-  const float inv = 1.0f / ws;
+  const real inv = 1.0f / ws;
   v3 n = vnormalize(fl, mk(wsum.x * inv, wsum.y * inv, wsum.z * inv));
   n = orient_toward_camera(fl, n, cp);
   if (vnorm(n) <= 1e-6f) n = cn;
@@ -481,20 +512,20 @@ static int surface_normal(const vo_config* c, const float* depth, const vo_intri
 /* cuda_tsdf_integrator.cu:429-450, voxel_hash_tsdf.h:556-584 */
 float vo_observation_weight(const vo_config* c, float depth, float sd, float trunc, float view) {
   if (depth <= 0.0f || trunc <= 1e-6f) return 0.0f;
-  const float dr = depth / c->depth_sigma;
-  const float dw = 1.0f / (1.0f + dr * dr);
-  const float nr = fabsf(sd) / trunc;
-  float rw = 1.0f;
+  const real dr = depth / c->depth_sigma;
+  const real dw = 1.0f / (1.0f + dr * dr);
+  const real nr = VO_FABS(sd) / trunc;
+  real rw = 1.0f;
   if (nr > c->huber_delta) rw = c->huber_delta / nr;
-  const float bw = 1.0f - 0.5f * clamp_f(nr, 0.0f, 1.0f);
-  const float base = fmax_f(c->min_obs_weight, dw * rw * bw);
-  const float aw = clamp_f(view, c->min_view_weight, 1.0f);
+  const real bw = 1.0f - 0.5f * clamp_f(nr, 0.0f, 1.0f);
+  const real base = fmax_f(c->min_obs_weight, dw * rw * bw);
+  const real aw = clamp_f(view, c->min_view_weight, 1.0f);
   return base * aw;
 }
 
 /* cuda_tsdf_integrator.cu:228-243, voxel_hash_tsdf.h:239-254 */
 static inline int dominant_direction(v3 n) {
-  const float nx = fabsf(n.x), ny = fabsf(n.y), nz = fabsf(n.z);
+  const real nx = VO_FABS(n.x), ny = VO_FABS(n.y), nz = VO_FABS(n.z);
   if (nx <= 1e-6f && ny <= 1e-6f && nz <= 1e-6f) return -1;
   if (nx >= ny && nx >= nz) return n.x >= 0.0f ? 0 : 1;
   if (ny >= nx && ny >= nz) return n.y >= 0.0f ? 2 : 3;
@@ -502,7 +533,7 @@ static inline int dominant_direction(v3 n) {
 }
 
 /* GPU: cuda_tsdf_integrator.cu:296-313; CPU: voxel_hash_tsdf.h:311-330 (dot with the unit axis) */
-static inline float coordinate_along(int fl, v3 p, int d) {
+static inline real coordinate_along(int fl, v3 p, int d) {
   if (fl == GPU) {
     switch (d) {
       case 0: return p.x;
@@ -513,32 +544,32 @@ static inline float coordinate_along(int fl, v3 p, int d) {
       default: return -p.z;
     }
   }
-  static const float axes[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  static const real axes[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
   return vdot(p, mk(axes[d][0], axes[d][1], axes[d][2]));
 }
 
-static inline float sign_not_zero(float v) { return v >= 0.0f ? 1.0f : -1.0f; }
+static inline real sign_not_zero(real v) { return v >= 0.0f ? 1.0f : -1.0f; }
 
 /* GPU: cuda_tsdf_integrator.cu:253-278 (floorf(x*65535+0.5)); CPU: voxel_hash_tsdf.h:268-289 (lround) */
 static uint32_t pack_normal(int fl, v3 raw) {
   const v3 n = vnormalize(fl, raw);
-  const float s = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
+  const real s = VO_FABS(n.x) + VO_FABS(n.y) + VO_FABS(n.z);
   if (s <= 1e-6f) return 0U;
   v3 p = vdivs(n, s);
   if (p.z < 0.0f) {
-    const float px = (1.0f - fabsf(p.y)) * sign_not_zero(p.x);
-    const float py = (1.0f - fabsf(p.x)) * sign_not_zero(p.y);
+    const real px = (1.0f - VO_FABS(p.y)) * sign_not_zero(p.x);
+    const real py = (1.0f - VO_FABS(p.x)) * sign_not_zero(p.y);
     p.x = px;
     p.y = py;
   }
   uint32_t q[2];
-  const float comp[2] = {p.x, p.y};
+  const real comp[2] = {p.x, p.y};
   for (int i = 0; i < 2; ++i) {
-    const float cl = clamp_f(comp[i] * 0.5f + 0.5f, 0.0f, 1.0f);
+    const real cl = clamp_f(comp[i] * 0.5f + 0.5f, 0.0f, 1.0f);
     if (fl == GPU) {
-      q[i] = (uint32_t)floorf(cl * 65535.0f + 0.5f);
+      q[i] = (uint32_t)VO_FLOOR(cl * 65535.0f + 0.5f);
     } else {
-      q[i] = (uint32_t)lroundf(cl * 65535.0f);
+      q[i] = (uint32_t)VO_LROUND(cl * 65535.0f);
     }
   }
   return q[0] | (q[1] << 16U);
@@ -548,19 +579,19 @@ static uint32_t pack_normal(int fl, v3 raw) {
  * GPU mesh extractor: cuda_mesh_extractor.cu:233-257 ((0,0,1) on degenerate);
  * CPU: voxel_hash_tsdf.h:291-309 (normalized). */
 static v3 unpack_normal(int fl, int mesh_variant, uint32_t packed) {
-  v3 n = mk((float)(packed & 0xffffU) / 65535.0f * 2.0f - 1.0f,
-            (float)((packed >> 16U) & 0xffffU) / 65535.0f * 2.0f - 1.0f, 0.0f);
-  n.z = 1.0f - fabsf(n.x) - fabsf(n.y);
+  v3 n = mk((real)(packed & 0xffffU) / 65535.0f * 2.0f - 1.0f,
+            (real)((packed >> 16U) & 0xffffU) / 65535.0f * 2.0f - 1.0f, 0.0f);
+  n.z = 1.0f - VO_FABS(n.x) - VO_FABS(n.y);
   if (n.z < 0.0f) {
-    const float px = (1.0f - fabsf(n.y)) * sign_not_zero(n.x);
-    const float py = (1.0f - fabsf(n.x)) * sign_not_zero(n.y);
+    const real px = (1.0f - VO_FABS(n.y)) * sign_not_zero(n.x);
+    const real py = (1.0f - VO_FABS(n.x)) * sign_not_zero(n.y);
     n.x = px;
     n.y = py;
   }
   if (fl == GPU && mesh_variant) {
-    const float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+    const real len = VO_SQRT(n.x * n.x + n.y * n.y + n.z * n.z);
     if (len <= 1e-6f) return mk(0.0f, 0.0f, 1.0f);
-    const float inv = 1.0f / len;
+    const real inv = 1.0f / len;
     return mk(n.x * inv, n.y * inv, n.z * inv);
   }
   return vnormalize(fl, n);
@@ -592,9 +623,9 @@ static void sort_layers(vo_layer* L) {
 }
 
 /* cuda_tsdf_integrator.cu:338-372, voxel_hash_tsdf.h:357-392 */
-static int find_layer_slot(int fl, const vo_layer* L, float sc, v3 n, float tol, float min_cos) {
+static int find_layer_slot(int fl, const vo_layer* L, real sc, v3 n, real tol, real min_cos) {
   int empty = -1, best = -1;
-  float best_delta = fl == GPU ? 1e30f : FLT_MAX;
+  real best_delta = fl == GPU ? 1e30f : FLT_MAX;
   for (int i = 0; i < LAYERS; ++i) {
     if (!(L[i].weight > 0.0f)) {
       if (empty < 0) empty = i;
@@ -602,7 +633,7 @@ static int find_layer_slot(int fl, const vo_layer* L, float sc, v3 n, float tol,
     }
     const v3 ln = unpack_normal(fl, 0, L[i].packed_normal);
     if (vdot(ln, n) < min_cos) continue;
-    const float delta = fabsf(L[i].surface_coord - sc);
+    const real delta = VO_FABS(L[i].surface_coord - sc);
     if (delta < best_delta) {
       best_delta = delta;
       best = i;
@@ -613,22 +644,22 @@ static int find_layer_slot(int fl, const vo_layer* L, float sc, v3 n, float tol,
 }
 
 /* cuda_tsdf_integrator.cu:374-427, voxel_hash_tsdf.h:479-529 */
-static void integrate_sample(const vo_config* c, float vs, vo_voxel* voxel, int d, float sc, v3 sp, v3 nw,
-                             float obs) {
+static void integrate_sample(const vo_config* c, real vs, vo_voxel* voxel, int d, real sc, v3 sp, v3 nw,
+                             real obs) {
   const int fl = c->flavor;
   if (d < 0 || d >= DIRS || obs <= 0.0f) return;
   const v3 n = vnormalize(fl, nw);
   if (vnorm(n) <= 1e-6f) return;
-  const float plane_offset = vdot(n, sp);
-  const float tol = fmax_f(1e-6f, vs * c->layer_merge_scale);
+  const real plane_offset = vdot(n, sp);
+  const real tol = fmax_f(1e-6f, vs * c->layer_merge_scale);
   vo_layer* L = voxel->layers[d];
   const int li = find_layer_slot(fl, L, sc, n, tol, c->layer_normal_cos);
   if (li < 0) return;
   vo_layer* layer = &L[li];
-  const float pw = layer->weight;
-  const float ew = fmin_f(obs, fmax_f(0.0f, c->max_weight - pw));
+  const real pw = layer->weight;
+  const real ew = fmin_f(obs, fmax_f(0.0f, c->max_weight - pw));
   if (ew <= 0.0f) return;
-  const float nwt = pw + ew;
+  const real nwt = pw + ew;
   v3 blended = n;
   layer->surface_coord = pw > 0.0f ? ((layer->surface_coord * pw + sc * ew) / nwt) : sc;
   layer->plane_offset = pw > 0.0f ? ((layer->plane_offset * pw + plane_offset * ew) / nwt) : plane_offset;
@@ -752,17 +783,17 @@ static int key_cmp(const void* a, const void* b) {
 
 /* GPU: cuda_block_allocator.cu:198-272 (floorf(p / (8 vs)), 27 neighbours, range-checked packing);
  * CPU: voxel_hash_tsdf.h:595-671 (floorDiv(floor(p / vs), 8), 27 neighbours). */
-static int insert_neighbourhood(int fl, v3 p, float vs, keymap* set) {
+static int insert_neighbourhood(int fl, v3 p, real vs, keymap* set) {
   int bx, by, bz;
   if (fl == GPU) {
-    const float bws = vs * 8.0f;
-    bx = (int)floorf(p.x / bws);
-    by = (int)floorf(p.y / bws);
-    bz = (int)floorf(p.z / bws);
+    const real bws = vs * 8.0f;
+    bx = (int)VO_FLOOR(p.x / bws);
+    by = (int)VO_FLOOR(p.y / bws);
+    bz = (int)VO_FLOOR(p.z / bws);
   } else {
-    bx = floor_div((int)floorf(p.x / vs), BLOCK);
-    by = floor_div((int)floorf(p.y / vs), BLOCK);
-    bz = floor_div((int)floorf(p.z / vs), BLOCK);
+    bx = floor_div((int)VO_FLOOR(p.x / vs), BLOCK);
+    by = floor_div((int)VO_FLOOR(p.y / vs), BLOCK);
+    bz = floor_div((int)VO_FLOOR(p.z / vs), BLOCK);
   }
   for (int dz = -1; dz <= 1; ++dz)
     for (int dy = -1; dy <= 1; ++dy)
@@ -777,14 +808,14 @@ static int insert_neighbourhood(int fl, v3 p, float vs, keymap* set) {
   return 1;
 }
 
-static int collect_into(const vo_config* c, const float* depth, const vo_intrinsics* K, const vo_pose* T, float vs,
-                        float trunc, int32_t stride, keymap* set) {
+static int collect_into(const vo_config* c, const float* depth, const vo_intrinsics* K, const vo_pose* T, real vs,
+                        real trunc, int32_t stride, keymap* set) {
   const int fl = c->flavor;
   const int s = stride > 1 ? stride : 1;
   const v3 cam = mk(T->t[0], T->t[1], T->t[2]);
   for (int v = 0; v < K->height; v += s) {
     for (int u = 0; u < K->width; u += s) {
-      const float d = depth[(size_t)v * K->width + u];
+      const real d = depth[(size_t)v * K->width + u];
       if (d <= 0.0f) continue;
       const v3 pc = back_project(u, v, d, K);
       const v3 pw = pose_point(T, pc);
@@ -827,19 +858,19 @@ int64_t vo_collect_blocks(const vo_config* c, const float* depth, const vo_intri
  * the end cell or when the next crossing lies past the segment (t > 1), and the end cell is always added.
  * Every visited key must pack into 21 bits per axis.  The point, ray and segment ends are computed as the
  * GPU flavour of the reference rule computes them (cuda_block_allocator.cu:231-258). */
-static int insert_band(v3 a, v3 b, float bws, keymap* set) {
-  int c[3] = {(int)floorf(a.x / bws), (int)floorf(a.y / bws), (int)floorf(a.z / bws)};
-  const int e[3] = {(int)floorf(b.x / bws), (int)floorf(b.y / bws), (int)floorf(b.z / bws)};
-  const float o[3] = {a.x, a.y, a.z};
-  const float d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
+static int insert_band(v3 a, v3 b, real bws, keymap* set) {
+  int c[3] = {(int)VO_FLOOR(a.x / bws), (int)VO_FLOOR(a.y / bws), (int)VO_FLOOR(a.z / bws)};
+  const int e[3] = {(int)VO_FLOOR(b.x / bws), (int)VO_FLOOR(b.y / bws), (int)VO_FLOOR(b.z / bws)};
+  const real o[3] = {a.x, a.y, a.z};
+  const real d[3] = {b.x - a.x, b.y - a.y, b.z - a.z};
   int st[3];
-  float tmax[3], tdel[3];
+  real tmax[3], tdel[3];
   for (int k = 0; k < 3; ++k) {
     st[k] = d[k] > 0.0f ? 1 : (d[k] < 0.0f ? -1 : 0);
     if (st[k] != 0) {
-      const float edge = (float)(c[k] + (st[k] > 0 ? 1 : 0)) * bws;
+      const real edge = (real)(c[k] + (st[k] > 0 ? 1 : 0)) * bws;
       tmax[k] = (edge - o[k]) / d[k];
-      tdel[k] = bws / fabsf(d[k]);
+      tdel[k] = bws / VO_FABS(d[k]);
     } else {
       tmax[k] = 3.0e38f;
       tdel[k] = 3.0e38f;
@@ -870,12 +901,12 @@ int64_t vo_collect_band_blocks(const float* depth, const vo_intrinsics* K, const
                                int32_t stride, vo_key* out, int64_t max_out) {
   const int s = stride > 1 ? stride : 1;
   const v3 cam = mk(T->t[0], T->t[1], T->t[2]);
-  const float bws = vs * 8.0f;
+  const real bws = vs * 8.0f;
   keymap set;
   keymap_init(&set, 1024);
   for (int v = 0; v < K->height; v += s) {
     for (int u = 0; u < K->width; u += s) {
-      const float d = depth[(size_t)v * K->width + u];
+      const real d = depth[(size_t)v * K->width + u];
       if (!(d > 0.0f)) continue;
       const v3 pw = pose_point(T, back_project(u, v, d, K));
       const v3 ray = vnormalize(GPU, vsub(pw, cam));
@@ -901,7 +932,7 @@ int64_t vo_collect_band_blocks(const float* depth, const vo_intrinsics* K, const
 /* ------------------------------------------------------------------ volume */
 struct vo_volume {
   vo_config cfg;
-  float vs, trunc;
+  real vs, trunc;
   keymap map;
   vo_key* keys;
   vo_voxel* voxels;
@@ -995,32 +1026,32 @@ static void integrate_block(void* p, int64_t i) {
   const int64_t bi = g->idx[i];
   const vo_key key = vol->keys[bi];
   vo_voxel* vox = &vol->voxels[bi * BLOCK_VOLUME];
-  const float vs = vol->vs, trunc = vol->trunc;
+  const real vs = vol->vs, trunc = vol->trunc;
   for (int lz = 0; lz < BLOCK; ++lz)
     for (int ly = 0; ly < BLOCK; ++ly)
       for (int lx = 0; lx < BLOCK; ++lx) {
-        const v3 pw = mk(((float)(key.x * BLOCK + lx) + 0.5f) * vs, ((float)(key.y * BLOCK + ly) + 0.5f) * vs,
-                         ((float)(key.z * BLOCK + lz) + 0.5f) * vs);
+        const v3 pw = mk(((real)(key.x * BLOCK + lx) + 0.5f) * vs, ((real)(key.y * BLOCK + ly) + 0.5f) * vs,
+                         ((real)(key.z * BLOCK + lz) + 0.5f) * vs);
         const v3 pc = pose_point(&g->T_cw, pw);
         if (pc.z <= 0.0f) continue;
-        float u = 0.0f, v = 0.0f;
+        real u = 0.0f, v = 0.0f;
         if (!project_point(pc, g->K, &u, &v)) continue;
-        float d = 0.0f;
+        real d = 0.0f;
         if (!sample_bilinear(c, g->depth, g->K, u, v, &d)) continue;
-        const float sd = d - pc.z;
+        const real sd = d - pc.z;
         if (sd <= -trunc) continue;
         const v3 view = vnormalize(fl, pc);
-        float view_w = 1.0f;
+        real view_w = 1.0f;
         v3 nc = vmul(view, -1.0f);
-        if (surface_normal(c, g->depth, g->K, u, v, &nc)) view_w = fabsf(vdot(nc, view));
-        const float obs = vo_observation_weight(c, d, sd, trunc, view_w);
+        if (surface_normal(c, g->depth, g->K, u, v, &nc)) view_w = VO_FABS(vdot(nc, view));
+        const real obs = vo_observation_weight(c, d, sd, trunc, view_w);
         if (obs <= 0.0f) continue;
         const v3 spc = back_project_cont(u, v, d, g->K);
         const v3 spw = pose_point(g->T_wc, spc);
         const v3 nw = vnormalize(fl, pose_vector(g->T_wc, nc));
         const int dir = dominant_direction(nw);
         if (dir < 0 || dir >= DIRS) continue;
-        const float sc = coordinate_along(fl, spw, dir);
+        const real sc = coordinate_along(fl, spw, dir);
         integrate_sample(c, vs, &vox[lx + BLOCK * (ly + BLOCK * lz)], dir, sc, spw, nw, obs);
       }
 }
@@ -1087,15 +1118,15 @@ static const vo_voxel* find_voxel(const vo_volume* v, int vx, int vy, int vz) {
 }
 
 /* cuda_mesh_extractor.cu:259-262, voxel_hash_tsdf.h:336-339 */
-static inline float plane_sd(int fl, const vo_layer* L, v3 p) {
+static inline real plane_sd(int fl, const vo_layer* L, v3 p) {
   const v3 n = unpack_normal(fl, 1, L->packed_normal);
   return n.x * p.x + n.y * p.y + n.z * p.z - L->plane_offset;
 }
 
 /* cuda_mesh_extractor.cu:305-356, voxel_hash_tsdf.h:423-477 */
-static int complete_cube(float values[8], int valid[8]) {
+static int complete_cube(real values[8], int valid[8]) {
   int cnt = 0;
-  float sum = 0.0f;
+  real sum = 0.0f;
   for (int c = 0; c < 8; ++c) {
     if (!valid[c]) continue;
     ++cnt;
@@ -1103,10 +1134,10 @@ static int complete_cube(float values[8], int valid[8]) {
   }
   if (cnt == 8) return 1;
   if (cnt < 6) return 0;
-  const float global = cnt > 0 ? (sum / (float)cnt) : 0.0f;
+  const real global = cnt > 0 ? (sum / (real)cnt) : 0.0f;
   for (int c = 0; c < 8; ++c) {
     if (valid[c]) continue;
-    float ns = 0.0f;
+    real ns = 0.0f;
     int nc = 0;
     for (int e = 0; e < 12; ++e) {
       const int c0 = kEdge[e][0], c1 = kEdge[e][1];
@@ -1120,17 +1151,17 @@ static int complete_cube(float values[8], int valid[8]) {
       ns += values[nb];
       ++nc;
     }
-    values[c] = nc > 0 ? (ns / (float)nc) : global;
+    values[c] = nc > 0 ? (ns / (real)nc) : global;
     valid[c] = 1;
   }
   return 1;
 }
 
 /* marching_cubes.h:34-46, cuda_mesh_extractor.cu:358-374 */
-static inline v3 interp_vertex(v3 p0, v3 p1, float v0, float v1, float iso) {
-  const float delta = v1 - v0;
-  if (fabsf(delta) < 1e-6f) return p0;
-  const float t = clamp_f((iso - v0) / delta, 0.0f, 1.0f);
+static inline v3 interp_vertex(v3 p0, v3 p1, real v0, real v1, real iso) {
+  const real delta = v1 - v0;
+  if (VO_FABS(delta) < 1e-6f) return p0;
+  const real t = clamp_f((iso - v0) / delta, 0.0f, 1.0f);
   return mk(p0.x + (p1.x - p0.x) * t, p0.y + (p1.y - p0.y) * t, p0.z + (p1.z - p0.z) * t);
 }
 
@@ -1157,7 +1188,7 @@ static void tri_push(tri_buf* b, v3 a, v3 c, v3 d) {
 }
 
 /* marching_cubes.h:48-94, cuda_mesh_extractor.cu:376-437 */
-static void polygonise(const v3 pos[8], const float val[8], float iso, tri_buf* out) {
+static void polygonise(const v3 pos[8], const real val[8], real iso, tri_buf* out) {
   int ci = 0;
   for (int c = 0; c < 8; ++c)
     if (val[c] < iso) ci |= (1 << c);
@@ -1179,7 +1210,7 @@ static void polygonise(const v3 pos[8], const float val[8], float iso, tri_buf* 
 
 typedef struct {
   const vo_volume* vol;
-  float iso;
+  real iso;
   int dir;
   tri_buf* bufs;
 } mesh_ctx;
@@ -1190,8 +1221,8 @@ static void mesh_block(void* p, int64_t bi) {
   const vo_volume* vol = m->vol;
   const vo_config* c = &vol->cfg;
   const int fl = c->flavor, d = m->dir;
-  const float vs = vol->vs;
-  const float tol = fmax_f(1e-6f, vs * c->layer_extract_scale);
+  const real vs = vol->vs;
+  const real tol = fmax_f(1e-6f, vs * c->layer_extract_scale);
   const vo_key key = vol->keys[bi];
   tri_buf* out = &m->bufs[bi];
   out->n = 0;
@@ -1201,18 +1232,18 @@ static void mesh_block(void* p, int64_t bi) {
         const int bx = key.x * BLOCK + lx, by = key.y * BLOCK + ly, bz = key.z * BLOCK + lz;
         v3 cc;
         if (fl == GPU) {
-          cc = mk(((float)bx + 1.0f) * vs, ((float)by + 1.0f) * vs, ((float)bz + 1.0f) * vs);
+          cc = mk(((real)bx + 1.0f) * vs, ((real)by + 1.0f) * vs, ((real)bz + 1.0f) * vs);
         } else {
-          cc = mk(((float)bx + 0.5f) * vs + 0.5f * vs, ((float)by + 0.5f) * vs + 0.5f * vs,
-                  ((float)bz + 0.5f) * vs + 0.5f * vs);
+          cc = mk(((real)bx + 0.5f) * vs + 0.5f * vs, ((real)by + 0.5f) * vs + 0.5f * vs,
+                  ((real)bz + 0.5f) * vs + 0.5f * vs);
         }
         const vo_voxel* corners[8];
         v3 pos[8];
-        float cand[24];
+        real cand[24];
         int nc = 0;
         for (int k = 0; k < 8; ++k) {
           const int vx = bx + kCorner[k][0], vy = by + kCorner[k][1], vz = bz + kCorner[k][2];
-          pos[k] = mk(((float)vx + 0.5f) * vs, ((float)vy + 0.5f) * vs, ((float)vz + 0.5f) * vs);
+          pos[k] = mk(((real)vx + 0.5f) * vs, ((real)vy + 0.5f) * vs, ((real)vz + 0.5f) * vs);
           corners[k] = find_voxel(vol, vx, vy, vz);
           if (!corners[k]) continue;
           for (int l = 0; l < LAYERS; ++l) {
@@ -1224,7 +1255,7 @@ static void mesh_block(void* p, int64_t bi) {
         if (nc <= 0) continue;
         /* insertion sort (GPU, :264-274); std::sort (CPU) yields the same order */
         for (int i = 1; i < nc; ++i) {
-          const float x = cand[i];
+          const real x = cand[i];
           int j = i - 1;
           while (j >= 0 && cand[j] > x) {
             cand[j + 1] = cand[j];
@@ -1232,12 +1263,12 @@ static void mesh_block(void* p, int64_t bi) {
           }
           cand[j + 1] = x;
         }
-        float centers[24];
+        real centers[24];
         int sizes[24];
         int ncl = 0;
         for (int i = 0; i < nc; ++i) {
-          const float key_i = cand[i];
-          if (ncl == 0 || fabsf(key_i - centers[ncl - 1]) > tol) {
+          const real key_i = cand[i];
+          if (ncl == 0 || VO_FABS(key_i - centers[ncl - 1]) > tol) {
             centers[ncl] = key_i;
             sizes[ncl] = 1;
             ++ncl;
@@ -1245,21 +1276,21 @@ static void mesh_block(void* p, int64_t bi) {
           }
           const int last = ncl - 1;
           const int cnt = sizes[last];
-          centers[last] = (centers[last] * (float)cnt + key_i) / (float)(cnt + 1);
+          centers[last] = (centers[last] * (real)cnt + key_i) / (real)(cnt + 1);
           sizes[last] = cnt + 1;
         }
         for (int ci = 0; ci < ncl; ++ci) {
-          const float sk = centers[ci];
-          float values[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          const real sk = centers[ci];
+          real values[8] = {0, 0, 0, 0, 0, 0, 0, 0};
           int valid[8] = {0, 0, 0, 0, 0, 0, 0, 0};
           for (int k = 0; k < 8; ++k) {
             if (!corners[k]) continue;
             int best = -1;
-            float best_delta = fl == GPU ? 1e30f : FLT_MAX;
+            real best_delta = fl == GPU ? 1e30f : FLT_MAX;
             for (int l = 0; l < LAYERS; ++l) {
               const vo_layer* L = &corners[k]->layers[d][l];
               if (!(L->weight > 0.0f)) continue;
-              const float delta = fabsf(plane_sd(fl, L, cc) - sk);
+              const real delta = VO_FABS(plane_sd(fl, L, cc) - sk);
               if (delta <= tol && delta < best_delta) {
                 best_delta = delta;
                 best = l;
@@ -1318,18 +1349,18 @@ typedef struct {
   const vo_volume* v;
   const vo_intrinsics* K;
   const vo_pose* T;
-  float min_depth, max_depth, step;
+  real min_depth, max_depth, step;
   float* out;
 } raycast_ctx;
 
-static int ray_plane_distance(const vo_volume* v, int gx, int gy, int gz, v3 x, v3 dw, float* sdf) {
+static int ray_plane_distance(const vo_volume* v, int gx, int gy, int gz, v3 x, v3 dw, real* sdf) {
   const vo_key k = {floor_div(gx, BLOCK), floor_div(gy, BLOCK), floor_div(gz, BLOCK)};
   const int64_t bi = keymap_find(&v->map, k);
   if (bi < 0) return 0;
   const int li = positive_mod(gx, BLOCK) + BLOCK * (positive_mod(gy, BLOCK) + BLOCK * positive_mod(gz, BLOCK));
   const vo_voxel* vox = &v->voxels[bi * BLOCK_VOLUME + li];
   int any = 0;
-  float best = 0.0f, best_w = 0.0f;
+  real best = 0.0f, best_w = 0.0f;
   for (int d = 0; d < DIRS; ++d) {
     for (int l = 0; l < LAYERS; ++l) {
       const vo_layer* L = &vox->layers[d][l];
@@ -1347,16 +1378,16 @@ static int ray_plane_distance(const vo_volume* v, int gx, int gy, int gz, v3 x, 
   return any;
 }
 
-static int ray_blended_distance(const vo_volume* v, v3 x, v3 dw, float* sdf) {
-  const float vs = v->vs;
-  const float fx = x.x / vs - 0.5f, fy = x.y / vs - 0.5f, fz = x.z / vs - 0.5f;
-  const int x0 = (int)floorf(fx), y0 = (int)floorf(fy), z0 = (int)floorf(fz);
-  const float tx = fx - (float)x0, ty = fy - (float)y0, tz = fz - (float)z0;
-  float ws = 0.0f, acc = 0.0f;
+static int ray_blended_distance(const vo_volume* v, v3 x, v3 dw, real* sdf) {
+  const real vs = v->vs;
+  const real fx = x.x / vs - 0.5f, fy = x.y / vs - 0.5f, fz = x.z / vs - 0.5f;
+  const int x0 = (int)VO_FLOOR(fx), y0 = (int)VO_FLOOR(fy), z0 = (int)VO_FLOOR(fz);
+  const real tx = fx - (real)x0, ty = fy - (real)y0, tz = fz - (real)z0;
+  real ws = 0.0f, acc = 0.0f;
   for (int k = 0; k < 8; ++k) {
     const int ax = k & 1, ay = (k >> 1) & 1, az = k >> 2;
-    const float w = (ax ? tx : 1.0f - tx) * (ay ? ty : 1.0f - ty) * (az ? tz : 1.0f - tz);
-    float s = 0.0f;
+    const real w = (ax ? tx : 1.0f - tx) * (ay ? ty : 1.0f - ty) * (az ? tz : 1.0f - tz);
+    real s = 0.0f;
     if (!ray_plane_distance(v, x0 + ax, y0 + ay, z0 + az, x, dw, &s)) continue;
     acc += w * s;
     ws += w;
@@ -1370,33 +1401,33 @@ static void raycast_row(void* p, int64_t row) {
   const raycast_ctx* c = (const raycast_ctx*)p;
   const vo_volume* v = c->v;
   const vo_intrinsics* K = c->K;
-  const float vs = v->vs;
+  const real vs = v->vs;
   for (int u = 0; u < K->width; ++u) {
-    const v3 dc = mk(((float)u - K->cx) / K->fx, ((float)row - K->cy) / K->fy, 1.0f);
+    const v3 dc = mk(((real)u - K->cx) / K->fx, ((real)row - K->cy) / K->fy, 1.0f);
     const v3 dw = pose_vector(c->T, dc);
     const v3 o = mk(c->T->t[0], c->T->t[1], c->T->t[2]);
-    const float dz = c->step * vs / vnorm(dc);
-    float z = c->min_depth, prev_sdf = 0.0f, prev_z = 0.0f, result = 0.0f;
+    const real dz = c->step * vs / vnorm(dc);
+    real z = c->min_depth, prev_sdf = 0.0f, prev_z = 0.0f, result = 0.0f;
     int prev_ok = 0;
     for (int it = 0; it < (1 << 16) && z <= c->max_depth; ++it) {
       const v3 x = mk(o.x + dw.x * z, o.y + dw.y * z, o.z + dw.z * z);
-      const int gx = (int)floorf(x.x / vs), gy = (int)floorf(x.y / vs), gz = (int)floorf(x.z / vs);
+      const int gx = (int)VO_FLOOR(x.x / vs), gy = (int)VO_FLOOR(x.y / vs), gz = (int)VO_FLOOR(x.z / vs);
       const int bx = floor_div(gx, BLOCK), by = floor_div(gy, BLOCK), bz = floor_div(gz, BLOCK);
       const vo_key k = {bx, by, bz};
       const int64_t bi = keymap_find(&v->map, k);
       if (bi < 0) {
         prev_ok = 0;
-        float zexit = 3.0e38f;
+        real zexit = 3.0e38f;
         const int bb[3] = {bx, by, bz};
-        const float oo[3] = {o.x, o.y, o.z}, dd[3] = {dw.x, dw.y, dw.z};
+        const real oo[3] = {o.x, o.y, o.z}, dd[3] = {dw.x, dw.y, dw.z};
         for (int a = 0; a < 3; ++a) {
-          if (dd[a] > 0.0f) zexit = fminf(zexit, ((float)((bb[a] + 1) * BLOCK) * vs - oo[a]) / dd[a]);
-          if (dd[a] < 0.0f) zexit = fminf(zexit, ((float)(bb[a] * BLOCK) * vs - oo[a]) / dd[a]);
+          if (dd[a] > 0.0f) zexit = VO_FMIN(zexit, ((real)((bb[a] + 1) * BLOCK) * vs - oo[a]) / dd[a]);
+          if (dd[a] < 0.0f) zexit = VO_FMIN(zexit, ((real)(bb[a] * BLOCK) * vs - oo[a]) / dd[a]);
         }
-        z = fmaxf(z + dz, zexit + 0.25f * dz);
+        z = VO_FMAX(z + dz, zexit + 0.25f * dz);
         continue;
       }
-      float sdf = 0.0f;
+      real sdf = 0.0f;
       if (!ray_blended_distance(v, x, dw, &sdf)) {
         prev_ok = 0;
         z += dz;

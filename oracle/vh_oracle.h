@@ -28,8 +28,12 @@
  * Pins: the REF_CPU flavour is checked bit-exactly against the reference CPU
  * sources compiled from the reference tree; the REF_GPU flavour (with
  * VO_EXP_LIBM) against the reference .cu sources compiled as host C++ under a
- * CUDA emulation prelude (oracle/build_ref.py), and both through the committed
+ * CUDA emulation prelude (oracle/build.py), and both through the committed
  * fixtures in tests/golden/.
+ *
+ * FP64 transcription: the same source built with -DVO_FP64 (liboracle64.so)
+ * computes in double with libm's double functions; this interface, the inputs
+ * and the stored voxel records stay float.
  */
 #ifndef VH_ORACLE_H
 #define VH_ORACLE_H

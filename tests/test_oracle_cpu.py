@@ -6,7 +6,9 @@
 * against the live reference build (oracle/_ref/libref.so) where the reference tree is present, on more
   frames and strides;
 * known-answer tests of the key hash, key packing, octahedral packing and the observation weight;
-* the product's exponential against float64 exp.
+* the product's exponential against float64 exp;
+* the restatement against the FP64 transcription (the same source in double arithmetic), with stated
+  tolerances.
 """
 import hashlib
 import os
@@ -224,3 +226,51 @@ def test_band_rule_is_a_walk_of_the_segment(O):
             safe = np.all((frac > 1e-3) & (frac < 1 - 1e-3), axis=1)
             need = {tuple(k) for k in np.floor(g[safe]).astype(np.int64).tolist()}
             assert need <= band_set, "a cell on a pixel's segment is missing from the band"
+
+
+def test_fp64_transcription_bounds_the_float_path(O):
+    """The restatement (float arithmetic, bit-identical to the reference and to the product's plain form) against
+    the same equations in FP64 (oracle/liboracle64.so), on the small orbit scene over four frames.  Stated
+    tolerances: filtered depth within 1e-6 relative with the same valid pixels; the same block keys; per layer
+    occupied in both, weight and surface coordinate within 1e-5 relative to max(|x|, 1) for all but 1e-4 of
+    the layers (the rest are observations that a rounding moved to another layer), plane offset within 1e-5 at
+    the 99th percentile; marching-cubes vertices within 1e-4 voxel at the median and 1e-2 voxel at the 99th
+    percentile (interpolation divides by corner-value differences)."""
+    from voxelhashmt_gb300 import scenes
+    sc = scenes.orbit_scene(seed=7, frames=24, width=64, height=48, fx=277.0 * 0.2, fy=277.0 * 0.2, cx=32.0, cy=24.0)
+    sc.voxel_size, sc.truncation = 0.02, 0.06
+    K = sc.intrinsics
+    cfg = O.config(O.FLAVOR_REF_GPU, O.EXP_OWN, threads=4)
+    v32 = O.Volume(cfg, sc.voxel_size, sc.truncation)
+    v64 = O.Volume(cfg, sc.voxel_size, sc.truncation, fp64=True)
+    for f in (0, 6, 12, 18):
+        d = scenes.render_depth(sc, f)
+        a, b = O.filter_depth(cfg, d, K), O.filter_depth(cfg, d, K, fp64=True)
+        assert np.array_equal(a > 0, b > 0)
+        ok = b > 0
+        assert np.max(np.abs(a[ok].astype(np.float64) - b[ok]) / b[ok]) <= 1e-6
+        k32 = O.collect_blocks(cfg, d, K, sc.poses[f], sc.voxel_size, sc.truncation)
+        k64 = O.collect_blocks(cfg, d, K, sc.poses[f], sc.voxel_size, sc.truncation, fp64=True)
+        assert np.array_equal(k32, k64)
+        v32.integrate(d, K, sc.poses[f], 1)
+        v64.integrate(d, K, sc.poses[f], 1)
+    ka, xa = O.sort_blocks(*v32.blocks())
+    kb, xb = O.sort_blocks(*v64.blocks())
+    assert np.array_equal(ka, kb)
+    occ_a, occ_b = xa["weight"] > 0, xb["weight"] > 0
+    both = occ_a & occ_b
+    assert (occ_a != occ_b).sum() <= 1e-4 * both.sum()
+    rel = {}
+    for name in ("weight", "surface_coord", "plane_offset"):
+        x, y = xa[name][both].astype(np.float64), xb[name][both].astype(np.float64)
+        rel[name] = np.abs(x - y) / np.maximum(np.abs(y), 1.0)
+    assert (rel["weight"] > 1e-5).mean() <= 1e-4
+    assert (rel["surface_coord"] > 1e-5).mean() <= 1e-4
+    assert np.quantile(rel["plane_offset"], 0.99) <= 1e-5
+    from scipy.spatial import cKDTree
+    ta, tb = v32.extract_mesh(), v64.extract_mesh()
+    assert abs(ta.shape[0] - tb.shape[0]) <= 1e-3 * tb.shape[0]
+    dist = cKDTree(tb.reshape(-1, 3).astype(np.float64)).query(ta.reshape(-1, 3).astype(np.float64))[0]
+    dist /= sc.voxel_size
+    assert np.median(dist) <= 1e-4 and np.quantile(dist, 0.99) <= 1e-2
+    assert v32.observed_voxels() == v64.observed_voxels()
