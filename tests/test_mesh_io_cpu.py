@@ -80,3 +80,19 @@ def test_weld_known_answer():
     assert faces.tolist() == [[0, 1, 2], [2, 1, 3], [3, 2, 4], [7, 0, 1], [8, 2, 3]]
     v0, f0 = mesh_io.weld(np.zeros((0, 9), np.float32))
     assert v0.shape == (0, 3) and f0.shape == (0, 3)
+
+
+def test_indexed_ply_round_trip(soup, tmp_path):
+    """The welded mesh written as an indexed PLY reads back with the same vertices and faces, and unit
+    area-weighted vertex normals."""
+    from voxelhashmt_gb300 import mesh_io
+    verts, faces = mesh_io.weld(soup)
+    out = os.path.join(str(tmp_path), "welded.ply")
+    mesh_io.write_ply_indexed(out, verts, faces)
+    v, f = mesh_io.read_ply(out)
+    assert np.array_equal(v[:, :3].view(np.uint32), verts.view(np.uint32))
+    assert np.array_equal(f, faces)
+    length = np.linalg.norm(v[:, 3:].astype(np.float64), axis=1)
+    used = np.zeros(verts.shape[0], bool)
+    used[faces.reshape(-1)] = True
+    assert np.allclose(length[used], 1.0, atol=1e-5)
