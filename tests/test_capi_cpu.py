@@ -71,3 +71,33 @@ def test_backend_preference_parsing():
     assert backend.parse_compute_backend_preference("auto") is backend.ComputeBackendPreference.AUTO
     with pytest.raises(ValueError):
         backend.parse_compute_backend_preference("tpu")
+
+
+def test_header_is_plain_c_and_a_c_program_links(product_lib, tmp_path):
+    """The boundary is a C ABI: the public header compiles as pedantic C99, and a C program linked against the
+    library runs its device-free calls (defaults, status strings, the device query)."""
+    import os
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not present")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib_dir = os.path.dirname(product_lib.LIB_PATH)
+    src = os.path.join(str(tmp_path), "client.c")
+    with open(src, "w") as f:
+        f.write('#include <stdio.h>\n#include "voxelhash_gb300.h"\n'
+                "int main(void) {\n"
+                "  vh_params p; vh_algorithm a; char msg[128];\n"
+                "  vh_params_default(&p); vh_algorithm_default(&a);\n"
+                "  vh_status s = vh_query_device(msg, sizeof msg);\n"
+                '  printf("%g %g %d %s|%s\\n", p.voxel_size, a.filter_sigma_spatial, (int)s, vh_status_string(s), '
+                "msg);\n"
+                "  return (p.voxel_size > 0.0f && a.filter_radius == 2) ? 0 : 1;\n"
+                "}\n")
+    exe = os.path.join(str(tmp_path), "client")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(root, "include"),
+                    src, "-L", lib_dir, "-lvoxelhash_gb300", "-Wl,-rpath," + lib_dir, "-o", exe], check=True,
+                   capture_output=True)
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert res.stdout.startswith("0.01 1.5 ")
