@@ -159,12 +159,17 @@ vh_status vh_visible_block_keys(vh_volume* volume, int32_t* keys_out, size_t max
  * cudaMalloc once running (real-time tracking loops that forbid allocator calls, applications whose own pool
  * owns the whole device): the same keys-only allocation as vh_allocate, with the hash table, visible list and
  * counters in a fixed static device array of the library (20 MiB per GPU, held until the process exits).
- * depth: device memory, width*height floats; keys_out: device memory, 3 int32 per key (NULL: count only).
+ * depth: device memory, width*height floats, already written when the stream reaches this call (a producer on
+ * another stream records an event that this stream waits for; the call orders itself against nothing else).
+ * keys_out: DEVICE memory, 3 int32 per key (unlike vh_allocate, whose keys_out is host memory); NULL: count
+ * only.  Runs on `stream` (NULL = the legacy default stream) and synchronises it.
  * Limit: at most 32,768 sampled pixels per call (e.g. 640x480 at allocation_stride 4, 181x181 at stride 1);
- * larger requests return VH_ERR_CAPACITY.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress) with that device current; make that first call before any stream capture.
- * Every call clears the table it uses, so no state carries over, but all calls share the one array:
- * calls that overlap on the same GPU race.  Synchronises the stream. */
+ * larger requests return VH_ERR_CAPACITY.  Each call looks up the array's device address
+ * (cudaGetSymbolAddress) with the call's device current -- a host-side query, so the address stays right after
+ * a cudaDeviceReset; the first call on a device may load the library's device code, so make it before any
+ * stream capture.  Every call clears the table it uses, so no state carries over, but all calls share the one
+ * array: calls that overlap on the same GPU race.  *count is 0 on every error except VH_ERR_BUFFER_TOO_SMALL,
+ * where it holds the number of keys. */
 vh_status vh_allocate_static_scratch(const float* depth, const vh_intrinsics* K, const vh_pose* T_wc,
                                      float voxel_size, float truncation_distance, int32_t allocation_stride,
                                      int32_t* keys_out, size_t max_keys, size_t* count, void* stream);
@@ -270,6 +275,19 @@ vh_status vh_profile_read(vh_volume* volume, double ms[4], uint64_t* frames);
 vh_status vh_render_depth(const float* prims, int32_t n_prims, const vh_intrinsics* K, const vh_pose* T_wc,
                           uint32_t seed, uint32_t frame, float sigma_z2, float dropout, float max_depth,
                           float* depth_out, void* stream);
+
+/* ---- The device exponential (diagnostics) ----
+ * The reference's Gaussian weights call expf (src/cuda_tsdf_integrator.cu:173-175); on a host that is the C
+ * library's expf.  The plain form evaluates them with a device restatement of that function which returns the
+ * same float for every argument.  vh_expf_eval: y[i] = that exponential of x[i] (device buffers, n floats),
+ * asynchronous on the stream.  vh_expf_check: for every float whose bit pattern lies in
+ * [first_bits, first_bits + count), compares the restatement's fast single-precision path with its
+ * double-precision sequence (the C library's operations) on the device; *mismatches receives the number of
+ * arguments (NaNs excluded) whose results differ and *first_mismatch the smallest such bit pattern
+ * (0xffffffff if none).  Synchronises. */
+vh_status vh_expf_eval(const float* x, float* y, uint64_t n, void* stream);
+vh_status vh_expf_check(uint32_t first_bits, uint64_t count, uint64_t* mismatches, uint32_t* first_mismatch,
+                        void* stream);
 
 /* ---- Multi-scene batch (no reference counterpart) ----
  * Many independent volumes fused together: each vh_batch_integrate call is one step in which every active

@@ -83,6 +83,9 @@ def _load(path):
     L.vo_config_default.argtypes = [C.POINTER(VoConfig), C.c_int32]
     L.vo_expf_own.argtypes = [C.c_float]
     L.vo_expf_own.restype = C.c_float
+    L.vo_expf_array.argtypes = [_fp, _fp, C.c_size_t]
+    L.vo_expf_compare_libm.argtypes = [C.c_uint32, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
+                                       C.POINTER(C.c_uint32)]
     L.vo_filter_depth.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp]
     L.vo_depth_normals.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp,
                                    C.POINTER(C.c_uint8)]
@@ -154,6 +157,22 @@ def pose(P) -> VoPose:
 
 def expf_own(x: float) -> float:
     return lib().vo_expf_own(x)
+
+
+def expf_array(x):
+    """vo_expf_own element-wise over a float32 array."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.empty_like(x)
+    lib().vo_expf_array(x.ctypes.data_as(_fp), y.ctypes.data_as(_fp), x.size)
+    return y
+
+
+def expf_compare_libm(first_bits, count, threads=8):
+    """(mismatches, smallest mismatching bit pattern or 0xffffffff) of vo_expf_own vs the C library's expf over the
+    float bit patterns [first_bits, first_bits + count), NaNs excluded."""
+    n, f = C.c_uint64(), C.c_uint32()
+    lib().vo_expf_compare_libm(first_bits, count, threads, C.byref(n), C.byref(f))
+    return n.value, f.value
 
 
 def filter_depth(cfg, depth, K, fp64=False):

@@ -127,39 +127,107 @@ static inline int project_point(v3 pc, const vo_intrinsics* K, real* u, real* v)
 }
 
 /* ---------------------------------------------------------------------- exp */
-/* Own single-precision exp used by the CUDA product (same constants, same fmaf sequence):
- * Cody-Waite reduction x = k ln2 + r with ln2 split into an 11-trailing-zero high part and a low part,
- * then e^r by the degree-7 Taylor polynomial in Horner form (|r| <= ln2/2, truncation < 6e-9 relative),
- * then scaling by 2^k through the exponent field (two steps below 2^-126). */
+/* The C library's single-precision exp, restated.  The reference's Gaussian weights call expf
+ * (cuda_tsdf_integrator.cu:173-175, voxel_hash_tsdf.h:552-554); compiled for a host, that resolves to the GNU C
+ * library's expf, which since glibc 2.28 is the table-driven algorithm published in ARM's optimized-routines
+ * (N = 32): z = x * N/ln2 and k = z rounded to the nearest integer in double, r = fma(N/ln2, x, -k),
+ * y = 2^(k/N) * (1 + C2 r + C1 r^2 + C0 r^3) in double with 2^(j/N) from a table, result (float) y.
+ * Pinned against glibc 2.39 (x86_64, the host the reference was compiled on): equal for every float argument
+ * (vo_expf_compare_libm, tests/test_oracle_cpu.py).  The CUDA product evaluates the same function on the
+ * device (vh_expf), so the product is compared bit-for-bit with both VO_EXP_OWN and VO_EXP_LIBM. */
+static const uint64_t k_exp2_tab[32] = {
+    /* bits of the double nearest 2^(j/32) minus (j << 47): adding k << 47 scales by 2^floor(k/32) */
+    0x3ff0000000000000ULL, 0x3fefd9b0d3158574ULL, 0x3fefb5586cf9890fULL, 0x3fef9301d0125b51ULL,
+    0x3fef72b83c7d517bULL, 0x3fef54873168b9aaULL, 0x3fef387a6e756238ULL, 0x3fef1e9df51fdee1ULL,
+    0x3fef06fe0a31b715ULL, 0x3feef1a7373aa9cbULL, 0x3feedea64c123422ULL, 0x3feece086061892dULL,
+    0x3feebfdad5362a27ULL, 0x3feeb42b569d4f82ULL, 0x3feeab07dd485429ULL, 0x3feea47eb03a5585ULL,
+    0x3feea09e667f3bcdULL, 0x3fee9f75e8ec5f74ULL, 0x3feea11473eb0187ULL, 0x3feea589994cce13ULL,
+    0x3feeace5422aa0dbULL, 0x3feeb737b0cdc5e5ULL, 0x3feec49182a3f090ULL, 0x3feed503b23e255dULL,
+    0x3feee89f995ad3adULL, 0x3feeff76f2fb5e47ULL, 0x3fef199bdd85529cULL, 0x3fef3720dcef9069ULL,
+    0x3fef5818dcfba487ULL, 0x3fef7c97337b9b5fULL, 0x3fefa4afa2a490daULL, 0x3fefd0765b6e4540ULL};
+
 float vo_expf_own(float x) {
-  if (!(x > -104.0f)) return 0.0f;
-  if (x > 0x1.62e42ep+6f) return INFINITY;
-  const float k = rintf(x * 0x1.715476p+0f);
-  float r = fmaf(k, -0x1.62e400p-1f, x);
-  r = fmaf(k, -0x1.7f7d1cp-20f, r);
-  float p = 0x1.a01a02p-13f;
-  p = fmaf(p, r, 0x1.6c16c2p-10f);
-  p = fmaf(p, r, 0x1.111112p-7f);
-  p = fmaf(p, r, 0x1.555556p-5f);
-  p = fmaf(p, r, 0x1.555556p-3f);
-  p = fmaf(p, r, 0x1.000000p-1f);
-  p = fmaf(p, r, 1.0f);
-  p = fmaf(p, r, 1.0f);
-  const int ki = (int)k;
+  static const double inv_ln2_n = 0x1.71547652b82fep+0 * 32.0, shift = 0x1.8p+52;
+  static const double c0 = 0x1.c6af84b912394p-20, c1 = 0x1.ebfce50fac4f3p-13, c2 = 0x1.62e42ff0c52d6p-6;
+  if (x != x) return x + x;
+  if (x < -0x1.9fe368p6f) return 0.0f;        /* below log(2^-150) */
+  if (x > 0x1.62e42ep6f) return INFINITY;     /* above log(2^128) */
   union {
-    uint32_t u;
-    float f;
-  } s;
-  if (ki > 127) {
-    s.u = (uint32_t)(127 + 127) << 23;
-    return (p * s.f) * 2.0f;
+    double d;
+    uint64_t u;
+  } kd, s;
+  const double xd = (double)x;
+  const double z = inv_ln2_n * xd;
+  kd.d = z + shift;
+  const uint64_t ki = kd.u;
+  const double k = kd.d - shift;
+  const double r = fma(inv_ln2_n, xd, -k);
+  s.u = k_exp2_tab[ki % 32] + (ki << 47);
+  const double p = fma(c0, r, c1);
+  const double r2 = r * r;
+  double y = fma(c2, r, 1.0);
+  y = fma(p, r2, y);
+  y = y * s.d;
+  return (float)y;
+}
+
+/* Element-wise vo_expf_own (test helper). */
+void vo_expf_array(const float* x, float* y, size_t n) {
+  for (size_t i = 0; i < n; ++i) y[i] = vo_expf_own(x[i]);
+}
+
+/* Compares vo_expf_own with the C library's expf on every float whose bit pattern lies in [first, first + count),
+ * NaNs excluded, on `threads` threads: the number of differing results and the smallest differing pattern
+ * (0xffffffff if none). */
+typedef struct {
+  uint64_t first, count, stride, offset, bad;
+  uint32_t first_bad;
+} cmp_slice;
+static void* cmp_worker(void* arg) {
+  cmp_slice* S = (cmp_slice*)arg;
+  S->bad = 0;
+  S->first_bad = 0xffffffffU;
+  for (uint64_t i = S->offset; i < S->count; i += S->stride) {
+    union {
+      uint32_t u;
+      float f;
+    } x, a, b;
+    x.u = (uint32_t)(S->first + i);
+    if (x.f != x.f) continue;
+    a.f = vo_expf_own(x.f);
+    b.f = expf(x.f);
+    if (a.u != b.u) {
+      ++S->bad;
+      if (x.u < S->first_bad) S->first_bad = x.u;
+    }
   }
-  if (ki >= -126) {
-    s.u = (uint32_t)(ki + 127) << 23;
-    return p * s.f;
+  return NULL;
+}
+void vo_expf_compare_libm(uint32_t first, uint64_t count, int threads, uint64_t* mismatches, uint32_t* first_mismatch) {
+  cmp_slice S[256];
+  pthread_t tid[256];
+  if (threads < 1) threads = 1;
+  if (threads > 256) threads = 256;
+  int started = 0;
+  for (int t = 0; t < threads; ++t) {
+    S[t].first = first;
+    S[t].count = count;
+    S[t].stride = (uint64_t)threads;
+    S[t].offset = (uint64_t)t;
   }
-  s.u = (uint32_t)(ki + 127 + 64) << 23;
-  return (p * s.f) * 0x1p-64f;
+  for (int t = 0; t < threads; ++t) {
+    if (pthread_create(&tid[t], NULL, cmp_worker, &S[t]) != 0) break;
+    ++started;
+  }
+  /* slices whose thread did not start run here */
+  for (int t = started; t < threads; ++t) cmp_worker(&S[t]);
+  for (int t = 0; t < started; ++t) pthread_join(tid[t], NULL);
+  *mismatches = 0;
+  *first_mismatch = 0xffffffffU;
+  for (int t = 0; t < threads; ++t) {
+    *mismatches += S[t].bad;
+    if (S[t].first_bad < *first_mismatch) *first_mismatch = S[t].first_bad;
+  }
 }
 
 static inline real vo_exp(const vo_config* c, real x) {

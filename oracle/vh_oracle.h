@@ -18,9 +18,10 @@
  *                      include/tsdfmc/marching_cubes.h:34-94 (polygoniser)
  *
  * Exponentials: VO_EXP_LIBM calls expf() like both reference paths do on their
- * own compilers; VO_EXP_OWN calls vo_expf_own(), the exp the CUDA product uses
- * (Cody-Waite reduction + degree-7 Taylor/Horner in fmaf), so the product is
- * compared bit-for-bit with the oracle and expf vs own-exp is a stated tolerance.
+ * own compilers; VO_EXP_OWN calls vo_expf_own(), a restatement of the C library's
+ * expf algorithm (glibc >= 2.28) that returns the same float for every argument on
+ * the host the reference was compiled on.  The CUDA product evaluates that same
+ * function on the device, so it is compared bit-for-bit with both.
  *
  * Build with -ffp-contract=off (no fused multiply-add contraction) and without
  * -ffast-math: every a*b+c must round twice, as in the reference source.
@@ -106,6 +107,8 @@ typedef struct {
 void vo_config_default(vo_config* cfg, int32_t flavor);
 
 float vo_expf_own(float x);
+void vo_expf_array(const float* x, float* y, size_t n);
+void vo_expf_compare_libm(uint32_t first, uint64_t count, int threads, uint64_t* mismatches, uint32_t* first_mismatch);
 
 /* depth bilateral filter (both flavours): out[W*H] */
 void vo_filter_depth(const vo_config* cfg, const float* depth, const vo_intrinsics* K, float* out);

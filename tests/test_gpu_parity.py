@@ -1,9 +1,9 @@
 """GPU parity: the CUDA path (through the C ABI) against the oracle on the same seeded inputs.
 
 Plain FP32 form: filtered depth, filter normals, block-key sets, every voxel layer word, observed-voxel
-counts and the marching-cubes soup must be bit-identical to the oracle's REF_GPU flavour with the
-product's exp (VO_EXP_OWN).  Against the oracle with the C library expf (the reference's own exp), TSDF
-fields and weights must agree within 1e-5 relative and vertices within 1e-4 voxel.
+counts and the marching-cubes soup must be bit-identical to the oracle's REF_GPU flavour -- with its
+restatement of the C library's expf (VO_EXP_OWN) and with the C library's expf itself (VO_EXP_LIBM, the
+reference's own exponential), which are the same function.
 """
 import ctypes as C
 
@@ -235,38 +235,24 @@ def test_mesh_bit_exact_and_deterministic(env, small_orbit):
     vol.close()
 
 
-def test_reference_expf_tolerance(env, small_orbit):
-    """Own exp vs the C library expf (the exp the reference calls).  Block keys, layer occupancy and
-    triangle counts are identical; weight, surface_coord and plane_offset agree within 1e-5 relative to
-    max(|value|, 1) (metres for the two coordinates); matched vertices agree within 5e-3 voxel at the
-    99.9th percentile and 5e-2 voxel at most (marching cubes divides by the corner-value difference, which
-    amplifies the 1-ulp exp differences where that difference is small)."""
+def test_bit_exact_with_c_library_expf(env, small_orbit):
+    """Against the oracle evaluated with the C library's expf -- the exponential the reference calls -- the voxel
+    words and the triangle soup are bit-identical (where this host's C library is the restated algorithm)."""
     backend, O = env
-    from scipy.spatial import cKDTree
-    from voxelhashmt_gb300 import scenes
+    import os
+    n, first = O.expf_compare_libm(0x80000000, 0x7F800001, threads=max(os.cpu_count() or 1, 1))
+    # allowed: the one non-positive argument where an unfused reduction step rounds differently
+    if not (n == 0 or (n == 1 and first == 0xC27C65D9)):
+        pytest.skip("this host's C library expf is not the restated algorithm")
     sc = small_orbit
-    vol, _ = _integrate_both(backend, O, sc, frames=[0, 6, 12])
-    ref = O.Volume(O.config(O.FLAVOR_REF_GPU, O.EXP_LIBM, threads=8), sc.voxel_size, sc.truncation)
-    for f in [0, 6, 12]:
-        ref.integrate(scenes.render_depth(sc, f), sc.intrinsics, sc.poses[f])
+    vol, ref = _integrate_both(backend, O, sc, frames=[0, 6, 12], exp_impl=O.EXP_LIBM)
     gk, gv = O.sort_blocks(*vol.export_blocks())
     rk, rv = O.sort_blocks(*ref.blocks())
     assert np.array_equal(gk, rk)
-    g = gv.view(np.float32).reshape(-1, 4)
-    r = rv.view(np.float32).reshape(-1, 4)
-    assert np.array_equal(g[:, 0] > 0, r[:, 0] > 0)
-    both = g[:, 0] > 0
-    assert both.sum() > 1000
-    for col in range(3):
-        a, b = g[both, col].astype(np.float64), r[both, col].astype(np.float64)
-        err = np.abs(a - b) / np.maximum(np.abs(b), 1.0)
-        assert err.max() <= 1e-5, (col, float(err.max()))
+    assert np.array_equal(gv.reshape(len(gk), -1), rv.view(np.uint32).reshape(len(rk), -1))
     gm = backend.extract_mesh_cuda(vol)
     rm = ref.extract_mesh()
-    assert gm.shape == rm.shape
-    _, idx = cKDTree(rm.reshape(-1, 3, 3).mean(1)).query(gm.reshape(-1, 3, 3).mean(1))
-    dv = np.abs(gm.astype(np.float64) - rm[idx]).max(axis=1) / sc.voxel_size
-    assert np.quantile(dv, 0.999) <= 5e-3 and dv.max() <= 5e-2, (float(np.quantile(dv, 0.999)), float(dv.max()))
+    assert np.array_equal(O.canonical_triangles(gm).view(np.uint32), O.canonical_triangles(rm).view(np.uint32))
     vol.close()
 
 

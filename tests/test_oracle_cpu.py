@@ -39,12 +39,15 @@ def golden_scene():
     return {"depth": g["depth"], "K": K, "poses": poses, "vs": float(g["voxel_size"]), "trunc": float(g["truncation"])}
 
 
+@pytest.mark.parametrize("exp_name", ["libm", "own"])
 @pytest.mark.parametrize("flavor_name", ["gpu", "cpu"])
-def test_oracle_matches_reference_fixtures(O, golden_scene, flavor_name):
+def test_oracle_matches_reference_fixtures(O, golden_scene, flavor_name, exp_name):
+    """With the C library's expf, and with its restatement (which makes the check independent of the host's C
+    library), the oracle reproduces the reference's own outputs bit for bit."""
     gs = golden_scene
     ref = np.load(os.path.join(GOLDEN, "golden_%s.npz" % flavor_name))
     flavor = O.FLAVOR_REF_GPU if flavor_name == "gpu" else O.FLAVOR_REF_CPU
-    cfg = O.config(flavor, O.EXP_LIBM, threads=4)
+    cfg = O.config(flavor, O.EXP_LIBM if exp_name == "libm" else O.EXP_OWN, threads=4)
     K = gs["K"]
     d0 = gs["depth"][0]
     assert np.array_equal(_bits(O.filter_depth(cfg, d0, K)), _bits(ref["filtered0"]))
@@ -93,19 +96,41 @@ def test_known_answers(O):
         assert np.float32(got).view(np.uint32) == np.float32(w).view(np.uint32)
 
 
-def test_own_exp_accuracy(O):
-    """vh_expf (product) == vo_expf_own (oracle): within 1 ulp of exp over the arguments the path uses."""
+def _glibc_expf_host():
+    import platform
+    lib, ver = platform.libc_ver()
+    try:
+        major, minor = (int(v) for v in ver.split(".")[:2])
+    except ValueError:
+        return False
+    return lib == "glibc" and (major, minor) >= (2, 28)
+
+
+@pytest.mark.skipif(not _glibc_expf_host(), reason="the restated expf is the GNU C library's (glibc >= 2.28)")
+def test_own_exp_is_the_c_library_expf(O):
+    """vo_expf_own (restated in the oracle and, identically, on the device as vh_expf) returns the C library's
+    expf for every float argument: all non-positive floats (the path's arguments, -sq / (2 sigma^2)) and all
+    positive ones, exhaustively."""
+    threads = max(os.cpu_count() or 1, 1)
+    for first in (0x80000000, 0x00000000):  # -0 ... -inf, then +0 ... +inf
+        n, bad = O.expf_compare_libm(first, 0x7F800001, threads=threads)
+        assert n == 0, "%d differing arguments, the first %08x" % (n, bad)
     L = O.lib()
+    assert L.vo_expf_own(0.0) == 1.0 and L.vo_expf_own(-0.0) == 1.0
+    assert L.vo_expf_own(-200.0) == 0.0 and L.vo_expf_own(float("-inf")) == 0.0
+    assert L.vo_expf_own(100.0) == float("inf") and np.isnan(L.vo_expf_own(float("nan")))
+
+
+def test_own_exp_accuracy(O):
+    """vo_expf_own is within 0.51 ulp of exp (float64 reference) over the arguments the path uses."""
     xs = np.concatenate([-np.logspace(-8, np.log10(103.0), 20000), np.linspace(-20.0, 0.0, 20001),
                          np.linspace(0.0, 80.0, 2001)]).astype(np.float32)
-    got = np.array([L.vo_expf_own(float(x)) for x in xs], np.float32)
+    got = O.expf_array(xs)
     want = np.exp(xs.astype(np.float64))
     normal = want > np.float64(np.finfo(np.float32).tiny)
     ulp = np.spacing(want[normal].astype(np.float32)).astype(np.float64)
     err = np.abs(got[normal].astype(np.float64) - want[normal]) / ulp
-    assert err.max() <= 1.0, float(err.max())
-    assert L.vo_expf_own(0.0) == 1.0
-    assert L.vo_expf_own(-200.0) == 0.0
+    assert err.max() <= 0.51, float(err.max())
 
 
 ref_only = pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(HERE), "oracle", "_ref", "libref.so")),

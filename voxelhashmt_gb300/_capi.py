@@ -152,6 +152,8 @@ _SIGNATURES = {
     "vh_profile_read": (C.c_int, [_vp, C.POINTER(C.c_double), _u64p]),
     "vh_render_depth": (C.c_int, [_vp, C.c_int32, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_uint32,
                                   C.c_uint32, C.c_float, C.c_float, C.c_float, _vp, _vp]),
+    "vh_expf_eval": (C.c_int, [_vp, _vp, C.c_uint64, _vp]),
+    "vh_expf_check": (C.c_int, [C.c_uint32, C.c_uint64, _u64p, C.POINTER(C.c_uint32), _vp]),
 }
 
 

@@ -3,9 +3,9 @@
 // Every floating-point expression below is written in the operation order of the reference CUDA
 // sources (src/cuda_tsdf_integrator.cu, src/cuda_block_allocator.cu, src/cuda_mesh_extractor.cu) and
 // the library is compiled with -fmad=false, so each a*b+c rounds twice exactly as the source reads;
-// IEEE division and square root are the nvcc defaults (-prec-div=true -prec-sqrt=true).  The only
-// deliberate difference from the reference is vh_expf (see below), which makes the plain FP32 form
-// reproducible bit-for-bit on the host.
+// IEEE division and square root are the nvcc defaults (-prec-div=true -prec-sqrt=true), and vh_expf returns
+// the C library's expf bit for bit (see below), so the plain FP32 form reproduces the reference compiled for
+// a host bit for bit.
 #pragma once
 
 #include <cstdint>
@@ -170,28 +170,151 @@ __device__ __forceinline__ f3 backproject(float u, float v, float d, const Param
   return mk3((u - p.cx) * d / p.fx, (v - p.cy) * d / p.fy, d);
 }
 
-// Single-precision exp: Cody-Waite reduction x = k ln2 + r (ln2 split in an 11-trailing-zero high part and a
-// low part), e^r by the degree-7 Taylor polynomial in Horner form with fused multiply-adds (|r| <= ln2/2,
-// truncation error < 6e-9 relative), scaling by 2^k through the exponent field (two steps below 2^-126).
-// The host oracle evaluates the identical fmaf sequence, so results agree bit-for-bit.
+// ---- Single-precision exponential, bit-identical to the C library's expf ----
+//
+// The reference weighs its bilateral taps with expf (cuda_tsdf_integrator.cu:173-175).  Compiled for a host,
+// that is the GNU C library's expf (glibc >= 2.28, the table-driven algorithm of ARM's optimized-routines):
+//   z = x * 32/ln2 (double), k = z rounded to the nearest integer (ties to even), r = fma(32/ln2, x, -k),
+//   y = 2^(k/32) * (1 + C2 r + C1 r^2 + C0 r^3) in double arithmetic (2^(j/32) from a 32-entry table),
+//   result = (float) y.
+// vh_expf returns exactly that float for every argument.  The GB300 runs FP64 at a small fraction of its FP32
+// rate, so the common path evaluates the same polynomial in float-float arithmetic (error below 2^-45.7 of
+// the result over every finite float argument) and rounds it itself; only when that value lies within 2^-40
+// of a rounding boundary (about 5 arguments in a million) does it run the double-precision sequence
+// (expf_double).  Every operation is an explicit round-to-nearest intrinsic, so the fast-math compile
+// evaluates it identically.
+namespace expf_detail {
+// bits of the double nearest 2^(j/32), minus j << 47 (so that adding k << 47 scales by 2^floor(k/32))
+static __device__ const unsigned long long kTab[32] = {
+    0x3ff0000000000000ULL, 0x3fefd9b0d3158574ULL, 0x3fefb5586cf9890fULL, 0x3fef9301d0125b51ULL,
+    0x3fef72b83c7d517bULL, 0x3fef54873168b9aaULL, 0x3fef387a6e756238ULL, 0x3fef1e9df51fdee1ULL,
+    0x3fef06fe0a31b715ULL, 0x3feef1a7373aa9cbULL, 0x3feedea64c123422ULL, 0x3feece086061892dULL,
+    0x3feebfdad5362a27ULL, 0x3feeb42b569d4f82ULL, 0x3feeab07dd485429ULL, 0x3feea47eb03a5585ULL,
+    0x3feea09e667f3bcdULL, 0x3fee9f75e8ec5f74ULL, 0x3feea11473eb0187ULL, 0x3feea589994cce13ULL,
+    0x3feeace5422aa0dbULL, 0x3feeb737b0cdc5e5ULL, 0x3feec49182a3f090ULL, 0x3feed503b23e255dULL,
+    0x3feee89f995ad3adULL, 0x3feeff76f2fb5e47ULL, 0x3fef199bdd85529cULL, 0x3fef3720dcef9069ULL,
+    0x3fef5818dcfba487ULL, 0x3fef7c97337b9b5fULL, 0x3fefa4afa2a490daULL, 0x3fefd0765b6e4540ULL};
+// the same 2^(j/32) as a float pair (high part, next 24 bits)
+static __device__ const float2 kTabF[32] = {
+    {0x1.000000p+0f, 0.0f},           {0x1.059b0ep+0f, -0x1.9d4f52p-25f}, {0x1.0b5586p+0f, 0x1.9f3122p-25f},
+    {0x1.11301ep+0f, -0x1.fdb496p-25f}, {0x1.172b84p+0f, -0x1.c15742p-27f}, {0x1.1d4874p+0f, -0x1.d2e8cap-25f},
+    {0x1.2387a6p+0f, 0x1.ceac48p-25f},  {0x1.29e9e0p+0f, -0x1.5c0424p-25f}, {0x1.306fe0p+0f, 0x1.4636e2p-25f},
+    {0x1.371a74p+0f, -0x1.18aac6p-25f}, {0x1.3dea64p+0f, 0x1.824684p-25f},  {0x1.44e086p+0f, 0x1.8624b4p-30f},
+    {0x1.4bfdaep+0f, -0x1.593abcp-25f}, {0x1.5342b6p+0f, -0x1.2c5610p-25f}, {0x1.5ab07ep+0f, -0x1.5bd5ecp-27f},
+    {0x1.6247ecp+0f, -0x1.f8b550p-25f}, {0x1.6a09e6p+0f, 0x1.9fcef4p-26f},  {0x1.71f75ep+0f, 0x1.1d8beep-25f},
+    {0x1.7a1148p+0f, -0x1.829fd0p-25f}, {0x1.82589ap+0f, -0x1.accc7cp-26f}, {0x1.8ace54p+0f, 0x1.15506ep-27f},
+    {0x1.93737cp+0f, -0x1.e64744p-25f}, {0x1.9c4918p+0f, 0x1.51f848p-27f},  {0x1.a5503cp+0f, -0x1.b83b54p-25f},
+    {0x1.ae89fap+0f, -0x1.a94b14p-26f}, {0x1.b7f770p+0f, -0x1.a09438p-25f}, {0x1.c199bep+0f, -0x1.3d56b2p-27f},
+    {0x1.cb720ep+0f, -0x1.8837ccp-27f}, {0x1.d5818ep+0f, -0x1.822dbcp-27f}, {0x1.dfc974p+0f, -0x1.908c94p-25f},
+    {0x1.ea4afap+0f, 0x1.52486cp-27f},  {0x1.f50766p+0f, -0x1.246eb0p-26f}};
+constexpr double kInvLn2N = 0x1.71547652b82fep+0 * 32.0;
+constexpr double kShift = 0x1.8p+52;
+constexpr double kC0 = 0x1.c6af84b912394p-20, kC1 = 0x1.ebfce50fac4f3p-13, kC2 = 0x1.62e42ff0c52d6p-6;
+constexpr float kLo = -0x1.9fe368p6f;  // below: the result rounds to 0 (log 2^-150)
+constexpr float kHi = 0x1.62e42ep6f;   // above: +inf (log 2^128)
+// float splits: kInvLn2N = kIH + kIM + kIL exactly; kCi = kCiH + kCiM (+ < 2^-48 relative)
+constexpr float kIH = 0x1.715476p+5f, kIM = 0x1.4ae0c0p-21f, kIL = -0x1p-46f;
+constexpr float kC0H = 0x1.c6af84p-20f, kC0M = 0x1.722472p-45f;
+constexpr float kC1H = 0x1.ebfce6p-13f, kC1M = -0x1.e0a762p-38f;
+constexpr float kC2H = 0x1.62e430p-6f, kC2M = -0x1.e75a54p-35f;
+constexpr float kWindow = 0x1p-40f;
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {  // |a| >= |b|
+  s = __fadd_rn(a, b);
+  e = __fsub_rn(b, __fsub_rn(s, a));
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+  p = __fmul_rn(a, b);
+  e = __fmaf_rn(a, b, -p);
+}
+}  // namespace expf_detail
+
+// The C library's double-precision sequence, operation for operation.
+static __device__ __noinline__ float expf_double(float x) {
+  using namespace expf_detail;
+  if (!(x >= kLo)) return x != x ? __fadd_rn(x, x) : 0.0f;
+  if (x > kHi) return __int_as_float(0x7f800000);
+  const double xd = static_cast<double>(x);
+  const double z = __dmul_rn(kInvLn2N, xd);
+  double kd = __dadd_rn(z, kShift);
+  const unsigned long long ki = static_cast<unsigned long long>(__double_as_longlong(kd));
+  kd = __dsub_rn(kd, kShift);
+  const double r = __fma_rn(kInvLn2N, xd, -kd);
+  const double s = __longlong_as_double(static_cast<long long>(kTab[ki % 32] + (ki << 47)));
+  const double c = __fma_rn(kC0, r, kC1);
+  const double r2 = __dmul_rn(r, r);
+  double y = __fma_rn(kC2, r, 1.0);
+  y = __fma_rn(c, r2, y);
+  y = __dmul_rn(y, s);
+  return __double2float_rn(y);
+}
+
 __device__ __forceinline__ float vh_expf(float x) {
-  if (!(x > -104.0f)) return 0.0f;
-  if (x > 0x1.62e42ep+6f) return __int_as_float(0x7f800000);
-  const float k = rintf(x * 0x1.715476p+0f);
-  float r = __fmaf_rn(k, -0x1.62e400p-1f, x);
-  r = __fmaf_rn(k, -0x1.7f7d1cp-20f, r);
-  float q = 0x1.a01a02p-13f;
-  q = __fmaf_rn(q, r, 0x1.6c16c2p-10f);
-  q = __fmaf_rn(q, r, 0x1.111112p-7f);
-  q = __fmaf_rn(q, r, 0x1.555556p-5f);
-  q = __fmaf_rn(q, r, 0x1.555556p-3f);
-  q = __fmaf_rn(q, r, 0x1.000000p-1f);
-  q = __fmaf_rn(q, r, 1.0f);
-  q = __fmaf_rn(q, r, 1.0f);
+  using namespace expf_detail;
+  if (!(x >= kLo && x <= kHi)) return expf_double(x);
+  // P = x * 32/ln2 exactly, as p0 + e0 + p1 + e1 + p2 (the last product's rounding is below 2^-59)
+  float p0, e0, p1, e1;
+  two_prod(x, kIH, p0, e0);
+  two_prod(x, kIM, p1, e1);
+  const float p2 = __fmul_rn(x, kIL);
+  float k = rintf(p0);
+  float s1, t1, rh, rl;
+  two_sum(e0, p1, s1, t1);
+  two_sum(__fsub_rn(p0, k), s1, rh, rl);  // p0 - k is exact
+  rl = __fadd_rn(rl, __fadd_rn(__fadd_rn(t1, e1), p2));
+  // k = the nearest integer to P; P within 2^-20 of a half-integer: the double sequence decides the tie
+  if (fabsf(__fsub_rn(fabsf(rh), 0.5f)) < 0x1p-20f) return expf_double(x);
+  if (rh > 0.5f) {
+    k = __fadd_rn(k, 1.0f);
+    rh = __fsub_rn(rh, 1.0f);
+  } else if (rh < -0.5f) {
+    k = __fsub_rn(k, 1.0f);
+    rh = __fadd_rn(rh, 1.0f);
+  }
+  // q = C2 r + C1 r^2 + C0 r^3 = r (C2 + r (C1 + r C0)), float-float
+  float t, te, vh, vl, m, me, wh, wl, qh, ql;
+  two_prod(kC0H, rh, t, te);
+  te = __fmaf_rn(kC0H, rl, __fmaf_rn(kC0M, rh, te));
+  two_sum(kC1H, t, vh, vl);
+  vl = __fadd_rn(vl, __fadd_rn(te, kC1M));
+  two_prod(rh, vh, m, me);
+  me = __fmaf_rn(rh, vl, __fmaf_rn(rl, vh, me));
+  fast_two_sum(kC2H, m, wh, wl);
+  wl = __fadd_rn(wl, __fadd_rn(me, kC2M));
+  two_prod(rh, wh, qh, ql);
+  ql = __fmaf_rn(rh, wl, __fmaf_rn(rl, wh, ql));
+  // Z = 2^(j/32) (1 + q), result = Z * 2^e with k = 32 e + j
   const int ki = static_cast<int>(k);
-  if (ki > 127) return (q * __int_as_float((127 + 127) << 23)) * 2.0f;
-  if (ki >= -126) return q * __int_as_float((ki + 127) << 23);
-  return (q * __int_as_float((ki + 127 + 64) << 23)) * 0x1p-64f;
+  const int e = ki >> 5;
+  const float2 T = kTabF[ki & 31];
+  float zh1, zl1, Zh, Zl;
+  two_prod(T.x, qh, zh1, zl1);
+  zl1 = __fadd_rn(zl1, __fmaf_rn(T.x, ql, __fmaf_rn(T.y, qh, T.y)));
+  fast_two_sum(T.x, zh1, Zh, Zl);
+  fast_two_sum(Zh, __fadd_rn(Zl, zl1), Zh, Zl);
+  const uint32_t zb = __float_as_uint(Zh);
+  const int ez = static_cast<int>(zb >> 23) - 127;
+  if (ez + e >= -126) {  // normal result: Zh unless Z lies within the window of a rounding boundary
+    const float ulp_up = __uint_as_float(static_cast<uint32_t>(ez + 104) << 23);
+    const float ulp_dn = (zb & 0x7fffffU) == 0U ? __fmul_rn(ulp_up, 0.5f) : ulp_up;
+    const float half = __fmul_rn(0.5f, Zl >= 0.0f ? ulp_up : ulp_dn);
+    if (__fsub_rn(half, fabsf(Zl)) <= kWindow) return expf_double(x);
+    return __uint_as_float(zb + (static_cast<uint32_t>(e) << 23));
+  }
+  // subnormal result: round Z * 2^(149 + e) to an integer n, the result's bit pattern
+  const float f = __uint_as_float(static_cast<uint32_t>(149 + e + 127) << 23);
+  const float zsh = __fmul_rn(Zh, f);
+  float n = rintf(zsh);
+  const float frac = __fadd_rn(__fsub_rn(zsh, n), __fmul_rn(Zl, f));
+  if (fabsf(__fsub_rn(fabsf(frac), 0.5f)) <= __fmul_rn(kWindow, f)) return expf_double(x);
+  if (frac > 0.5f) n = __fadd_rn(n, 1.0f);
+  else if (frac < -0.5f) n = __fsub_rn(n, 1.0f);
+  return __uint_as_float(static_cast<uint32_t>(static_cast<int>(n)));
 }
 
 // x / 65535.0f for x in {0, 1, ..., 65535}: reciprocal multiply plus one fused correction step (Markstein's

@@ -13,8 +13,6 @@
 // (issued on different streams or from different host threads) race on it.
 #include <cuda_runtime.h>
 
-#include <mutex>
-
 #include "../../include/voxelhash_gb300.h"
 #include "vh_common.cuh"
 #include "vh_kernels.h"
@@ -31,24 +29,22 @@ constexpr size_t kScratchBytes = kCountersOffset + 256;  // 20 MiB + 256 B
 
 static __device__ __align__(256) unsigned char g_vh_static_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-// Once per device, with that device current: the device address of the array.
+// The device address of the array in the current device's context.  The runtime resolves it on the host (no
+// allocation, no stream operation).  It is looked up on every call rather than cached per device: a
+// cudaDeviceReset destroys the context, and the next context may load the library's device code, and with it
+// the array, at another address.
 vh_status scratch_for_current_device(void** out) {
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return VH_ERR_NO_DEVICE;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_vh_static_scratch) != cudaSuccess || ptr == nullptr) {
-      cudaGetLastError();
-      return VH_ERR_CUDA;
-    }
-    g_scratch_ptr[dev] = ptr;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return VH_ERR_NO_DEVICE;
   }
-  *out = g_scratch_ptr[dev];
+  void* ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_vh_static_scratch) != cudaSuccess || ptr == nullptr) {
+    cudaGetLastError();
+    return VH_ERR_CUDA;
+  }
+  *out = ptr;
   return VH_OK;
 }
 
@@ -68,6 +64,7 @@ extern "C" vh_status vh_allocate_static_scratch(const float* depth, const vh_int
       !(voxel_size > 0.0f) || !(truncation_distance > 0.0f)) {
     return VH_ERR_INVALID_ARGUMENT;
   }
+  *count = 0;  // every later return leaves a defined count
   const int stride = allocation_stride > 1 ? allocation_stride : 1;
   const uint64_t samples = static_cast<uint64_t>((K->width + stride - 1) / stride) *
                            static_cast<uint64_t>((K->height + stride - 1) / stride);
@@ -123,12 +120,13 @@ extern "C" vh_status vh_allocate_static_scratch(const float* depth, const vh_int
   }
   if (c.error & vh::kErrKeyRange) return VH_ERR_KEY_RANGE;
   if (c.error & vh::kErrHashFull) return VH_ERR_HASH_FULL;
-  *count = c.visible_count;
+  *count = c.visible_count;  // also on VH_ERR_BUFFER_TOO_SMALL: the size the caller needs
   if (c.visible_count == 0U) return VH_OK;
   if (!keys_out) return VH_OK;
   if (c.visible_count > max_keys) return VH_ERR_BUFFER_TOO_SMALL;
   if (vh::launch_visible_keys(V, keys_out, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
     cudaGetLastError();
+    *count = 0;
     return VH_ERR_CUDA;
   }
   return VH_OK;
