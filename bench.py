@@ -222,11 +222,12 @@ def run_reference(args):
     K = sc.intrinsics
     cfg = O.config(O.FLAVOR_REF_CPU, O.EXP_LIBM, threads=threads)
     vol = O.Volume(cfg, sc.voxel_size, sc.truncation)
+    # frames from the host restatement of the device renderer: bit-identical to the GPU arm's frames
     for f in range(warm):
-        vol.integrate(scenes.render_depth(sc, f), K, sc.poses[f])
+        vol.integrate(O.render_depth(sc, f), K, sc.poses[f])
     elapsed, done = 0.0, 0
     while done < max_frames and elapsed < budget:
-        d = scenes.render_depth(sc, warm + done)
+        d = O.render_depth(sc, warm + done)
         t0 = time.perf_counter()
         vol.integrate(d, K, sc.poses[warm + done])
         elapsed += time.perf_counter() - t0

@@ -84,6 +84,8 @@ def _load(path):
     L.vo_expf_own.argtypes = [C.c_float]
     L.vo_expf_own.restype = C.c_float
     L.vo_expf_array.argtypes = [_fp, _fp, C.c_size_t]
+    L.vo_render_depth.argtypes = [_fp, C.c_int32, C.POINTER(VoIntrinsics), C.POINTER(VoPose), C.c_uint32, C.c_uint32,
+                                  C.c_float, C.c_float, C.c_float, _fp]
     L.vo_expf_compare_libm.argtypes = [C.c_uint32, C.c_uint64, C.c_int, C.POINTER(C.c_uint64),
                                        C.POINTER(C.c_uint32)]
     L.vo_filter_depth.argtypes = [C.POINTER(VoConfig), _fp, C.POINTER(VoIntrinsics), _fp]
@@ -116,6 +118,7 @@ def _load(path):
     L.vo_volume_find_block.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
     L.vo_volume_find_block.restype = C.c_int64
     L.vo_volume_set_block.argtypes = [C.c_void_p, C.c_int32 * 3, C.c_void_p]
+    L.vo_volume_apply_flat_blocks.argtypes = [C.c_void_p, _ip, C.c_void_p, C.c_int64]
     L.vo_volume_extract_mesh.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_void_p)]
     L.vo_volume_extract_mesh.restype = C.c_int64
     L.vo_free.argtypes = [C.c_void_p]
@@ -157,6 +160,18 @@ def pose(P) -> VoPose:
 
 def expf_own(x: float) -> float:
     return lib().vo_expf_own(x)
+
+
+def render_depth(scene, frame, noise=True):
+    """The device renderer's frame (vh_render_depth), restated on the host: bit-identical float32 HxW depth."""
+    K = scene.intrinsics
+    prims = np.ascontiguousarray(scene.prims, np.float32)
+    out = np.empty((K.height, K.width), np.float32)
+    Ki, Pi = intrinsics(K), pose(scene.poses[frame])
+    lib().vo_render_depth(prims.ctypes.data_as(_fp), prims.shape[0], C.byref(Ki), C.byref(Pi), scene.seed, frame,
+                          scene.noise_sigma_z2 if noise else 0.0, scene.dropout if noise else 0.0, scene.max_depth,
+                          out.ctypes.data_as(_fp))
+    return out
 
 
 def expf_array(x):
@@ -281,6 +296,14 @@ class Volume:
     def set_block(self, key, voxels):
         v = np.ascontiguousarray(voxels, VOXEL_DTYPE)
         self.L.vo_volume_set_block(self.h, (C.c_int32 * 3)(*map(int, key)), v.ctypes.data)
+
+    def apply_flat_blocks(self, keys, voxels):
+        """applyFlatBlocks (voxel_hash_tsdf.h:183-188): keys (N,3) int32, voxels (N,512,6,3) VOXEL_DTYPE or the
+        same bytes as a flat array, applied in order."""
+        k = np.ascontiguousarray(keys, np.int32).reshape(-1, 3)
+        v = np.ascontiguousarray(voxels).view(np.uint8).reshape(k.shape[0], -1)
+        assert v.shape[1] == BLOCK_VOXELS * VOXEL_DTYPE.itemsize
+        self.L.vo_volume_apply_flat_blocks(self.h, k.ctypes.data_as(_ip), v.ctypes.data, k.shape[0])
 
     def extract_mesh(self, iso=0.0):
         ptr = C.c_void_p()

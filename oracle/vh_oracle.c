@@ -1059,6 +1059,12 @@ void vo_volume_set_block(vo_volume* v, vo_key key, const vo_voxel* voxels) {
   memcpy(&v->voxels[idx * BLOCK_VOLUME], voxels, BLOCK_VOLUME * sizeof(vo_voxel));
 }
 
+/* VoxelHashTSDF::applyFlatBlocks (voxel_hash_tsdf.h:183-188): for each record in order, blocks_[key] (created
+ * if absent) takes the record's 512 voxels; a key given twice keeps the later record. */
+void vo_volume_apply_flat_blocks(vo_volume* v, const vo_key* keys, const vo_voxel* voxels, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) vo_volume_set_block(v, keys[i], voxels + i * BLOCK_VOLUME);
+}
+
 /* voxel_hash_tsdf.h:113-123, cuda_tsdf_integrator.cu:905-930 */
 int64_t vo_volume_observed_voxels(const vo_volume* v) {
   int64_t n = 0;
@@ -1518,4 +1524,183 @@ void vo_raycast_depth(const vo_volume* v, const vo_intrinsics* K, const vo_pose*
                       float step_voxels, float* out) {
   raycast_ctx c = {v, K, T_wc, min_depth, max_depth, step_voxels, out};
   parallel_for(v->cfg.threads, K->height, raycast_row, &c);
+}
+
+/* ------------------------------------------------------------- synthetic renderer */
+/* Host restatement of the device renderer (voxelhashmt_gb300/csrc/vh_render.cu, vh_render_depth): the analytic
+ * scenes ray-cast with FP32 geometry (IEEE add, multiply, divide, square root, no contraction), then Box-Muller
+ * noise in FP64 from a counter-based hash, with the renderer's own logarithm and cosine series.  The same
+ * operations in the same order, with explicit float and double types (independent of VO_FP64), so the frames are
+ * bit-identical to the device's.  The reference renders its demo frames the same way in spirit
+ * (src/main.cpp:189-335: ray-primitive hits, camera z, Gaussian noise, dropouts). */
+typedef struct {
+  float x, y, z;
+} rf3;
+static inline rf3 rmk(float x, float y, float z) {
+  rf3 r = {x, y, z};
+  return r;
+}
+static inline float rdot(rf3 a, rf3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline rf3 rsub(rf3 a, rf3 b) { return rmk(a.x - b.x, a.y - b.y, a.z - b.z); }
+
+static uint32_t r_lowbias32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7FEB352DU;
+  x ^= x >> 15;
+  x *= 0x846CA68BU;
+  x ^= x >> 16;
+  return x;
+}
+static double r_uniform01(uint32_t seed, uint32_t frame, uint32_t idx, uint32_t stream) {
+  const uint32_t key = seed * 0x9E3779B1U + frame * 0x85EBCA77U + stream * 0xC2B2AE3DU;
+  const uint32_t h = r_lowbias32(idx ^ r_lowbias32(key));
+  return ((double)h + 0.5) * 0x1p-32;
+}
+static const double r_atanh_c[11] = {0x1.0000000000000p+0, 0x1.5555555555555p-2, 0x1.999999999999ap-3,
+                                     0x1.2492492492492p-3, 0x1.c71c71c71c71cp-4, 0x1.745d1745d1746p-4,
+                                     0x1.3b13b13b13b14p-4, 0x1.1111111111111p-4, 0x1.e1e1e1e1e1e1ep-5,
+                                     0x1.af286bca1af28p-5, 0x1.8618618618618p-5};
+static const double r_cos_c[10] = {0x1.0000000000000p+0, 0x1.0000000000000p-1, 0x1.5555555555555p-5,
+                                   0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-16, 0x1.27e4fb7789f5cp-22,
+                                   0x1.1eed8eff8d898p-29, 0x1.93974a8c07c9dp-37, 0x1.ae7f3e733b81fp-45,
+                                   0x1.6827863b97d97p-53};
+static const double r_sin_c[10] = {0x1.0000000000000p+0, 0x1.5555555555555p-3, 0x1.1111111111111p-7,
+                                   0x1.a01a01a01a01ap-13, 0x1.71de3a556c734p-19, 0x1.ae64567f544e4p-26,
+                                   0x1.6124613a86d09p-33, 0x1.ae7f3e733b81fp-41, 0x1.952c77030ad4ap-49,
+                                   0x1.2f49b46814157p-57};
+static double r_noise_log(double u) {
+  int e = 0;
+  double m = frexp(u, &e);
+  if (m < 0x1.6a09e667f3bcdp-1) {
+    m = m * 2.0;
+    e -= 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double s2 = s * s;
+  double q = r_atanh_c[10];
+  for (int k = 9; k >= 0; --k) q = q * s2 + r_atanh_c[k];
+  return (double)e * 0x1.62e42fefa39efp-1 + 2.0 * (s * q);
+}
+static double r_noise_cos2pi(double w) {
+  double a = fabs(w >= 0.5 ? w - 1.0 : w);
+  double sign = 1.0;
+  if (a > 0.25) {
+    a = 0.5 - a;
+    sign = -1.0;
+  }
+  double r;
+  if (a <= 0.125) {
+    const double x = 0x1.921fb54442d18p+2 * a, x2 = x * x;
+    double q = r_cos_c[9];
+    for (int k = 8; k >= 0; --k) q = q * -x2 + r_cos_c[k];
+    r = q;
+  } else {
+    const double y = 0x1.921fb54442d18p+2 * (0.25 - a), y2 = y * y;
+    double q = r_sin_c[9];
+    for (int k = 8; k >= 0; --k) q = q * -y2 + r_sin_c[k];
+    r = y * q;
+  }
+  return sign * r;
+}
+static float r_intersect(const float* pr, rf3 o, rf3 d) {
+  const float kInf = 3.0e38f, kEps = 1e-4f;
+  const int kind = (int)pr[0];
+  const rf3 a = rmk(pr[1], pr[2], pr[3]);
+  const rf3 b = rmk(pr[4], pr[5], pr[6]);
+  const float r = pr[7], h = pr[8];
+  if (kind == 0) {
+    const float den = rdot(d, a);
+    if (fabsf(den) < 1e-12f) return kInf;
+    const float t = (r - rdot(o, a)) / den;
+    return t > kEps ? t : kInf;
+  }
+  if (kind == 1) {
+    const rf3 oc = rsub(o, a);
+    const float bb = rdot(d, oc);
+    const float c = rdot(oc, oc) - r * r;
+    const float disc = bb * bb - c;
+    if (disc < 0.0f) return kInf;
+    const float sq = sqrtf(disc);
+    const float t0 = -bb - sq, t1 = -bb + sq;
+    const float t = t0 > kEps ? t0 : t1;
+    return t > kEps ? t : kInf;
+  }
+  if (kind == 2 || kind == 4) {
+    float tmin = -kInf, tmax = kInf;
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z}, lo[3] = {a.x, a.y, a.z}, hi[3] = {b.x, b.y, b.z};
+    for (int k = 0; k < 3; ++k) {
+      if (fabsf(dd[k]) < 1e-12f) {
+        if (oo[k] < lo[k] || oo[k] > hi[k]) return kInf;
+        continue;
+      }
+      const float inv = 1.0f / dd[k];
+      float t0 = (lo[k] - oo[k]) * inv, t1 = (hi[k] - oo[k]) * inv;
+      if (t0 > t1) {
+        const float t = t0;
+        t0 = t1;
+        t1 = t;
+      }
+      tmin = fmaxf(tmin, t0);
+      tmax = fminf(tmax, t1);
+    }
+    if (kind == 2) {
+      if (tmax < tmin || tmax <= kEps) return kInf;
+      return tmin > kEps ? tmin : tmax;
+    }
+    return tmax > kEps ? tmax : kInf;
+  }
+  if (kind == 3) {
+    const float ox = o.x - a.x, oy = o.y - a.y;
+    const float qa = d.x * d.x + d.y * d.y;
+    const float qb = ox * d.x + oy * d.y;
+    const float qc = ox * ox + oy * oy - r * r;
+    float best = kInf;
+    const float disc = qb * qb - qa * qc;
+    if (qa > 1e-12f && disc >= 0.0f) {
+      const float sq = sqrtf(disc);
+      const float ts[2] = {(-qb - sq) / qa, (-qb + sq) / qa};
+      for (int k = 0; k < 2; ++k) {
+        const float z = o.z + ts[k] * d.z;
+        if (ts[k] > kEps && z >= a.z && z <= a.z + h && ts[k] < best) best = ts[k];
+      }
+    }
+    if (fabsf(d.z) > 1e-12f) {
+      const float zc[2] = {a.z, a.z + h};
+      for (int k = 0; k < 2; ++k) {
+        const float t = (zc[k] - o.z) / d.z;
+        const float px = ox + t * d.x, py = oy + t * d.y;
+        if (t > kEps && px * px + py * py <= r * r && t < best) best = t;
+      }
+    }
+    return best;
+  }
+  return kInf;
+}
+void vo_render_depth(const float* prims, int32_t n_prims, const vo_intrinsics* K, const vo_pose* T_wc, uint32_t seed,
+                     uint32_t frame, float sigma_z2, float dropout, float max_depth, float* out) {
+  const float kInf = 3.0e38f;
+  const int n = K->width * K->height;
+  const float* R = T_wc->R;
+  const rf3 o = rmk(T_wc->t[0], T_wc->t[1], T_wc->t[2]);
+  for (int i = 0; i < n; ++i) {
+    const int u = i % K->width, v = i / K->width;
+    rf3 dc = rmk(((float)u - K->cx) / K->fx, ((float)v - K->cy) / K->fy, 1.0f);
+    const float inv = 1.0f / sqrtf(rdot(dc, dc));
+    dc = rmk(dc.x * inv, dc.y * inv, dc.z * inv);
+    const rf3 dw = rmk(R[0] * dc.x + R[1] * dc.y + R[2] * dc.z, R[3] * dc.x + R[4] * dc.y + R[5] * dc.z,
+                       R[6] * dc.x + R[7] * dc.y + R[8] * dc.z);
+    float t = kInf;
+    for (int k = 0; k < n_prims; ++k) t = fminf(t, r_intersect(prims + 10 * k, o, dw));
+    float z = t < kInf ? t * dc.z : 0.0f;
+    if (z > 0.0f && sigma_z2 > 0.0f) {
+      const double u1 = r_uniform01(seed, frame, (uint32_t)i, 0U);
+      const double u2 = r_uniform01(seed, frame, (uint32_t)i, 1U);
+      const double g = sqrt(-2.0 * r_noise_log(u1)) * r_noise_cos2pi(u2);
+      const double zd = (double)z;
+      z = (float)(zd + ((g * (double)sigma_z2) * zd) * zd);
+    }
+    if (r_uniform01(seed, frame, (uint32_t)i, 2U) < (double)dropout) z = 0.0f;
+    if (z < 0.1f || z > max_depth) z = 0.0f;
+    out[i] = z;
+  }
 }

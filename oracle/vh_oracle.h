@@ -109,6 +109,9 @@ void vo_config_default(vo_config* cfg, int32_t flavor);
 float vo_expf_own(float x);
 void vo_expf_array(const float* x, float* y, size_t n);
 void vo_expf_compare_libm(uint32_t first, uint64_t count, int threads, uint64_t* mismatches, uint32_t* first_mismatch);
+/* The device renderer (vh_render_depth) restated: prims n x 10 floats, out width*height floats. */
+void vo_render_depth(const float* prims, int32_t n_prims, const vo_intrinsics* K, const vo_pose* T_wc, uint32_t seed,
+                     uint32_t frame, float sigma_z2, float dropout, float max_depth, float* out);
 
 /* depth bilateral filter (both flavours): out[W*H] */
 void vo_filter_depth(const vo_config* cfg, const float* depth, const vo_intrinsics* K, float* out);
@@ -144,6 +147,8 @@ void vo_volume_get_block(const vo_volume* vol, int64_t i, vo_key* key, vo_voxel*
 int64_t vo_volume_find_block(const vo_volume* vol, int32_t x, int32_t y, int32_t z);
 /* inserts/overwrites a block (applyFlatBlocks, voxel_hash_tsdf.h:183-188) */
 void vo_volume_set_block(vo_volume* vol, vo_key key, const vo_voxel* voxels);
+/* applyFlatBlocks: n records (keys[i], voxels[i * 512 ...]) applied in order */
+void vo_volume_apply_flat_blocks(vo_volume* vol, const vo_key* keys, const vo_voxel* voxels, int64_t n);
 /* marching cubes over all blocks and 6 directions; *out is malloc'd (free with vo_free) */
 int64_t vo_volume_extract_mesh(const vo_volume* vol, float iso, vo_triangle** out);
 void vo_free(void* p);

@@ -376,6 +376,45 @@ def test_checkpoint_export_import_round_trip(env, small_orbit):
     b.close()
 
 
+def test_import_matches_apply_flat_blocks(env, small_orbit):
+    """vh_import_blocks against the oracle's restatement of applyFlatBlocks (voxel_hash_tsdf.h:183-188): records
+    exported from a volume fused from other views -- keys that overwrite blocks of the target and keys that
+    are new to it -- applied to a fused volume on both sides give the same blocks, voxel words and observed
+    count; fusing a further frame and meshing afterwards stay bit-identical."""
+    backend, O = env
+    from voxelhashmt_gb300 import scenes
+    sc = small_orbit
+    vol, ora = _integrate_both(backend, O, sc, frames=[0, 4, 8])
+    src = _volume(backend, sc)
+    for f in (12, 16):
+        backend.integrate_depth_frame_cuda(src, backend.DepthFrame(sc.intrinsics, scenes.render_depth(sc, f)),
+                                           sc.poses[f])
+    keys, vox = src.export_blocks()
+    src.close()
+    have = {tuple(k) for k in vol.export_blocks()[0]}
+    overwrite = np.array([tuple(k) in have for k in keys])
+    assert overwrite.sum() > 10 and (~overwrite).sum() > 10  # both kinds of record
+    vol.import_blocks(keys, vox)
+    ora.apply_flat_blocks(keys, vox)
+    gk, gv = O.sort_blocks(*vol.export_blocks())
+    ok, ov = O.sort_blocks(*ora.blocks())
+    assert np.array_equal(gk, ok)
+    assert np.array_equal(gv.reshape(len(gk), -1), ov.view(np.uint32).reshape(len(ok), -1))
+    assert vol.observed_voxel_count() == ora.observed_voxels() == vol.recount_observed_voxels()
+    d = scenes.render_depth(sc, 20)
+    backend.integrate_depth_frame_cuda(vol, backend.DepthFrame(sc.intrinsics, d), sc.poses[20])
+    ora.integrate(d, sc.intrinsics, sc.poses[20])
+    gk, gv = O.sort_blocks(*vol.export_blocks())
+    ok, ov = O.sort_blocks(*ora.blocks())
+    assert np.array_equal(gk, ok)
+    assert np.array_equal(gv.reshape(len(gk), -1), ov.view(np.uint32).reshape(len(ok), -1))
+    assert vol.observed_voxel_count() == ora.observed_voxels()
+    assert np.array_equal(_bits(O.canonical_triangles(backend.extract_mesh_cuda(vol))),
+                          _bits(O.canonical_triangles(ora.extract_mesh())))
+    vol.close()
+    ora.close()
+
+
 def test_raycast_bit_exact_and_close_to_scene(env, small_orbit):
     """Depth ray-cast of the fused plain volume: bit-identical to the oracle's restatement, and within a
     voxel of the analytic depth where both see the surface."""

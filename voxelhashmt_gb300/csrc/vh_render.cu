@@ -5,6 +5,11 @@
 // voxelhashmt_gb300/scenes.py (plane, sphere, box, vertical cylinder, room interior) with the same counter-
 // based noise (lowbias32 hash of (seed, frame, pixel), Box-Muller, sigma = k z^2, dropouts), so frames can be
 // generated on the device at the rate the fusion path consumes them.
+//
+// Reproducible on a host: the ray geometry is FP32 with only IEEE-rounded additions, multiplications,
+// divisions and square roots (the library is compiled without contraction), and the noise is FP64 with its
+// own logarithm and cosine built from the same basic operations, so a host program that performs the same
+// operations in the same order (the oracle's vo_render_depth) renders bit-identical frames.
 #include "vh_common.cuh"
 #include "vh_kernels.h"
 
@@ -24,10 +29,67 @@ __device__ __forceinline__ uint32_t lowbias32(uint32_t x) {
   return x;
 }
 
-__device__ __forceinline__ float uniform01(uint32_t seed, uint32_t frame, uint32_t idx, uint32_t stream) {
+// (h + 0.5) / 2^32 for the hash h of (seed, frame, pixel, stream): exact in double, in (0, 1)
+__device__ __forceinline__ double uniform01(uint32_t seed, uint32_t frame, uint32_t idx, uint32_t stream) {
   const uint32_t key = seed * 0x9E3779B1U + frame * 0x85EBCA77U + stream * 0xC2B2AE3DU;
   const uint32_t h = lowbias32(idx ^ lowbias32(key));
-  return (static_cast<float>(h) + 0.5f) * 2.3283064365386963e-10f;
+  return __dmul_rn(__dadd_rn(static_cast<double>(h), 0.5), 0x1p-32);
+}
+
+// 1 / (2k + 1), k = 0..10 (the atanh series) and 1 / (2k)!, 1 / (2k + 1)!, k = 0..9, correctly rounded
+__constant__ double kAtanhC[11] = {0x1.0000000000000p+0, 0x1.5555555555555p-2, 0x1.999999999999ap-3,
+                                   0x1.2492492492492p-3, 0x1.c71c71c71c71cp-4, 0x1.745d1745d1746p-4,
+                                   0x1.3b13b13b13b14p-4, 0x1.1111111111111p-4, 0x1.e1e1e1e1e1e1ep-5,
+                                   0x1.af286bca1af28p-5, 0x1.8618618618618p-5};
+__constant__ double kCosC[10] = {0x1.0000000000000p+0, 0x1.0000000000000p-1, 0x1.5555555555555p-5,
+                                 0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-16, 0x1.27e4fb7789f5cp-22,
+                                 0x1.1eed8eff8d898p-29, 0x1.93974a8c07c9dp-37, 0x1.ae7f3e733b81fp-45,
+                                 0x1.6827863b97d97p-53};
+__constant__ double kSinC[10] = {0x1.0000000000000p+0, 0x1.5555555555555p-3, 0x1.1111111111111p-7,
+                                 0x1.a01a01a01a01ap-13, 0x1.71de3a556c734p-19, 0x1.ae64567f544e4p-26,
+                                 0x1.6124613a86d09p-33, 0x1.ae7f3e733b81fp-41, 0x1.952c77030ad4ap-49,
+                                 0x1.2f49b46814157p-57};
+constexpr double kLn2 = 0x1.62e42fefa39efp-1;
+constexpr double kTwoPi = 0x1.921fb54442d18p+2;
+
+// ln u for u in (0, 1]: u = m 2^e with m in [sqrt(1/2), sqrt(2)), ln u = e ln 2 + 2 atanh(s) with
+// s = (m - 1) / (m + 1), |s| <= 0.1716, the atanh series to s^21 in Horner form
+__device__ double noise_log(double u) {
+  int e = 0;
+  double m = frexp(u, &e);  // m in [0.5, 1), exact
+  if (m < 0x1.6a09e667f3bcdp-1) {
+    m = __dmul_rn(m, 2.0);
+    e -= 1;
+  }
+  const double s = __ddiv_rn(__dadd_rn(m, -1.0), __dadd_rn(m, 1.0));
+  const double s2 = __dmul_rn(s, s);
+  double q = kAtanhC[10];
+  for (int k = 9; k >= 0; --k) q = __dadd_rn(__dmul_rn(q, s2), kAtanhC[k]);
+  return __dadd_rn(__dmul_rn(static_cast<double>(e), kLn2), __dmul_rn(2.0, __dmul_rn(s, q)));
+}
+
+// cos(2 pi w) for w in [0, 1): folded exactly to a in [0, 1/4], then the cosine series of 2 pi a (a <= 1/8) or
+// the sine series of 2 pi (1/4 - a), each to the 19th power
+__device__ double noise_cos2pi(double w) {
+  double a = fabs(w >= 0.5 ? __dadd_rn(w, -1.0) : w);
+  double sign = 1.0;
+  if (a > 0.25) {
+    a = __dadd_rn(0.5, -a);
+    sign = -1.0;
+  }
+  double r;
+  if (a <= 0.125) {
+    const double x = __dmul_rn(kTwoPi, a), x2 = __dmul_rn(x, x);
+    double q = kCosC[9];
+    for (int k = 8; k >= 0; --k) q = __dadd_rn(__dmul_rn(q, -x2), kCosC[k]);
+    r = q;
+  } else {
+    const double y = __dmul_rn(kTwoPi, __dadd_rn(0.25, -a)), y2 = __dmul_rn(y, y);
+    double q = kSinC[9];
+    for (int k = 8; k >= 0; --k) q = __dadd_rn(__dmul_rn(q, -y2), kSinC[k]);
+    r = __dmul_rn(y, q);
+  }
+  return __dmul_rn(sign, r);
 }
 
 __device__ float intersect(const float* pr, f3 o, f3 d) {
@@ -117,7 +179,7 @@ __global__ void __launch_bounds__(256) render_kernel(const float* __restrict__ p
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int u = i % p.width, v = i / p.width;
     f3 dc = mk3((static_cast<float>(u) - p.cx) / p.fx, (static_cast<float>(v) - p.cy) / p.fy, 1.0f);
-    const float inv = rsqrtf(dot3(dc, dc));
+    const float inv = 1.0f / sqrtf(dot3(dc, dc));
     dc = mul3(dc, inv);
     const f3 dw = xform_vector(p.T_wc, dc);
     const f3 o = mk3(p.T_wc.t[0], p.T_wc.t[1], p.T_wc.t[2]);
@@ -125,12 +187,13 @@ __global__ void __launch_bounds__(256) render_kernel(const float* __restrict__ p
     for (int k = 0; k < n_prims; ++k) t = fminf(t, intersect(s_prims + k * kPrimFields, o, dw));
     float z = t < kInf ? t * dc.z : 0.0f;
     if (z > 0.0f && sigma_z2 > 0.0f) {
-      const float u1 = uniform01(seed, frame, static_cast<uint32_t>(i), 0U);
-      const float u2 = uniform01(seed, frame, static_cast<uint32_t>(i), 1U);
-      const float g = sqrtf(-2.0f * logf(u1)) * cosf(6.283185307179586f * u2);
-      z = z + g * sigma_z2 * z * z;
+      const double u1 = uniform01(seed, frame, static_cast<uint32_t>(i), 0U);
+      const double u2 = uniform01(seed, frame, static_cast<uint32_t>(i), 1U);
+      const double g = __dmul_rn(__dsqrt_rn(__dmul_rn(-2.0, noise_log(u1))), noise_cos2pi(u2));
+      const double zd = static_cast<double>(z);
+      z = __double2float_rn(__dadd_rn(zd, __dmul_rn(__dmul_rn(__dmul_rn(g, static_cast<double>(sigma_z2)), zd), zd)));
     }
-    if (uniform01(seed, frame, static_cast<uint32_t>(i), 2U) < dropout) z = 0.0f;
+    if (uniform01(seed, frame, static_cast<uint32_t>(i), 2U) < static_cast<double>(dropout)) z = 0.0f;
     if (z < 0.1f || z > max_depth) z = 0.0f;
     out[i] = z;
   }
