@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--form", default="chosen", choices=["chosen", "plain"],
                     help="form reported as the headline value (the other is measured beside it)")
     ap.add_argument("--no-chamfer", action="store_true", help="skip the Chamfer distances of the fused meshes")
+    ap.add_argument("--room-only", action="store_true",
+                    help="skip the legs beside the room workload (the small orbit configuration, the 64-scene batch)")
     ap.add_argument("--workload", default="room", choices=["room", "batch", "denoiser"],
                     help="room: the room-scale workload (the headline); batch: N object scans fused as one batch; "
                          "denoiser: train the learned filter and compare Chamfer with the bilateral filter")
@@ -278,14 +280,51 @@ def surface_points(sc, torch, capi, stride=4, every=20, max_points=200_000):
     return metrics.observed_surface_points(sc, sel, depth_maps=maps, stride=stride, max_points=max_points)
 
 
-def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
-    """Time K frames of one form (after W warm-up frames) and extract the mesh; returns the measurements."""
+def tune_launch_shape(torch, backend, capi, sc, frames, form, max_blocks):
+    """The layer-update launch shape chosen by the volume's own autotuner (vh_algorithm.autotune), before any
+    timed frame: a scratch volume integrates the workload's frames (cycled when there are fewer than the tuner
+    needs) until the tuner has timed every shape and kept the fastest.  None for forms without a tuned kernel."""
+    algo_kw, layer_format = form
+    if algo_kw.get("normal_mode", 0) != 1:
+        return None
+    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=max_blocks,
+                                device=torch.cuda.current_device(),
+                                algorithm=capi.default_algorithm(autotune=1, **algo_kw), layer_format=layer_format)
+    bk = backend.TsdfIntegrationBackend("gpu")
+    stream = torch.cuda.current_stream()
+    K = sc.intrinsics
+    n = frames.shape[0]
+    tuned, used = None, 0
+    for i in range(200):
+        f = i % n
+        if i and f == 0:
+            vol.reset(stream)
+        bk.integrate(vol, backend.DepthFrame(K, frames[f].view(-1)), sc.poses[f], 1, stream=stream, synchronize=True)
+        used = i + 1
+        r = vol.autotune_result()
+        if r["variant"] >= 0:
+            tuned = r
+            break
+    vol.close()
+    if tuned is not None:
+        tuned = dict(tuned, tuning_frames=used, note="chosen by the volume's autotuner on a scratch volume before "
+                                                     "the timed frames; the timed volume runs this shape")
+    return tuned
+
+
+def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world, launch=None, max_blocks=None):
+    """Time K frames of one form (after W warm-up frames) and extract the mesh; returns the measurements.
+    launch: the layer-update launch shape found by tune_launch_shape (the timed volume does not tune)."""
     import ctypes as C
     K = sc.intrinsics
     px = K.width * K.height
     stream = torch.cuda.current_stream()
-    max_blocks = int(os.environ.get("VH_BENCH_MAX_BLOCKS", "900000"))
+    if max_blocks is None:
+        max_blocks = int(os.environ.get("VH_BENCH_MAX_BLOCKS", "900000"))
     algo_kw, layer_format = form
+    algo_kw = dict(algo_kw)
+    if launch is not None:
+        algo_kw.update(autotune=0, launch_variant=launch["variant"])
     vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=max_blocks,
                                 device=torch.cuda.current_device(), algorithm=capi.default_algorithm(**algo_kw),
                                 layer_format=layer_format)
@@ -355,7 +394,7 @@ def fuse_form(args, torch, backend, capi, sc, frames, form, flush, world):
     torch.cuda.synchronize()
     weld = {"ms": round(w0.elapsed_time(w1), 3), "vertices": nv_w.value, "faces": nf_w.value}
     observed = vol.observed_voxel_count()
-    tuned = vol.autotune_result()
+    tuned = launch
 
     # per-frame updated / active voxels of the last 16 frames (algorithmic bytes), on a replay
     vol.reset(stream)
@@ -426,6 +465,31 @@ def graph_leg(args, torch, backend, capi, sc, frames, flush):
             "ms_per_step": round(total_ms / args.steps, 4), "launch": "one cudaGraphLaunch per frame"}
 
 
+def orbit_leg(args, torch, backend, capi, metrics, flush):
+    """The small plain-method configuration: the orbit scene (plane, sphere r 0.5 m, 0.4 x 0.3 x 0.6 m box),
+    320x240, fx = fy = 277, 64 frames on a 1.5 m orbit at 0.8 m, 1 cm voxels, 4 cm truncation, 2^16 buckets;
+    both forms, 4 warm-up and 60 timed frames with the same timing rules as the room legs."""
+    import types
+    from voxelhashmt_gb300 import scenes
+    sc = scenes.orbit_scene(seed=args.seed + 11, frames=64)
+    frames = render_all(sc, torch, None, capi)
+    sub = types.SimpleNamespace(**dict(vars(args), warmup=4, steps=60))
+    out = {"config": {"workload": "orbit 320x240, plane + sphere + box, 64-frame orbit r 1.5 m h 0.8 m, voxel "
+                                  "10 mm, trunc 40 mm, 65536 hash buckets", "warmup": 4, "steps": 60}}
+    pts = None if args.no_chamfer else surface_points(sc, torch, capi, stride=2, every=4)
+    for name, form in FORMS.items():
+        launch = tune_launch_shape(torch, backend, capi, sc, frames, form, 60000)
+        r = fuse_form(sub, torch, backend, capi, sc, frames, form, flush, 1, launch, max_blocks=60000)
+        out[name] = {"integrated_mpix_per_s": round(r["value"], 3), "ms_per_step": round(r["max_ms"] / 60, 4),
+                     "e2e_mpix_per_s": round(r["e2e_value"], 3), "mc_blocks_per_s": round(r["mc_blocks_per_s"], 1),
+                     "blocks": r["nblocks"], "mc_triangles": r["triangles"],
+                     "update_launch_shape": launch if launch else "fixed (no tuned kernel in this form)",
+                     "chamfer": None if pts is None else {k: (round(v, 4) if isinstance(v, float) else v)
+                                                          for k, v in metrics.chamfer(r["tris"], sc, pts).items()}}
+    out["speedup_vs_plain"] = round(out["chosen"]["integrated_mpix_per_s"] / out["plain"]["integrated_mpix_per_s"], 3)
+    return out
+
+
 def run_gb300(args):
     import torch
 
@@ -444,9 +508,16 @@ def run_gb300(args):
     px = K.width * K.height
     frames = render_all(sc, torch, None, _capi)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    res = {name: fuse_form(args, torch, backend, _capi, sc, frames, form, flush, world)
+    max_blocks = int(os.environ.get("VH_BENCH_MAX_BLOCKS", "900000"))
+    launch = {name: tune_launch_shape(torch, backend, _capi, sc, frames, form, max_blocks)
+              for name, form in FORMS.items()}
+    res = {name: fuse_form(args, torch, backend, _capi, sc, frames, form, flush, world, launch[name])
            for name, form in FORMS.items()}
     graph = graph_leg(args, torch, backend, _capi, sc, frames, flush)
+    extra_legs = {}
+    if rank == 0 and world == 1 and not args.room_only:
+        extra_legs["small_orbit"] = orbit_leg(args, torch, backend, _capi, metrics, flush)
+        extra_legs["batch"] = batch_leg(args, torch, emit=False)
     quality = {}
     if rank == 0 and not args.no_chamfer:
         pts = surface_points(sc, torch, _capi)
@@ -494,7 +565,7 @@ def run_gb300(args):
                 "stage_ms_per_frame": {k: round(v / max(1, r["nprof"]), 4) for k, v in r["stage_ms"].items()},
                 "visible_blocks_last_frame": r["fstats"]["visible_blocks"],
                 "updated_voxels_per_frame": round(r["upd_mean"]), "active_voxels_per_frame": round(r["act_mean"]),
-                "update_launch_shape": r["autotune"] if r["autotune"]["variant"] >= 0 else None,
+                "update_launch_shape": r["autotune"] if r["autotune"] else "fixed (no tuned kernel in this form)",
                 "mc_incremental_last_100_frames": r["mc_recent"],
                 "mesh_weld": r["weld"],
                 "chamfer": quality.get(name)}
@@ -519,6 +590,7 @@ def run_gb300(args):
             "speedup_vs_plain": round(res["chosen"]["value"] / res["plain"]["value"], 3),
             "chosen_as_cuda_graph": graph,
         }
+        line.update(extra_legs)
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -538,18 +610,24 @@ def prim_area(p):
 
 
 def run_batch(args):
+    import torch
+    from voxelhashmt_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    batch_leg(args, torch, emit=True)
+    return 0
+
+
+def batch_leg(args, torch, emit):
     """Batched multi-scene workload: N object scans (scenes.object_scan_scene), each one frame per step while
     it has frames, fused (a) as one batch per step (vh_batch, CUDA graph) and (b) one scene at a time through
     the single-volume API, same opt-in settings and FP16 storage.  Frames are rendered to device memory first;
     both runs are timed with CUDA events around all steps, after an untimed pass over the whole workload
-    (buffer sizing, graph capture) and a volume reset."""
+    (buffer sizing, graph capture) and a volume reset.  emit: print the JSON line (the batch workload) or
+    return the measurements (a leg of the default run)."""
     import ctypes as C
 
-    import torch
     from voxelhashmt_gb300 import _capi, backend, metrics, scenes
-    from voxelhashmt_gb300 import build as pbuild
-    pbuild.build()
-    torch.cuda.set_device(0)
     scs = [scenes.object_scan_scene(seed=args.seed * 1000 + i) for i in range(args.scenes)]
     frames = [render_all(sc, torch, None, _capi) for sc in scs]
     total_px = sum(len(sc.poses) * sc.intrinsics.width * sc.intrinsics.height for sc in scs)
@@ -641,8 +719,9 @@ def run_batch(args):
         "mc_blocks_per_s": round(sum(blocks) / (mc_ms / 1000.0), 1), "blocks": int(sum(blocks)),
         "chamfer_mm_sampled_scenes": [round(q, 4) for q in quality], "clocks": clock_info,
     }
-    print(json.dumps(line))
-    return 0
+    if emit:
+        print(json.dumps(line))
+    return line
 
 
 def run_denoiser(args):

@@ -37,6 +37,7 @@ class VoConfig(C.Structure):
         ("max_weight", C.c_float), ("depth_sigma", C.c_float), ("huber_delta", C.c_float),
         ("min_obs_weight", C.c_float), ("min_view_weight", C.c_float),
         ("threads", C.c_int32),
+        ("alloc_mode", C.c_int32), ("normal_mode", C.c_int32), ("layer_format", C.c_int32),
     ]
 
 
@@ -302,7 +303,7 @@ class Volume:
         same bytes as a flat array, applied in order."""
         k = np.ascontiguousarray(keys, np.int32).reshape(-1, 3)
         v = np.ascontiguousarray(voxels).view(np.uint8).reshape(k.shape[0], -1)
-        assert v.shape[1] == BLOCK_VOXELS * VOXEL_DTYPE.itemsize
+        assert v.shape[1] == BLOCK_VOXELS * VOXEL_BYTES
         self.L.vo_volume_apply_flat_blocks(self.h, k.ctypes.data_as(_ip), v.ctypes.data, k.shape[0])
 
     def extract_mesh(self, iso=0.0):

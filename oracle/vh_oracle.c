@@ -997,6 +997,268 @@ int64_t vo_collect_band_blocks(const float* depth, const vo_intrinsics* K, const
   return n;
 }
 
+
+/* ---------------------------------------------- the library's opt-in forms */
+/* Restatements of the GPU library's opt-in switches as its exact compile evaluates them (no reference
+ * counterpart; voxelhashmt_gb300/csrc/vh_common.cuh and vh_integrate.cu): the per-voxel interpolation of the
+ * per-pixel normal map (map_normal) and the FP16 bin (decode_bin16, encode_bin16, integrate_bin16).  Explicit
+ * float arithmetic, every operation rounded once, as the device's -fmad=false compile and its _rn intrinsics. */
+typedef union {
+  float f;
+  uint32_t u;
+} fbits;
+static inline float u_as_f(uint32_t u) {
+  fbits b;
+  b.u = u;
+  return b.f;
+}
+static inline uint32_t f_as_u(float f) {
+  fbits b;
+  b.f = f;
+  return b.u;
+}
+/* binary16 -> float (exact) */
+static float h2f(uint32_t h) {
+  const uint32_t sign = (h & 0x8000U) << 16, e = (h >> 10) & 0x1fU, m = h & 0x3ffU;
+  if (e == 0U) {
+    const float f = (float)m * 0x1p-24f;
+    return sign ? -f : f;
+  }
+  if (e == 31U) return u_as_f(sign | 0x7f800000U | (m << 13));
+  return u_as_f(sign | ((e + 112U) << 23) | (m << 13));
+}
+/* float -> binary16, round to nearest even, with subnormals and overflow to infinity */
+static uint32_t f2h(float f) {
+  const uint32_t x = f_as_u(f);
+  const uint32_t sign = (x >> 16) & 0x8000U, ax = x & 0x7fffffffU;
+  if (ax >= 0x7f800000U) return sign | (ax > 0x7f800000U ? 0x7e00U : 0x7c00U);
+  if (ax >= 0x477ff000U) return sign | 0x7c00U; /* >= 65520 rounds to infinity */
+  if (ax <= 0x33000000U) return sign;          /* <= 2^-25 rounds to zero */
+  const int e = (int)(ax >> 23) - 127;
+  const uint32_t m = (ax & 0x7fffffU) | 0x800000U;
+  if (e < -14) {
+    const int shift = -1 - e;                  /* subnormal result: units of 2^-24 */
+    uint32_t r = m >> shift;
+    const uint32_t rem = m & ((1U << shift) - 1U), half = 1U << (shift - 1);
+    if (rem > half || (rem == half && (r & 1U))) ++r;
+    return sign | r;
+  }
+  uint32_t r = ((uint32_t)(e + 15) << 10) | ((m >> 13) & 0x3ffU);
+  const uint32_t rem = m & 0x1fffU;
+  if (rem > 0x1000U || (rem == 0x1000U && (r & 1U))) ++r;
+  return sign | r;
+}
+/* 1/sqrt(x) correctly rounded (the device's __frsqrt_rn), for positive normal x: the double estimate, then the
+ * nearest float decided exactly by the sign of m^2 x - 1 at the midpoints m to its neighbours (m^2 is exact in
+ * double and the fused multiply-add rounds the product-minus-one once, so its sign is the exact sign). */
+static float cr_rsqrtf(float x) {
+  const double xd = (double)x;
+  float r = (float)(1.0 / sqrt(xd));
+  for (int it = 0; it < 4; ++it) {
+    const float up = nextafterf(r, INFINITY);
+    double m = ((double)r + (double)up) * 0.5;
+    if (fma(m * m, xd, -1.0) < 0.0) {
+      r = up;
+      continue;
+    }
+    const float dn = nextafterf(r, 0.0f);
+    m = ((double)dn + (double)r) * 0.5;
+    if (fma(m * m, xd, -1.0) > 0.0) {
+      r = dn;
+      continue;
+    }
+    break;
+  }
+  return r;
+}
+float vo_rsqrtf_rn(float x) { return cr_rsqrtf(x); }
+
+typedef struct {
+  float x, y, z;
+} f3o;
+static inline f3o f3mk(float x, float y, float z) {
+  f3o r = {x, y, z};
+  return r;
+}
+static inline float f3dot(f3o a, f3o b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+/* vh_common.cuh: bin_normal (octahedral decode, normalised with the correctly rounded reciprocal root) */
+static f3o bin_normal(uint32_t packed) {
+  float x = (float)(packed & 0xffffU) / 65535.0f * 2.0f + -1.0f;
+  float y = (float)(packed >> 16U) / 65535.0f * 2.0f + -1.0f;
+  const float z = (1.0f + -fabsf(x)) + -fabsf(y);
+  if (z < 0.0f) {
+    const float fx = copysignf(1.0f + -fabsf(y), x >= 0.0f ? 1.0f : -1.0f);
+    const float fy = copysignf(1.0f + -fabsf(x), y >= 0.0f ? 1.0f : -1.0f);
+    x = fx;
+    y = fy;
+  }
+  const float inv = cr_rsqrtf((x * x + y * y) + z * z);
+  return f3mk(x * inv, y * inv, z * inv);
+}
+static inline float axis_coord(f3o p, int d) {
+  const float a = (d >> 1) == 0 ? p.x : ((d >> 1) == 1 ? p.y : p.z);
+  return (d & 1) ? -a : a;
+}
+static inline f3o voxel_centre_f(vo_key k, int li, float vs) {
+  const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
+  return f3mk(((float)(k.x * BLOCK + lx) + 0.5f) * vs, ((float)(k.y * BLOCK + ly) + 0.5f) * vs,
+              ((float)(k.z * BLOCK + lz) + 0.5f) * vs);
+}
+/* decode_layer16 / decode_bin16: the three layer records of a bin, w[8] = {A.x, A.y, A.z, A.w, B.x .. B.w} */
+static void decode_bin16(const uint32_t* w, f3o c, int d, float vs, vo_layer* L) {
+  const float cd = axis_coord(c, d);
+  const uint32_t wt[3] = {w[0] & 0xffffU, w[1] >> 16, w[3] & 0xffffU};
+  const uint32_t st[3] = {w[0] >> 16, w[2] & 0xffffU, w[3] >> 16};
+  const uint32_t pt[3] = {w[1] & 0xffffU, w[2] >> 16, w[4] & 0xffffU};
+  for (int l = 0; l < 3; ++l) {
+    memset(&L[l], 0, sizeof(vo_layer));
+    if (wt[l] == 0U) continue;
+    const uint32_t packed = w[5 + l];
+    const f3o n = bin_normal(packed);
+    L[l].weight = h2f(wt[l]);
+    L[l].surface_coord = cd + h2f(st[l]) * vs;
+    L[l].plane_offset = f3dot(n, c) + h2f(pt[l]) * vs;
+    L[l].packed_normal = packed;
+  }
+}
+/* encode_bin16 (the store of decoded records: imports) */
+static void encode_bin16(const vo_layer* L, f3o c, int d, float inv_vs, uint32_t* w) {
+  const float cd = axis_coord(c, d);
+  uint32_t ws[3] = {0U, 0U, 0U}, pp[3] = {0U, 0U, 0U}, nn[3] = {0U, 0U, 0U};
+  for (int l = 0; l < 3; ++l) {
+    if (!(L[l].weight > 0.0f)) continue;
+    nn[l] = L[l].packed_normal;
+    const f3o n = bin_normal(nn[l]);
+    uint32_t wt = f2h(L[l].weight);
+    if (wt == 0U) wt = 1U;
+    ws[l] = wt | (f2h((L[l].surface_coord + -cd) * inv_vs) << 16);
+    pp[l] = f2h((L[l].plane_offset + -f3dot(n, c)) * inv_vs);
+  }
+  w[0] = ws[0];
+  w[1] = pp[0] | ((ws[1] & 0xffffU) << 16);
+  w[2] = (ws[1] >> 16) | (pp[1] << 16);
+  w[3] = ws[2];
+  w[4] = pp[2];
+  w[5] = nn[0];
+  w[6] = nn[1];
+  w[7] = nn[2];
+}
+/* integrate_bin16 (vh_integrate.cu): findLayerSlotForObservationGpu + integrateDirectionalSampleGpu
+ * (cuda_tsdf_integrator.cu:338-427) on the binary16 triplets of one bin; returns 1 when a layer was updated */
+static int integrate_bin16_o(const vo_config* cfg, float vs, float inv_vs, uint32_t* w, f3o c, int dir, float sc,
+                             v3 sp, v3 nw, float obs) {
+  if (obs <= 0.0f) return 0;
+  const v3 n = vnormalize(GPU, nw);
+  if (vnorm(n) <= 1e-6f) return 0;
+  const float merge_tol = fmax_f(1e-6f, vs * cfg->layer_merge_scale);
+  const float cd = axis_coord(c, dir);
+  uint32_t w16[3] = {w[0] & 0xffffU, w[1] >> 16, w[3] & 0xffffU};
+  uint32_t s16[3] = {w[0] >> 16, w[2] & 0xffffU, w[3] >> 16};
+  uint32_t p16[3] = {w[1] & 0xffffU, w[2] >> 16, w[4] & 0xffffU};
+  uint32_t nk[3] = {w[5], w[6], w[7]};
+  float ls[3];
+  f3o ln[3];
+  int empty = -1, best = -1;
+  float best_delta = 1e30f;
+  for (int l = 0; l < 3; ++l) {
+    ls[l] = cd + h2f(s16[l]) * vs;
+    ln[l] = f3mk(0.0f, 0.0f, 1.0f);
+    if (w16[l] == 0U) {
+      if (empty < 0) empty = l;
+      continue;
+    }
+    const float delta = fabsf(ls[l] - sc);
+    if (!(delta <= merge_tol)) continue;
+    ln[l] = bin_normal(nk[l]);
+    if (ln[l].x * n.x + ln[l].y * n.y + ln[l].z * n.z < cfg->layer_normal_cos) continue;
+    if (delta < best_delta) {
+      best_delta = delta;
+      best = l;
+    }
+  }
+  const int li = (best >= 0 && best_delta <= merge_tol) ? best : empty;
+  if (li < 0) return 0;
+  const int had = w16[li] != 0U;
+  const float pw = had ? h2f(w16[li]) : 0.0f;
+  const float ew = fmin_f(obs, fmax_f(0.0f, cfg->max_weight - pw));
+  if (ew <= 0.0f) return 0;
+  const float nwt = pw + ew;
+  const float plane_offset = vdot(n, sp);
+  const v3 pn = mk(ln[li].x, ln[li].y, ln[li].z);
+  float new_s = sc, new_p = plane_offset;
+  v3 blended = n;
+  if (had) {
+    const float old_s = ls[li];
+    const float old_p = f3dot(ln[li], c) + h2f(p16[li]) * vs;
+    new_s = (old_s * pw + sc * ew) / nwt;
+    new_p = (old_p * pw + plane_offset * ew) / nwt;
+    blended = vnormalize(GPU, vmul(vadd(vmul(pn, pw), vmul(n, ew)), 1.0f / nwt));
+    if (vnorm(blended) <= 1e-6f) blended = n;
+  }
+  const uint32_t packed = pack_normal(GPU, blended);
+  uint32_t nwt16 = f2h(nwt);
+  if (nwt16 == 0U) nwt16 = 1U;
+  const uint32_t ns16 = f2h((new_s + -cd) * inv_vs);
+  const uint32_t np16 = f2h((new_p + -f3dot(bin_normal(packed), c)) * inv_vs);
+  w16[li] = nwt16;
+  s16[li] = ns16;
+  p16[li] = np16;
+  nk[li] = packed;
+  ls[li] = new_s;
+  if (w16[1] != 0U || w16[2] != 0U) {
+    static const int pairs[3][2] = {{0, 1}, {1, 2}, {0, 1}};
+    for (int k = 0; k < 3; ++k) {
+      const int a = pairs[k][0], b = pairs[k][1];
+      const int av = w16[a] != 0U, bv = w16[b] != 0U;
+      if ((!av && bv) || (av && bv && ls[a] > ls[b])) {
+        uint32_t t = w16[a];
+        w16[a] = w16[b];
+        w16[b] = t;
+        t = s16[a];
+        s16[a] = s16[b];
+        s16[b] = t;
+        t = p16[a];
+        p16[a] = p16[b];
+        p16[b] = t;
+        t = nk[a];
+        nk[a] = nk[b];
+        nk[b] = t;
+        const float tf = ls[a];
+        ls[a] = ls[b];
+        ls[b] = tf;
+      }
+    }
+  }
+  w[0] = w16[0] | (s16[0] << 16);
+  w[1] = p16[0] | (w16[1] << 16);
+  w[2] = s16[1] | (p16[1] << 16);
+  w[3] = w16[2] | (s16[2] << 16);
+  w[4] = p16[2];
+  w[5] = w16[0] ? nk[0] : 0U;
+  w[6] = w16[1] ? nk[1] : 0U;
+  w[7] = w16[2] ? nk[2] : 0U;
+  return 1;
+}
+/* map_normal (vh_integrate.cu): the normal at (u, v), bilinear blend of the valid map taps, renormalised;
+ * nmap: 4 floats per pixel (normal, valid 1/0) */
+static int map_normal_o(const float* nmap, const vo_intrinsics* K, float u, float v, v3* n) {
+  const int x0 = (int)floorf(u), y0 = (int)floorf(v);
+  const int x1 = x0 + 1 < K->width - 1 ? x0 + 1 : K->width - 1;
+  const int y1 = y0 + 1 < K->height - 1 ? y0 + 1 : K->height - 1;
+  const float tx = u - (float)x0, ty = v - (float)y0;
+  const float* a = nmap + 4 * ((size_t)y0 * K->width + x0);
+  const float* b = nmap + 4 * ((size_t)y0 * K->width + x1);
+  const float* c = nmap + 4 * ((size_t)y1 * K->width + x0);
+  const float* d = nmap + 4 * ((size_t)y1 * K->width + x1);
+  const float wa = (1.0f - tx) * (1.0f - ty) * a[3], wb = tx * (1.0f - ty) * b[3];
+  const float wc = (1.0f - tx) * ty * c[3], wd = tx * ty * d[3];
+  const v3 s = mk(wa * a[0] + wb * b[0] + wc * c[0] + wd * d[0], wa * a[1] + wb * b[1] + wc * c[1] + wd * d[1],
+                  wa * a[2] + wb * b[2] + wc * c[2] + wd * d[2]);
+  if (wa + wb + wc + wd <= 1e-6f || vnorm(s) <= 1e-6f) return 0;
+  *n = vnormalize(GPU, s);
+  return 1;
+}
+
 /* ------------------------------------------------------------------ volume */
 struct vo_volume {
   vo_config cfg;
@@ -1004,8 +1266,10 @@ struct vo_volume {
   keymap map;
   vo_key* keys;
   vo_voxel* voxels;
+  uint32_t* bins16; /* layer_format 1: 8 words per (block, voxel, direction) */
   int64_t count, cap;
 };
+#define BIN16_WORDS (BLOCK_VOLUME * DIRS * 8)
 
 vo_volume* vo_volume_new(const vo_config* c, float vs, float trunc) {
   vo_volume* v = (vo_volume*)calloc(1, sizeof(vo_volume));
@@ -1021,6 +1285,7 @@ void vo_volume_free(vo_volume* v) {
   keymap_free(&v->map);
   free(v->keys);
   free(v->voxels);
+  free(v->bins16);
   free(v);
 }
 
@@ -1033,11 +1298,13 @@ static int64_t volume_ensure(vo_volume* v, vo_key k) {
     const int64_t nc = v->cap ? v->cap * 2 : 64;
     v->keys = (vo_key*)realloc(v->keys, (size_t)nc * sizeof(vo_key));
     v->voxels = (vo_voxel*)realloc(v->voxels, (size_t)nc * BLOCK_VOLUME * sizeof(vo_voxel));
+    if (v->cfg.layer_format == 1) v->bins16 = (uint32_t*)realloc(v->bins16, (size_t)nc * BIN16_WORDS * sizeof(uint32_t));
     v->cap = nc;
   }
   const int64_t idx = v->count++;
   v->keys[idx] = k;
   memset(&v->voxels[idx * BLOCK_VOLUME], 0, BLOCK_VOLUME * sizeof(vo_voxel));
+  if (v->cfg.layer_format == 1) memset(&v->bins16[idx * BIN16_WORDS], 0, BIN16_WORDS * sizeof(uint32_t));
   keymap_insert(&v->map, k, idx);
   return idx;
 }
@@ -1054,9 +1321,29 @@ void vo_volume_get_block(const vo_volume* v, int64_t i, vo_key* key, vo_voxel* v
   if (voxels) memcpy(voxels, &v->voxels[i * BLOCK_VOLUME], BLOCK_VOLUME * sizeof(vo_voxel));
 }
 
+/* layer_format 1: the voxel records of block idx decoded from its bins (the library's export) */
+static void decode_block16(vo_volume* v, int64_t idx) {
+  const float vs = (float)v->vs;
+  for (int li = 0; li < BLOCK_VOLUME; ++li) {
+    const f3o c = voxel_centre_f(v->keys[idx], li, vs);
+    for (int d = 0; d < DIRS; ++d)
+      decode_bin16(&v->bins16[idx * BIN16_WORDS + ((size_t)li * DIRS + d) * 8], c, d, vs,
+                   v->voxels[idx * BLOCK_VOLUME + li].layers[d]);
+  }
+}
+
 void vo_volume_set_block(vo_volume* v, vo_key key, const vo_voxel* voxels) {
   const int64_t idx = volume_ensure(v, key);
   memcpy(&v->voxels[idx * BLOCK_VOLUME], voxels, BLOCK_VOLUME * sizeof(vo_voxel));
+  if (v->cfg.layer_format == 1) { /* the library encodes imported records into bins */
+    const float vs = (float)v->vs, inv_vs = 1.0f / vs;
+    for (int li = 0; li < BLOCK_VOLUME; ++li) {
+      const f3o c = voxel_centre_f(key, li, vs);
+      for (int d = 0; d < DIRS; ++d)
+        encode_bin16(voxels[li].layers[d], c, d, inv_vs, &v->bins16[idx * BIN16_WORDS + ((size_t)li * DIRS + d) * 8]);
+    }
+    decode_block16(v, idx);
+  }
 }
 
 /* VoxelHashTSDF::applyFlatBlocks (voxel_hash_tsdf.h:183-188): for each record in order, blocks_[key] (created
@@ -1086,6 +1373,7 @@ typedef struct {
   vo_volume* vol;
   const int64_t* idx;
   const float* depth;
+  const float* nmap; /* normal_mode 1: the per-pixel normal map of depth */
   const vo_intrinsics* K;
   const vo_pose* T_wc;
   vo_pose T_cw;
@@ -1117,7 +1405,9 @@ static void integrate_block(void* p, int64_t i) {
         const v3 view = vnormalize(fl, pc);
         real view_w = 1.0f;
         v3 nc = vmul(view, -1.0f);
-        if (surface_normal(c, g->depth, g->K, u, v, &nc)) view_w = VO_FABS(vdot(nc, view));
+        if (c->normal_mode == 1 ? map_normal_o(g->nmap, g->K, (float)u, (float)v, &nc)
+                                : surface_normal(c, g->depth, g->K, u, v, &nc))
+          view_w = VO_FABS(vdot(nc, view));
         const real obs = vo_observation_weight(c, d, sd, trunc, view_w);
         if (obs <= 0.0f) continue;
         const v3 spc = back_project_cont(u, v, d, g->K);
@@ -1126,8 +1416,15 @@ static void integrate_block(void* p, int64_t i) {
         const int dir = dominant_direction(nw);
         if (dir < 0 || dir >= DIRS) continue;
         const real sc = coordinate_along(fl, spw, dir);
-        integrate_sample(c, vs, &vox[lx + BLOCK * (ly + BLOCK * lz)], dir, sc, spw, nw, obs);
+        const int li = lx + BLOCK * (ly + BLOCK * lz);
+        if (c->layer_format == 1) {
+          integrate_bin16_o(c, (float)vs, 1.0f / (float)vs, &vol->bins16[bi * BIN16_WORDS + ((size_t)li * DIRS + dir) * 8],
+                            voxel_centre_f(key, li, (float)vs), dir, (float)sc, spw, nw, (float)obs);
+        } else {
+          integrate_sample(c, vs, &vox[li], dir, sc, spw, nw, obs);
+        }
       }
+  if (c->layer_format == 1) decode_block16(vol, bi);
 }
 
 void vo_volume_integrate_blocks(vo_volume* vol, const vo_key* keys, int64_t n, const float* depth,
@@ -1138,10 +1435,29 @@ void vo_volume_integrate_blocks(vo_volume* vol, const vo_key* keys, int64_t n, c
   g.vol = vol;
   g.idx = idx;
   g.depth = depth;
+  g.nmap = NULL;
+  float* nmap = NULL;
+  if (vol->cfg.normal_mode == 1) { /* the map over the frame, as the library's map pass */
+    const size_t np = (size_t)K->width * (size_t)K->height;
+    nmap = (float*)calloc(np * 4, sizeof(float));
+    for (int y = 0; y < K->height; ++y)
+      for (int x = 0; x < K->width; ++x) {
+        v3 n = mk(0.0f, 0.0f, 0.0f);
+        if (surface_normal(&vol->cfg, depth, K, (real)x, (real)y, &n)) {
+          float* o = nmap + 4 * ((size_t)y * K->width + x);
+          o[0] = (float)n.x;
+          o[1] = (float)n.y;
+          o[2] = (float)n.z;
+          o[3] = 1.0f;
+        }
+      }
+    g.nmap = nmap;
+  }
   g.K = K;
   g.T_wc = T_wc;
   pose_inverse(T_wc, &g.T_cw);
   parallel_for(vol->cfg.threads, n, integrate_block, &g);
+  free(nmap);
   free(idx);
 }
 
@@ -1155,7 +1471,23 @@ int64_t vo_volume_integrate_frame(vo_volume* vol, const float* depth, const vo_i
   vo_filter_depth(&vol->cfg, depth, K, filtered);
   keymap set;
   keymap_init(&set, 1024);
-  if (!collect_into(&vol->cfg, filtered, K, T_wc, vol->vs, vol->trunc, stride, &set)) {
+  if (vol->cfg.alloc_mode == 1) { /* truncation band: the same walk as vo_collect_band_blocks */
+    const int s = stride > 1 ? stride : 1;
+    const v3 cam = mk(T_wc->t[0], T_wc->t[1], T_wc->t[2]);
+    const real bws = vol->vs * 8.0f;
+    for (int v = 0; v < K->height; v += s)
+      for (int u = 0; u < K->width; u += s) {
+        const real d = filtered[(size_t)v * K->width + u];
+        if (!(d > 0.0f)) continue;
+        const v3 pw = pose_point(T_wc, back_project(u, v, d, K));
+        const v3 ray = vnormalize(GPU, vsub(pw, cam));
+        if (!insert_band(vsub(pw, vmul(ray, vol->trunc)), vadd(pw, vmul(ray, vol->trunc)), bws, &set)) {
+          keymap_free(&set);
+          free(filtered);
+          return -1;
+        }
+      }
+  } else if (!collect_into(&vol->cfg, filtered, K, T_wc, vol->vs, vol->trunc, stride, &set)) {
     keymap_free(&set);
     free(filtered);
     return -1;

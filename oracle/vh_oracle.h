@@ -100,6 +100,11 @@ typedef struct {
   float max_weight, depth_sigma, huber_delta, min_obs_weight, min_view_weight;
   /* worker threads for the embarrassingly parallel loops (1 = literal serial order) */
   int32_t threads;
+  /* The GPU library's opt-in switches in their exact compile (no reference counterpart; all 0 = the reference):
+   * alloc_mode 1: truncation-band allocation (vo_collect_band_blocks); normal_mode 1: the per-pixel normal
+   * map (surface_normal at every pixel centre) interpolated bilinearly per voxel; layer_format 1: FP16 bins
+   * (32 bytes per voxel and direction), decoded into the voxel records after every update. */
+  int32_t alloc_mode, normal_mode, layer_format;
 } vo_config;
 
 /* Fills the constant set of the given reference flavour

@@ -389,3 +389,45 @@ def test_autotuned_launch_shapes_give_identical_volumes(backend, orbit_half, fas
             assert np.quantile(e, 0.999) <= 1e-3, (col, float(np.quantile(e, 0.999)))
     tuned.close()
     fixed.close()
+
+
+@pytest.mark.parametrize("scene", ["small", "half"])
+@pytest.mark.parametrize("alloc,fp16", [(1, 1), (0, 1), (1, 0), (0, 0)])
+def test_opt_in_switches_bit_exact_in_the_exact_compile(backend, oracle_lib, small_orbit, orbit_half, scene, alloc,
+                                                        fp16):
+    """The headline form's switches without fast math -- per-pixel normal map (normal_mode 1), truncation-band
+    allocation (allocation_mode 1) and FP16 bins (layer_format 1) -- against the oracle's restatement of the
+    same switches (vo_config.alloc_mode / normal_mode / layer_format): the visible block count of every frame,
+    every voxel word as exported (FP16 bins decoded), the observed-voxel count and the marching-cubes soup are
+    bit-identical.  Only the fast-math compile of the form is left to the statistical tests above."""
+    O = oracle_lib
+    from voxelhashmt_gb300 import _capi, scenes
+    if scene == "small":
+        sc, frames = small_orbit, [0, 5, 10, 15, 20]
+        depths = {f: scenes.render_depth(sc, f) for f in frames}
+    else:
+        (sc, dl, _), frames = orbit_half, [0, 3, 6, 9, 12, 15]
+        depths = {f: dl[f] for f in frames}
+    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=1 << 16, max_blocks=16384,
+                                algorithm=_capi.default_algorithm(allocation_mode=alloc, normal_mode=1, fast_math=0,
+                                                                  autotune=0),
+                                layer_format=fp16)
+    cfg = O.config(O.FLAVOR_REF_GPU, O.EXP_OWN, threads=8, alloc_mode=alloc, normal_mode=1, layer_format=fp16)
+    ora = O.Volume(cfg, sc.voxel_size, sc.truncation)
+    bk = backend.TsdfIntegrationBackend("gpu")
+    for f in frames:
+        bk.integrate(vol, backend.DepthFrame(sc.intrinsics, depths[f]), sc.poses[f], 1)
+        n = ora.integrate(depths[f], sc.intrinsics, sc.poses[f])
+        assert vol.frame_stats()["visible_blocks"] == n, f
+    gk, gv = O.sort_blocks(*vol.export_blocks())
+    ok, ov = O.sort_blocks(*ora.blocks())
+    assert np.array_equal(gk, ok)
+    assert np.array_equal(gv.reshape(len(gk), -1), ov.view(np.uint32).reshape(len(ok), -1))
+    assert vol.observed_voxel_count() == ora.observed_voxels() == vol.recount_observed_voxels()
+    tris = backend.extract_mesh_cuda(vol)
+    assert tris.shape[0] > 1000
+    assert np.array_equal(O.canonical_triangles(tris).view(np.uint32),
+                          O.canonical_triangles(ora.extract_mesh()).view(np.uint32))
+    vol.close()
+    ora.close()
+

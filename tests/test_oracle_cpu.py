@@ -320,3 +320,25 @@ def test_renderer_restatement_matches_float64_render(O, kind):
             assert both.sum() > 1000
             rel = np.abs(a[both].astype(np.float64) - b[both]) / b[both]
             assert rel.max() <= 2e-4 and np.quantile(rel, 0.999) <= 2e-5, (float(rel.max()), frame, noise)
+
+
+def test_reciprocal_root_is_correctly_rounded(O):
+    """The oracle's restatement of the FP16 codec's normalisation (the device's __frsqrt_rn, correctly rounded
+    by definition) returns the float nearest to 1/sqrt(x), checked at 100 digits on the squared lengths of
+    octahedral directions, [1/3, 1]: a seeded sample and both ends."""
+    import ctypes as C
+    import mpmath
+    L = O.lib()
+    L.vo_rsqrtf_rn.argtypes = [C.c_float]
+    L.vo_rsqrtf_rn.restype = C.c_float
+    mpmath.mp.dps = 100
+    rng = np.random.default_rng(8)
+    lo, hi = int(np.float32(1.0 / 3.0).view(np.uint32)), int(np.float32(1.0).view(np.uint32))
+    bits = np.concatenate([rng.integers(lo, hi + 1, 20000), np.arange(lo, lo + 50), np.arange(hi - 50, hi + 1)])
+    for b in bits.astype(np.uint32):
+        x = float(np.uint32(b).view(np.float32))
+        got = np.float32(L.vo_rsqrtf_rn(x))
+        exact = 1 / mpmath.sqrt(mpmath.mpf(x))
+        up, dn = np.nextafter(got, np.float32(2)), np.nextafter(got, np.float32(0))
+        err = abs(mpmath.mpf(float(got)) - exact)
+        assert err <= abs(mpmath.mpf(float(up)) - exact) and err <= abs(mpmath.mpf(float(dn)) - exact), x
