@@ -120,6 +120,7 @@ def _load(path):
     L.vo_volume_find_block.restype = C.c_int64
     L.vo_volume_set_block.argtypes = [C.c_void_p, C.c_int32 * 3, C.c_void_p]
     L.vo_volume_apply_flat_blocks.argtypes = [C.c_void_p, _ip, C.c_void_p, C.c_int64]
+    L.vo_volume_remove_blocks.argtypes = [C.c_void_p, _ip, C.c_int64]
     L.vo_volume_extract_mesh.argtypes = [C.c_void_p, C.c_float, C.POINTER(C.c_void_p)]
     L.vo_volume_extract_mesh.restype = C.c_int64
     L.vo_free.argtypes = [C.c_void_p]
@@ -305,6 +306,11 @@ class Volume:
         v = np.ascontiguousarray(voxels).view(np.uint8).reshape(k.shape[0], -1)
         assert v.shape[1] == BLOCK_VOXELS * VOXEL_BYTES
         self.L.vo_volume_apply_flat_blocks(self.h, k.ctypes.data_as(_ip), v.ctypes.data, k.shape[0])
+
+    def remove_blocks(self, keys):
+        """The library's eviction of these blocks (no reference counterpart)."""
+        k = np.ascontiguousarray(keys, np.int32).reshape(-1, 3)
+        self.L.vo_volume_remove_blocks(self.h, k.ctypes.data_as(_ip), k.shape[0])
 
     def extract_mesh(self, iso=0.0):
         ptr = C.c_void_p()

@@ -1352,6 +1352,32 @@ void vo_volume_apply_flat_blocks(vo_volume* v, const vo_key* keys, const vo_voxe
   for (int64_t i = 0; i < n; ++i) vo_volume_set_block(v, keys[i], voxels + i * BLOCK_VOLUME);
 }
 
+/* Removes the given keys (absent keys are ignored); the remaining blocks keep their relative order.  The state
+ * of a volume after the library's eviction of those blocks (which has no reference counterpart). */
+void vo_volume_remove_blocks(vo_volume* v, const vo_key* keys, int64_t n) {
+  char* drop = (char*)calloc((size_t)(v->count > 0 ? v->count : 1), 1);
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t idx = keymap_find(&v->map, keys[i]);
+    if (idx >= 0) drop[idx] = 1;
+  }
+  int64_t m = 0;
+  for (int64_t i = 0; i < v->count; ++i) {
+    if (drop[i]) continue;
+    if (m != i) {
+      v->keys[m] = v->keys[i];
+      memmove(&v->voxels[m * BLOCK_VOLUME], &v->voxels[i * BLOCK_VOLUME], BLOCK_VOLUME * sizeof(vo_voxel));
+      if (v->cfg.layer_format == 1)
+        memmove(&v->bins16[m * BIN16_WORDS], &v->bins16[i * BIN16_WORDS], BIN16_WORDS * sizeof(uint32_t));
+    }
+    ++m;
+  }
+  v->count = m;
+  keymap_free(&v->map);
+  keymap_init(&v->map, 1024);
+  for (int64_t i = 0; i < m; ++i) keymap_insert(&v->map, v->keys[i], i);
+  free(drop);
+}
+
 /* voxel_hash_tsdf.h:113-123, cuda_tsdf_integrator.cu:905-930 */
 int64_t vo_volume_observed_voxels(const vo_volume* v) {
   int64_t n = 0;

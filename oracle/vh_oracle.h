@@ -154,6 +154,8 @@ int64_t vo_volume_find_block(const vo_volume* vol, int32_t x, int32_t y, int32_t
 void vo_volume_set_block(vo_volume* vol, vo_key key, const vo_voxel* voxels);
 /* applyFlatBlocks: n records (keys[i], voxels[i * 512 ...]) applied in order */
 void vo_volume_apply_flat_blocks(vo_volume* vol, const vo_key* keys, const vo_voxel* voxels, int64_t n);
+/* removes the given keys (the state after the library evicts those blocks) */
+void vo_volume_remove_blocks(vo_volume* vol, const vo_key* keys, int64_t n);
 /* marching cubes over all blocks and 6 directions; *out is malloc'd (free with vo_free) */
 int64_t vo_volume_extract_mesh(const vo_volume* vol, float iso, vo_triangle** out);
 void vo_free(void* p);

@@ -408,7 +408,7 @@ def test_opt_in_switches_bit_exact_in_the_exact_compile(backend, oracle_lib, sma
     else:
         (sc, dl, _), frames = orbit_half, [0, 3, 6, 9, 12, 15]
         depths = {f: dl[f] for f in frames}
-    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=1 << 16, max_blocks=16384,
+    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=1 << 18, max_blocks=60000,
                                 algorithm=_capi.default_algorithm(allocation_mode=alloc, normal_mode=1, fast_math=0,
                                                                   autotune=0),
                                 layer_format=fp16)

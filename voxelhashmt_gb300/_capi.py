@@ -153,6 +153,9 @@ _SIGNATURES = {
     "vh_render_depth": (C.c_int, [_vp, C.c_int32, C.POINTER(VhIntrinsics), C.POINTER(VhPose), C.c_uint32,
                                   C.c_uint32, C.c_float, C.c_float, C.c_float, _vp, _vp]),
     "vh_expf_eval": (C.c_int, [_vp, _vp, C.c_uint64, _vp]),
+    "vh_evict_blocks": (C.c_int, [_vp, C.c_uint32, C.c_uint64, C.c_int32, _vp, _vp, C.c_uint64, C.c_int32, _u64p,
+                                  _vp]),
+    "vh_restore_blocks": (C.c_int, [_vp, _vp, _vp, C.c_uint64, C.c_int32, _vp]),
     "vh_expf_check": (C.c_int, [C.c_uint32, C.c_uint64, _u64p, C.POINTER(C.c_uint32), _vp]),
 }
 

@@ -209,6 +209,40 @@ class VoxelHashTSDF:
                                                  C.c_void_p(v.ctypes.data), k.shape[0], 0, None), self.handle)
 
 
+    def evict_blocks(self, min_age_frames, target_blocks=0, native=True):
+        """Evicts the blocks not updated within the last min_age_frames frames (and, with target_blocks, the oldest
+        further ones until at most target_blocks remain); returns (keys (N,3) int32, data): the volume's own block
+        images (N, block bytes) uint8 for restore_blocks when native, else the reference Voxel layout as
+        export_blocks returns it.  Host memory."""
+        return self._evict_into(min_age_frames, target_blocks, native, self.block_count())
+
+    def _evict_into(self, min_age_frames, target_blocks, native, hint):
+        bpb = (98304 if self.layer_format == 1 else 147456) if native else 147456
+        cap = max(int(hint), 1)
+        while True:
+            keys = np.zeros((cap, 3), np.int32)
+            data = np.zeros((cap, bpb), np.uint8)
+            n = C.c_uint64()
+            st = _capi.lib().vh_evict_blocks(self.handle, int(min_age_frames), int(target_blocks), 1 if native else 0,
+                                             keys.ctypes.data_as(C.POINTER(C.c_int32)), C.c_void_p(data.ctypes.data),
+                                             cap, 0, C.byref(n), None)
+            if st == _capi.VH_ERR_BUFFER_TOO_SMALL:
+                cap = int(n.value)
+                continue
+            _capi.check(st, self.handle)
+            m = int(n.value)
+            if native:
+                return keys[:m], data[:m]
+            return keys[:m], data[:m].view(np.uint32).reshape(m, 512, 6, 3, 4)
+
+    def restore_blocks(self, keys, data):
+        """Puts back blocks saved by evict_blocks(native=True), bit for bit."""
+        k = np.ascontiguousarray(keys, np.int32).reshape(-1, 3)
+        d = np.ascontiguousarray(data)
+        _capi.check(_capi.lib().vh_restore_blocks(self.handle, k.ctypes.data_as(C.POINTER(C.c_int32)),
+                                                  C.c_void_p(d.ctypes.data), k.shape[0], 0, None), self.handle)
+
+
 class TsdfIntegrationBackend:
     """reconstruction_backend.h:18-42, GPU only."""
 

@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, "libvoxelhash_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["vh_filter.cu", "vh_alloc.cu", "vh_integrate.cu", "vh_mesh.cu", "vh_misc.cu", "vh_render.cu",
-           "vh_raycast.cu", "vh_static_scratch.cu", "vh_weld.cu", "vh_expf.cu", "vh_capi.cpp", "vh_png.cpp", "vh_dataset.cpp"]
+           "vh_raycast.cu", "vh_static_scratch.cu", "vh_weld.cu", "vh_expf.cu", "vh_evict.cu", "vh_capi.cpp", "vh_png.cpp", "vh_dataset.cpp"]
 # second compile of the update pass: the fast-math form (vh::fast), object name and extra device flags
 VARIANTS = [("vh_integrate.cu", "vh_integrate_fast", ["-DVH_FAST_MATH", "-use_fast_math", "-fmad=true"]),
             # the denoiser's kernels: ordinary FP32 rounding (contraction allowed), no parity contract

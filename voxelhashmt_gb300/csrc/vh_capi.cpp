@@ -69,6 +69,13 @@ struct vh_volume {
   int* d_export_keys = nullptr;
   uint32_t* d_import_idx = nullptr;
   size_t export_capacity = 0;  // blocks
+  // eviction scratch (vh_evict_blocks): victim and source lists (max_blocks words each), per-CTA scan counts,
+  // age histogram, two totals
+  uint32_t* d_evict_list = nullptr;
+  uint32_t* d_evict_src = nullptr;
+  uint32_t* d_evict_cta = nullptr;
+  uint32_t* d_evict_hist = nullptr;
+  uint32_t* d_evict_total = nullptr;
   bool profile = false;
   std::vector<cudaEvent_t> event_pool;
   std::vector<std::vector<cudaEvent_t>> profiled;  // 4 events per recorded frame
@@ -550,6 +557,11 @@ void vh_destroy(vh_volume* v) {
   dfree(V.dir_mask);
   dfree(V.block_stamp);
   dfree(V.counters);
+  dfree(v->d_evict_list);
+  dfree(v->d_evict_src);
+  dfree(v->d_evict_cta);
+  dfree(v->d_evict_hist);
+  dfree(v->d_evict_total);
   if (v->h_counters) cudaFreeHost(v->h_counters);
   dfree(v->d_depth_in);
   if (v->copy_stream) {
@@ -689,6 +701,158 @@ vh_status vh_integrate(vh_volume* v, const float* depth, int32_t on_device, cons
     v->profiled.push_back(std::move(ev));
   }
   return VH_OK;
+}
+
+// ---- eviction and restore ----
+
+namespace {
+
+size_t native_block_bytes(const vh_volume* v) {
+  return v->dev.layers16 != nullptr
+             ? static_cast<size_t>(vh::kDirs) * vh::kBlockVoxels * vh::kBinWords16 * sizeof(uint4)
+             : kBlockBytes;
+}
+
+vh_status ensure_staging(vh_volume* v) {
+  if (!v->d_export) {
+    VH_CUDA(v, cudaMalloc(reinterpret_cast<void**>(&v->d_export), kExportChunk * kBlockBytes));
+    VH_CUDA(v, dalloc(&v->d_export_keys, 3 * kExportChunk));
+    v->export_capacity = kExportChunk;
+  }
+  if (!v->d_import_idx) VH_CUDA(v, dalloc(&v->d_import_idx, kExportChunk));
+  return VH_OK;
+}
+
+vh_status ensure_evict_scratch(vh_volume* v) {
+  if (v->d_evict_list) return VH_OK;
+  const size_t nb = std::max<size_t>(v->dev.max_blocks, 1);
+  VH_CUDA(v, dalloc(&v->d_evict_list, nb));
+  VH_CUDA(v, dalloc(&v->d_evict_src, nb));
+  VH_CUDA(v, dalloc(&v->d_evict_cta, nb / 1024 + 2));
+  VH_CUDA(v, dalloc(&v->d_evict_hist, vh::kAgeBins));
+  VH_CUDA(v, dalloc(&v->d_evict_total, 2));
+  return VH_OK;
+}
+
+vh_status recount_into_counters(vh_volume* v, cudaStream_t s) {
+  VH_CUDA(v, vh::launch_recount(v->dev, v->d_scalar + 1, s));
+  VH_CUDA(v, cudaMemcpyAsync(&v->dev.counters->observed_voxels, v->d_scalar + 1, sizeof(unsigned long long),
+                             cudaMemcpyDeviceToDevice, s));
+  return VH_OK;
+}
+
+}  // namespace
+
+vh_status vh_evict_blocks(vh_volume* v, uint32_t min_age_frames, uint64_t target_blocks, int32_t format,
+                          int32_t* keys_out, void* data_out, uint64_t max_out, int32_t out_on_device,
+                          uint64_t* evicted, void* stream) {
+  if (!v || !evicted || (format != 0 && format != 1)) {
+    return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_evict_blocks: bad argument");
+  }
+  *evicted = 0;
+  if (v->dev.max_blocks == 0) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_evict_blocks: keys-only volume");
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  vh_status st = ensure_evict_scratch(v);
+  if (st == VH_OK) st = ensure_staging(v);
+  if (st == VH_OK) st = read_counters(v, s);
+  if (st != VH_OK) return st;
+  const uint32_t n = static_cast<uint32_t>(block_total(v));
+  if (n == 0) return VH_OK;
+  // threshold: age >= min_age_frames, lowered through the age histogram until at most target_blocks remain
+  uint32_t threshold = min_age_frames;
+  if (target_blocks > 0 && target_blocks < n) {
+    std::vector<uint32_t> hist(vh::kAgeBins);
+    VH_CUDA(v, vh::launch_age_hist(v->dev, v->d_evict_hist, s));
+    VH_CUDA(v, cudaMemcpyAsync(hist.data(), v->d_evict_hist, vh::kAgeBins * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    VH_CUDA(v, cudaStreamSynchronize(s));
+    const uint64_t need = n - target_blocks;
+    uint64_t acc = 0;
+    uint32_t t = vh::kAgeBins - 1;
+    for (int bin = vh::kAgeBins - 1; bin >= 0; --bin) {
+      acc += hist[bin];
+      t = static_cast<uint32_t>(bin);
+      if (acc >= need) break;
+    }
+    threshold = std::min(threshold, t);
+  }
+  VH_CUDA(v, vh::launch_select(v->dev, n, threshold, 0, 0U, v->d_evict_cta, v->d_evict_total, v->d_evict_list, s));
+  uint32_t nv = 0;
+  VH_CUDA(v, cudaMemcpyAsync(&nv, v->d_evict_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  if (nv == 0) return VH_OK;
+  if ((keys_out || data_out) && nv > max_out) {
+    *evicted = nv;
+    return fail(v, VH_ERR_BUFFER_TOO_SMALL, "vh_evict_blocks: output buffers hold fewer blocks than are evicted");
+  }
+  // 1. copy the victims out (staging buffer, then the caller's memory)
+  const size_t bytes = format == 1 ? native_block_bytes(v) : kBlockBytes;
+  const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (keys_out || data_out) {
+    for (uint64_t done = 0; done < nv; done += kExportChunk) {
+      const uint32_t c = static_cast<uint32_t>(std::min<uint64_t>(kExportChunk, nv - done));
+      VH_CUDA(v, vh::launch_copy_out(v->dev, v->d_evict_list + done, c, format, v->d_export_keys, v->d_export, s));
+      if (data_out) {
+        VH_CUDA(v, cudaMemcpyAsync(static_cast<char*>(data_out) + done * bytes, v->d_export, c * bytes, kind, s));
+      }
+      if (keys_out) {
+        VH_CUDA(v, cudaMemcpyAsync(keys_out + 3 * done, v->d_export_keys, 3 * c * sizeof(int32_t), kind, s));
+      }
+    }
+  }
+  // 2. the survivors above the new block count move into the victims' slots below it
+  const uint32_t live = n - nv;
+  VH_CUDA(v, vh::launch_select(v->dev, n, threshold, 1, live, v->d_evict_cta, v->d_evict_total + 1, v->d_evict_src, s));
+  uint32_t nmove = 0;
+  VH_CUDA(v, cudaMemcpyAsync(&nmove, v->d_evict_total + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  VH_CUDA(v, cudaStreamSynchronize(s));
+  // the victims below `live` are the first nmove entries of the ascending victim list
+  VH_CUDA(v, vh::launch_move_blocks(v->dev, v->d_evict_src, v->d_evict_list, nmove, s));
+  // 3. the freed tail [live, n) back to zero, the hash rebuilt from the live keys
+  vh::Volume& V = v->dev;
+  const size_t tail = n - live;
+  const size_t nb_bytes = native_block_bytes(v);
+  char* pool = V.layers16 != nullptr ? reinterpret_cast<char*>(V.layers16) : reinterpret_cast<char*>(V.layers);
+  VH_CUDA(v, cudaMemsetAsync(pool + static_cast<size_t>(live) * nb_bytes, 0, tail * nb_bytes, s));
+  VH_CUDA(v, cudaMemsetAsync(V.block_keys + live, 0, tail * sizeof(int4), s));
+  VH_CUDA(v, cudaMemsetAsync(V.obs_mask + static_cast<size_t>(live) * (vh::kBlockVoxels / 32), 0,
+                             tail * (vh::kBlockVoxels / 32) * sizeof(uint32_t), s));
+  VH_CUDA(v, cudaMemsetAsync(V.dir_mask + live, 0, tail * sizeof(uint32_t), s));
+  VH_CUDA(v, cudaMemsetAsync(V.block_stamp + live, 0, tail * sizeof(uint32_t), s));
+  VH_CUDA(v, vh::launch_rehash(V, live, s));
+  // 4. counters: the new block count, no visible list, observed voxels recounted
+  vh::Counters c = *v->h_counters;
+  c.num_blocks = live;
+  c.visible_count = 0;
+  c.new_blocks = 0;
+  VH_CUDA(v, cudaMemcpyAsync(V.counters, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+  st = recount_into_counters(v, s);
+  if (st != VH_OK) return st;
+  *evicted = nv;
+  v->mesh_triangles = 0;
+  return vh_synchronize(v, stream);
+}
+
+vh_status vh_restore_blocks(vh_volume* v, const int32_t* keys, const void* data, uint64_t count, int32_t in_on_device,
+                            void* stream) {
+  if (!v || (count && (!keys || !data))) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_restore_blocks: bad argument");
+  if (v->dev.max_blocks == 0) return fail(v, VH_ERR_INVALID_ARGUMENT, "vh_restore_blocks: keys-only volume");
+  DeviceGuard guard(v->params.device);
+  const cudaStream_t s = as_stream(stream);
+  vh_status st = ensure_staging(v);
+  if (st != VH_OK) return st;
+  const size_t bytes = native_block_bytes(v);
+  const cudaMemcpyKind kind = in_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  for (uint64_t done = 0; done < count; done += kExportChunk) {
+    const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(kExportChunk, count - done));
+    VH_CUDA(v, cudaMemcpyAsync(v->d_export_keys, keys + 3 * done, 3 * n * sizeof(int32_t), kind, s));
+    VH_CUDA(v, cudaMemcpyAsync(v->d_export, static_cast<const char*>(data) + done * bytes, n * bytes, kind, s));
+    VH_CUDA(v, vh::launch_import_keys(v->dev, v->d_export_keys, n, v->d_import_idx, s));
+    VH_CUDA(v, vh::launch_restore_native(v->dev, v->d_export, n, v->d_import_idx, s));
+  }
+  st = recount_into_counters(v, s);
+  if (st != VH_OK) return st;
+  return vh_synchronize(v, stream);
 }
 
 vh_status vh_autotune_result(vh_volume* v, int32_t* variant, int32_t* threads_per_cta, int32_t* min_ctas_per_sm,

@@ -82,6 +82,25 @@ cudaError_t launch_export(const Volume& V, uint32_t first, uint32_t count, int* 
 // import blocks in the reference layout (insert or overwrite); idx: n scratch words
 cudaError_t launch_import(const Volume& V, const int* keys, const float4* voxels, uint32_t n, uint32_t* idx,
                           cudaStream_t s);
+// insert (or find) n keys; idx[i] receives the pool block of key i (kInvalidBlock when the pool is full)
+cudaError_t launch_import_keys(const Volume& V, const int* keys, uint32_t n, uint32_t* idx, cudaStream_t s);
+
+// ---- eviction (vh_evict.cu) ----
+constexpr int kAgeBins = 4096;  // block-age histogram: ages 0..4094 frames, the last bin everything older
+cudaError_t launch_age_hist(const Volume& V, uint32_t* hist, cudaStream_t s);
+// pool blocks of [0, n) in ascending order into list, their number into *total (device); what 0: blocks whose
+// age (frames since their last layer update; never updated = oldest) is >= threshold; what 1: blocks of [lo, n)
+// whose age is below it.  cta_scratch: ceil(n / 1024) words.
+cudaError_t launch_select(const Volume& V, uint32_t n, uint32_t threshold, int what, uint32_t lo,
+                          uint32_t* cta_scratch, uint32_t* total, uint32_t* list, cudaStream_t s);
+// listed blocks with their keys into a staging buffer: native 1 the pool's own block image, 0 the reference layout
+cudaError_t launch_copy_out(const Volume& V, const uint32_t* list, uint32_t n, int native, int* keys, void* out,
+                            cudaStream_t s);
+cudaError_t launch_move_blocks(const Volume& V, const uint32_t* src, const uint32_t* dst, uint32_t n, cudaStream_t s);
+// empties the hash and inserts the keys of pool blocks [0, live)
+cudaError_t launch_rehash(const Volume& V, uint32_t live, cudaStream_t s);
+// block images in into the pool blocks idx[0..n) (kInvalidBlock: skipped), masks rebuilt, stamped with the frame
+cudaError_t launch_restore_native(const Volume& V, const void* in, uint32_t n, const uint32_t* idx, cudaStream_t s);
 // depth ray-cast of the fused volume from pose p.T_wc: out[W*H] camera depth of the first plane crossing, 0 = none
 cudaError_t launch_raycast(const Volume& V, const Params& p, float min_depth, float max_depth, float step, float* out,
                            cudaStream_t s);

@@ -139,6 +139,12 @@ __global__ void __launch_bounds__(256) import_voxels_kernel(const Volume V, cons
 
 }  // namespace
 
+cudaError_t launch_import_keys(const Volume& V, const int* keys, uint32_t n, uint32_t* idx, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  import_keys_kernel<<<(n + 255) / 256, 256, 0, s>>>(V, keys, n, idx);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_import(const Volume& V, const int* keys, const float4* voxels, uint32_t n, uint32_t* idx,
                           cudaStream_t s) {
   if (n == 0) return cudaSuccess;
