@@ -105,10 +105,11 @@ typedef struct vh_algorithm {
    * depth samples); 1: the same normal evaluated once per pixel, bilinearly interpolated per voxel. */
   int32_t normal_mode;
   /* 1 (default): with normal_mode 1, the first frames cycle the layer-update kernel through its launch shapes
-   * (threads per CTA x minimum resident CTAs per SM), time each with CUDA events and keep the fastest
+   * (threads per CTA x minimum resident CTAs per SM x voxel slots a thread tests per pass), time each with CUDA
+   * events and keep the fastest
    * (results do not depend on the shape); 0: the shape launch_variant. */
   int32_t autotune;
-  int32_t launch_variant; /* the layer-update launch shape used without autotuning (0..5, default 0) */
+  int32_t launch_variant; /* the layer-update launch shape used without autotuning (0..9, default 0) */
   /* 0 (default): the reference's bilateral depth filter; 1: the learned depth denoiser set with
    * vh_set_depth_denoiser (the bilateral filter until weights are set). */
   int32_t depth_filter;

@@ -362,8 +362,8 @@ def test_autotuned_launch_shapes_give_identical_volumes(backend, orbit_half, fas
     differ in the last bits: identical keys and occupancy on 99.9% of bins, fields within 1e-3 voxel
     (99.9%)."""
     sc, depths, _ = orbit_half
-    # 52 frames: 24 before tuning, 6 shapes x 4 rounds of tuning, then the kept shape
-    frames = list(range(16)) * 3 + list(range(4))
+    # 68 frames: 24 before tuning, 10 shapes x 4 rounds of tuning, then the kept shape
+    frames = list(range(16)) * 4 + list(range(4))
     from oracle import oracle as O
     algo = dict(allocation_mode=1, fast_math=fast_math, normal_mode=1)
     tuned, _ = _fuse(backend, sc, frames, depths, **algo)

@@ -831,17 +831,17 @@ __device__ __forceinline__ bool map_update_voxel(const float* __restrict__ depth
 // shared-memory queue with their projection, and updates them one per thread in batches of kT (survivors
 // carry over between chunks).  The expensive part runs on compacted threads, and the dynamic order keeps every
 // CTA busy until the last chunk.
-template <int kT>
+template <int kT, int kS = 1>
 struct MapQueue {
-  static constexpr int kQueue = 2 * kT;
+  static constexpr int kQueue = kT * kS + kT;  // a pass's survivors plus fewer than kT carried over
   uint32_t code[kQueue];  // (pool block << 9) | voxel
   float u[kQueue], v[kQueue], d[kQueue], x[kQueue], y[kQueue], z[kQueue];
   uint32_t count;
 };
 
-template <int kT>
+template <class Queue>
 __device__ __forceinline__ void map_update_entry(const float* __restrict__ depth, const float4* __restrict__ nmap,
-                                                 const Volume& V, const Params& p, const MapQueue<kT>& Q, int e,
+                                                 const Volume& V, const Params& p, const Queue& Q, int e,
                                                  bool& updated, bool& newly) {
   const uint32_t code = Q.code[e];
   updated = map_update_voxel(depth, nmap, V, p, code >> 9, static_cast<int>(code & 511U), mk3(Q.x[e], Q.y[e], Q.z[e]),
@@ -864,21 +864,23 @@ __device__ __forceinline__ void tally_updates(CtaStats& st, bool updated, bool n
   }
 }
 
-// kT threads per CTA (a divisor of 512), at least kMinBlocks resident CTAs per SM (which caps the registers).
-// Survivors carry over between chunks: a chunk's survivors are appended to the queue, and whenever it holds at
-// least kT entries the CTA updates the last kT of them, one per thread, so every thread of the update phase has
-// a voxel; the rest are updated when the work queue is empty.  Each voxel is updated by exactly one thread and
-// the updates of different voxels touch different bins, so the order does not change the result.
-template <int kT, int kMinBlocks>
+// kT threads per CTA, kS voxel slots per thread and pass (kT * kS divides 512, so a pass's chunk lies in one
+// visible block), at least kMinBlocks resident CTAs per SM (which caps the registers).  A pass runs the prefix
+// of its kS slots with independent loads, appends the survivors to the queue, then updates full batches of kT
+// entries (the last kT entries, one per thread) while the queue holds kT or more; fewer than kT carry over to
+// the next pass, and the rest is updated when the work queue is empty.  Each voxel is updated by exactly one
+// thread and the updates of different voxels touch different bins, so the order does not change the result.
+template <int kT, int kMinBlocks, int kS = 1>
 __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const float* __restrict__ depth,
                                                                      const float4* __restrict__ nmap, const Volume V,
                                                                      const Params p) {
-  static_assert(kBlockVoxels % kT == 0, "CTA size must divide the block's voxel count");
-  __shared__ MapQueue<kT> Q;
+  static_assert(kBlockVoxels % (kT * kS) == 0, "a pass's chunk must divide the block's voxel count");
+  constexpr int kChunk = kT * kS;
+  __shared__ MapQueue<kT, kS> Q;
   __shared__ uint32_t s_item;
   __shared__ CtaStats s_stats;
   const uint32_t nvis = V.counters->visible_count;
-  const uint32_t nchunks = nvis * static_cast<uint32_t>(kBlockVoxels / kT);
+  const uint32_t nchunks = nvis * static_cast<uint32_t>(kBlockVoxels / kChunk);
   const int tid = threadIdx.x, lane = tid & 31;
   if (tid == 0) {
     Q.count = 0U;
@@ -899,49 +901,61 @@ __global__ void __launch_bounds__(kT, kMinBlocks) fused_update_kernel(const floa
     uint32_t next = 0U;
     if (tid == 0 && !drained) next = atomicAdd(&V.counters->update_queue, 1U);
     if (!drained) {
-      // 1. prefix of one slot per thread, survivors appended to the queue (fewer than kT entries carried over)
-      const unsigned long long i = static_cast<unsigned long long>(item) * kT + tid;
-      const int li = static_cast<int>(i & 511U);
-      const int4 vk = V.visible_keys[static_cast<uint32_t>(i >> 9)];
+      // 1. prefix of kS slots per thread (one visible block per chunk), survivors appended to the queue
+      const unsigned long long base_slot = static_cast<unsigned long long>(item) * kChunk;
+      const int4 vk = V.visible_keys[static_cast<uint32_t>(base_slot >> 9)];
       const uint32_t b = static_cast<uint32_t>(vk.w);
-      bool pass = false;
-      f3 pc = mk3(0.0f, 0.0f, 0.0f);
-      float u = 0.0f, v = 0.0f, d = 0.0f;
-      if (li == 0 && b != kInvalidBlock) V.block_stamp[b] = frame;  // for incremental meshing
-      if (b != kInvalidBlock) pass = voxel_prefix(depth, p, vk, li, pc, u, v, d);
-      const uint32_t ballot = __ballot_sync(0xffffffffU, pass);
-      uint32_t base = 0U;
-      if (lane == 0 && ballot) {
-        base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
-        atomicAdd(&s_stats.active, static_cast<uint32_t>(__popc(ballot)));
+      if ((base_slot & 511ULL) == 0ULL && tid == 0 && b != kInvalidBlock) V.block_stamp[b] = frame;
+      bool pass[kS];
+      f3 pc[kS];
+      float u[kS], v[kS], d[kS];
+#pragma unroll
+      for (int j = 0; j < kS; ++j) {
+        const int li = static_cast<int>((base_slot + static_cast<unsigned long long>(j * kT + tid)) & 511ULL);
+        pass[j] = false;
+        pc[j] = mk3(0.0f, 0.0f, 0.0f);
+        u[j] = v[j] = d[j] = 0.0f;
+        if (b != kInvalidBlock) pass[j] = voxel_prefix(depth, p, vk, li, pc[j], u[j], v[j], d[j]);
       }
-      base = __shfl_sync(0xffffffffU, base, 0);
-      if (pass) {
-        const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
-        Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
-        Q.u[e] = u;
-        Q.v[e] = v;
-        Q.d[e] = d;
-        Q.x[e] = pc.x;
-        Q.y[e] = pc.y;
-        Q.z[e] = pc.z;
+#pragma unroll
+      for (int j = 0; j < kS; ++j) {
+        const uint32_t ballot = __ballot_sync(0xffffffffU, pass[j]);
+        uint32_t base = 0U;
+        if (lane == 0 && ballot) {
+          base = atomicAdd(&Q.count, static_cast<uint32_t>(__popc(ballot)));
+          atomicAdd(&s_stats.active, static_cast<uint32_t>(__popc(ballot)));
+        }
+        base = __shfl_sync(0xffffffffU, base, 0);
+        if (pass[j]) {
+          const int li = static_cast<int>((base_slot + static_cast<unsigned long long>(j * kT + tid)) & 511ULL);
+          const uint32_t e = base + __popc(ballot & ((1U << lane) - 1U));
+          Q.code[e] = (b << 9) | static_cast<uint32_t>(li);
+          Q.u[e] = u[j];
+          Q.v[e] = v[j];
+          Q.d[e] = d[j];
+          Q.x[e] = pc[j].x;
+          Q.y[e] = pc[j].y;
+          Q.z[e] = pc[j].z;
+        }
       }
     }
     __syncthreads();
-    // 2. entries [first, n), one per thread: a full batch (the last kT entries; [0, n - kT) stay for later
-    // chunks), nothing while fewer than kT are queued, and the carried-over rest once the work queue is empty.
-    // One call site, so every voxel runs the same instructions (with contraction on, two inlined copies of
-    // the update could round differently).
-    const uint32_t n = Q.count;
-    const uint32_t first = drained ? 0U : (n >= static_cast<uint32_t>(kT) ? n - static_cast<uint32_t>(kT) : n);
-    bool updated = false, newly = false;
-    if (first + static_cast<uint32_t>(tid) < n) {
-      map_update_entry(depth, nmap, V, p, Q, static_cast<int>(first) + tid, updated, newly);
+    // 2. batches of kT entries from the end of the queue, one per thread: while kT or more are queued, and the
+    // rest once the work queue is empty.  One call site, so every voxel runs the same instructions (with
+    // contraction on, two inlined copies of the update could round differently).
+    uint32_t n = Q.count;
+    while (n >= static_cast<uint32_t>(kT) || (drained && n > 0U)) {
+      const uint32_t first = n >= static_cast<uint32_t>(kT) ? n - static_cast<uint32_t>(kT) : 0U;
+      bool updated = false, newly = false;
+      if (first + static_cast<uint32_t>(tid) < n) {
+        map_update_entry(depth, nmap, V, p, Q, static_cast<int>(first) + tid, updated, newly);
+      }
+      tally_updates(s_stats, updated, newly, lane);
+      n = first;
     }
-    tally_updates(s_stats, updated, newly, lane);
-    __syncthreads();  // the batch's entries and s_item are rewritten by the next chunk
+    __syncthreads();  // the batches' entries and s_item are rewritten by the next chunk
     if (tid == 0) {
-      Q.count = first;
+      Q.count = n;
       s_item = next;
     }
     if (drained) break;
@@ -1310,17 +1324,20 @@ struct FusedVariant {
   int threads;
 };
 
-template <int kT, int kMinB>
+template <int kT, int kMinB, int kS>
 void launch_fused_variant(int grid, cudaStream_t s, const float* depth, const float4* nmap, const Volume& V,
                           const Params& p) {
-  fused_update_kernel<kT, kMinB><<<grid, kT, 0, s>>>(depth, nmap, V, p);
+  fused_update_kernel<kT, kMinB, kS><<<grid, kT, 0, s>>>(depth, nmap, V, p);
 }
 
-#define VH_FUSED_VARIANT(T, B) \
-  FusedVariant { reinterpret_cast<const void*>(fused_update_kernel<T, B>), launch_fused_variant<T, B>, T }
+// (threads per CTA, minimum resident CTAs per SM, voxel slots per thread and pass)
+#define VH_FUSED_VARIANT(T, B, S) \
+  FusedVariant { reinterpret_cast<const void*>(fused_update_kernel<T, B, S>), launch_fused_variant<T, B, S>, T }
 static const FusedVariant kFusedVariants[] = {
-    VH_FUSED_VARIANT(256, 4), VH_FUSED_VARIANT(128, 8),  VH_FUSED_VARIANT(256, 6),
-    VH_FUSED_VARIANT(128, 12), VH_FUSED_VARIANT(512, 2), VH_FUSED_VARIANT(64, 16),
+    VH_FUSED_VARIANT(256, 4, 1), VH_FUSED_VARIANT(128, 8, 1),  VH_FUSED_VARIANT(256, 6, 1),
+    VH_FUSED_VARIANT(128, 12, 1), VH_FUSED_VARIANT(512, 2, 1), VH_FUSED_VARIANT(64, 16, 1),
+    VH_FUSED_VARIANT(128, 8, 4),  VH_FUSED_VARIANT(256, 4, 2), VH_FUSED_VARIANT(128, 12, 2),
+    VH_FUSED_VARIANT(256, 6, 2),
 };
 #undef VH_FUSED_VARIANT
 constexpr int kNumFusedVariants = static_cast<int>(sizeof(kFusedVariants) / sizeof(kFusedVariants[0]));
@@ -1328,7 +1345,7 @@ constexpr int kNumFusedVariants = static_cast<int>(sizeof(kFusedVariants) / size
 int fused_variant_count() { return kNumFusedVariants; }
 
 void fused_variant_shape(int variant, int* threads, int* min_blocks) {
-  static const int kMin[] = {4, 8, 6, 12, 2, 16};
+  static const int kMin[] = {4, 8, 6, 12, 2, 16, 8, 4, 12, 6};
   static_assert(sizeof(kMin) / sizeof(kMin[0]) == kNumFusedVariants, "one entry per variant");
   const int v = (variant >= 0 && variant < kNumFusedVariants) ? variant : 0;
   *threads = kFusedVariants[v].threads;

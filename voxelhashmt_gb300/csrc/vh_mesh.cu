@@ -110,6 +110,21 @@ __device__ __forceinline__ f3 interp(f3 p0, f3 p1, float v0, float v1, float iso
   return mk3(p0.x + (p1.x - p0.x) * t, p0.y + (p1.y - p0.y) * t, p0.z + (p1.z - p0.z) * t);
 }
 
+// value k of an 8-value register array, selected without indexing it (a run-time index would move the array
+// to local memory)
+__device__ __forceinline__ float pick8(const float (&a)[8], int k) {
+  float r = a[0];
+#pragma unroll
+  for (int i = 1; i < 8; ++i) r = k == i ? a[i] : r;
+  return r;
+}
+
+// corner k of the cell at grid (gx, gy, gz): ((g + corner) + 0.5) * vs per axis (loadCubeForSurface, :276-303)
+__device__ __forceinline__ f3 corner_pos(int gx, int gy, int gz, int k, float vs) {
+  return mk3((static_cast<float>(gx + c_corner[k][0]) + 0.5f) * vs, (static_cast<float>(gy + c_corner[k][1]) + 0.5f) * vs,
+             (static_cast<float>(gz + c_corner[k][2]) + 0.5f) * vs);
+}
+
 // One cell of one direction: returns its triangle count; with kEmit writes them to out (9 floats each).
 template <bool kEmit>
 __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, int gz, int lx, int ly, int lz, int t,
@@ -117,9 +132,9 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
   const float vs = p.voxel_size;
   const f3 cc = mk3((static_cast<float>(gx) + 1.0f) * vs, (static_cast<float>(gy) + 1.0f) * vs,
                     (static_cast<float>(gz) + 1.0f) * vs);
-  int si[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) si[k] = staged_index(lx + c_corner[k][0], ly + c_corner[k][1], lz + c_corner[k][2]);
+  const int s0 = staged_index(lx, ly, lz);
+  // staged index of corner k: s0 + (dx + 9 dy + 81 dz)
+  auto si = [&](int k) { return s0 + c_corner[k][0] + kSide * c_corner[k][1] + kSide * kSide * c_corner[k][2]; };
 
   // collectSurfaceClusters (:439-507); candidates in shared memory, column `t` of S.cand
   float* cand = const_cast<float*>(&S.cand[0][0]) + t;
@@ -129,8 +144,8 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
   for (int k = 0; k < 8; ++k) {
 #pragma unroll
     for (int l = 0; l < kLayers; ++l) {
-      if (S.valid[l][si[k]]) {
-        const float c = plane_sd(S.plane[l][si[k]], cc);
+      if (S.valid[l][si(k)]) {
+        const float c = plane_sd(S.plane[l][si(k)], cc);
         cand[nc * kThreads] = c;
         nearest = fminf(nearest, fabsf(c - p.iso));
         ++nc;
@@ -172,16 +187,14 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
     last_size += 1;
   }
 
-  f3 pos[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    pos[k] = mk3((static_cast<float>(gx + c_corner[k][0]) + 0.5f) * vs,
-                 (static_cast<float>(gy + c_corner[k][1]) + 0.5f) * vs,
-                 (static_cast<float>(gz + c_corner[k][2]) + 0.5f) * vs);
-  }
+  // A cluster's corner values are planes within tol of its key at the cell centre, evaluated at most sqrt(3)/2
+  // voxel away (and means of such values): a key farther than tol + that from iso (with the rounding margin)
+  // gives cube index 0 or 255, no triangles.  Skipped without changing the output.
+  const float cluster_reject = tol * 1.00001f + reject;
   int total = 0;
   for (int ci = 0; ci < ncl; ++ci) {
     const float key = cand[ci * kThreads];
+    if (fabsf(key - p.iso) > cluster_reject) continue;
     // loadCubeForSurface + selectClosestLayerForSurfaceGpu (:276-303, :509-551)
     float val[8];
     uint32_t mask = 0U;
@@ -191,8 +204,8 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
       float best_delta = 1e30f;
 #pragma unroll
       for (int l = 0; l < kLayers; ++l) {
-        if (!S.valid[l][si[k]]) continue;
-        const float delta = fabsf(plane_sd(S.plane[l][si[k]], cc) - key);
+        if (!S.valid[l][si(k)]) continue;
+        const float delta = fabsf(plane_sd(S.plane[l][si(k)], cc) - key);
         if (delta <= tol && delta < best_delta) {
           best_delta = delta;
           best = l;
@@ -200,7 +213,7 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
       }
       val[k] = 0.0f;
       if (best >= 0) {
-        val[k] = plane_sd(S.plane[best][si[k]], pos[k]);
+        val[k] = plane_sd(S.plane[best][si(k)], corner_pos(gx, gy, gz, k, vs));
         mask |= 1U << k;
       }
     }
@@ -243,20 +256,16 @@ __device__ int process_cell(const Shared& S, const Params& p, int gx, int gy, in
     int ntri = 0;
     while (ntri < 5 && S.tri[cube][3 * ntri] >= 0) ++ntri;
     if (kEmit) {
-      f3 ev[12];
-#pragma unroll
-      for (int e = 0; e < 12; ++e) {
-        ev[e] = mk3(0.0f, 0.0f, 0.0f);
-        if (em & (1 << e)) {
-          const int c0 = c_edge_corners[e][0], c1 = c_edge_corners[e][1];
-          ev[e] = interp(pos[c0], pos[c1], val[c0], val[c1], p.iso);
-        }
-      }
       for (int t = 0; t < ntri; ++t) {
         float* o = out + static_cast<size_t>(total + t) * 9;
 #pragma unroll
         for (int q = 0; q < 3; ++q) {
-          const f3 v = ev[S.tri[cube][3 * t + q]];
+          // the vertex on edge e (interpolateVertexGpu, :358-374), computed where it is used: the same
+          // operations on the same values wherever an edge's vertex is needed
+          const int e = S.tri[cube][3 * t + q];
+          const int c0 = c_edge_corners[e][0], c1 = c_edge_corners[e][1];
+          const f3 v = interp(corner_pos(gx, gy, gz, c0, vs), corner_pos(gx, gy, gz, c1, vs), pick8(val, c0),
+                              pick8(val, c1), p.iso);
           o[3 * q] = v.x;
           o[3 * q + 1] = v.y;
           o[3 * q + 2] = v.z;

@@ -10,6 +10,10 @@ This module generates the workloads the fusion path is measured on with the same
 * ``room_scene`` -- the inside of a 4x5x3 m box room holding seeded spheres (r 0.1-0.6 m),
   boxes (0.1-1 m sides) and vertical cylinders; a hand-held random walk (1 cm/frame
   translation, 1 degree/frame yaw/pitch jitter); 640x480, fx=fy=525, cx=319.5, cy=239.5.
+* ``multi_room_scene`` -- the large streaming configuration: a 20x20x4 m floor of 4x4 rooms (5x5 m,
+  0.1 m walls with 1 m door gaps) holding 400 primitives in all; the camera walks room to room
+  through the doors (about 1.25 cm/frame over 6000 frames) sweeping its yaw; 1280x720,
+  fx=fy=1050 (the room configuration's field of view), 3 mm voxels, 1.2 cm truncation, 2^22 buckets.
 
 Noise model for both: depth += N(0, (0.0012 z^2)^2) and 1 % of pixels dropped to 0.
 
@@ -198,6 +202,98 @@ def room_scene(seed=0, frames=1000, width=640, height=480, fx=525.0, fy=525.0, c
         pitch = float(np.clip(pitch + rng.uniform(-jitter, jitter), -0.5, 0.5))
     return Scene(np.asarray(prims, np.float32), K, poses, seed, name="room",
                  voxel_size=0.005, truncation=0.02, hash_buckets=1 << 20, max_depth=8.0)
+
+
+def multi_room_scene(seed=0, frames=6000, width=1280, height=720, fx=1050.0, fy=1050.0, cx=639.5, cy=359.5,
+                     n_prims=400, rooms=4, room_size=5.0, height_m=4.0, door=1.0, wall=0.1) -> Scene:
+    """A rooms x rooms grid of room_size rooms inside one shell: interior walls are boxes with a door gap
+    (full height) in the middle of every room side, the rest of the n_prims primitives are seeded spheres,
+    boxes and cylinders kept clear of the walk and the walls.  The walk visits the rooms in serpentine order,
+    room centre -> door -> next room centre, at 1.5 m height; the camera looks along the walk with a slow
+    +-50 degree yaw sweep and small pitch jitter."""
+    rng = np.random.default_rng(seed)
+    side = rooms * room_size
+    prims = [_prim(ROOM, (0.0, 0.0, 0.0), (side, side, height_m))]
+    hw = wall / 2
+    for k in range(1, rooms):  # interior wall lines x = k * room_size and y = k * room_size
+        w = k * room_size
+        for j in range(rooms):
+            a, b = j * room_size, (j + 1) * room_size
+            mid = (a + b) / 2
+            for lo_, hi_ in ((a, mid - door / 2), (mid + door / 2, b)):
+                prims.append(_prim(BOX, (w - hw, lo_, 0.0), (w + hw, hi_, height_m)))
+                prims.append(_prim(BOX, (lo_, w - hw, 0.0), (hi_, w + hw, height_m)))
+    # the walk: serpentine over the room grid, through the door in the shared wall
+    order = []
+    for row in range(rooms):
+        cols = range(rooms) if row % 2 == 0 else range(rooms - 1, -1, -1)
+        order += [(c, row) for c in cols]
+
+    def centre(c, r):
+        return np.array([(c + 0.5) * room_size, (r + 0.5) * room_size, 1.5])
+
+    way = [centre(*order[0])]
+    for (c0, r0), (c1, r1) in zip(order, order[1:]):
+        way.append((centre(c0, r0) + centre(c1, r1)) / 2)  # the door between two adjacent rooms
+        way.append(centre(c1, r1))
+    way = np.asarray(way)
+    seg = np.linalg.norm(np.diff(way, axis=0), axis=1)
+    cum = np.concatenate([[0.0], np.cumsum(seg)])
+
+    def clear_of_walk(p, r):
+        for a, b in zip(way[:-1], way[1:]):
+            ab = b - a
+            t = np.clip(np.dot(p[:2] - a[:2], ab[:2]) / max(np.dot(ab[:2], ab[:2]), 1e-9), 0.0, 1.0)
+            if np.linalg.norm(p[:2] - (a[:2] + t * ab[:2])) < r + 0.7:
+                return False
+        return True
+
+    def clear_of_walls(p, r):
+        for k in range(1, rooms):
+            w = k * room_size
+            if abs(p[0] - w) < r + hw + 0.05 or abs(p[1] - w) < r + hw + 0.05:
+                return False
+        return True
+
+    placed = len(prims)
+    while placed < n_prims:
+        kind = rng.integers(0, 3)
+        c = np.array([rng.uniform(0.3, side - 0.3), rng.uniform(0.3, side - 0.3), rng.uniform(0.2, height_m - 0.5)])
+        if kind == 0:
+            r = rng.uniform(0.1, 0.5)
+            if not (clear_of_walk(c, r) and clear_of_walls(c, r)):
+                continue
+            prims.append(_prim(SPHERE, c, r=r))
+        elif kind == 1:
+            s = rng.uniform(0.1, 0.9, size=3)
+            rr = float(np.linalg.norm(s[:2])) / 2
+            if not (clear_of_walk(c, rr) and clear_of_walls(c, rr)):
+                continue
+            prims.append(_prim(BOX, c - s / 2, c + s / 2))
+        else:
+            r = rng.uniform(0.08, 0.35)
+            h = rng.uniform(0.3, 2.5)
+            base = np.array([c[0], c[1], 0.0])
+            if not (clear_of_walk(base, r) and clear_of_walls(base, r)):
+                continue
+            prims.append(_prim(CYLINDER, base, r=r, h=min(h, height_m)))
+        placed += 1
+    K = Intrinsics(width, height, fx, fy, cx, cy)
+    poses = []
+    s_at = np.linspace(0.0, cum[-1], frames)
+    jitter = math.radians(1.0)
+    pitch = 0.0
+    for i, sv in enumerate(s_at):
+        k = min(int(np.searchsorted(cum, sv, side="right")) - 1, len(seg) - 1)
+        t = (sv - cum[k]) / seg[k]
+        pos = way[k] + t * (way[k + 1] - way[k])
+        d = way[k + 1] - way[k]
+        yaw = math.atan2(d[1], d[0]) + math.radians(50.0) * math.sin(2 * math.pi * i / 600.0)
+        pitch = float(np.clip(pitch + rng.uniform(-jitter, jitter), -0.3, 0.3))
+        fwd = np.array([math.cos(pitch) * math.cos(yaw), math.cos(pitch) * math.sin(yaw), math.sin(pitch)])
+        poses.append(look_at(pos, pos + fwd))
+    return Scene(np.asarray(prims, np.float32), K, poses, seed, name="multi_room",
+                 voxel_size=0.003, truncation=0.012, hash_buckets=1 << 22, max_depth=8.0)
 
 
 def _hash_u32(x):
