@@ -63,7 +63,9 @@ def parse():
     ap.add_argument("--no-chamfer", action="store_true", help="skip the Chamfer distances of the fused meshes")
     ap.add_argument("--room-only", action="store_true",
                     help="skip the legs beside the room workload (the small orbit configuration, the 64-scene batch)")
-    ap.add_argument("--workload", default="room", choices=["room", "batch", "denoiser"],
+    ap.add_argument("--stream-frames", type=int, default=6000, help="streaming workload: frames of the walk")
+    ap.add_argument("--stream-max-blocks", type=int, default=2_000_000, help="streaming workload: pool blocks")
+    ap.add_argument("--workload", default="room", choices=["room", "batch", "denoiser", "streaming"],
                     help="room: the room-scale workload (the headline); batch: N object scans fused as one batch; "
                          "denoiser: train the learned filter and compare Chamfer with the bilateral filter")
     ap.add_argument("--scenes", type=int, default=64, help="scenes of the batch workload")
@@ -797,6 +799,150 @@ def run_denoiser(args):
     return 0
 
 
+def run_streaming(args):
+    """Large streaming configuration: the 20x20x4 m multi-room walk (scenes.multi_room_scene: 400 primitives,
+    1280x720, 3 mm voxels, 1.2 cm truncation, 2^22 buckets) fused 30 frames per step into a pool of at most
+    --stream-max-blocks FP16 blocks (opt-in form).  Whenever the pool is over 90 % full after a step, the
+    oldest blocks (longest since their last layer update) are evicted down to 80 % and streamed out to pinned
+    host memory as the pool's own block images (vh_evict_blocks); every 100 frames, marching cubes runs over the
+    blocks the layer update touched in the last 100 frames (vh_extract_mesh_recent).  Frames are rendered on
+    the device before each step, outside the timed region.  value = pixels fused / summed CUDA-event time of
+    the fusion steps; the eviction and meshing times are reported beside it, and the wall clock over
+    fusion + eviction + meshing gives the sustained rate."""
+    import ctypes as C
+
+    import torch
+    from voxelhashmt_gb300 import _capi, backend, metrics, scenes
+    from voxelhashmt_gb300 import build as pbuild
+    pbuild.build()
+    torch.cuda.set_device(0)
+    sc = scenes.multi_room_scene(seed=args.seed, frames=args.stream_frames)
+    K = sc.intrinsics
+    px = K.width * K.height
+    step_frames = 30
+    max_blocks = int(args.stream_max_blocks)
+    algo_kw, fmt = FORMS["chosen"]
+    prims = torch.from_numpy(np.ascontiguousarray(sc.prims, np.float32)).cuda()
+    buf = torch.empty((step_frames, K.height, K.width), dtype=torch.float32, device="cuda")
+    Kc = _capi.intrinsics(K)
+    stream = torch.cuda.current_stream()
+
+    def render(f0, n):
+        for i in range(n):
+            P = _capi.pose(sc.poses[f0 + i])
+            _capi.check(_capi.lib().vh_render_depth(C.c_void_p(prims.data_ptr()), prims.shape[0], C.byref(Kc),
+                                                    C.byref(P), sc.seed, f0 + i, sc.noise_sigma_z2, sc.dropout,
+                                                    sc.max_depth, C.c_void_p(buf[i].data_ptr()),
+                                                    C.c_void_p(stream.cuda_stream)))
+
+    # the layer-update launch shape, tuned on the first frames before the timed walk
+    nf = min(step_frames, len(sc.poses))
+    render(0, nf)
+    launch = tune_launch_shape(torch, backend, _capi, sc, buf[:nf], FORMS["chosen"], 200000)
+    algo = dict(algo_kw)
+    if launch is not None:
+        algo.update(autotune=0, launch_variant=launch["variant"])
+    vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=max_blocks,
+                                algorithm=_capi.default_algorithm(**algo), layer_format=fmt)
+    bk = backend.TsdfIntegrationBackend("gpu")
+    # evicted blocks stream out to host memory in rounds of about chunk blocks (an age bin can add one frame's
+    # blocks to a round, hence the larger buffer)
+    chunk = max(1, min(60000, max_blocks // 20))
+    evict_cap = 4 * chunk
+    bpb = 98304 if fmt == 1 else 147456
+    host_keys = np.empty((evict_cap, 3), np.int32)
+    host_data = np.empty((evict_cap, bpb), np.uint8)
+    fuse_ms, evict_ms, mc_ms = 0.0, 0.0, 0.0
+    evictions, evicted_blocks, mc_runs, mc_blocks, mc_tris, peak_blocks = 0, 0, 0, 0, 0, 0
+    n_frames = len(sc.poses)
+    clocks = ClockSampler(0)
+    clocks.start()
+    wall0 = time.perf_counter()
+    wall_render = 0.0
+    for f0 in range(0, n_frames, step_frames):
+        n = min(step_frames, n_frames - f0)
+        r0 = time.perf_counter()
+        render(f0, n)
+        torch.cuda.synchronize()
+        wall_render += time.perf_counter() - r0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(n):
+            bk.integrate(vol, backend.DepthFrame(K, buf[i].view(-1)), sc.poses[f0 + i], 1, stream=stream,
+                         synchronize=False)
+        e1.record(stream)
+        vol.synchronize(stream)
+        fuse_ms += e0.elapsed_time(e1)
+        nb = vol.block_count()
+        peak_blocks = max(peak_blocks, nb)
+        if nb > 0.9 * max_blocks:
+            t0 = time.perf_counter()
+            while nb > 0.8 * max_blocks:
+                cnt = C.c_uint64()
+                _capi.check(_capi.lib().vh_evict_blocks(vol.handle, 0xffffffff, int(max(0.8 * max_blocks, nb - chunk)),
+                                                        1, C.c_void_p(host_keys.ctypes.data),
+                                                        C.c_void_p(host_data.ctypes.data), evict_cap, 0, C.byref(cnt),
+                                                        C.c_void_p(stream.cuda_stream)), vol.handle)
+                evicted_blocks += cnt.value
+                nb = vol.block_count()
+                if cnt.value == 0:
+                    break
+            evict_ms += 1000 * (time.perf_counter() - t0)
+            evictions += 1
+        if (f0 + n) % 100 < step_frames or f0 + n == n_frames:
+            m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ntri = C.c_size_t()
+            m0.record(stream)
+            _capi.check(_capi.lib().vh_extract_mesh_recent(vol.handle, 0.0, 100, C.byref(ntri),
+                                                           C.c_void_p(stream.cuda_stream)), vol.handle)
+            m1.record(stream)
+            torch.cuda.synchronize()
+            mc_ms += m0.elapsed_time(m1)
+            mc_runs += 1
+            mc_tris += ntri.value
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0 - wall_render
+    clock_info = clocks.stop()
+    # quality of the last incremental mesh (blocks of the last 100 frames) against the analytic surface those
+    # frames see
+    tris = backend.extract_mesh_cuda(vol, recent_frames=100)
+    chamfer = None
+    if not args.no_chamfer:
+        sel = list(range(max(0, n_frames - 100), n_frames, 10))
+        maps = []
+        out = torch.empty((K.height, K.width), dtype=torch.float32, device="cuda")
+        for f in sel:
+            P = _capi.pose(sc.poses[f])
+            _capi.check(_capi.lib().vh_render_depth(C.c_void_p(prims.data_ptr()), prims.shape[0], C.byref(Kc),
+                                                    C.byref(P), sc.seed, f, 0.0, 0.0, sc.max_depth,
+                                                    C.c_void_p(out.data_ptr()), C.c_void_p(stream.cuda_stream)))
+            maps.append(out.cpu().numpy())
+        pts = metrics.observed_surface_points(sc, sel, depth_maps=maps, stride=4, max_points=200_000)
+        chamfer = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in metrics.chamfer(tris, sc, pts).items()}
+    line = {
+        "metric": "integrated_mpix_per_s", "value": round(n_frames * px / (fuse_ms / 1000.0) / 1e6, 3),
+        "unit": "Mpix/s", "n_gpus": 1, "steps": (n_frames + step_frames - 1) // step_frames,
+        "warmup": "launch shape tuned on a scratch volume", "ms_per_step": round(fuse_ms / ((n_frames + step_frames - 1) // step_frames), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "multi-room 20x20x4 m, 400 primitives, %d-frame walk at 1280x720, 30 frames per step, "
+                               "voxel 3 mm, trunc 12 mm, 2^22 buckets, pool %d FP16 blocks, evict oldest to 80 %% "
+                               "above 90 %%, incremental MC over the last 100 frames every 100 frames" % (n_frames, max_blocks),
+                   "form": FORM_NOTE["chosen"], "l2": "inputs larger than L2 (a 30-frame step)"},
+        "update_launch_shape": launch,
+        "sustained_mpix_per_s": round(n_frames * px / wall / 1e6, 3),
+        "sustained_note": "wall clock over fusion + eviction + incremental meshing (frame rendering excluded)",
+        "peak_blocks": peak_blocks, "final_blocks": vol.block_count(),
+        "eviction": {"events": evictions, "blocks": evicted_blocks, "gb_streamed_out": round(evicted_blocks * bpb / 1e9, 2),
+                     "ms_total": round(evict_ms, 1)},
+        "incremental_mc": {"runs": mc_runs, "ms_total": round(mc_ms, 1), "triangles_last": tris.shape[0],
+                           "ms_per_run": round(mc_ms / max(1, mc_runs), 2)},
+        "chamfer_last_100_frames": chamfer, "clocks": clock_info,
+    }
+    vol.close()
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -805,6 +951,8 @@ def main():
         return run_batch(args)
     if args.workload == "denoiser":
         return run_denoiser(args)
+    if args.workload == "streaming":
+        return run_streaming(args)
     return run_gb300(args)
 
 
