@@ -701,6 +701,12 @@ def batch_leg(args, torch, emit):
             quality.append(metrics.chamfer(backend.extract_mesh_cuda(vols[k]), sc, pts)["chamfer_mm"])
     ms_seq = timed(sequential_pass)
     batch.close()
+    # the same step as one persistent cooperative launch (phases separated by grid-wide barriers)
+    batch = backend.VolumeBatch(vols, use_graph="persistent")
+    batched_pass()  # untimed: buffer sizing
+    torch.cuda.synchronize()
+    ms_persist = timed(batched_pass)
+    batch.close()
     for v in vols:
         v.close()
     res = {(sc.intrinsics.width, sc.intrinsics.height) for sc in scs}
@@ -715,6 +721,9 @@ def batch_leg(args, torch, emit):
                    "pixels": total_px, "pool_gb": round(pool_gb, 2)},
         "batched": {"integrated_mpix_per_s": round(total_px / (ms_batch / 1000.0) / 1e6, 3), "ms": round(ms_batch, 3),
                     "launch": "3 work-queue kernels per step in one CUDA graph launch"},
+        "batched_persistent": {"integrated_mpix_per_s": round(total_px / (ms_persist / 1000.0) / 1e6, 3),
+                               "ms": round(ms_persist, 3),
+                               "launch": "one persistent cooperative launch per step (grid-wide barriers)"},
         "per_scene_launches": {"integrated_mpix_per_s": round(total_px / (ms_seq / 1000.0) / 1e6, 3),
                                "ms": round(ms_seq, 3), "launch": "4 kernels per scene per step"},
         "speedup_vs_per_scene_launches": round(ms_seq / ms_batch, 3),

@@ -315,8 +315,11 @@ vh_status vh_expf_check(uint32_t first_bits, uint64_t count, uint64_t* mismatche
  * Many independent volumes fused together: each vh_batch_integrate call is one step in which every active
  * scene integrates one depth frame.  The step runs as three work-queue kernels over all scenes' work (filter
  * tiles; allocation and normal-map tiles; chunks of visible voxels), so small and large scenes share the GPU
- * without per-scene launches; with use_graph the step (descriptor upload, queue reset, three kernels) is one
- * CUDA graph launch.  Volumes: same device, vh_algorithm.normal_mode 1 (the per-pixel normal map) and the same
+ * without per-scene launches.  use_graph 0: the step's kernels are launched one after another; 1: the step
+ * (descriptor upload, queue reset, three kernels) is one CUDA graph launch; 2: the step is one persistent
+ * cooperative launch whose phases are separated by grid-wide barriers (waits bounded to about a second; a wait
+ * that gives up sets VH_ERR_TIMEOUT on the step's volumes).  Volumes: same device, vh_algorithm.normal_mode 1
+ * (the per-pixel normal map) and the same
  * fast_math setting; at most 256 per batch; a volume keeps its own counters and statistics
  * (vh_frame_stats_get, vh_synchronize).  Results equal integrating each scene alone with the same settings. */
 typedef struct vh_batch vh_batch;

@@ -1,5 +1,6 @@
 """GPU tests of the multi-scene batch (vh_batch_*): many volumes of different resolutions, voxel sizes, storage
-formats and frame counts fused in shared work-queue kernels, with and without CUDA-graph capture.
+formats and frame counts fused in shared work-queue kernels: launched one by one, captured in a CUDA graph, and as
+one persistent cooperative launch per step.
 
 In the exact compile (fast_math 0) every scene's volume is bit-identical to fusing that scene alone with the
 same settings; the fast-math batch with and without the graph are bit-identical to each other, and its
@@ -72,7 +73,7 @@ def _run_alone(backend, scs, fast):
     return vols
 
 
-@pytest.mark.parametrize("use_graph", [False, True])
+@pytest.mark.parametrize("use_graph", [False, True, "persistent"])
 def test_batch_equals_scenes_alone_exact(backend, oracle_lib, use_graph):
     O = oracle_lib
     scs = _scenes()
@@ -119,7 +120,7 @@ def test_batch_fast_math_graph_and_stream_agree(backend, oracle_lib):
         v.close()
 
 
-@pytest.mark.parametrize("use_graph", [False, True])
+@pytest.mark.parametrize("use_graph", [False, True, "persistent"])
 def test_batch_scene_with_full_pool_does_not_affect_the_others(backend, oracle_lib, use_graph):
     """One scene of a batch runs out of pool blocks: its error surfaces on its own volume (vh_synchronize
     reports VH_ERR_POOL_FULL, the blocks that fit are kept and consistently counted), its visible entries

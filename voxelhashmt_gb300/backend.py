@@ -346,14 +346,16 @@ def visible_block_keys(volume: VoxelHashTSDF, stream=None):
 
 class VolumeBatch:
     """Many volumes fused together (vh_batch_*): each integrate() is one step in which every active scene
-    integrates one device-resident depth frame, as three work-queue kernels over all scenes (one CUDA graph
-    launch with use_graph).  Volumes need algorithm.normal_mode 1 and the same fast_math setting."""
+    integrates one device-resident depth frame, as three work-queue kernels over all scenes: launched one by one
+    (use_graph False), as one CUDA graph launch (True), or as one persistent cooperative launch
+    (use_graph="persistent").  Volumes need algorithm.normal_mode 1 and the same fast_math setting."""
 
     def __init__(self, volumes, use_graph=True):
         self.volumes = list(volumes)
         handles = (C.c_void_p * len(self.volumes))(*[v.handle.value for v in self.volumes])
         h = C.c_void_p()
-        _capi.check(_capi.lib().vh_batch_create(handles, len(self.volumes), 1 if use_graph else 0, C.byref(h)))
+        mode = 2 if use_graph == "persistent" else (1 if use_graph else 0)
+        _capi.check(_capi.lib().vh_batch_create(handles, len(self.volumes), mode, C.byref(h)))
         self.handle = h
 
     def close(self):

@@ -1253,9 +1253,10 @@ struct vh_batch {
   int fast = 0;
   bool band = false;  // every volume allocates by the truncation-band rule (smaller tile sets)
   bool use_graph = false;
+  bool persistent = false;          // the step as one cooperative launch (use_graph 2)
   size_t bytes = 0;                 // header + descriptors
   unsigned char* d_buf = nullptr;   // [BatchHeader][SceneDesc x n]
-  uint32_t* d_queue = nullptr;      // 3 work-queue counters
+  uint32_t* d_queue = nullptr;      // 3 work-queue counters, then (at 4) the persistent step's 2 barrier words
   unsigned char* h_stage[2] = {nullptr, nullptr};  // pinned, alternate steps
   cudaEvent_t done[2] = {nullptr, nullptr};         // step that last used h_stage[k] has finished
   cudaGraphExec_t exec[2] = {nullptr, nullptr};
@@ -1273,6 +1274,10 @@ static cudaError_t batch_launch(vh_batch* b, int slot, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   const auto* hdr = reinterpret_cast<const vh::BatchHeader*>(b->d_buf);
   const auto* desc = reinterpret_cast<const vh::SceneDesc*>(b->d_buf + sizeof(vh::BatchHeader));
+  if (b->persistent) {
+    return b->fast ? vh::fast::launch_batch_persistent(desc, hdr, b->d_queue, b->d_queue + 4, b->band, s)
+                   : vh::exact::launch_batch_persistent(desc, hdr, b->d_queue, b->d_queue + 4, b->band, s);
+  }
   return b->fast ? vh::fast::launch_batch(desc, hdr, b->d_queue, b->band, s)
                  : vh::exact::launch_batch(desc, hdr, b->d_queue, b->band, s);
 }
@@ -1293,7 +1298,9 @@ void vh_batch_destroy(vh_batch* b) {
 }
 
 vh_status vh_batch_create(vh_volume* const* volumes, int32_t count, int32_t use_graph, vh_batch** out) {
-  if (!volumes || !out || count <= 0 || count > vh::kMaxBatchScenes) return VH_ERR_INVALID_ARGUMENT;
+  if (!volumes || !out || count <= 0 || count > vh::kMaxBatchScenes || use_graph < 0 || use_graph > 2) {
+    return VH_ERR_INVALID_ARGUMENT;
+  }
   *out = nullptr;
   for (int i = 0; i < count; ++i) {
     const vh_volume* v = volumes[i];
@@ -1309,11 +1316,13 @@ vh_status vh_batch_create(vh_volume* const* volumes, int32_t count, int32_t use_
   b->fast = volumes[0]->algo.fast_math;
   b->band = true;
   for (int i = 0; i < count; ++i) b->band = b->band && volumes[i]->algo.allocation_mode == 1;
-  b->use_graph = use_graph != 0;
+  b->use_graph = use_graph == 1;
+  b->persistent = use_graph == 2;
   b->bytes = sizeof(vh::BatchHeader) + static_cast<size_t>(count) * sizeof(vh::SceneDesc);
   DeviceGuard guard(b->device);
   cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&b->d_buf), b->bytes);
-  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_queue), 4 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_queue), 8 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(b->d_queue, 0, 8 * sizeof(uint32_t));
   for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
     e = cudaMallocHost(reinterpret_cast<void**>(&b->h_stage[k]), b->bytes);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done[k], cudaEventDisableTiming);

@@ -1014,18 +1014,18 @@ __global__ void batch_begin_kernel(const SceneDesc* __restrict__ descs, const Ba
 
 // 1. filter + allocation tiles of all scenes (filter_alloc_kernel per tile)
 template <bool kBand>
-__global__ void __launch_bounds__(filt::kTX * filt::kTY) batch_filter_alloc_kernel(const SceneDesc* __restrict__ descs,
-                                                                                   const BatchHeader* __restrict__ hdr,
-                                                                                   uint32_t* __restrict__ queue) {
+union FilterAllocSmem {
+  filt::Smem f;
+  alloc::TileSets<kBand> a;
+};
+
+template <bool kBand>
+__device__ __forceinline__ void batch_filter_alloc_body(const SceneDesc* __restrict__ descs,
+                                                        const BatchHeader* __restrict__ hdr, uint32_t* __restrict__ queue,
+                                                        FilterAllocSmem<kBand>& S, SceneDesc& D, uint32_t& s_item,
+                                                        int& s_scene) {
   constexpr int kT = filt::kTX * filt::kTY;
   static_assert(filt::kTX == alloc::kTX && filt::kTY == alloc::kTY, "one tile for both passes");
-  __shared__ union Shared {
-    filt::Smem f;
-    alloc::TileSets<kBand> a;
-  } S;
-  __shared__ SceneDesc D;
-  __shared__ uint32_t s_item;
-  __shared__ int s_scene;
   const int tid = threadIdx.x;
   const int nsc = static_cast<int>(hdr->nscenes);
   const uint32_t total = hdr->filter_total;
@@ -1059,16 +1059,23 @@ __global__ void __launch_bounds__(filt::kTX * filt::kTY) batch_filter_alloc_kern
   }
 }
 
-// 2. normal-map tiles of all scenes; the tiles of a scene also write its visible list's {key, pool index}
-// entries (the list is final after kernel 1), tile L of M taking entries L * 256 + tid + j * M * 256
-__global__ void __launch_bounds__(kMapTX * kMapTY) batch_map_kernel(const SceneDesc* __restrict__ descs,
-                                                                    const BatchHeader* __restrict__ hdr,
-                                                                    uint32_t* __restrict__ queue) {
-  constexpr int kT = kMapTX * kMapTY;
-  __shared__ MapSmem M;
+template <bool kBand>
+__global__ void __launch_bounds__(filt::kTX * filt::kTY) batch_filter_alloc_kernel(const SceneDesc* __restrict__ descs,
+                                                                                   const BatchHeader* __restrict__ hdr,
+                                                                                   uint32_t* __restrict__ queue) {
+  __shared__ FilterAllocSmem<kBand> S;
   __shared__ SceneDesc D;
   __shared__ uint32_t s_item;
   __shared__ int s_scene;
+  batch_filter_alloc_body<kBand>(descs, hdr, queue, S, D, s_item, s_scene);
+}
+
+// 2. normal-map tiles of all scenes; the tiles of a scene also write its visible list's {key, pool index}
+// entries (the list is final after kernel 1), tile L of M taking entries L * 256 + tid + j * M * 256
+__device__ __forceinline__ void batch_map_body(const SceneDesc* __restrict__ descs, const BatchHeader* __restrict__ hdr,
+                                               uint32_t* __restrict__ queue, MapSmem& M, SceneDesc& D, uint32_t& s_item,
+                                               int& s_scene) {
+  constexpr int kT = kMapTX * kMapTY;
   const int tid = threadIdx.x;
   const int nsc = static_cast<int>(hdr->nscenes);
   const uint32_t total = hdr->stage2_total;
@@ -1106,21 +1113,36 @@ __global__ void __launch_bounds__(kMapTX * kMapTY) batch_map_kernel(const SceneD
   }
 }
 
+__global__ void __launch_bounds__(kMapTX * kMapTY) batch_map_kernel(const SceneDesc* __restrict__ descs,
+                                                                    const BatchHeader* __restrict__ hdr,
+                                                                    uint32_t* __restrict__ queue) {
+  __shared__ MapSmem M;
+  __shared__ SceneDesc D;
+  __shared__ uint32_t s_item;
+  __shared__ int s_scene;
+  batch_map_body(descs, hdr, queue, M, D, s_item, s_scene);
+}
+
 // Survivors carry over between the chunks of a scene as in fused_update_kernel; when the CTA's next chunk
 // belongs to another scene, it first updates the scene's remaining survivors and flushes its statistics.
 // kUT threads per CTA (the chunk of voxel slots), at least kUMinB resident CTAs per SM.  128 x 12 (40
 // registers, a small spill) measured fastest, as the single-volume autotuner also finds for its kernel:
 // 64-scene batch 3,614 Mpix/s, against 3,485 for 256 x 6 and 3,221 for 256 x 4 (64 registers).
-template <int kUT, int kUMinB>
-__global__ void __launch_bounds__(kUT, kUMinB) batch_update_kernel(const SceneDesc* __restrict__ descs,
-                                                                const BatchHeader* __restrict__ hdr,
-                                                                uint32_t* __restrict__ queue) {
-  __shared__ MapQueue<kUT> Q;
-  __shared__ SceneDesc D;
-  __shared__ uint32_t s_first[kMaxBatchScenes + 1];
-  __shared__ uint32_t s_item;
-  __shared__ int s_scene;
-  __shared__ CtaStats s_stats;
+template <int kUT>
+struct BatchUpdateSmem {
+  MapQueue<kUT> Q;
+  uint32_t s_first[kMaxBatchScenes + 1];
+  CtaStats s_stats;
+};
+
+template <int kUT>
+__device__ __forceinline__ void batch_update_body(const SceneDesc* __restrict__ descs,
+                                                  const BatchHeader* __restrict__ hdr, uint32_t* __restrict__ queue,
+                                                  BatchUpdateSmem<kUT>& U, SceneDesc& D, uint32_t& s_item,
+                                                  int& s_scene) {
+  MapQueue<kUT>& Q = U.Q;
+  uint32_t* s_first = U.s_first;
+  CtaStats& s_stats = U.s_stats;
   const int tid = threadIdx.x, lane = tid & 31;
   const int nsc = static_cast<int>(hdr->nscenes);
   constexpr uint32_t kChunksPerBlock = kBlockVoxels / kUT;
@@ -1221,6 +1243,103 @@ __global__ void __launch_bounds__(kUT, kUMinB) batch_update_kernel(const SceneDe
       cur = -1;
     }
   }
+}
+
+
+template <int kUT, int kUMinB>
+__global__ void __launch_bounds__(kUT, kUMinB) batch_update_kernel(const SceneDesc* __restrict__ descs,
+                                                                const BatchHeader* __restrict__ hdr,
+                                                                uint32_t* __restrict__ queue) {
+  __shared__ BatchUpdateSmem<kUT> U;
+  __shared__ SceneDesc D;
+  __shared__ uint32_t s_item;
+  __shared__ int s_scene;
+  batch_update_body<kUT>(descs, hdr, queue, U, D, s_item, s_scene);
+}
+
+// ---- the batch step as one persistent launch ----
+//
+// batch_persistent_kernel runs the four phases of a step (start, filter + allocation, normal map, layer update)
+// in one cooperative launch: every CTA is resident, and a grid-wide barrier separates the phases (each phase
+// reads what the previous one wrote on other SMs).  Data written in a phase is first read in a later phase, so
+// no SM holds a stale copy of it when the barrier's fences have run.  The waits are bounded: after about a
+// second of %globaltimer time a CTA stops waiting, marks every scene of the step with the timeout bit (which
+// vh_synchronize reports as VH_ERR_TIMEOUT) and returns.
+constexpr int kPersistThreads = 256, kPersistMinB = 4;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bar[0]: arrivals, bar[1]: generation.  Returns false when the wait gave up.
+__device__ __forceinline__ bool grid_barrier(uint32_t* bar, uint32_t nctas, int& s_ok) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile uint32_t* gen = bar + 1;
+    const uint32_t g = *gen;
+    __threadfence();
+    bool ok = true;
+    if (atomicAdd(&bar[0], 1U) == nctas - 1U) {
+      bar[0] = 0U;  // reset before the release, so the next barrier counts from zero
+      __threadfence();
+      atomicAdd(&bar[1], 1U);
+    } else {
+      const unsigned long long t0 = global_ns();
+      uint32_t polls = 0;
+      while (*gen == g) {
+        if ((++polls & 63U) == 0U && global_ns() - t0 > 1000000000ULL) {
+          ok = false;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    s_ok = ok ? 1 : 0;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__device__ __forceinline__ void mark_step_timeout(const SceneDesc* __restrict__ descs, const BatchHeader* __restrict__ hdr) {
+  if (threadIdx.x != 0) return;
+  for (uint32_t k = 0; k < hdr->nscenes; ++k) {
+    if (descs[k].active) atomicOr(&descs[k].V.counters->error, kErrTimeout);
+  }
+}
+
+template <bool kBand>
+__global__ void __launch_bounds__(kPersistThreads, kPersistMinB)
+    batch_persistent_kernel(const SceneDesc* __restrict__ descs, const BatchHeader* __restrict__ hdr,
+                            uint32_t* __restrict__ queue, uint32_t* __restrict__ bar) {
+  static_assert(kPersistThreads == filt::kTX * filt::kTY && kPersistThreads == kMapTX * kMapTY,
+                "one CTA shape for every phase");
+  __shared__ union {
+    FilterAllocSmem<kBand> fa;
+    MapSmem m;
+    BatchUpdateSmem<kPersistThreads> u;
+  } S;
+  __shared__ SceneDesc D;
+  __shared__ uint32_t s_item;
+  __shared__ int s_scene;
+  __shared__ int s_ok;
+  const uint32_t nctas = gridDim.x;
+  // 0. the step's start: work-queue counters cleared, every active scene's frame started
+  if (blockIdx.x == 0) {
+    if (threadIdx.x < 3) queue[threadIdx.x] = 0U;
+    const int nsc = static_cast<int>(hdr->nscenes);
+    for (int k = threadIdx.x; k < nsc; k += blockDim.x) {
+      if (descs[k].active) filt::begin_frame(descs[k].V.counters);
+    }
+  }
+  if (!grid_barrier(bar, nctas, s_ok)) return mark_step_timeout(descs, hdr);
+  batch_filter_alloc_body<kBand>(descs, hdr, queue, S.fa, D, s_item, s_scene);
+  if (!grid_barrier(bar, nctas, s_ok)) return mark_step_timeout(descs, hdr);
+  batch_map_body(descs, hdr, queue, S.m, D, s_item, s_scene);
+  if (!grid_barrier(bar, nctas, s_ok)) return mark_step_timeout(descs, hdr);
+  batch_update_body<kPersistThreads>(descs, hdr, queue, S.u, D, s_item, s_scene);
 }
 
 // the depth filter of one frame in this compile (the fast-math form's filter in the fast compile)
@@ -1387,6 +1506,26 @@ cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_
   batch_map_kernel<<<grids[2], kMapTX * kMapTY, 0, s>>>(descs, hdr, queue);
   batch_update_kernel<kBatchUT, kBatchUMinB><<<grids[3], kBatchUT, 0, s>>>(descs, hdr, queue);
   return cudaGetLastError();
+}
+
+// The step as one cooperative launch of batch_persistent_kernel (queue: 3 work-queue words; bar: 2 barrier words,
+// zero before the first launch and left at zero arrivals by every completed launch).
+cudaError_t launch_batch_persistent(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, uint32_t* bar,
+                                    bool band, cudaStream_t s) {
+  static int grids[2] = {0, 0};
+  const void* fn = band ? reinterpret_cast<const void*>(batch_persistent_kernel<true>)
+                        : reinterpret_cast<const void*>(batch_persistent_kernel<false>);
+  int& grid = grids[band ? 1 : 0];
+  if (grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPersistThreads, 0);
+    if (sms <= 0 || per_sm <= 0) return cudaErrorLaunchOutOfResources;
+    grid = sms * per_sm;
+  }
+  void* args[] = {const_cast<SceneDesc**>(&descs), const_cast<BatchHeader**>(&hdr), &queue, &bar};
+  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kPersistThreads), args, 0, s);
 }
 
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,

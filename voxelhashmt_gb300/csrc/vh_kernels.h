@@ -27,6 +27,9 @@ cudaError_t launch_filter_alloc(const float* in, float* out, const Volume& V, co
 // one step of a multi-scene batch: filter + allocation, normal map, update, each a work-queue kernel over all
 // scenes (queue: 3 counters, cleared here); band: every scene uses the truncation-band allocation rule
 cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, bool band, cudaStream_t s);
+// the same step as one cooperative launch of a persistent kernel (bar: two zeroed words kept by the batch)
+cudaError_t launch_batch_persistent(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, uint32_t* bar,
+                                    bool band, cudaStream_t s);
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
@@ -46,6 +49,9 @@ cudaError_t launch_filter_alloc(const float* in, float* out, const Volume& V, co
 // one step of a multi-scene batch: filter + allocation, normal map, update, each a work-queue kernel over all
 // scenes (queue: 3 counters, cleared here); band: every scene uses the truncation-band allocation rule
 cudaError_t launch_batch(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, bool band, cudaStream_t s);
+// the same step as one cooperative launch of a persistent kernel (bar: two zeroed words kept by the batch)
+cudaError_t launch_batch_persistent(const SceneDesc* descs, const BatchHeader* hdr, uint32_t* queue, uint32_t* bar,
+                                    bool band, cudaStream_t s);
 cudaError_t launch_integrate(const float* depth, const Volume& V, const Params& p, int grid, float4* nmap,
                              cudaStream_t s);
 cudaError_t launch_integrate_prepare(const float* depth, const Volume& V, const Params& p, float4* nmap,
