@@ -24,6 +24,7 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
+# the reference tree (read-only): VH_REFERENCE_ROOT, else the build container's mount point
 REFERENCE = os.environ.get("VH_REFERENCE_ROOT", "/root/reference")
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 ORACLE64_SO = os.path.join(HERE, "liboracle64.so")
@@ -121,6 +122,7 @@ def _compile_unit(rel, driver, emulated, obj):
 
 def build_ref(force=False):
     if not reference_available():
+        sys.stderr.write("reference not present at %s (set VH_REFERENCE_ROOT); oracle/_ref not built\n" % REFERENCE)
         return None
     os.makedirs(REF_DIR, exist_ok=True)
     inputs = [os.path.join(REFERENCE, u[0]) for u in _UNITS]

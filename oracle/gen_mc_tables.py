@@ -19,7 +19,9 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "..", "voxelhashmt_gb300", "csrc", "vh_mc_tables.h")
-DEFAULT_REF = "/root/reference/include/tsdfmc/marching_cubes_tables.h"
+# the reference tree: VH_REFERENCE_ROOT, else the build container's mount point (as oracle/build.py)
+DEFAULT_REF = os.path.join(os.environ.get("VH_REFERENCE_ROOT", "/root/reference"), "include", "tsdfmc",
+                           "marching_cubes_tables.h")
 
 EDGE_CORNERS = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4),
                 (0, 4), (1, 5), (2, 6), (3, 7)]
@@ -49,6 +51,8 @@ def parse_reference(path):
 
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF
+    if not os.path.exists(ref):
+        sys.exit("reference not present: %s (set VH_REFERENCE_ROOT or pass the header's path)" % ref)
     edge = computed_edge_table()
     ref_edge, tri = parse_reference(ref)
     assert edge == ref_edge, "computed edge table differs from the reference table"
