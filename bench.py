@@ -559,10 +559,21 @@ def run_gb300(args):
         except Exception as e:  # the baseline is reported, never the target
             cpu = {"value": None, "unit": "Mpix/s", "cores": 0, "kind": "port", "sample": "failed: %s" % e}
 
+    def mc_roofline(r, name):
+        # the survey's algorithmic bytes of one extraction: per block one read of its 512 voxels' bins in all 6
+        # directions, the one-voxel halo (217 voxels x 6 directions), and 36 B per emitted triangle
+        bin_b = BIN_BYTES[FORMS[name][1]]
+        nbytes = r["nblocks"] * (512 + 217) * 6 * bin_b + 36 * r["triangles"]
+        ach = nbytes / (r["mc_ms"] / 1000.0) / 1e9
+        return {"kernels": "mc_count_kernel + scan_kernel + mc_emit_kernel (one full extraction)", "bound": "hbm",
+                "achieved": round(ach, 2), "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 5),
+                "algorithmic_bytes": int(nbytes), "ms": round(r["mc_ms"], 3)}
+
     def summary(r, name):
         return {"form": FORM_NOTE[name], "integrated_mpix_per_s": round(r["value"], 3),
                 "ms_per_step": round(r["max_ms"] / args.steps, 4), "mc_blocks_per_s": round(r["mc_blocks_per_s"], 1),
                 "mc_ms": round(r["mc_ms"], 3), "mc_triangles": r["triangles"], "blocks": r["nblocks"],
+                "mc_roofline": mc_roofline(r, name),
                 "observed_voxels": r["observed"], "e2e_mpix_per_s": round(r["e2e_value"], 3),
                 "stage_ms_per_frame": {k: round(v / max(1, r["nprof"]), 4) for k, v in r["stage_ms"].items()},
                 "visible_blocks_last_frame": r["fstats"]["visible_blocks"],
@@ -579,6 +590,7 @@ def run_gb300(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": dict(workload_config(sc, args.steps, args.warmup), form=FORM_NOTE[args.form]),
             "mc_blocks_per_s": round(head["mc_blocks_per_s"], 1),
+            "mc_roofline": mc_roofline(head, args.form),
             "e2e": {"value": round(head["e2e_value"], 3), "unit": "Mpix/s", "h2d_bytes_per_step": px * 4,
                     "d2h_bytes_per_step": 64,
                     "note": "wall clock over back-to-back frames through TsdfIntegrationBackend.integrate from "
