@@ -282,10 +282,11 @@ def surface_points(sc, torch, capi, stride=4, every=20, max_points=200_000):
     return metrics.observed_surface_points(sc, sel, depth_maps=maps, stride=stride, max_points=max_points)
 
 
-def tune_launch_shape(torch, backend, capi, sc, frames, form, max_blocks):
+def tune_launch_shape(torch, backend, capi, sc, frames, form, max_blocks, cycle=None):
     """The layer-update launch shape chosen by the volume's own autotuner (vh_algorithm.autotune), before any
-    timed frame: a scratch volume integrates the workload's frames (cycled when there are fewer than the tuner
-    needs) until the tuner has timed every shape and kept the fastest.  None for forms without a tuned kernel."""
+    timed frame: a scratch volume integrates the workload's frames (cycled, the volume reset at each cycle,
+    when there are fewer than the tuner needs, or every `cycle` frames) until the tuner has timed every shape
+    and kept the fastest.  None for forms without a tuned kernel."""
     algo_kw, layer_format = form
     if algo_kw.get("normal_mode", 0) != 1:
         return None
@@ -295,7 +296,7 @@ def tune_launch_shape(torch, backend, capi, sc, frames, form, max_blocks):
     bk = backend.TsdfIntegrationBackend("gpu")
     stream = torch.cuda.current_stream()
     K = sc.intrinsics
-    n = frames.shape[0]
+    n = frames.shape[0] if cycle is None else min(cycle, frames.shape[0])
     tuned, used = None, 0
     for i in range(200):
         f = i % n
@@ -859,7 +860,7 @@ def run_streaming(args):
     # the layer-update launch shape, tuned on the first frames before the timed walk
     nf = min(step_frames, len(sc.poses))
     render(0, nf)
-    launch = tune_launch_shape(torch, backend, _capi, sc, buf[:nf], FORMS["chosen"], 200000)
+    launch = tune_launch_shape(torch, backend, _capi, sc, buf[:nf], FORMS["chosen"], max_blocks, cycle=8)
     algo = dict(algo_kw)
     if launch is not None:
         algo.update(autotune=0, launch_variant=launch["variant"])
