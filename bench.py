@@ -69,8 +69,10 @@ def parse():
                     help="room: the room-scale workload (the headline); batch: N object scans fused as one batch; "
                          "denoiser: train the learned filter and compare Chamfer with the bilateral filter")
     ap.add_argument("--scenes", type=int, default=64, help="scenes of the batch workload")
-    ap.add_argument("--train-rooms", type=int, default=4, help="denoiser workload: training rooms")
-    ap.add_argument("--train-frames", type=int, default=250, help="denoiser workload: frames per training room")
+    ap.add_argument("--train-rooms", type=int, default=20, help="denoiser workload: training rooms")
+    ap.add_argument("--train-frames", type=int, default=1000, help="denoiser workload: frames per training room")
+    ap.add_argument("--train-crop", type=int, default=0,
+                    help="denoiser workload: train on random crops of this size (0: whole 640x480 frames)")
     ap.add_argument("--train-steps", type=int, default=0, help="denoiser workload: Adam steps (0: two epochs)")
     ap.add_argument("--eval-frames", type=int, default=300, help="denoiser workload: frames of the held-out room")
     return ap.parse_args()
@@ -762,7 +764,7 @@ def run_denoiser(args):
     for target in ("raycast", "clean"):
         t0 = time.perf_counter()
         raws, tgts = denoiser.make_training_pairs(seeds, frames_per_scene=args.train_frames, crops_per_frame=20,
-                                                  target=target)
+                                                  crop=args.train_crop, target=target)
         torch.cuda.synchronize()
         t_data = time.perf_counter() - t0
         net = denoiser.DepthDenoiser(seed=args.seed)
@@ -809,9 +811,10 @@ def run_denoiser(args):
         vol.close()
     line = {"metric": "chamfer_mm", "value": results["chosen_learned"]["chamfer_mm"], "unit": "mm",
             "higher_is_better": False, "n_gpus": 1, "data": "synthetic",
-            "config": {"workload": "room 640x480 (held-out seed 2001, %d frames); net trained on crops 128x128 of "
+            "config": {"workload": "room 640x480 (held-out seed 2001, %d frames); net trained on %s of "
                                    "%d new-seed rooms x %d frames, Adam lr 1e-3, batch 16" % (
-                                       len(sc.poses), len(seeds), args.train_frames),
+                                       len(sc.poses), ("%dx%d crops" % (args.train_crop, args.train_crop))
+                                       if args.train_crop else "whole 640x480 frames", len(seeds), args.train_frames),
                        "net": "3x3 conv 4-32-32-32-1, ReLU, residual; BF16 tensor-core hidden layers",
                        "targets": "raycast: depth ray-cast from the plain FP32 volume fused from all frames of the "
                                   "training room (the configuration's target); clean: noise-free analytic depth"},

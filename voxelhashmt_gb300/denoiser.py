@@ -120,11 +120,12 @@ class DepthDenoiser:
 
 def make_training_pairs(seeds, frames_per_scene=120, crops_per_frame=16, crop=128, width=640, height=480,
                         fuse_frames=None, rng_seed=0, target="raycast"):
-    """Random crops (raw, target) from rooms (scenes.room_scene) of the given seeds: raw = the noisy
-    rendered frame; target = the depth ray-cast at the frame's pose from the plain FP32 volume fused from
-    `fuse_frames` frames of the same walk (all of them by default), or with target="clean" the noise-free
-    analytic depth of the frame.  Returns two (N, crop, crop) CUDA tensors; crops keep windows where at
-    least half the pixels are valid in both."""
+    """Pairs (raw, target) from rooms (scenes.room_scene) of the given seeds: raw = the noisy rendered frame;
+    target = the depth ray-cast at the frame's pose from the plain FP32 volume fused from `fuse_frames` frames
+    of the same walk (all of them by default), or with target="clean" the noise-free analytic depth of the
+    frame.  crop > 0: random crop x crop windows, crops_per_frame per frame; crop = 0 (or None): whole frames.
+    Returns two (N, h, w) CUDA tensors; windows (and frames) are kept where at least half the pixels are valid
+    in both."""
     import torch
     from . import backend, scenes
     rng = np.random.default_rng(rng_seed)
@@ -156,6 +157,11 @@ def make_training_pairs(seeds, frames_per_scene=120, crops_per_frame=16, crop=12
                 tgt = backend.raycast_depth(vol, sc.intrinsics, sc.poses[f], 0.1, sc.max_depth, 0.5,
                                             device_out="cuda")
             raw = frames[f]
+            if not crop:
+                if float(((raw > 0) & (tgt > 0)).float().mean()) >= 0.5:
+                    raws.append(raw.clone())
+                    tgts.append(tgt.clone())
+                continue
             taken = 0
             for _ in range(crops_per_frame * 4):  # bounded retries for windows with too little valid depth
                 if taken >= crops_per_frame:
