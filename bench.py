@@ -65,6 +65,7 @@ def parse():
                     help="skip the legs beside the room workload (the small orbit configuration, the 64-scene batch)")
     ap.add_argument("--stream-frames", type=int, default=6000, help="streaming workload: frames of the walk")
     ap.add_argument("--stream-max-blocks", type=int, default=2_000_000, help="streaming workload: pool blocks")
+    ap.add_argument("--stream-log", action="store_true", help="streaming workload: progress lines on stderr")
     ap.add_argument("--workload", default="room", choices=["room", "batch", "denoiser", "streaming"],
                     help="room: the room-scale workload (the headline); batch: N object scans fused as one batch; "
                          "denoiser: train the learned filter and compare Chamfer with the bilateral filter")
@@ -827,9 +828,9 @@ def run_denoiser(args):
 def run_streaming(args):
     """Large streaming configuration: the 20x20x4 m multi-room walk (scenes.multi_room_scene: 400 primitives,
     1280x720, 3 mm voxels, 1.2 cm truncation, 2^22 buckets) fused 30 frames per step into a pool of at most
-    --stream-max-blocks FP16 blocks (opt-in form).  Whenever the pool is over 90 % full after a step, the
-    oldest blocks (longest since their last layer update) are evicted down to 80 % and streamed out to pinned
-    host memory as the pool's own block images (vh_evict_blocks); every 100 frames, marching cubes runs over the
+    --stream-max-blocks FP16 blocks (opt-in form).  The block count is read every 10 frames; whenever the next 10
+    frames could overfill the pool, the oldest blocks (longest since their last layer update) are evicted and
+    streamed out to host memory as the pool's own block images (vh_evict_blocks); every 100 frames, marching cubes runs over the
     blocks the layer update touched in the last 100 frames (vh_extract_mesh_recent).  Frames are rendered on
     the device before each step, outside the timed region.  value = pixels fused / summed CUDA-event time of
     the fusion steps; the eviction and meshing times are reported beside it, and the wall clock over
@@ -884,36 +885,49 @@ def run_streaming(args):
     clocks.start()
     wall0 = time.perf_counter()
     wall_render = 0.0
+    # the pool is checked every check_frames frames (a host read of the block count); eviction starts when the
+    # next check_frames could overfill it at twice the largest growth seen so far, and goes down to four times
+    # that growth below the pool size (at most 80 %, at least 50 % of it)
+    check_frames = 10
+    growth = 0.02 * max_blocks
+    nb = 0
     for f0 in range(0, n_frames, step_frames):
         n = min(step_frames, n_frames - f0)
         r0 = time.perf_counter()
         render(f0, n)
         torch.cuda.synchronize()
         wall_render += time.perf_counter() - r0
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for i in range(n):
-            bk.integrate(vol, backend.DepthFrame(K, buf[i].view(-1)), sc.poses[f0 + i], 1, stream=stream,
-                         synchronize=False)
-        e1.record(stream)
-        vol.synchronize(stream)
-        fuse_ms += e0.elapsed_time(e1)
-        nb = vol.block_count()
-        peak_blocks = max(peak_blocks, nb)
-        if nb > 0.9 * max_blocks:
-            t0 = time.perf_counter()
-            while nb > 0.8 * max_blocks:
-                cnt = C.c_uint64()
-                _capi.check(_capi.lib().vh_evict_blocks(vol.handle, 0xffffffff, int(max(0.8 * max_blocks, nb - chunk)),
-                                                        1, C.c_void_p(host_keys.ctypes.data),
-                                                        C.c_void_p(host_data.ctypes.data), evict_cap, 0, C.byref(cnt),
-                                                        C.c_void_p(stream.cuda_stream)), vol.handle)
-                evicted_blocks += cnt.value
-                nb = vol.block_count()
-                if cnt.value == 0:
-                    break
-            evict_ms += 1000 * (time.perf_counter() - t0)
-            evictions += 1
+        for c0 in range(0, n, check_frames):
+            c1 = min(n, c0 + check_frames)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for i in range(c0, c1):
+                bk.integrate(vol, backend.DepthFrame(K, buf[i].view(-1)), sc.poses[f0 + i], 1, stream=stream,
+                             synchronize=False)
+            e1.record(stream)
+            vol.synchronize(stream)
+            fuse_ms += e0.elapsed_time(e1)
+            nb_prev, nb = nb, vol.block_count()
+            growth = max(growth, nb - nb_prev)
+            peak_blocks = max(peak_blocks, nb)
+            if nb + 2 * growth > max_blocks:
+                target = int(max(0.5 * max_blocks, min(0.8 * max_blocks, max_blocks - 4 * growth)))
+                t0 = time.perf_counter()
+                while nb > target:
+                    cnt = C.c_uint64()
+                    _capi.check(_capi.lib().vh_evict_blocks(vol.handle, 0xffffffff, int(max(target, nb - chunk)), 1,
+                                                            C.c_void_p(host_keys.ctypes.data),
+                                                            C.c_void_p(host_data.ctypes.data), evict_cap, 0,
+                                                            C.byref(cnt), C.c_void_p(stream.cuda_stream)), vol.handle)
+                    evicted_blocks += cnt.value
+                    nb = vol.block_count()
+                    if cnt.value == 0:
+                        break
+                evict_ms += 1000 * (time.perf_counter() - t0)
+                evictions += 1
+        if args.stream_log and (f0 + n) % 600 < step_frames:
+            print("streaming: frame %d blocks %d peak %d growth/%d frames %d evicted %d" % (
+                f0 + n, nb, peak_blocks, check_frames, growth, evicted_blocks), file=sys.stderr, flush=True)
         if (f0 + n) % 100 < step_frames or f0 + n == n_frames:
             m0, m1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             ntri = C.c_size_t()
@@ -950,8 +964,8 @@ def run_streaming(args):
         "warmup": "launch shape tuned on a scratch volume", "ms_per_step": round(fuse_ms / ((n_frames + step_frames - 1) // step_frames), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "multi-room 20x20x4 m, 400 primitives, %d-frame walk at 1280x720, 30 frames per step, "
-                               "voxel 3 mm, trunc 12 mm, 2^22 buckets, pool %d FP16 blocks, evict oldest to 80 %% "
-                               "above 90 %%, incremental MC over the last 100 frames every 100 frames" % (n_frames, max_blocks),
+                               "voxel 3 mm, trunc 12 mm, 2^22 buckets, pool %d FP16 blocks, evict oldest before the "
+                               "pool can overfill, incremental MC over the last 100 frames every 100 frames" % (n_frames, max_blocks),
                    "form": FORM_NOTE["chosen"], "l2": "inputs larger than L2 (a 30-frame step)"},
         "update_launch_shape": launch,
         "sustained_mpix_per_s": round(n_frames * px / wall / 1e6, 3),
