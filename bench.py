@@ -43,11 +43,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
-# DRAM bytes (read + write) per active voxel of the layer-update kernel of each form, from the ncu captures
-# summarised in profiles/ (plain: update_kernel_room640.md, one launch over 6.55 M active voxels; opt-in form:
-# fused_update_room640.md, one launch over 3.16 M active voxels); scaled by the active voxels of a launch.
-UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL = {"plain": (539.49e6 + 267.04e6) / 6.548e6,
-                                         "chosen": (189.351e6 + 57.310e6) / 3.163e6}
+# DRAM bytes of the layer-update kernel of each form from the ncu captures summarised in profiles/, as (read
+# bytes per active voxel, written bytes per updated voxel), scaled by the active and updated voxels of a launch
+# (plain: update_kernel_room640.md, one launch over 6.55 M active voxels, read + write per active voxel;
+# opt-in form: fused_update_room640.md, one launch over 3.16 M active and 2.86 M updated voxels).
+UPDATE_TRAFFIC_BYTES = {"plain": ((539.49e6 + 267.04e6) / 6.548e6, 0.0),
+                        "chosen": (189.529e6 / 3.163e6, 58.035e6 / 2.860e6)}
 
 
 def parse():
@@ -66,6 +67,11 @@ def parse():
     ap.add_argument("--stream-frames", type=int, default=6000, help="streaming workload: frames of the walk")
     ap.add_argument("--stream-max-blocks", type=int, default=2_000_000, help="streaming workload: pool blocks")
     ap.add_argument("--stream-log", action="store_true", help="streaming workload: progress lines on stderr")
+    ap.add_argument("--stream-denoiser", default="",
+                    help="streaming workload: parameters of a trained denoiser (.npy, as --save-denoiser writes) run "
+                         "inline in place of the bilateral filter (with its per-pixel fallback to it)")
+    ap.add_argument("--save-denoiser", default="",
+                    help="denoiser workload: directory to write the trained parameters to (denoiser_<target>.npy)")
     ap.add_argument("--workload", default="room", choices=["room", "batch", "denoiser", "streaming"],
                     help="room: the room-scale workload (the headline); batch: N object scans fused as one batch; "
                          "denoiser: train the learned filter and compare Chamfer with the bilateral filter")
@@ -536,17 +542,21 @@ def run_gb300(args):
     pk = peaks()
     upd_ms = head["stage_ms"]["update"] / max(1, head["nprof"])
     bin_bytes = BIN_BYTES[FORMS[args.form][1]]
-    upd_bytes = head["upd_mean"] * 2 * bin_bytes + px * 4
+    # every active voxel (inside the truncation band of a valid depth, so with a positive observation weight)
+    # reads its bin to pick a layer; the updated ones write it back
+    upd_bytes = (head["act_mean"] + head["upd_mean"]) * bin_bytes + px * 4
     achieved = upd_bytes / (upd_ms / 1000.0) / 1e9
-    traffic_per_active = UPDATE_TRAFFIC_BYTES_PER_ACTIVE_VOXEL.get(args.form)
+    per_active, per_updated = UPDATE_TRAFFIC_BYTES[args.form]
     roofline = {"kernel": UPDATE_KERNEL[args.form], "bound": "hbm", "achieved": round(achieved, 2),
                 "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 5),
-                "traffic": int(traffic_per_active * head["act_mean"]) if traffic_per_active else None,
+                "traffic": int(per_active * head["act_mean"] + per_updated * head["upd_mean"]),
                 "peak_source": pk["source"], "algorithmic_bytes_per_launch": int(upd_bytes),
                 "ms_per_launch": round(upd_ms, 5),
-                "note": "layer-update kernel alone (CUDA events around its launch); algorithmic bytes = updated "
-                        "voxels x 2 x %d B (read + write of one 3-layer bin) + 4 B/px depth; traffic = ncu DRAM "
-                        "bytes per active voxel x active voxels" % bin_bytes}
+                "note": "layer-update kernel alone (CUDA events around its launch); algorithmic bytes = active "
+                        "voxels x %d B (the read of the voxel's 3-layer bin) + updated voxels x %d B (its write) "
+                        "+ 4 B/px depth; traffic = ncu DRAM bytes per active and per updated voxel of one captured "
+                        "launch x the active and updated voxels"
+                        % (bin_bytes, bin_bytes)}
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_budget_s > 0:
@@ -773,6 +783,9 @@ def run_denoiser(args):
         t0 = time.perf_counter()
         hist = denoiser.train(net, raws, tgts, steps=steps, batch=16, seed=args.seed)
         t_train = time.perf_counter() - t0
+        if args.save_denoiser:
+            os.makedirs(args.save_denoiser, exist_ok=True)
+            np.save(os.path.join(args.save_denoiser, "denoiser_%s.npy" % target), net.params_numpy())
         trained[target] = (net.params_numpy(), {
             "pairs": int(raws.shape[0]), "data_s": round(t_data, 2), "train_s": round(t_train, 2), "steps": steps,
             "rmse_first_mm": round(1000 * float(np.mean(hist[:10])), 3),
@@ -868,16 +881,24 @@ def run_streaming(args):
     algo = dict(algo_kw)
     if launch is not None:
         algo.update(autotune=0, launch_variant=launch["variant"])
+    learned = None
+    if args.stream_denoiser:
+        learned = np.ascontiguousarray(np.load(args.stream_denoiser), np.float32)
+        algo.update(depth_filter=1)
     vol = backend.VoxelHashTSDF(sc.voxel_size, sc.truncation, hash_buckets=sc.hash_buckets, max_blocks=max_blocks,
                                 algorithm=_capi.default_algorithm(**algo), layer_format=fmt)
+    if learned is not None:
+        _capi.check(_capi.lib().vh_set_depth_denoiser(vol.handle, learned.ctypes.data_as(C.POINTER(C.c_float))),
+                    vol.handle)
     bk = backend.TsdfIntegrationBackend("gpu")
     # evicted blocks stream out to host memory in rounds of about chunk blocks (an age bin can add one frame's
     # blocks to a round, hence the larger buffer)
     chunk = max(1, min(60000, max_blocks // 20))
     evict_cap = 4 * chunk
     bpb = 98304 if fmt == 1 else 147456
-    host_keys = np.empty((evict_cap, 3), np.int32)
-    host_data = np.empty((evict_cap, bpb), np.uint8)
+    # page-locked, so that the copies out run as DMA at the host link's rate
+    host_keys = torch.empty((evict_cap, 3), dtype=torch.int32, pin_memory=True)
+    host_data = torch.empty((evict_cap, bpb), dtype=torch.uint8, pin_memory=True)
     fuse_ms, evict_ms, mc_ms = 0.0, 0.0, 0.0
     evictions, evicted_blocks, mc_runs, mc_blocks, mc_tris, peak_blocks = 0, 0, 0, 0, 0, 0
     n_frames = len(sc.poses)
@@ -916,8 +937,8 @@ def run_streaming(args):
                 while nb > target:
                     cnt = C.c_uint64()
                     _capi.check(_capi.lib().vh_evict_blocks(vol.handle, 0xffffffff, int(max(target, nb - chunk)), 1,
-                                                            C.c_void_p(host_keys.ctypes.data),
-                                                            C.c_void_p(host_data.ctypes.data), evict_cap, 0,
+                                                            C.c_void_p(host_keys.data_ptr()),
+                                                            C.c_void_p(host_data.data_ptr()), evict_cap, 0,
                                                             C.byref(cnt), C.c_void_p(stream.cuda_stream)), vol.handle)
                     evicted_blocks += cnt.value
                     nb = vol.block_count()
@@ -966,7 +987,10 @@ def run_streaming(args):
         "config": {"workload": "multi-room 20x20x4 m, 400 primitives, %d-frame walk at 1280x720, 30 frames per step, "
                                "voxel 3 mm, trunc 12 mm, 2^22 buckets, pool %d FP16 blocks, evict oldest before the "
                                "pool can overfill, incremental MC over the last 100 frames every 100 frames" % (n_frames, max_blocks),
-                   "form": FORM_NOTE["chosen"], "l2": "inputs larger than L2 (a 30-frame step)"},
+                   "form": FORM_NOTE["chosen"], "l2": "inputs larger than L2 (a 30-frame step)",
+                   "depth_filter": ("learned denoiser %s inline, per-pixel bilateral fallback beyond the "
+                                    "discontinuity threshold" % os.path.basename(args.stream_denoiser))
+                   if args.stream_denoiser else "bilateral"},
         "update_launch_shape": launch,
         "sustained_mpix_per_s": round(n_frames * px / wall / 1e6, 3),
         "sustained_note": "wall clock over fusion + eviction + incremental meshing (frame rendering excluded)",
