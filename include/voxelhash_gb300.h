@@ -341,6 +341,12 @@ vh_status vh_nn_pack_conv32_weights(const float* w, void* packed, int32_t transp
 vh_status vh_nn_conv32(const void* in, const void* packed_w, const float* bias, const void* mask, void* out,
                        int32_t batch, int32_t width, int32_t height, int32_t mode, int32_t relu, uint32_t* error,
                        void* stream);
+/* vh_nn_wgrad32: weight and bias gradients of a 32 -> 32 3x3 convolution with zero padding on the tensor cores
+ * (tcgen05, FP32 accumulation): dw[co][ci][ky][kx] += sum_p grad[p][co] x[p + (ky - 1, kx - 1)][ci] and
+ * db[co] += sum_p grad[p][co] over the batch (x: the layer input, grad: the gradient at the layer output, NHWC
+ * BF16 with 32 channels; dw: 9,216 and db: 32 FP32, device memory, accumulated into).  *error: as vh_nn_conv32. */
+vh_status vh_nn_wgrad32(const void* x, const void* grad, float* dw, float* db, int32_t batch, int32_t width,
+                        int32_t height, uint32_t* error, void* stream);
 /* vh_nn_conv32 whose input loads start only once *gate (device memory) is nonzero.  A gate that stays zero
  * makes every wait of the kernel give up after about a second: *error gets the timeout bit (8, which the
  * volume calls report as VH_ERR_TIMEOUT), `out` is left unwritten and the CUDA context stays usable.  This is

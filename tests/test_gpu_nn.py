@@ -86,6 +86,36 @@ def test_conv32_input_gradient_matches_reference(capi):
     assert nbad == 0, (nbad, worst)
 
 
+@pytest.mark.parametrize("shape", [(1, 3, 64), (2, 17, 150), (1, 35, 331), (3, 1, 7)])
+def test_wgrad32_matches_reference(capi, shape):
+    """vh_nn_wgrad32 (the weight and bias gradients of a 32 -> 32 layer on the tensor cores) against float64 on
+    the same BF16 operands: partial strips and row blocks, a one-row image.  The products of BF16 values are exact
+    in FP32; the tolerance covers FP32 accumulation in any order: 1e-5 of the sum of the terms' magnitudes."""
+    B, H, W = shape
+    g = torch.Generator().manual_seed(B * 7919 + H * 31 + W)
+    x = torch.randn(B, H, W, 32, generator=g).to(torch.bfloat16)
+    dy = torch.randn(B, H, W, 32, generator=g).to(torch.bfloat16)
+    dw0 = torch.randn(32 * 32 * 9, generator=g).float()  # accumulated into
+    db0 = torch.randn(32, generator=g).float()
+    dw, db = dw0.clone().cuda(), db0.clone().cuda()
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    xd, gd = x.cuda().contiguous(), dy.cuda().contiguous()
+    capi.check(capi.lib().vh_nn_wgrad32(_ptr(xd), _ptr(gd), _ptr(dw), _ptr(db), B, W, H,
+                                        C.cast(C.c_void_p(err.data_ptr()), C.POINTER(C.c_uint32)), None))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0, "tensor cores did not signal completion"
+    xn, gn = x.double().permute(0, 3, 1, 2), dy.double().permute(0, 3, 1, 2)
+    ref = torch.nn.grad.conv2d_weight(xn, (32, 32, 3, 3), gn, padding=1).reshape(-1)
+    mag = torch.nn.grad.conv2d_weight(xn.abs(), (32, 32, 3, 3), gn.abs(), padding=1).reshape(-1)
+    got = dw.double().cpu() - dw0.double()
+    bad = (got - ref).abs() > 1e-5 * mag + 1e-6 * (1.0 + dw0.double().abs())
+    assert int(bad.sum()) == 0, (int(bad.sum()), float((got - ref).abs().max()))
+    bref = gn.sum(dim=(0, 2, 3))
+    bmag = gn.abs().sum(dim=(0, 2, 3))
+    bgot = db.double().cpu() - db0.double()
+    assert bool(((bgot - bref).abs() <= 1e-5 * bmag + 1e-6 * (1.0 + db0.double().abs())).all())
+
+
 def _bf(t):
     """BF16 rounding in the forward pass, identity in the backward (straight-through)."""
     return t + (t.to(torch.bfloat16).double() - t).detach()

@@ -133,6 +133,7 @@ _SIGNATURES = {
                                C.POINTER(C.c_uint32), _vp]),
     "vh_nn_conv32_gated": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                                      C.c_int32, _vp, C.POINTER(C.c_uint32), _vp]),
+    "vh_nn_wgrad32": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_uint32), _vp]),
     "vh_nn_param_count": (C.c_int32, []),
     "vh_nn_workspace_bytes": (C.c_uint64, [C.c_int32, C.c_int32, C.c_int32]),
     "vh_nn_pack": (C.c_int, [_vp, _vp, _vp]),

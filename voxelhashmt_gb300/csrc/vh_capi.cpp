@@ -1439,6 +1439,15 @@ vh_status vh_nn_conv32_gated(const void* in, const void* packed_w, const float* 
   return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
 }
 
+vh_status vh_nn_wgrad32(const void* x, const void* grad, float* dw, float* db, int32_t batch, int32_t width,
+                        int32_t height, uint32_t* error, void* stream) {
+  if (!x || !grad || !dw || !db || !error || batch <= 0 || width <= 0 || height <= 0) return VH_ERR_INVALID_ARGUMENT;
+  const cudaError_t e = vh::nn::launch_wgrad32(static_cast<const __nv_bfloat16*>(x),
+                                               static_cast<const __nv_bfloat16*>(grad), dw, db, batch, width, height,
+                                               error, as_stream(stream));
+  return e == cudaSuccess ? VH_OK : VH_ERR_CUDA;
+}
+
 int32_t vh_nn_param_count(void) { return vh::nn::param_count(); }
 
 uint64_t vh_nn_workspace_bytes(int32_t batch, int32_t width, int32_t height) {

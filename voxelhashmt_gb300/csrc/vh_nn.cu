@@ -16,8 +16,9 @@
 // applies ReLU, or, for the input gradient, multiplies by the ReLU mask of the layer's input, and stores BF16.
 //
 // The input gradient of a 32 -> 32 layer is the same convolution with the weights flipped in space and
-// transposed in channels, so the backward pass reuses the kernel.  The 4-channel input layer, the 1-channel
-// output layer, the weight gradients (reductions over pixels) and Adam run on the CUDA cores in FP32.
+// transposed in channels, so the backward pass reuses the kernel.  The weight gradient of a 32 -> 32 layer (a
+// reduction over pixels) is a second tensor-core kernel, wgrad32_tc_kernel.  The 4-channel input layer, the
+// 1-channel output layer, their weight gradients and Adam run on the CUDA cores in FP32.
 //
 // Safety: the descriptors address only staged bytes: an A operand reads at most 8,608 bytes into its 8,704-byte
 // slot (pixels dx .. dx + 127 of each plane), the B operand exactly kBBytes, followed by a margin; the layout is
@@ -538,6 +539,249 @@ cudaError_t launch_pack_w32(const float* w, __nv_bfloat16* out, int transpose_fl
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- weight gradient of a 32 -> 32 layer (tensor cores)
+//
+// dW[co][ci][ky][kx] += sum_p G[p][co] X[p + (ky - 1, kx - 1)][ci] and db[co] += sum_p G[p][co] over a batch of
+// NHWC BF16 images (X: the layer's input activations, G: the gradient at its output, zero outside the image).
+// As a GEMM per output row: M = (copy kx, input channel) = 3 x 32 rows plus a 32-row pad copy (M = 128), N = the
+// 32 output channels, K = the row's pixels, one FP32 accumulator in tensor memory per tap row ky (3 x 32
+// columns), summed over every output row the CTA takes and added to dW once at the end.
+//
+// A CTA takes items of kWgRows output rows of one kWgStrip-pixel strip.  Each input row is staged once, as three
+// copies shifted by kx - 1 pixels and a pad copy, transposed into the canonical no-swizzle K-major layout
+// [pixel group of 8 (K)][copy][channel][8 pixels]: the A operand of tap row ky of output row y is then the
+// staged input row y - 1 + ky, its M rows (copy, channel) at a uniform 128-byte stride per 8 rows, and the pad
+// copy feeds only accumulator rows that are never read.  The gradient row is staged the same way as the B
+// operand, [pixel group][output channel][8 pixels].  A thread loads a channel pair over 10 (8) pixels as 32-bit
+// words and writes the transposed 16-byte rows with byte permutes.  Rows live in rings (kWgXSlots input rows,
+// two gradient rows); thread 0 issues an output row's 12 MMAs (3 tap rows x 4 k-steps of 16 pixels) and commits
+// them to an mbarrier, and a ring slot is rewritten only after the MMAs that read it have completed, so the
+// staging of a row overlaps the MMAs of the row before.  Waits are bounded as in conv32_tc_kernel; a timeout is
+// agreed on by every thread (__syncthreads_and) before the CTA leaves its loop.
+namespace {
+
+constexpr int kWgStrip = 64;                         // pixels of an output row per item (K of a row)
+constexpr int kWgGroups = kWgStrip / 8;              // pixel groups of 8 (16 bytes of BF16)
+constexpr int kWgCopies = 4;                         // kx = 0, 1, 2 and the pad copy
+constexpr int kWgCore = kC * 16;                     // one copy of one pixel group: 32 channels x 16 bytes
+constexpr int kWgXLbo = kWgCopies * kWgCore;         // A operand: bytes between pixel groups (K)
+constexpr int kWgXRow = kWgGroups * kWgXLbo;         // one staged input row: 16,384 bytes
+constexpr int kWgGRow = kWgGroups * kWgCore;         // one staged gradient row: 4,096 bytes
+constexpr int kWgXSlots = 5;                         // an output row reads 3 input rows; one more is staged
+                                                     // while the previous row's MMAs run
+constexpr int kWgGSlots = 2;
+constexpr int kWgRows = 16;                          // output rows per item
+constexpr int kWgThreads = 128;                      // thread t stages pixel group t / 16, channel pair t % 16
+constexpr int kWgTmemCols = 128;                     // 3 accumulators x 32 columns, allocated as a power of 2
+constexpr int kWgSmem = 128 + kWgXSlots * kWgXRow + kWgGSlots * kWgGRow + 2 * 8 + 16;
+static_assert(kWgThreads == kWgGroups * (kC / 2), "one (pixel group, channel pair) per thread");
+
+__global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc_kernel(const __nv_bfloat16* __restrict__ X,
+                                                                    const __nv_bfloat16* __restrict__ G,
+                                                                    float* __restrict__ dW, float* __restrict__ db,
+                                                                    int batch, int width, int height,
+                                                                    unsigned int* __restrict__ error) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned char* smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  unsigned char* sX = smem;
+  unsigned char* sG = smem + kWgXSlots * kWgXRow;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(sG + kWgGSlots * kWgGRow);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int pg = tid >> 4, cp = tid & 15;  // staging: pixel group, channel pair
+
+  // the pad copies: any finite value would do (they reach only discarded accumulator rows); zero
+  for (int i = tid; i < kWgXSlots * kWgGroups * (kWgCore / 16); i += kWgThreads) {
+    const int row = i / (kWgGroups * (kWgCore / 16)), rest = i % (kWgGroups * (kWgCore / 16));
+    const int grp = rest / (kWgCore / 16), k = rest % (kWgCore / 16);
+    reinterpret_cast<uint4*>(sX + row * kWgXRow + grp * kWgXLbo + 3 * kWgCore)[k] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kWgTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&bars[i])));
+    asm volatile("fence.mbarrier_init.release.cluster;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t xs0 = smem_u32(sX), gs0 = smem_u32(sG), bar0 = smem_u32(&bars[0]);
+
+  const uint32_t strips = static_cast<uint32_t>((width + kWgStrip - 1) / kWgStrip);
+  const uint32_t rblocks = static_cast<uint32_t>((height + kWgRows - 1) / kWgRows);
+  const uint32_t nitems = static_cast<uint32_t>(batch) * rblocks * strips;
+
+  bool ok = true;
+  uint32_t xq = 0;      // input rows staged
+  uint32_t oq = 0;      // output rows issued (MMA groups), group g commits to bars[g & 1]
+  uint32_t waited = 0;  // groups whose completion has been waited for, in order
+  int reader[kWgXSlots];  // the last group that reads each input-row slot
+#pragma unroll
+  for (int k = 0; k < kWgXSlots; ++k) reader[k] = -1;
+  float bsum0 = 0.0f, bsum1 = 0.0f;
+
+  // waits, in order, for the groups up to g: a group's barrier phase is waited for before the group two later
+  // commits to the same barrier, so a parity never refers to a phase two completions old
+  auto wait_through = [&](int g) {
+    while (ok && static_cast<int>(waited) <= g) {
+      if (!mbar_wait(bar0 + 8u * (waited & 1u), (waited >> 1) & 1u)) {
+        ok = false;
+        break;
+      }
+      ++waited;
+    }
+  };
+
+  for (uint32_t it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+    const uint32_t rest = it / strips;
+    const int xs = static_cast<int>(it - rest * strips) * kWgStrip;
+    const uint32_t img = rest / rblocks;
+    const int y0 = static_cast<int>(rest - img * rblocks) * kWgRows;
+    const int rows = min(kWgRows, height - y0);
+    const uint32_t xa = xq;  // ring index of input row y0 - 1
+    const size_t img_base = static_cast<size_t>(img) * height;
+    for (int i = -2; i < rows; ++i) {
+      // stage input row y0 + i + 1 and, for i >= 0, gradient row y0 + i; then issue output row y0 + i
+      const uint32_t sx = xq % kWgXSlots;
+      if (reader[sx] >= 0) wait_through(reader[sx]);
+      if (i >= 0 && oq >= 2) wait_through(static_cast<int>(oq) - 2);
+      if (ok) {
+        const int y = y0 + i + 1;
+        uint32_t wv[10];
+        const bool rok = y >= 0 && y < height;
+        const unsigned int* rowp =
+            reinterpret_cast<const unsigned int*>(X + (img_base + (rok ? y : 0)) * width * kC) + cp;
+#pragma unroll
+        for (int j = 0; j < 10; ++j) {
+          const int px = xs - 1 + 8 * pg + j;
+          wv[j] = (rok && px >= 0 && px < width) ? __ldg(rowp + static_cast<size_t>(px) * (kC / 2)) : 0u;
+        }
+        unsigned char* dst = sX + sx * kWgXRow + pg * kWgXLbo + (2 * cp) * 16;
+#pragma unroll
+        for (int kx = 0; kx < 3; ++kx) {
+          uint4 lo, hi;
+          lo.x = __byte_perm(wv[kx + 0], wv[kx + 1], 0x5410);
+          lo.y = __byte_perm(wv[kx + 2], wv[kx + 3], 0x5410);
+          lo.z = __byte_perm(wv[kx + 4], wv[kx + 5], 0x5410);
+          lo.w = __byte_perm(wv[kx + 6], wv[kx + 7], 0x5410);
+          hi.x = __byte_perm(wv[kx + 0], wv[kx + 1], 0x7632);
+          hi.y = __byte_perm(wv[kx + 2], wv[kx + 3], 0x7632);
+          hi.z = __byte_perm(wv[kx + 4], wv[kx + 5], 0x7632);
+          hi.w = __byte_perm(wv[kx + 6], wv[kx + 7], 0x7632);
+          *reinterpret_cast<uint4*>(dst + kx * kWgCore) = lo;
+          *reinterpret_cast<uint4*>(dst + kx * kWgCore + 16) = hi;
+        }
+        if (i >= 0) {
+          uint32_t gv[8];
+          const unsigned int* growp =
+              reinterpret_cast<const unsigned int*>(G + (img_base + (y0 + i)) * width * kC) + cp;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int px = xs + 8 * pg + j;
+            gv[j] = px < width ? __ldg(growp + static_cast<size_t>(px) * (kC / 2)) : 0u;
+            bsum0 += __uint_as_float(gv[j] << 16);
+            bsum1 += __uint_as_float(gv[j] & 0xffff0000u);
+          }
+          unsigned char* gdst = sG + (oq % kWgGSlots) * kWgGRow + pg * kWgCore + (2 * cp) * 16;
+          uint4 lo, hi;
+          lo.x = __byte_perm(gv[0], gv[1], 0x5410);
+          lo.y = __byte_perm(gv[2], gv[3], 0x5410);
+          lo.z = __byte_perm(gv[4], gv[5], 0x5410);
+          lo.w = __byte_perm(gv[6], gv[7], 0x5410);
+          hi.x = __byte_perm(gv[0], gv[1], 0x7632);
+          hi.y = __byte_perm(gv[2], gv[3], 0x7632);
+          hi.z = __byte_perm(gv[4], gv[5], 0x7632);
+          hi.w = __byte_perm(gv[6], gv[7], 0x7632);
+          *reinterpret_cast<uint4*>(gdst) = lo;
+          *reinterpret_cast<uint4*>(gdst + 16) = hi;
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the staged rows, for the MMAs' reads
+      ok = __syncthreads_and(ok) != 0;
+      ++xq;
+      if (!ok) break;
+      if (i < 0) continue;
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;\n");
+        const uint32_t b_row = gs0 + (oq % kWgGSlots) * kWgGRow;
+        for (int ky = 0; ky < 3; ++ky) {
+          const uint32_t a_row = xs0 + ((xa + static_cast<uint32_t>(i + ky)) % kWgXSlots) * kWgXRow;
+          for (int ks = 0; ks < kWgStrip / 16; ++ks) {
+            const uint64_t a = smem_desc(a_row + ks * 2 * kWgXLbo, kWgXLbo, 128);
+            const uint64_t b = smem_desc(b_row + ks * 2 * kWgCore, kWgCore, 128);
+            mma(tmem + 32u * ky, a, b, (oq == 0 && ks == 0) ? 0u : 1u);
+          }
+        }
+        commit(bar0 + 8u * (oq & 1u));
+      }
+#pragma unroll
+      for (int ky = 0; ky < 3; ++ky) reader[(xa + static_cast<uint32_t>(i + ky)) % kWgXSlots] = static_cast<int>(oq);
+      ++oq;
+    }
+  }
+  if (ok && oq > 0) wait_through(static_cast<int>(oq) - 1);
+  ok = __syncthreads_and(ok) != 0;
+  if (ok && oq > 0 && warp < 3) {  // warp kx reads TMEM lanes 32 kx .. 32 kx + 31 = input channel `lane`
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    for (int ky = 0; ky < 3; ++ky) {
+      float acc[32];
+      tmem_ld32(tmem + 32u * ky + (static_cast<uint32_t>(warp * 32) << 16), acc);
+#pragma unroll
+      for (int co = 0; co < kC; ++co) atomicAdd(&dW[(co * kC + lane) * 9 + ky * 3 + warp], acc[co]);
+    }
+  }
+  if (ok) {
+    // pixel groups pg and pg + 1 of a channel pair are lanes l and l ^ 16 of one warp
+    bsum0 += __shfl_xor_sync(0xffffffffu, bsum0, 16);
+    bsum1 += __shfl_xor_sync(0xffffffffu, bsum1, 16);
+    if (lane < 16 && oq > 0) {
+      atomicAdd(&db[2 * cp], bsum0);
+      atomicAdd(&db[2 * cp + 1], bsum1);
+    }
+  }
+  if (!ok) {
+    if (lane == 0) atomicOr(error, kErrorBit);
+    // the MMA groups still in flight complete before tensor memory is freed (bounded waits)
+    if (tid == 0) {
+      for (uint32_t w = waited; w < oq; ++w) mbar_wait(bar0 + 8u * (w & 1u), (w >> 1) & 1u);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n");
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kWgTmemCols));
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_wgrad32(const __nv_bfloat16* x, const __nv_bfloat16* g, float* dw, float* db, int batch, int width,
+                           int height, unsigned int* error, cudaStream_t s) {
+  static int ctas = 0;
+  if (ctas == 0) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(wgrad32_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kWgSmem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    ctas = 2 * (sms > 0 ? sms : 152);
+  }
+  if (reinterpret_cast<uintptr_t>(x) % 4 != 0 || reinterpret_cast<uintptr_t>(g) % 4 != 0) return cudaErrorInvalidValue;
+  const long long nitems = static_cast<long long>(batch) * ((height + kWgRows - 1) / kWgRows) *
+                           ((width + kWgStrip - 1) / kWgStrip);
+  if (nitems > 0x7fffffffLL) return cudaErrorInvalidValue;  // the item arithmetic is 32-bit
+  const int grid = static_cast<int>(nitems < ctas ? nitems : ctas);
+  if (grid <= 0) return cudaSuccess;
+  wgrad32_tc_kernel<<<grid, kWgThreads, kWgSmem, s>>>(x, g, dw, db, batch, width, height, error);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- the rest of the net (CUDA cores)
 //
 // Parameters, one FP32 array (kParamCount): w1[32][4][3][3] b1[32] w2[32][32][3][3] b2[32] w3[32][32][3][3] b3[32]
@@ -782,20 +1026,29 @@ __global__ void __launch_bounds__(256) dgrad_out_kernel(const float* __restrict_
   }
 }
 
-// Weight gradients of a 3x3 convolution: dW[co][ci][t] = sum_p dY[p][co] X[p + off(t)][ci], db[co] = sum_p dY[p][co].
-// Thread (co, ci) keeps 9 accumulators over the CTA's row segments of kSeg pixels, staged in shared memory as
-// floats; one atomic flush per CTA.  X: BF16 with CI channels or FP32 float4 (CI = 4); dY: BF16 32 channels or
-// FP32 1 channel.
+// Weight gradients of the input and output layers (CUDA cores): dW[co][ci][t] = sum_p dY[p][co] X[p + off(t)][ci],
+// db[co] = sum_p dY[p][co].  X: BF16 with 32 channels (read as 16-byte vectors) or FP32 float4 (CI = 4); dY:
+// BF16 with 32 channels or FP32 with 1.  Each CTA stages row segments of kSeg pixels (three input rows with a
+// one-pixel halo, one gradient row) in shared memory as floats.  Thread (rep, co, ci) keeps 9 accumulators (and
+// the bias sum) over the pixels rep, rep + kRep, ... of each segment, so that CI x CO x kRep threads share a
+// segment; the kRep partial sums are added in shared memory and flushed with one atomic per weight per CTA.
 constexpr int kSeg = 64;
 
-template <int CI, int CO, bool kXBf16, bool kDyBf16>
-__global__ void __launch_bounds__(CI * CO) wgrad_kernel(const void* __restrict__ Xv, const void* __restrict__ dYv,
-                                                        float* __restrict__ dW, float* __restrict__ db, int batch,
-                                                        int w, int h) {
-  __shared__ float sX[3][kSeg + 2][CI];
-  __shared__ float sG[kSeg][CO];
+template <int CI, int CO, bool kXBf16, bool kDyBf16, int kRep>
+__global__ void __launch_bounds__(CI * CO * kRep) wgrad_kernel(const void* __restrict__ Xv, const void* __restrict__ dYv,
+                                                               float* __restrict__ dW, float* __restrict__ db,
+                                                               int batch, int w, int h) {
+  static_assert(!kXBf16 || CI == 32, "BF16 inputs carry 32 channels");
+  static_assert(kXBf16 || CI == 4, "FP32 inputs are float4 pixels");
+  static_assert(!kDyBf16 || CO == 32, "BF16 gradients carry 32 channels");
+  static_assert(kDyBf16 || CO == 1, "FP32 gradients carry one channel");
+  constexpr int kPairs = CI * CO, kT = kPairs * kRep;
+  __shared__ __align__(16) float sX[3][kSeg + 2][CI];
+  __shared__ __align__(16) float sG[kSeg][CO];
+  __shared__ float sRed[kRep > 1 ? kRep - 1 : 1][10][kPairs];
   const int tid = threadIdx.x;
-  const int co = tid / CI, ci = tid % CI;
+  const int pair = tid % kPairs, rep = tid / kPairs;
+  const int co = pair / CI, ci = pair % CI;
   float acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float bacc = 0.0f;
   const int segs_x = (w + kSeg - 1) / kSeg;
@@ -804,33 +1057,51 @@ __global__ void __launch_bounds__(CI * CO) wgrad_kernel(const void* __restrict__
     const int x0 = static_cast<int>(sgi % segs_x) * kSeg;
     const int y = static_cast<int>((sgi / segs_x) % h);
     const long long img = sgi / (static_cast<long long>(segs_x) * h);
-    for (int i = tid; i < 3 * (kSeg + 2) * CI; i += CI * CO) {
-      const int c = i % CI, px = (i / CI) % (kSeg + 2), r = i / (CI * (kSeg + 2));
-      const int sx = x0 - 1 + px, sy = y - 1 + r;
-      float v = 0.0f;
-      if (inside(sx, sy, w, h)) {
-        const long long p = (img * h + sy) * w + sx;
-        if (kXBf16) {
-          v = __bfloat162float(static_cast<const __nv_bfloat16*>(Xv)[p * CI + c]);
-        } else {
-          v = reinterpret_cast<const float*>(static_cast<const float4*>(Xv) + p)[c];
+    if (kXBf16) {  // 4 vectors of 8 channels per pixel
+      for (int i = tid; i < 3 * (kSeg + 2) * 4; i += kT) {
+        const int q = i & 3, px = (i >> 2) % (kSeg + 2), r = (i >> 2) / (kSeg + 2);
+        const int sx = x0 - 1 + px, sy = y - 1 + r;
+        uint4 u = make_uint4(0u, 0u, 0u, 0u);
+        if (inside(sx, sy, w, h)) {
+          u = reinterpret_cast<const uint4*>(static_cast<const __nv_bfloat16*>(Xv) + ((img * h + sy) * w + sx) * CI)[q];
         }
+        const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&u);
+        float4* dst = reinterpret_cast<float4*>(&sX[r][px][8 * q]);
+        const float2 f0 = __bfloat1622float2(b2[0]), f1 = __bfloat1622float2(b2[1]);
+        const float2 f2 = __bfloat1622float2(b2[2]), f3 = __bfloat1622float2(b2[3]);
+        dst[0] = make_float4(f0.x, f0.y, f1.x, f1.y);
+        dst[1] = make_float4(f2.x, f2.y, f3.x, f3.y);
       }
-      sX[r][px][c] = v;
+    } else {  // one float4 per pixel
+      for (int i = tid; i < 3 * (kSeg + 2); i += kT) {
+        const int px = i % (kSeg + 2), r = i / (kSeg + 2);
+        const int sx = x0 - 1 + px, sy = y - 1 + r;
+        float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (inside(sx, sy, w, h)) v = static_cast<const float4*>(Xv)[(img * h + sy) * w + sx];
+        *reinterpret_cast<float4*>(&sX[r][px][0]) = v;
+      }
     }
-    for (int i = tid; i < kSeg * CO; i += CI * CO) {
-      const int c = i % CO, px = i / CO;
-      const int sx = x0 + px;
-      float v = 0.0f;
-      if (sx < w) {
-        const long long p = (img * h + y) * w + sx;
-        v = kDyBf16 ? __bfloat162float(static_cast<const __nv_bfloat16*>(dYv)[p * CO + c])
-                    : static_cast<const float*>(dYv)[p * CO + c];
+    if (kDyBf16) {
+      for (int i = tid; i < kSeg * 4; i += kT) {
+        const int q = i & 3, px = i >> 2;
+        const int sx = x0 + px;
+        uint4 u = make_uint4(0u, 0u, 0u, 0u);
+        if (sx < w) u = reinterpret_cast<const uint4*>(static_cast<const __nv_bfloat16*>(dYv) + ((img * h + y) * w + sx) * CO)[q];
+        const __nv_bfloat162* b2 = reinterpret_cast<const __nv_bfloat162*>(&u);
+        float4* dst = reinterpret_cast<float4*>(&sG[px][8 * q]);
+        const float2 f0 = __bfloat1622float2(b2[0]), f1 = __bfloat1622float2(b2[1]);
+        const float2 f2 = __bfloat1622float2(b2[2]), f3 = __bfloat1622float2(b2[3]);
+        dst[0] = make_float4(f0.x, f0.y, f1.x, f1.y);
+        dst[1] = make_float4(f2.x, f2.y, f3.x, f3.y);
       }
-      sG[px][c] = v;
+    } else {
+      for (int i = tid; i < kSeg; i += kT) {
+        const int sx = x0 + i;
+        sG[i][0] = sx < w ? static_cast<const float*>(dYv)[(img * h + y) * w + sx] : 0.0f;
+      }
     }
     __syncthreads();
-    for (int px = 0; px < kSeg; ++px) {
+    for (int px = rep; px < kSeg; px += kRep) {
       const float g = sG[px][co];
 #pragma unroll
       for (int t = 0; t < 9; ++t) acc[t] += g * sX[t / 3][px + t % 3][ci];
@@ -838,9 +1109,26 @@ __global__ void __launch_bounds__(CI * CO) wgrad_kernel(const void* __restrict__
     }
     __syncthreads();
   }
+  if (kRep > 1) {
+    if (rep > 0) {
 #pragma unroll
-  for (int t = 0; t < 9; ++t) atomicAdd(&dW[(co * CI + ci) * 9 + t], acc[t]);
-  if (ci == 0) atomicAdd(&db[co], bacc);
+      for (int t = 0; t < 9; ++t) sRed[rep - 1][t][pair] = acc[t];
+      sRed[rep - 1][9][pair] = bacc;
+    }
+    __syncthreads();
+    if (rep == 0) {
+      for (int r = 0; r < kRep - 1; ++r) {
+#pragma unroll
+        for (int t = 0; t < 9; ++t) acc[t] += sRed[r][t][pair];
+        bacc += sRed[r][9][pair];
+      }
+    }
+  }
+  if (rep == 0) {
+#pragma unroll
+    for (int t = 0; t < 9; ++t) atomicAdd(&dW[(co * CI + ci) * 9 + t], acc[t]);
+    if (ci == 0) atomicAdd(&db[co], bacc);
+  }
 }
 
 __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
@@ -940,27 +1228,27 @@ cudaError_t backward(const float* params, const __nv_bfloat16* packed, const flo
   cudaError_t e = cudaMemsetAsync(grads, 0, kParams * sizeof(float), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(loss, 0, 2 * sizeof(float), s);
   if (e != cudaSuccess) return e;
-  const int wg = sm_count();
+  const int wg = 4 * sm_count();  // CUDA-core weight gradients: 256-thread CTAs, four per SM
   loss_grad_kernel<<<grid, 256, 0, s>>>(out, target, depth, dr, static_cast<long long>(n), loss);
   // layer 4: weights, then the gradient into A3
-  wgrad_kernel<kC, 1, true, false><<<wg, kC, 0, s>>>(A3, dr, grads + kOffW4, grads + kOffB4, batch, width, height);
+  wgrad_kernel<kC, 1, true, false, 8><<<wg, kC * 8, 0, s>>>(A3, dr, grads + kOffW4, grads + kOffB4, batch, width,
+                                                             height);
   dgrad_out_kernel<<<grid, 256, 0, s>>>(dr, params, A3, G1, batch, width, height);
   // layer 3
-  wgrad_kernel<kC, kC, true, true><<<wg, kC * kC, 0, s>>>(A2, G1, grads + kOffW3, grads + kOffB3, batch, width, height);
   e = cudaGetLastError();
+  if (e == cudaSuccess) e = launch_wgrad32(A2, G1, grads + kOffW3, grads + kOffB3, batch, width, height, error, s);
   if (e == cudaSuccess) {
     e = launch_conv32(G1, packed + 3 * 9 * kC * kC, nullptr, A2, G2, batch, width, height, kGrad, 0, error, s);
   }
   if (e != cudaSuccess) return e;
   // layer 2
-  wgrad_kernel<kC, kC, true, true><<<wg, kC * kC, 0, s>>>(A1, G2, grads + kOffW2, grads + kOffB2, batch, width, height);
-  e = cudaGetLastError();
+  e = launch_wgrad32(A1, G2, grads + kOffW2, grads + kOffB2, batch, width, height, error, s);
   if (e == cudaSuccess) {
     e = launch_conv32(G2, packed + 2 * 9 * kC * kC, nullptr, A1, G1, batch, width, height, kGrad, 0, error, s);
   }
   if (e != cudaSuccess) return e;
   // layer 1
-  wgrad_kernel<kCin, kC, false, true><<<wg, kCin * kC, 0, s>>>(X, G1, grads + kOffW1, grads + kOffB1, batch, width,
+  wgrad_kernel<kCin, kC, false, true, 2><<<wg, kCin * kC * 2, 0, s>>>(X, G1, grads + kOffW1, grads + kOffB1, batch, width,
                                                               height);
   return cudaGetLastError();
 }

@@ -16,6 +16,11 @@ enum { kForward = 0, kGrad = 1 };
 cudaError_t launch_conv32(const __nv_bfloat16* in, const __nv_bfloat16* wpack, const float* bias,
                           const __nv_bfloat16* mask, __nv_bfloat16* out, int batch, int width, int height, int mode,
                           int relu, unsigned int* error, cudaStream_t s, const unsigned int* gate = nullptr);
+// Weight gradient of a 32 -> 32 3x3 layer on the tensor cores: dw[co][ci][3][3] += sum_p g[p][co] x[p + off][ci],
+// db[co] += sum_p g[p][co] (x: the layer input, g: the gradient at its output, NHWC BF16, 4-byte aligned).
+// error: as launch_conv32.
+cudaError_t launch_wgrad32(const __nv_bfloat16* x, const __nv_bfloat16* g, float* dw, float* db, int batch, int width,
+                           int height, unsigned int* error, cudaStream_t s);
 // FP32 weights [co][ci][3][3] -> the B operand layout; transpose_flip gives the input-gradient weights
 cudaError_t launch_pack_w32(const float* w, __nv_bfloat16* out, int transpose_flip, cudaStream_t s);
 int conv32_smem_bytes();
