@@ -548,35 +548,43 @@ cudaError_t launch_pack_w32(const float* w, __nv_bfloat16* out, int transpose_fl
 // columns), summed over every output row the CTA takes and added to dW once at the end.
 //
 // A CTA takes items of kWgRows output rows of one kWgStrip-pixel strip.  Each input row is staged once, as three
-// copies shifted by kx - 1 pixels and a pad copy, transposed into the canonical no-swizzle K-major layout
+// copies shifted by kx - 1 pixels, transposed into the canonical no-swizzle K-major layout
 // [pixel group of 8 (K)][copy][channel][8 pixels]: the A operand of tap row ky of output row y is then the
-// staged input row y - 1 + ky, its M rows (copy, channel) at a uniform 128-byte stride per 8 rows, and the pad
-// copy feeds only accumulator rows that are never read.  The gradient row is staged the same way as the B
-// operand, [pixel group][output channel][8 pixels].  A thread loads a channel pair over 10 (8) pixels as 32-bit
-// words and writes the transposed 16-byte rows with byte permutes.  Rows live in rings (kWgXSlots input rows,
-// two gradient rows); thread 0 issues an output row's 12 MMAs (3 tap rows x 4 k-steps of 16 pixels) and commits
-// them to an mbarrier, and a ring slot is rewritten only after the MMAs that read it have completed, so the
-// staging of a row overlaps the MMAs of the row before.  Waits are bounded as in conv32_tc_kernel; a timeout is
-// agreed on by every thread (__syncthreads_and) before the CTA leaves its loop.
+// staged input row y - 1 + ky, its M rows (copy, channel) at a uniform 128-byte stride per 8 rows.  M rows
+// 96..127 (the fourth "copy") read the next pixel group's first copy, or for the last group of the last ring
+// slot the gradient ring that follows: staged values, finite, feeding only accumulator rows that are never
+// read.  The gradient row is staged the same way as the B operand, [pixel group][output channel][8 pixels].  A
+// thread loads a channel pair over 10 (8) pixels as 32-bit words and writes the transposed 16-byte rows with
+// byte permutes; the loads of a row are issued before the wait for its ring slot, so they overlap the MMAs
+// that still read the slot.  Rows live in rings (three input rows, two gradient rows); thread 0 issues an output
+// row's 12 MMAs (3 tap rows x 4 k-steps of 16 pixels) and commits them to an mbarrier, and a ring slot is
+// rewritten only after the MMAs that read it have completed.  Four CTAs per SM (their tensor memory fills the
+// SM's 512 columns).  Waits are bounded as in conv32_tc_kernel; a timeout is agreed on by every thread
+// (__syncthreads_and) before the CTA leaves its loop.
 namespace {
 
 constexpr int kWgStrip = 64;                         // pixels of an output row per item (K of a row)
 constexpr int kWgGroups = kWgStrip / 8;              // pixel groups of 8 (16 bytes of BF16)
-constexpr int kWgCopies = 4;                         // kx = 0, 1, 2 and the pad copy
+constexpr int kWgCopies = 3;                         // kx = 0, 1, 2
 constexpr int kWgCore = kC * 16;                     // one copy of one pixel group: 32 channels x 16 bytes
 constexpr int kWgXLbo = kWgCopies * kWgCore;         // A operand: bytes between pixel groups (K)
-constexpr int kWgXRow = kWgGroups * kWgXLbo;         // one staged input row: 16,384 bytes
+constexpr int kWgXRow = kWgGroups * kWgXLbo;         // one staged input row: 12,288 bytes
 constexpr int kWgGRow = kWgGroups * kWgCore;         // one staged gradient row: 4,096 bytes
-constexpr int kWgXSlots = 5;                         // an output row reads 3 input rows; one more is staged
-                                                     // while the previous row's MMAs run
+constexpr int kWgXSlots = 3;                         // an output row reads 3 input rows; the slot a new row
+                                                     // takes was last read by the previous output row
 constexpr int kWgGSlots = 2;
 constexpr int kWgRows = 16;                          // output rows per item
 constexpr int kWgThreads = 128;                      // thread t stages pixel group t / 16, channel pair t % 16
 constexpr int kWgTmemCols = 128;                     // 3 accumulators x 32 columns, allocated as a power of 2
+constexpr int kWgCtasPerSm = 4;
 constexpr int kWgSmem = 128 + kWgXSlots * kWgXRow + kWgGSlots * kWgGRow + 2 * 8 + 16;
+// the A operand reads up to 3,583 bytes from its start (a second pixel group at +LBO, 16 M groups of 128 bytes),
+// at most 511 bytes past its ring slot, which the next slot or the gradient ring covers
+static_assert(kWgGSlots * kWgGRow >= 4 * kWgCore, "the last slot's pad rows stay inside the gradient ring");
+static_assert(kWgCtasPerSm * kWgTmemCols <= 512, "tensor memory of the resident CTAs");
 static_assert(kWgThreads == kWgGroups * (kC / 2), "one (pixel group, channel pair) per thread");
 
-__global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc_kernel(const __nv_bfloat16* __restrict__ X,
+__global__ void __launch_bounds__(kWgThreads, kWgCtasPerSm) wgrad32_tc_kernel(const __nv_bfloat16* __restrict__ X,
                                                                     const __nv_bfloat16* __restrict__ G,
                                                                     float* __restrict__ dW, float* __restrict__ db,
                                                                     int batch, int width, int height,
@@ -590,11 +598,9 @@ __global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc_kernel(const __nv_bf
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int pg = tid >> 4, cp = tid & 15;  // staging: pixel group, channel pair
 
-  // the pad copies: any finite value would do (they reach only discarded accumulator rows); zero
-  for (int i = tid; i < kWgXSlots * kWgGroups * (kWgCore / 16); i += kWgThreads) {
-    const int row = i / (kWgGroups * (kWgCore / 16)), rest = i % (kWgGroups * (kWgCore / 16));
-    const int grp = rest / (kWgCore / 16), k = rest % (kWgCore / 16);
-    reinterpret_cast<uint4*>(sX + row * kWgXRow + grp * kWgXLbo + 3 * kWgCore)[k] = make_uint4(0u, 0u, 0u, 0u);
+  // the rings start zeroed, so that the pad rows read finite values before every slot has been staged
+  for (int i = tid; i < (kWgXSlots * kWgXRow + kWgGSlots * kWgGRow) / 16; i += kWgThreads) {
+    reinterpret_cast<uint4*>(sX)[i] = make_uint4(0u, 0u, 0u, 0u);
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
@@ -645,13 +651,11 @@ __global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc_kernel(const __nv_bf
     const uint32_t xa = xq;  // ring index of input row y0 - 1
     const size_t img_base = static_cast<size_t>(img) * height;
     for (int i = -2; i < rows; ++i) {
-      // stage input row y0 + i + 1 and, for i >= 0, gradient row y0 + i; then issue output row y0 + i
-      const uint32_t sx = xq % kWgXSlots;
-      if (reader[sx] >= 0) wait_through(reader[sx]);
-      if (i >= 0 && oq >= 2) wait_through(static_cast<int>(oq) - 2);
-      if (ok) {
-        const int y = y0 + i + 1;
-        uint32_t wv[10];
+      // stage input row y0 + i + 1 and, for i >= 0, gradient row y0 + i; then issue output row y0 + i.  The
+      // global loads go first: they do not touch the rings, so they overlap the wait for the slots.
+      const int y = y0 + i + 1;
+      uint32_t wv[10];
+      {
         const bool rok = y >= 0 && y < height;
         const unsigned int* rowp =
             reinterpret_cast<const unsigned int*>(X + (img_base + (rok ? y : 0)) * width * kC) + cp;
@@ -660,6 +664,21 @@ __global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc_kernel(const __nv_bf
           const int px = xs - 1 + 8 * pg + j;
           wv[j] = (rok && px >= 0 && px < width) ? __ldg(rowp + static_cast<size_t>(px) * (kC / 2)) : 0u;
         }
+      }
+      uint32_t gv[8];
+      if (i >= 0) {
+        const unsigned int* growp =
+            reinterpret_cast<const unsigned int*>(G + (img_base + (y0 + i)) * width * kC) + cp;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int px = xs + 8 * pg + j;
+          gv[j] = px < width ? __ldg(growp + static_cast<size_t>(px) * (kC / 2)) : 0u;
+        }
+      }
+      const uint32_t sx = xq % kWgXSlots;
+      if (reader[sx] >= 0) wait_through(reader[sx]);
+      if (i >= 0 && oq >= 2) wait_through(static_cast<int>(oq) - 2);
+      if (ok) {
         unsigned char* dst = sX + sx * kWgXRow + pg * kWgXLbo + (2 * cp) * 16;
 #pragma unroll
         for (int kx = 0; kx < 3; ++kx) {
@@ -676,13 +695,8 @@ __global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc_kernel(const __nv_bf
           *reinterpret_cast<uint4*>(dst + kx * kWgCore + 16) = hi;
         }
         if (i >= 0) {
-          uint32_t gv[8];
-          const unsigned int* growp =
-              reinterpret_cast<const unsigned int*>(G + (img_base + (y0 + i)) * width * kC) + cp;
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            const int px = xs + 8 * pg + j;
-            gv[j] = px < width ? __ldg(growp + static_cast<size_t>(px) * (kC / 2)) : 0u;
             bsum0 += __uint_as_float(gv[j] << 16);
             bsum1 += __uint_as_float(gv[j] & 0xffff0000u);
           }
@@ -770,7 +784,7 @@ cudaError_t launch_wgrad32(const __nv_bfloat16* x, const __nv_bfloat16* g, float
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    ctas = 2 * (sms > 0 ? sms : 152);
+    ctas = kWgCtasPerSm * (sms > 0 ? sms : 152);
   }
   if (reinterpret_cast<uintptr_t>(x) % 4 != 0 || reinterpret_cast<uintptr_t>(g) % 4 != 0) return cudaErrorInvalidValue;
   const long long nitems = static_cast<long long>(batch) * ((height + kWgRows - 1) / kWgRows) *

@@ -7,7 +7,7 @@ BF16 activations); the input and output layers and all weight gradients and Adam
 Every kernel is in the library (vh_nn_*); this module holds the buffers and runs the loop.
 
 Training pairs: raw noisy depth frames and the depth ray-cast (vh_raycast_depth) at the same pose from the
-volume fused from all frames of the scene with the plain FP32 pipeline, cut into random crops.
+volume fused from all frames of the scene with the plain FP32 pipeline, whole frames or random crops.
 """
 from __future__ import annotations
 
@@ -231,12 +231,61 @@ def _time_forward(frames=20, batch=1, seed=3):
     return e0.elapsed_time(e1) / frames
 
 
+def _time_train_step(steps=20, batch=16, seed=1):
+    """Adam steps of a seeded net on rendered 640x480 room frames (noise-free targets), after 3 warm-up steps:
+    (forward, backward, Adam + weight packing) ms per step, CUDA events."""
+    import torch
+    from . import build, scenes
+    build.build()
+    torch.cuda.set_device(0)
+    sc = scenes.room_scene(seed=5, frames=batch)
+    raw = render_frames(sc, torch)
+    sc.noise_sigma_z2, sc.dropout = 0.0, 0.0
+    tgt = render_frames(sc, torch)
+    net = DepthDenoiser(seed=seed)
+    b, h, w = raw.shape
+    lib = _capi.lib()
+    for _ in range(3):
+        net.train_step(raw, tgt)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    tf = tb = ta = 0.0
+    for _ in range(steps):
+        ev[0].record()
+        out = net.forward(raw)
+        ev[1].record()
+        _capi.check(lib.vh_nn_backward(_ptr(net.params), _ptr(net.packed), _ptr(raw), _ptr(tgt), _ptr(out), b, w, h,
+                                       _ptr(net._workspace(b, w, h)), _ptr(net.grads), _ptr(net.loss), net._err(),
+                                       None))
+        ev[2].record()
+        net.step_count += 1
+        _capi.check(lib.vh_nn_adam(_ptr(net.params), _ptr(net.grads), _ptr(net.m), _ptr(net.v), net.lr, net.beta1,
+                                   net.beta2, net.eps, net.step_count, None))
+        net._repack()
+        ev[3].record()
+        torch.cuda.synchronize()
+        tf += ev[0].elapsed_time(ev[1])
+        tb += ev[1].elapsed_time(ev[2])
+        ta += ev[2].elapsed_time(ev[3])
+    net.check_error()
+    return tf / steps, tb / steps, ta / steps
+
+
 if __name__ == "__main__":
-    # python -m voxelhashmt_gb300.denoiser [--frames N] [--batch B]: time the net's forward pass
+    # python -m voxelhashmt_gb300.denoiser [--frames N] [--batch B]: time the net's forward pass;
+    # with --train: time training steps (batch B, default 16)
     import argparse
     ap = argparse.ArgumentParser()
     ap.add_argument("--frames", type=int, default=20)
-    ap.add_argument("--batch", type=int, default=1)
+    ap.add_argument("--batch", type=int, default=0)
+    ap.add_argument("--train", action="store_true")
     a = ap.parse_args()
-    ms = _time_forward(a.frames, a.batch)
-    print("denoiser forward: %.4f ms per pass of %d 640x480 frame(s)" % (ms, a.batch))
+    if a.train:
+        bt = a.batch or 16
+        f, bw, ad = _time_train_step(a.frames, bt)
+        print("denoiser training step, batch %d x 640x480: forward %.3f ms, backward %.3f ms, Adam + packing %.3f ms"
+              % (bt, f, bw, ad))
+    else:
+        bt = a.batch or 1
+        ms = _time_forward(a.frames, bt)
+        print("denoiser forward: %.4f ms per pass of %d 640x480 frame(s)" % (ms, bt))
