@@ -49,6 +49,8 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # opt-in form: fused_update_room640.md, one launch over 3.16 M active and 2.86 M updated voxels).
 UPDATE_TRAFFIC_BYTES = {"plain": ((539.49e6 + 267.04e6) / 6.548e6, 0.0),
                         "chosen": (189.529e6 / 3.163e6, 58.035e6 / 2.860e6)}
+# warp instructions per active voxel of the layer-update kernel (smsp__inst_executed.sum of the same captures)
+UPDATE_WARP_INSTRUCTIONS = {"plain": 1514.374e6 / 6.548e6, "chosen": 111.551e6 / 3.163e6}
 
 
 def parse():
@@ -558,6 +560,21 @@ def run_gb300(args):
                         "launch x the active and updated voxels"
                         % (bin_bytes, bin_bytes)}
 
+    # the update kernels are issue-bound: the same launch against the schedulers' issue rate (one warp instruction
+    # per scheduler per cycle, 4 schedulers per SM, at the SM clock sampled during the timed frames)
+    sm_mhz = (head.get("clocks") or {}).get("sm_mhz") or 2070.0
+    n_sm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    winst = UPDATE_WARP_INSTRUCTIONS[args.form] * head["act_mean"]
+    issue_achieved = winst / (upd_ms / 1000.0) / 1e9
+    issue_peak = 4 * n_sm * sm_mhz / 1000.0
+    issue_roofline = {"kernel": UPDATE_KERNEL[args.form], "bound": "issue", "achieved": round(issue_achieved, 1),
+                      "peak": round(issue_peak, 1), "unit": "Gwarp-instructions/s",
+                      "frac": round(issue_achieved / issue_peak, 4),
+                      "warp_instructions_per_launch": int(winst),
+                      "note": "ncu warp instructions per active voxel of one captured launch x the active voxels, "
+                              "over the CUDA-event launch time; peak = 4 schedulers x %d SMs x the median SM clock "
+                              "under load" % n_sm}
+
     cpu = None
     if rank == 0 and world == 1 and args.cpu_budget_s > 0:
         try:
@@ -612,7 +629,7 @@ def run_gb300(args):
                             "statistics read per frame; no L2 flush between frames: each frame's layer update "
                             "alone moves about 230 MB of DRAM (ncu), more than the 129 MB L2, so consecutive "
                             "frames reuse only part of it"},
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": head["clocks"],
+            "roofline": roofline, "issue_roofline": issue_roofline, "cpu_baseline": cpu, "clocks": head["clocks"],
             "gpu_launches": args.steps * 4,
             args.form: summary(head, args.form), other: summary(res[other], other),
             "speedup_vs_plain": round(res["chosen"]["value"] / res["plain"]["value"], 3),
