@@ -908,16 +908,17 @@ def run_streaming(args):
         _capi.check(_capi.lib().vh_set_depth_denoiser(vol.handle, learned.ctypes.data_as(C.POINTER(C.c_float))),
                     vol.handle)
     bk = backend.TsdfIntegrationBackend("gpu")
-    # evicted blocks stream out to host memory in rounds of about chunk blocks (an age bin can add one frame's
-    # blocks to a round, hence the larger buffer)
+    # evicted blocks stream out to host memory in rounds of chunk blocks (vh_evict_blocks evicts exactly down to
+    # its target)
     chunk = max(1, min(60000, max_blocks // 20))
-    evict_cap = 4 * chunk
+    evict_cap = chunk
     bpb = 98304 if fmt == 1 else 147456
     # page-locked, so that the copies out run as DMA at the host link's rate
     host_keys = torch.empty((evict_cap, 3), dtype=torch.int32, pin_memory=True)
     host_data = torch.empty((evict_cap, bpb), dtype=torch.uint8, pin_memory=True)
     fuse_ms, evict_ms, mc_ms = 0.0, 0.0, 0.0
     evictions, evicted_blocks, mc_runs, mc_blocks, mc_tris, peak_blocks = 0, 0, 0, 0, 0, 0
+    evict_calls = []  # (blocks, seconds, pool blocks before) per vh_evict_blocks call
     n_frames = len(sc.poses)
     clocks = ClockSampler(0)
     clocks.start()
@@ -953,10 +954,12 @@ def run_streaming(args):
                 t0 = time.perf_counter()
                 while nb > target:
                     cnt = C.c_uint64()
+                    c0 = time.perf_counter()
                     _capi.check(_capi.lib().vh_evict_blocks(vol.handle, 0xffffffff, int(max(target, nb - chunk)), 1,
                                                             C.c_void_p(host_keys.data_ptr()),
                                                             C.c_void_p(host_data.data_ptr()), evict_cap, 0,
                                                             C.byref(cnt), C.c_void_p(stream.cuda_stream)), vol.handle)
+                    evict_calls.append((cnt.value, time.perf_counter() - c0, nb))
                     evicted_blocks += cnt.value
                     nb = vol.block_count()
                     if cnt.value == 0:
@@ -1013,7 +1016,9 @@ def run_streaming(args):
         "sustained_note": "wall clock over fusion + eviction + incremental meshing (frame rendering excluded)",
         "peak_blocks": peak_blocks, "final_blocks": vol.block_count(),
         "eviction": {"events": evictions, "blocks": evicted_blocks, "gb_streamed_out": round(evicted_blocks * bpb / 1e9, 2),
-                     "ms_total": round(evict_ms, 1)},
+                     "ms_total": round(evict_ms, 1), "calls": len(evict_calls),
+                     "ms_per_call": round(1000 * sum(c[1] for c in evict_calls) / max(1, len(evict_calls)), 2),
+                     "gbs_in_calls": round(sum(c[0] for c in evict_calls) * bpb / max(1e-9, sum(c[1] for c in evict_calls)) / 1e9, 1)},
         "incremental_mc": {"runs": mc_runs, "ms_total": round(mc_ms, 1), "triangles_last": tris.shape[0],
                            "ms_per_run": round(mc_ms / max(1, mc_runs), 2)},
         "chamfer_last_100_frames": chamfer, "clocks": clock_info,

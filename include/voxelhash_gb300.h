@@ -256,15 +256,16 @@ vh_status vh_import_blocks(vh_volume* volume, const int32_t* keys, const void* v
 /* Eviction, for trajectories longer than the pool holds (no reference counterpart: the reference's volume only
  * grows, voxel_hash_tsdf.h:133-139).  Removes every block whose layer update last ran at least min_age_frames
  * frames ago (blocks not updated since they were imported count as oldest) -- and, with target_blocks > 0,
- * also the oldest further blocks until at most target_blocks remain -- after copying them out: keys (3 int32 per
+ * also the oldest further blocks until exactly target_blocks remain (blocks of equal age, and all blocks older
+ * than 4,095 frames, in pool order) -- after copying them out: keys (3 int32 per
  * block) and contents, format 0 in the reference Voxel layout (147,456 bytes per block, as vh_export_blocks),
  * format 1 as the volume's own block image (147,456 bytes with FP32 layers, 98,304 with FP16 layers), which
  * vh_restore_blocks puts back bit for bit; to host memory (out_on_device = 0) or device memory (1), in
  * ascending pool order.  Either output pointer may be NULL.  *evicted receives the number of blocks; if the
  * buffers hold fewer (max_out), nothing is evicted, *evicted holds the number and the call returns
  * VH_ERR_BUFFER_TOO_SMALL.  The pool stays dense (surviving blocks move into the freed slots), the hash is
- * rebuilt from the surviving keys, the last frame's visible list is cleared and the observed voxels are
- * recounted; the last extracted mesh is discarded.  Synchronises. */
+ * rebuilt from the surviving keys, the last frame's visible list is cleared and the victims' observed voxels
+ * are taken off the count; the last extracted mesh is discarded.  Synchronises. */
 vh_status vh_evict_blocks(vh_volume* volume, uint32_t min_age_frames, uint64_t target_blocks, int32_t format,
                           int32_t* keys_out, void* data_out, uint64_t max_out, int32_t out_on_device,
                           uint64_t* evicted, void* stream);

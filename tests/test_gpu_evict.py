@@ -6,7 +6,8 @@ configuration that keep a bounded pool over a long trajectory.
   images gives back the volume that was never evicted -- keys, every voxel word, observed count and mesh -- for
   FP32 and FP16 storage.
 * Fusing on after an eviction equals the oracle's volume with the same blocks removed, bit for bit.
-* A target block count evicts the oldest blocks first; a short output buffer evicts nothing.
+* A target block count evicts the oldest blocks first, exactly down to the count; a short output buffer evicts
+  nothing.
 """
 import numpy as np
 import pytest
@@ -132,4 +133,22 @@ def test_target_evicts_oldest_first_and_short_buffers_evict_nothing(env, small_o
     ek, _ = vol.evict_blocks(1 << 30, target_blocks=target, native=True)
     assert vol.block_count() == target and len(ek) == n0 - target
     assert _rows(vol.export_blocks()[0]) == last
+    vol.close()
+
+
+def test_target_evicts_exactly_down_to_the_count(env, small_orbit):
+    """A target inside an age bin: the blocks of that age go in pool order until exactly target_blocks remain,
+    and every younger block stays."""
+    backend, O = env
+    sc = small_orbit
+    vol = _volume(backend, sc, False)
+    _fuse(backend, vol, sc, list(range(0, 24, 2)))
+    n0 = vol.block_count()
+    last = _rows(backend.visible_block_keys(vol))
+    target = len(last) + 3
+    assert target < n0
+    ek, _ = vol.evict_blocks(1 << 30, target_blocks=target, native=True)
+    kept = _rows(vol.export_blocks()[0])
+    assert vol.block_count() == target and len(ek) == n0 - target and len(kept) == target
+    assert last <= kept
     vol.close()

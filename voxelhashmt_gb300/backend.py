@@ -211,7 +211,7 @@ class VoxelHashTSDF:
 
     def evict_blocks(self, min_age_frames, target_blocks=0, native=True):
         """Evicts the blocks not updated within the last min_age_frames frames (and, with target_blocks, the oldest
-        further ones until at most target_blocks remain); returns (keys (N,3) int32, data): the volume's own block
+        further ones until exactly target_blocks remain); returns (keys (N,3) int32, data): the volume's own block
         images (N, block bytes) uint8 for restore_blocks when native, else the reference Voxel layout as
         export_blocks returns it.  Host memory."""
         return self._evict_into(min_age_frames, target_blocks, native, self.block_count())

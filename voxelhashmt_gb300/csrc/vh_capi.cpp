@@ -759,8 +759,9 @@ vh_status vh_evict_blocks(vh_volume* v, uint32_t min_age_frames, uint64_t target
   if (st != VH_OK) return st;
   const uint32_t n = static_cast<uint32_t>(block_total(v));
   if (n == 0) return VH_OK;
-  // threshold: age >= min_age_frames, lowered through the age histogram until at most target_blocks remain
-  uint32_t threshold = min_age_frames;
+  // the rule: age >= min_age_frames; with a target, the oldest further blocks until exactly target_blocks remain
+  // (the boundary age bin is found through the age histogram, its blocks taken in pool order up to the count)
+  vh::EvictRule rule{min_age_frames, static_cast<uint32_t>(vh::kAgeBins), 0U};
   if (target_blocks > 0 && target_blocks < n) {
     std::vector<uint32_t> hist(vh::kAgeBins);
     VH_CUDA(v, vh::launch_age_hist(v->dev, v->d_evict_hist, s));
@@ -774,9 +775,26 @@ vh_status vh_evict_blocks(vh_volume* v, uint32_t min_age_frames, uint64_t target
       t = static_cast<uint32_t>(bin);
       if (acc >= need) break;
     }
-    threshold = std::min(threshold, t);
+    if (t < min_age_frames) {
+      // victims whatever the cut: age >= min_age_frames or a bin above t
+      rule.tie_bin = t;
+      uint32_t sure = 0, ties = 0;
+      VH_CUDA(v, vh::launch_select(v->dev, n, rule, 0, 0U, v->d_evict_cta, v->d_evict_total, v->d_evict_list, s));
+      VH_CUDA(v, vh::launch_select(v->dev, n, rule, 2, 0U, v->d_evict_cta, v->d_evict_total + 1, v->d_evict_src, s));
+      VH_CUDA(v, cudaMemcpyAsync(&sure, v->d_evict_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      VH_CUDA(v, cudaMemcpyAsync(&ties, v->d_evict_total + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      VH_CUDA(v, cudaStreamSynchronize(s));
+      if (sure < need && ties > 0) {
+        // the boundary bin's blocks below `cut` make up the count: cut = 1 + the (need - sure)-th of them
+        const uint64_t take = std::min<uint64_t>(need - sure, ties);
+        uint32_t last = 0;
+        VH_CUDA(v, cudaMemcpyAsync(&last, v->d_evict_src + (take - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        VH_CUDA(v, cudaStreamSynchronize(s));
+        rule.cut = last + 1U;
+      }
+    }
   }
-  VH_CUDA(v, vh::launch_select(v->dev, n, threshold, 0, 0U, v->d_evict_cta, v->d_evict_total, v->d_evict_list, s));
+  VH_CUDA(v, vh::launch_select(v->dev, n, rule, 0, 0U, v->d_evict_cta, v->d_evict_total, v->d_evict_list, s));
   uint32_t nv = 0;
   VH_CUDA(v, cudaMemcpyAsync(&nv, v->d_evict_total, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   VH_CUDA(v, cudaStreamSynchronize(s));
@@ -800,9 +818,11 @@ vh_status vh_evict_blocks(vh_volume* v, uint32_t min_age_frames, uint64_t target
       }
     }
   }
+  // the victims' observed voxels, counted while their masks are still in place
+  VH_CUDA(v, vh::launch_victim_observed(v->dev, v->d_evict_list, nv, v->d_scalar + 1, s));
   // 2. the survivors above the new block count move into the victims' slots below it
   const uint32_t live = n - nv;
-  VH_CUDA(v, vh::launch_select(v->dev, n, threshold, 1, live, v->d_evict_cta, v->d_evict_total + 1, v->d_evict_src, s));
+  VH_CUDA(v, vh::launch_select(v->dev, n, rule, 1, live, v->d_evict_cta, v->d_evict_total + 1, v->d_evict_src, s));
   uint32_t nmove = 0;
   VH_CUDA(v, cudaMemcpyAsync(&nmove, v->d_evict_total + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   VH_CUDA(v, cudaStreamSynchronize(s));
@@ -820,14 +840,13 @@ vh_status vh_evict_blocks(vh_volume* v, uint32_t min_age_frames, uint64_t target
   VH_CUDA(v, cudaMemsetAsync(V.dir_mask + live, 0, tail * sizeof(uint32_t), s));
   VH_CUDA(v, cudaMemsetAsync(V.block_stamp + live, 0, tail * sizeof(uint32_t), s));
   VH_CUDA(v, vh::launch_rehash(V, live, s));
-  // 4. counters: the new block count, no visible list, observed voxels recounted
+  // 4. counters: the new block count, no visible list, the victims' observed voxels taken off
   vh::Counters c = *v->h_counters;
   c.num_blocks = live;
   c.visible_count = 0;
   c.new_blocks = 0;
   VH_CUDA(v, cudaMemcpyAsync(V.counters, &c, sizeof(c), cudaMemcpyHostToDevice, s));
-  st = recount_into_counters(v, s);
-  if (st != VH_OK) return st;
+  VH_CUDA(v, vh::launch_subtract_observed(V, v->d_scalar + 1, s));
   *evicted = nv;
   v->mesh_triangles = 0;
   return vh_synchronize(v, stream);

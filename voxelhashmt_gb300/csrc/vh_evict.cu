@@ -6,7 +6,8 @@
 // layout (the export path, copyBlocksToFlat, voxel_hash_tsdf.h:147-163) or as the pool's own block image --
 // and removed.  Removal keeps the pool dense, so every other kernel (marching cubes, export, recount) still
 // walks [0, num_blocks):
-//   1. victims: blocks with frame - block_stamp >= threshold, listed in ascending pool order (two-level scan);
+//   1. victims: blocks with frame - block_stamp >= min_age_frames, and, down to a target count, the oldest further
+//      ones (ties at the boundary age in pool order), listed in ascending pool order (two-level scan);
 //   2. victims are copied out through a staging buffer;
 //   3. the live blocks above the new count move down into the victims' slots below it (the two sets are
 //      disjoint, so the moves run in parallel), with their keys, masks and stamps;
@@ -35,15 +36,19 @@ __global__ void __launch_bounds__(256) age_hist_kernel(const Volume V, uint32_t*
   }
 }
 
-// predicate of the selection: 0 victims (age >= threshold) over [0, n); 1 survivors (age < threshold) over [lo, n)
-__device__ __forceinline__ bool selected(const Volume& V, uint32_t b, uint32_t frame, uint32_t threshold, int what,
+// predicate of the selection (EvictRule): 0 victims over [0, n); 1 survivors over [lo, n); 2 the blocks of the
+// boundary bin that are not victims by age (the candidates of the pool-order tie break)
+__device__ __forceinline__ bool selected(const Volume& V, uint32_t b, uint32_t frame, const EvictRule& r, int what,
                                          uint32_t lo) {
-  const bool victim = block_age(V, b, frame) >= threshold;
+  const uint32_t age = block_age(V, b, frame);
+  const uint32_t bin = min(age, static_cast<uint32_t>(kAgeBins - 1));
+  if (what == 2) return bin == r.tie_bin && age < r.min_age;
+  const bool victim = age >= r.min_age || bin > r.tie_bin || (bin == r.tie_bin && b < r.cut);
   return what == 0 ? victim : (b >= lo && !victim);
 }
 
 // per-CTA counts of the selected blocks of [cta * 1024, cta * 1024 + 1024)
-__global__ void __launch_bounds__(kScanThreads) select_count_kernel(const Volume V, uint32_t n, uint32_t threshold,
+__global__ void __launch_bounds__(kScanThreads) select_count_kernel(const Volume V, uint32_t n, const EvictRule rule,
                                                                     int what, uint32_t lo,
                                                                     uint32_t* __restrict__ cta_counts) {
   __shared__ uint32_t s_count;
@@ -51,7 +56,7 @@ __global__ void __launch_bounds__(kScanThreads) select_count_kernel(const Volume
   __syncthreads();
   const uint32_t frame = V.counters->frame;
   const uint32_t b = blockIdx.x * kScanThreads + threadIdx.x;
-  const bool sel = b < n && selected(V, b, frame, threshold, what, lo);
+  const bool sel = b < n && selected(V, b, frame, rule, what, lo);
   const uint32_t ballot = __ballot_sync(0xffffffffU, sel);
   if ((threadIdx.x & 31) == 0 && ballot) atomicAdd(&s_count, static_cast<uint32_t>(__popc(ballot)));
   __syncthreads();
@@ -98,7 +103,7 @@ __global__ void __launch_bounds__(kScanThreads) select_scan_kernel(uint32_t* __r
 }
 
 // the selected blocks in ascending order: list[offset of the CTA + rank within the CTA] = b
-__global__ void __launch_bounds__(kScanThreads) select_write_kernel(const Volume V, uint32_t n, uint32_t threshold,
+__global__ void __launch_bounds__(kScanThreads) select_write_kernel(const Volume V, uint32_t n, const EvictRule rule,
                                                                     int what, uint32_t lo,
                                                                     const uint32_t* __restrict__ cta_offsets,
                                                                     uint32_t* __restrict__ list) {
@@ -106,7 +111,7 @@ __global__ void __launch_bounds__(kScanThreads) select_write_kernel(const Volume
   const uint32_t frame = V.counters->frame;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t b = blockIdx.x * kScanThreads + tid;
-  const bool sel = b < n && selected(V, b, frame, threshold, what, lo);
+  const bool sel = b < n && selected(V, b, frame, rule, what, lo);
   const uint32_t ballot = __ballot_sync(0xffffffffU, sel);
   if (lane == 0) s_warp[warp] = static_cast<uint32_t>(__popc(ballot));
   __syncthreads();
@@ -179,6 +184,25 @@ __global__ void __launch_bounds__(256) copy_out_reference_kernel(const Volume V,
 }
 
 // block src[i] -> dst[i] with its key, masks and stamp: one CTA per move
+// observed voxels of the victims (set bits of their observed-voxel masks; a bit is set exactly when the voxel
+// has a layer of positive weight), subtracted from the volume's count once the victims are gone: the same
+// number a recount of the surviving pool gives, without reading the pool
+__global__ void __launch_bounds__(256) victim_observed_kernel(const Volume V, const uint32_t* __restrict__ list,
+                                                              uint32_t n, unsigned long long* __restrict__ out) {
+  constexpr uint32_t kWords = kBlockVoxels / 32;
+  unsigned long long local = 0ULL;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n * kWords; i += gridDim.x * blockDim.x) {
+    local += static_cast<unsigned long long>(__popc(V.obs_mask[static_cast<size_t>(list[i / kWords]) * kWords + i % kWords]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffU, local, o);
+  if ((threadIdx.x & 31) == 0 && local) atomicAdd(out, local);
+}
+
+__global__ void subtract_observed_kernel(Counters* __restrict__ c, const unsigned long long* __restrict__ removed) {
+  c->observed_voxels -= *removed;
+}
+
 __global__ void __launch_bounds__(256) move_blocks_kernel(const Volume V, const uint32_t* __restrict__ src,
                                                           const uint32_t* __restrict__ dst, uint32_t n) {
   const size_t words = block_words(V);
@@ -257,17 +281,17 @@ cudaError_t launch_age_hist(const Volume& V, uint32_t* hist, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_select(const Volume& V, uint32_t n, uint32_t threshold, int what, uint32_t lo,
+cudaError_t launch_select(const Volume& V, uint32_t n, const EvictRule& rule, int what, uint32_t lo,
                           uint32_t* cta_scratch, uint32_t* total, uint32_t* list, cudaStream_t s) {
   if (n == 0) return cudaMemsetAsync(total, 0, sizeof(uint32_t), s);
   const uint32_t nctas = (n + kScanThreads - 1) / kScanThreads;
-  select_count_kernel<<<nctas, kScanThreads, 0, s>>>(V, n, threshold, what, lo, cta_scratch);
+  select_count_kernel<<<nctas, kScanThreads, 0, s>>>(V, n, rule, what, lo, cta_scratch);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   select_scan_kernel<<<1, kScanThreads, 0, s>>>(cta_scratch, nctas, total);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  select_write_kernel<<<nctas, kScanThreads, 0, s>>>(V, n, threshold, what, lo, cta_scratch, list);
+  select_write_kernel<<<nctas, kScanThreads, 0, s>>>(V, n, rule, what, lo, cta_scratch, list);
   return cudaGetLastError();
 }
 
@@ -279,6 +303,19 @@ cudaError_t launch_copy_out(const Volume& V, const uint32_t* list, uint32_t n, i
   } else {
     copy_out_reference_kernel<<<152 * 8, 256, 0, s>>>(V, list, n, keys, static_cast<float4*>(out));
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_victim_observed(const Volume& V, const uint32_t* list, uint32_t n, unsigned long long* out,
+                                   cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess || n == 0) return e;
+  victim_observed_kernel<<<152 * 4, 256, 0, s>>>(V, list, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_subtract_observed(const Volume& V, const unsigned long long* removed, cudaStream_t s) {
+  subtract_observed_kernel<<<1, 1, 0, s>>>(V.counters, removed);
   return cudaGetLastError();
 }
 

@@ -94,14 +94,25 @@ cudaError_t launch_import_keys(const Volume& V, const int* keys, uint32_t n, uin
 // ---- eviction (vh_evict.cu) ----
 constexpr int kAgeBins = 4096;  // block-age histogram: ages 0..4094 frames, the last bin everything older
 cudaError_t launch_age_hist(const Volume& V, uint32_t* hist, cudaStream_t s);
-// pool blocks of [0, n) in ascending order into list, their number into *total (device); what 0: blocks whose
-// age (frames since their last layer update; never updated = oldest) is >= threshold; what 1: blocks of [lo, n)
-// whose age is below it.  cta_scratch: ceil(n / 1024) words.
-cudaError_t launch_select(const Volume& V, uint32_t n, uint32_t threshold, int what, uint32_t lo,
+// Which blocks an eviction removes.  age = frames since the block's last layer update (never updated: oldest),
+// bin = min(age, kAgeBins - 1).  A block is a victim when age >= min_age, or bin > tie_bin, or bin == tie_bin
+// and its pool index is below cut (ties at the boundary bin go in pool order).  {min_age, kAgeBins, 0}: every
+// block of age >= min_age.
+struct EvictRule {
+  uint32_t min_age, tie_bin, cut;
+};
+// pool blocks of [0, n) in ascending order into list, their number into *total (device); what 0: the victims;
+// what 1: the blocks of [lo, n) that are not; what 2: the blocks of bin tie_bin that are not victims by age.
+// cta_scratch: ceil(n / 1024) words.
+cudaError_t launch_select(const Volume& V, uint32_t n, const EvictRule& rule, int what, uint32_t lo,
                           uint32_t* cta_scratch, uint32_t* total, uint32_t* list, cudaStream_t s);
 // listed blocks with their keys into a staging buffer: native 1 the pool's own block image, 0 the reference layout
 cudaError_t launch_copy_out(const Volume& V, const uint32_t* list, uint32_t n, int native, int* keys, void* out,
                             cudaStream_t s);
+// observed voxels of the n listed victim blocks -> *out (zeroed here); the volume's count less *out
+cudaError_t launch_victim_observed(const Volume& V, const uint32_t* list, uint32_t n, unsigned long long* out,
+                                   cudaStream_t s);
+cudaError_t launch_subtract_observed(const Volume& V, const unsigned long long* removed, cudaStream_t s);
 cudaError_t launch_move_blocks(const Volume& V, const uint32_t* src, const uint32_t* dst, uint32_t n, cudaStream_t s);
 // empties the hash and inserts the keys of pool blocks [0, live)
 cudaError_t launch_rehash(const Volume& V, uint32_t live, cudaStream_t s);
