@@ -152,3 +152,34 @@ def test_target_evicts_exactly_down_to_the_count(env, small_orbit):
     assert vol.block_count() == target and len(ek) == n0 - target and len(kept) == target
     assert last <= kept
     vol.close()
+
+
+@pytest.mark.parametrize("fp16", [False, True])
+def test_evict_into_device_memory_matches_host(env, small_orbit, fp16):
+    """Evicting into device buffers (the copy kernel stores into them directly) gives the same keys and block
+    images as evicting into host memory, in both formats and both storage precisions."""
+    import ctypes as C
+    backend, O = env
+    from voxelhashmt_gb300 import _capi
+    sc = small_orbit
+    frames = list(range(0, 20, 2))
+    for native in (True, False):
+        a, b = _volume(backend, sc, fp16), _volume(backend, sc, fp16)
+        _fuse(backend, a, sc, frames)
+        _fuse(backend, b, sc, frames)
+        hk, hd = a.evict_blocks(6, native=native)
+        n = len(hk)
+        assert n > 0
+        bpb = hd.reshape(n, -1).view(np.uint8).shape[1]
+        dk = torch.zeros((n, 3), dtype=torch.int32, device="cuda")
+        dd = torch.zeros((n, bpb), dtype=torch.uint8, device="cuda")
+        cnt = C.c_uint64()
+        _capi.check(_capi.lib().vh_evict_blocks(b.handle, 6, 0, 1 if native else 0,
+                                                C.cast(C.c_void_p(dk.data_ptr()), C.POINTER(C.c_int32)),
+                                                C.c_void_p(dd.data_ptr()), n, 1, C.byref(cnt), None), b.handle)
+        assert cnt.value == n and b.block_count() == a.block_count()
+        got = {tuple(k): bytes(d) for k, d in zip(dk.cpu().numpy().tolist(), dd.cpu().numpy())}
+        want = {tuple(k): bytes(d) for k, d in zip(hk.tolist(), hd.reshape(n, -1).view(np.uint8))}
+        assert got == want
+        a.close()
+        b.close()

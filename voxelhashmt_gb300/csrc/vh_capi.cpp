@@ -803,12 +803,33 @@ vh_status vh_evict_blocks(vh_volume* v, uint32_t min_age_frames, uint64_t target
     *evicted = nv;
     return fail(v, VH_ERR_BUFFER_TOO_SMALL, "vh_evict_blocks: output buffers hold fewer blocks than are evicted");
   }
-  // 1. copy the victims out (staging buffer, then the caller's memory)
+  // 1. copy the victims out: into device memory directly (16-byte aligned), else through the staging buffer
   const size_t bytes = format == 1 ? native_block_bytes(v) : kBlockBytes;
   const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  // device (or managed) memory only: the copy kernel then stores into it; anything else goes through cudaMemcpy
+  auto device_memory = [](const void* ptr) {
+    if (!ptr) return true;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  };
+  const bool direct = out_on_device && reinterpret_cast<uintptr_t>(data_out) % 16 == 0 && device_memory(data_out) &&
+                      device_memory(keys_out);
   if (keys_out || data_out) {
     for (uint64_t done = 0; done < nv; done += kExportChunk) {
       const uint32_t c = static_cast<uint32_t>(std::min<uint64_t>(kExportChunk, nv - done));
+      if (direct) {
+        // the copy kernel writes the caller's buffers (a NULL one's part goes to the staging buffer)
+        VH_CUDA(v, vh::launch_copy_out(v->dev, v->d_evict_list + done, c, format,
+                                       keys_out ? keys_out + 3 * done : v->d_export_keys,
+                                       data_out ? static_cast<void*>(static_cast<char*>(data_out) + done * bytes)
+                                                : static_cast<void*>(v->d_export),
+                                       s));
+        continue;
+      }
       VH_CUDA(v, vh::launch_copy_out(v->dev, v->d_evict_list + done, c, format, v->d_export_keys, v->d_export, s));
       if (data_out) {
         VH_CUDA(v, cudaMemcpyAsync(static_cast<char*>(data_out) + done * bytes, v->d_export, c * bytes, kind, s));
