@@ -1044,7 +1044,7 @@ __global__ void __launch_bounds__(256) dgrad_out_kernel(const float* __restrict_
 // db[co] = sum_p dY[p][co].  X: BF16 with 32 channels (read as 16-byte vectors) or FP32 float4 (CI = 4); dY:
 // BF16 with 32 channels or FP32 with 1.  Each CTA stages row segments of kSeg pixels (three input rows with a
 // one-pixel halo, one gradient row) in shared memory as floats.  Thread (rep, co, ci) keeps 9 accumulators (and
-// the bias sum) over the pixels rep, rep + kRep, ... of each segment, so that CI x CO x kRep threads share a
+// the bias sum) over the rep-th of kRep contiguous runs of each segment, so that CI x CO x kRep threads share a
 // segment; the kRep partial sums are added in shared memory and flushed with one atomic per weight per CTA.
 constexpr int kSeg = 64;
 
@@ -1056,6 +1056,7 @@ __global__ void __launch_bounds__(CI * CO * kRep) wgrad_kernel(const void* __res
   static_assert(kXBf16 || CI == 4, "FP32 inputs are float4 pixels");
   static_assert(!kDyBf16 || CO == 32, "BF16 gradients carry 32 channels");
   static_assert(kDyBf16 || CO == 1, "FP32 gradients carry one channel");
+  static_assert(kSeg % kRep == 0, "replicas take equal runs of a segment");
   constexpr int kPairs = CI * CO, kT = kPairs * kRep;
   __shared__ __align__(16) float sX[3][kSeg + 2][CI];
   __shared__ __align__(16) float sG[kSeg][CO];
@@ -1115,10 +1116,27 @@ __global__ void __launch_bounds__(CI * CO * kRep) wgrad_kernel(const void* __res
       }
     }
     __syncthreads();
-    for (int px = rep; px < kSeg; px += kRep) {
+    // replica rep takes a contiguous run of the segment's pixels, so each tap row's three inputs slide along it:
+    // one new shared-memory read per row and pixel instead of three
+    constexpr int kRun = kSeg / kRep;
+    const int p0 = rep * kRun;
+    float w0[3], w1[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+      w0[r] = sX[r][p0][ci];
+      w1[r] = sX[r][p0 + 1][ci];
+    }
+    for (int px = p0; px < p0 + kRun; ++px) {
       const float g = sG[px][co];
 #pragma unroll
-      for (int t = 0; t < 9; ++t) acc[t] += g * sX[t / 3][px + t % 3][ci];
+      for (int r = 0; r < 3; ++r) {
+        const float w2 = sX[r][px + 2][ci];
+        acc[3 * r] += g * w0[r];
+        acc[3 * r + 1] += g * w1[r];
+        acc[3 * r + 2] += g * w2;
+        w0[r] = w1[r];
+        w1[r] = w2;
+      }
       bacc += g;
     }
     __syncthreads();
