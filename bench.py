@@ -47,10 +47,10 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # bytes per active voxel, written bytes per updated voxel), scaled by the active and updated voxels of a launch
 # (plain: update_kernel_room640.md, one launch over 6.55 M active voxels, read + write per active voxel;
 # opt-in form: fused_update_room640.md, one launch over 3.16 M active and 2.86 M updated voxels).
-UPDATE_TRAFFIC_BYTES = {"plain": ((539.49e6 + 267.04e6) / 6.548e6, 0.0),
+UPDATE_TRAFFIC_BYTES = {"plain": ((538.122e6 + 262.315e6) / 6.549e6, 0.0),
                         "chosen": (189.529e6 / 3.163e6, 58.035e6 / 2.860e6)}
 # warp instructions per active voxel of the layer-update kernel (smsp__inst_executed.sum of the same captures)
-UPDATE_WARP_INSTRUCTIONS = {"plain": 1514.374e6 / 6.548e6, "chosen": 111.551e6 / 3.163e6}
+UPDATE_WARP_INSTRUCTIONS = {"plain": 1813.602e6 / 6.549e6, "chosen": 111.551e6 / 3.163e6}
 
 
 def parse():
