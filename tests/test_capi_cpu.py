@@ -46,6 +46,10 @@ def test_status_strings_and_argument_checks(product_lib):
     err = (C.c_uint32 * 1)()
     assert L.vh_nn_conv32_gated(None, None, None, None, None, 1, 8, 8, 0, 0, None, err, None) == \
         capi.VH_ERR_INVALID_ARGUMENT
+    assert L.vh_nn_wgrad32(None, None, None, None, 1, 8, 8, err, None) == capi.VH_ERR_INVALID_ARGUMENT
+    ev = C.c_uint64()
+    assert L.vh_evict_blocks(None, 0, 0, 1, None, None, 0, 0, C.byref(ev), None) == capi.VH_ERR_INVALID_ARGUMENT
+    assert L.vh_restore_blocks(None, None, None, 1, 0, None) == capi.VH_ERR_INVALID_ARGUMENT
 
 
 def test_no_device_is_reported_not_faked(product_lib):
